@@ -1,0 +1,295 @@
+/*
+ * Minimal project-written stand-ins for the MCell4 classes that the reference's
+ * hot-path routines touch (Partition, Molecule, Wall, Collision, RxnClass,
+ * SimulationConfig, SimulationStats). The reference's own headers for these
+ * classes pull in libbng, boost, sparsehash and the whole World, none of which
+ * exist here, so the routines are compiled against these classes instead.
+ *
+ * Member names and signatures are the ones the routines call (they must match
+ * for the routines to compile unchanged):
+ *   Partition          src4/partition.h:198 (accessors :248-298, :641, :889)
+ *   Molecule           src4/molecule.h:52
+ *   Wall / rejection   src4/wall.h:200-350
+ *   Collision          src4/collision_structs.h:29-140
+ *   SimulationConfig   src4/simulation_config.h:28-135
+ * The bodies are this project's own. Test infrastructure only: this header is
+ * compiled into oracle/_ref and is never part of the product.
+ */
+#ifndef ORACLE_REF_SHIM_H
+#define ORACLE_REF_SHIM_H
+
+#include <map>
+#include <vector>
+#include <cstring>
+#include <cstdint>
+
+#include "defines.h"
+
+// ---- injected random numbers (replaces the single ISAAC64 stream) ----
+struct ShimRng {
+  const uint32_t* draws = nullptr;
+  size_t n = 0;
+  size_t used = 0;
+  bool overrun = false;
+  unsigned int next_uint() {
+    if (used >= n) {
+      overrun = true;
+      return 0;
+    }
+    return draws[used++];
+  }
+  double next_dbl() {
+    // rng_dbl is a 32-bit draw scaled by 2^-32 (src/isaac64.h isaac64_dbl32)
+    return (double)next_uint() * (1.0 / 4294967296.0);
+  }
+};
+#undef rng_state
+#undef rng_uint
+#undef rng_dbl
+#define rng_state ShimRng
+#define rng_uint(x) ((x)->next_uint())
+#define rng_dbl(x) ((x)->next_dbl())
+
+namespace BNG {
+
+const int PATHWAY_INDEX_NO_RXN = -2;
+const int PATHWAY_INDEX_LEAST_VALID = 0;
+typedef int rxn_class_pathway_index_t;
+const species_id_t SPECIES_FLAG_CAN_VOLWALL = 1u << 4;
+
+enum class RxnType { Invalid, Standard, Transparent, Reflect, AbsorbRegionBorder };
+
+// reaction class for one reactant pair: max_fixed_p and cumulative pathway probabilities
+class RxnClass {
+public:
+  RxnType type = RxnType::Standard;
+  std::vector<double> cum_probs;
+  size_t get_num_reactions() const { return cum_probs.size(); }
+  double get_max_fixed_p() const { return cum_probs.empty() ? 0.0 : cum_probs.back(); }
+  void update_rxn_rates_if_needed(const double) { }
+  double get_next_time_of_rxn_rate_update() const { return 1e20; }
+  bool is_transparent_type() const { return type == RxnType::Transparent; }
+  // pathway lookup; MCell3 uses binary_search_double over cum_probs (src/react_cond.c)
+  int get_pathway_index_for_probability(const double prob, const double local_prob_factor) const;
+};
+
+typedef std::vector<RxnClass*> RxnClassesVector;
+
+class Species {
+public:
+  uint flags = 0;
+  double space_step = 0;
+  double time_step = 1;
+  bool has_flag(uint f) const { return (flags & f) != 0; }
+  bool can_diffuse() const { return space_step != 0; }
+};
+
+} // namespace BNG
+
+namespace MCell {
+
+const uint MOLECULE_FLAG_DEFUNCT = 1u << 31;
+
+class Molecule {
+public:
+  molecule_id_t id = MOLECULE_ID_INVALID;
+  species_id_t species_id = BNG::SPECIES_ID_INVALID;
+  uint flags = 0;
+  struct {
+    Vec3 pos;
+    subpart_index_t subpart_index = SUBPART_INDEX_INVALID;
+  } v;
+  bool is_defunct() const { return (flags & MOLECULE_FLAG_DEFUNCT) != 0; }
+  bool is_vol() const { return true; }
+  bool is_surf() const { return false; }
+};
+
+class WallCollisionRejectionData {
+public:
+  Vec3 normal;
+  pos_t distance_to_origin = 0;
+};
+
+class Partition;
+
+class Wall: public WallCollisionRejectionData {
+public:
+  wall_index_t index = WALL_INDEX_INVALID;
+  wall_id_t id = 0;
+  vertex_index_t vertex_indices[3];
+  pos_t area = 0;
+  bool wall_constants_initialized = false;
+  pos_t uv_vert1_u = 0;
+  Vec2 uv_vert2;
+  Vec3 unit_u, unit_v;
+  uint surf_class_of_species_mask = 0; // unused by the routines
+  bool exists_in_partition() const { return id != WALL_ID_NOT_IN_PARTITION; }
+  bool is_overlapped_wall() const { return false; }
+  void initialize_wall_constants(const Partition& p);
+};
+
+class WallWithVertices: public Wall {
+public:
+  Vec3 vertices[3];
+};
+
+typedef uint_set<wall_index_t> WallsInSubpart;
+
+enum class CollisionType {
+  INVALID, WALL_REDO, WALL_MISS, WALL_FRONT, WALL_BACK,
+  VOLMOL_VOLMOL, SURFMOL_SURFMOL, VOLMOL_SURFMOL, UNIMOLECULAR, INTERMEMBRANE_SURFMOL_SURFMOL
+};
+
+enum class RayTraceState { UNDEFINED, HIT_SUBPARTITION, RAY_TRACE_HIT_WALL, FINISHED };
+
+class Collision {
+public:
+  Collision() : type(CollisionType::INVALID), partition(nullptr), diffused_molecule_id(0),
+      time(0), pos(0), colliding_molecule_id(0), rxn_class(nullptr), colliding_wall_index(0) { }
+  Collision(const CollisionType type_, Partition* p_, const molecule_id_t dm, const double time_,
+      const Vec3& pos_, const molecule_id_t cm, BNG::RxnClass* rc)
+    : type(type_), partition(p_), diffused_molecule_id(dm), time(time_), pos(pos_),
+      colliding_molecule_id(cm), rxn_class(rc), colliding_wall_index(WALL_INDEX_INVALID) { }
+  Collision(const CollisionType type_, Partition* p_, const molecule_id_t dm, const double time_,
+      const Vec3& pos_, const wall_index_t wi)
+    : type(type_), partition(p_), diffused_molecule_id(dm), time(time_), pos(pos_),
+      colliding_molecule_id(MOLECULE_ID_INVALID), rxn_class(nullptr), colliding_wall_index(wi) { }
+  bool is_vol_mol_vol_mol_collision() const { return type == CollisionType::VOLMOL_VOLMOL; }
+  bool is_wall_collision() const { return type == CollisionType::WALL_FRONT || type == CollisionType::WALL_BACK; }
+
+  CollisionType type;
+  Partition* partition;
+  molecule_id_t diffused_molecule_id;
+  double time;
+  Vec3 pos;
+  molecule_id_t colliding_molecule_id;
+  BNG::RxnClass* rxn_class;
+  wall_index_t colliding_wall_index;
+};
+
+typedef std::vector<Collision> CollisionsVector;
+
+class SimulationConfig {
+public:
+  pos_t partition_edge_length = 0;
+  uint num_subparts_per_partition_edge = 0;
+  uint num_subparts_per_partition_edge_squared = 0;
+  uint num_subparts = 0;
+  pos_t subpart_edge_length = 0;
+  pos_t subpart_edge_length_rcp = 0;
+  pos_t rxn_radius_3d = 0;
+  bool use_expanded_list = true;
+  double length_unit = 0.01;
+  double rcp_length_unit = 100;
+  void init_subpartition_edge_length();
+};
+
+class SimulationStats {
+public:
+  void inc_ray_voxel_tests() const { }
+  void inc_ray_polygon_tests() const { }
+  void inc_ray_polygon_colls() const { }
+  void inc_diffuse_3d_calls() const { }
+  void inc_mol_wall_reflections() const { }
+  void inc_vol_mol_vol_mol_collisions() const { }
+  template<typename A, typename B> void inc_rxn_skipped(const A&, const B*, double) const { }
+};
+
+class RxnContainerShim {
+public:
+  std::map<std::pair<uint, uint>, BNG::RxnClass*> bimol;
+  BNG::RxnClass* get_bimol_rxn_class(const species_id_t a, const species_id_t b) const {
+    auto it = bimol.find(std::make_pair(a, b));
+    return it == bimol.end() ? nullptr : it->second;
+  }
+};
+
+class SpeciesContainerShim {
+public:
+  std::vector<BNG::Species> species;
+  const BNG::Species& get(const species_id_t id) const { return species[id]; }
+};
+
+class Partition {
+public:
+  SimulationConfig config;
+  SimulationStats stats;
+  Vec3 origin_corner, opposite_corner;
+  std::vector<Vec3> vertices;
+  std::vector<Wall> walls;
+  std::vector<WallCollisionRejectionData> wall_collision_rejection_data;
+  std::vector<WallsInSubpart> walls_per_subpart;
+  std::vector<Molecule> molecules;
+  // reactants of species s in subpart p: molecules there that have a bimolecular rxn with s
+  std::map<std::pair<subpart_index_t, species_id_t>, uint_set<molecule_id_t>> reactants;
+  uint_set<molecule_id_t> empty_set;
+  RxnContainerShim rxns;
+  SpeciesContainerShim all_species;
+  // surface class kind per (wall, species): 0 reflect, 1 transparent, 2 absorptive
+  std::map<std::pair<wall_index_t, species_id_t>, int> wall_class;
+
+  const Vec3& get_origin_corner() const { return origin_corner; }
+  bool in_this_partition(const Vec3& pos) const {
+    return pos.x >= origin_corner.x && pos.y >= origin_corner.y && pos.z >= origin_corner.z &&
+           pos.x < opposite_corner.x && pos.y < opposite_corner.y && pos.z < opposite_corner.z;
+  }
+  bool is_subpart_index_in_range(const int index) const {
+    return index >= 0 && index < (int)config.num_subparts_per_partition_edge;
+  }
+  void get_subpart_3d_indices(const Vec3& pos, IVec3& res) const {
+    Vec3 rel = pos - origin_corner;
+    res = rel * config.subpart_edge_length_rcp;
+  }
+  subpart_index_t get_subpart_index_from_3d_indices_allow_outside(const IVec3& i) const {
+    return i.x + i.y * config.num_subparts_per_partition_edge +
+        i.z * config.num_subparts_per_partition_edge_squared;
+  }
+  subpart_index_t get_subpart_index_from_3d_indices(const IVec3& i) const {
+    return get_subpart_index_from_3d_indices_allow_outside(i);
+  }
+  subpart_index_t get_subpart_index_from_3d_indices(const int x, const int y, const int z) const {
+    return get_subpart_index_from_3d_indices(IVec3(x, y, z));
+  }
+  void get_subpart_3d_indices_from_index(const subpart_index_t index, IVec3& i) const {
+    uint32_t n = config.num_subparts_per_partition_edge;
+    i.x = index % n;
+    i.y = (index / n) % n;
+    i.z = (index / config.num_subparts_per_partition_edge_squared) % n;
+  }
+  subpart_index_t get_subpart_index(const Vec3& pos) const {
+    IVec3 i;
+    get_subpart_3d_indices(pos, i);
+    return get_subpart_index_from_3d_indices(i);
+  }
+  void get_subpart_llf_point(const subpart_index_t s, Vec3& llf) const {
+    IVec3 i;
+    get_subpart_3d_indices_from_index(s, i);
+    llf = origin_corner + Vec3(i) * Vec3(config.subpart_edge_length);
+  }
+  void get_subpart_urb_point_from_llf(const Vec3& llf, Vec3& urb) const {
+    urb = llf + Vec3(config.subpart_edge_length);
+  }
+  const Vec3& get_geometry_vertex(const vertex_index_t i) const { return vertices[i]; }
+  const Vec3& get_wall_vertex(const Wall& w, const uint k) const { return vertices[w.vertex_indices[k]]; }
+  Wall& get_wall(const wall_index_t i) { return walls[i]; }
+  const Wall& get_wall(const wall_index_t i) const { return walls[i]; }
+  const WallCollisionRejectionData& get_wall_collision_rejection_data(const wall_index_t i) const {
+    return wall_collision_rejection_data[i];
+  }
+  const WallsInSubpart& get_subpart_wall_indices(const subpart_index_t s) const {
+    return walls_per_subpart[s];
+  }
+  Molecule& get_m(const molecule_id_t id) { return molecules[id]; }
+  const Molecule& get_m(const molecule_id_t id) const { return molecules[id]; }
+  const uint_set<molecule_id_t>& get_volume_molecule_reactants(const subpart_index_t s, const species_id_t sp) const {
+    auto it = reactants.find(std::make_pair(s, sp));
+    return it == reactants.end() ? empty_set : it->second;
+  }
+  const RxnContainerShim& get_all_rxns() const { return rxns; }
+  const SpeciesContainerShim& get_all_species() const { return all_species; }
+  const BNG::Species& get_species(const species_id_t id) const { return all_species.get(id); }
+};
+
+} // namespace MCell
+
+#endif

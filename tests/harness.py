@@ -1,0 +1,206 @@
+"""Test harness: scenes, and ctypes bindings to the two CPU checkers.
+
+- the oracle port (oracle/_build/libmcell_oracle.so, built everywhere by build())
+- the reference's own routines (oracle/_ref/libmcell_ref{64,32}.so, built only
+  where the reference sources exist, i.e. not on the GPU host)
+
+Both expose the same scene / case entry points (prefix orc_ / ref_). Results of
+one diffusion case are float64 arrays of RES_SIZE (layout in oracle/mcell_oracle.h).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+from dataclasses import dataclass, field
+from pathlib import Path
+from typing import Optional
+
+import numpy as np
+
+from mcell_gb300 import conversion, geometry
+
+ROOT = Path(__file__).resolve().parent.parent
+RES_HDR, EV_SIZE, EV_MAX = 9, 8, 32
+RES_SIZE = RES_HDR + EV_SIZE * EV_MAX
+
+_vp = ctypes.c_void_p
+_d = ctypes.c_double
+_u = ctypes.c_uint
+
+
+def ptr(a):
+    return a.ctypes.data_as(_vp)
+
+
+@dataclass
+class Scene:
+    origin: np.ndarray
+    partition_edge: float
+    nsub: int
+    rxn_radius: float
+    verts: np.ndarray             # float64 [nv, 3] internal units
+    tris: np.ndarray              # uint32 [nw, 3]
+    space_steps: np.ndarray       # float64 [nspecies]
+    wall_class: np.ndarray        # uint8 [nw, nspecies]
+    rxn_ab: np.ndarray            # uint32 [nrxn, 2]
+    rxn_p: np.ndarray             # float64 [nrxn]
+    mol_pos: np.ndarray           # float64 [nmol, 3]
+    mol_species: np.ndarray       # uint32 [nmol]
+
+    def args(self):
+        o = np.ascontiguousarray(self.origin, np.float64)
+        keep = [o, np.ascontiguousarray(self.verts, np.float64), np.ascontiguousarray(self.tris, np.uint32),
+                np.ascontiguousarray(self.space_steps, np.float64),
+                np.ascontiguousarray(self.wall_class, np.uint8),
+                np.ascontiguousarray(self.rxn_ab, np.uint32).reshape(-1),
+                np.ascontiguousarray(self.rxn_p, np.float64),
+                np.ascontiguousarray(self.mol_pos, np.float64), np.ascontiguousarray(self.mol_species, np.uint32)]
+        self._keep = keep
+        return (ptr(keep[0]), _d(self.partition_edge), _u(self.nsub), _d(self.rxn_radius),
+                _u(len(self.verts)), ptr(keep[1]), _u(len(self.tris)), ptr(keep[2]),
+                _u(len(self.space_steps)), ptr(keep[3]), ptr(keep[4]),
+                _u(len(self.rxn_p)), ptr(keep[5]), ptr(keep[6]),
+                _u(len(self.mol_species)), ptr(keep[7]), ptr(keep[8]))
+
+
+class Checker:
+    """One of the two CPU checkers (oracle port or reference routines)."""
+
+    def __init__(self, path: Path, prefix: str):
+        self.lib = ctypes.CDLL(str(path))
+        self.p = prefix
+        f = self.fn("scene_new")
+        f.restype = _vp
+        self.fn("subpart_index").restype = _u
+        self.fn("scene_walls_in_subparts").restype = _u
+        self.fn("test_bimolecular").restype = ctypes.c_int
+        self.fn("time_of_unimol").restype = _d
+
+    def fn(self, name):
+        return getattr(self.lib, f"{self.p}_{name}")
+
+    def scene(self, sc: Scene):
+        h = _vp(self.fn("scene_new")(*sc.args()))
+        return _Handle(self, h)
+
+    def test_bimolecular(self, p, scaling, draw):
+        return self.fn("test_bimolecular")(_d(p), _d(scaling), _u(draw))
+
+    def time_of_unimol(self, k, draw):
+        return self.fn("time_of_unimol")(_d(k), _u(draw))
+
+
+class _Handle:
+    def __init__(self, chk: Checker, h):
+        self.c, self.h = chk, h
+
+    def __del__(self):
+        try:
+            self.c.fn("scene_free")(self.h)
+        except Exception:
+            pass
+
+    def info(self):
+        out = np.zeros(7)
+        self.c.fn("scene_info")(self.h, ptr(out))
+        return out
+
+    def wall_consts(self, nw):
+        out = np.zeros((nw, 14))
+        self.c.fn("scene_wall_consts")(self.h, ptr(out))
+        return out
+
+    def walls_in_subparts(self, nsub3, cap=1 << 22):
+        counts = np.zeros(nsub3, np.uint32)
+        lst = np.zeros(cap, np.uint32)
+        n = self.c.fn("scene_walls_in_subparts")(self.h, ptr(counts), ptr(lst), _u(cap))
+        return counts, lst[:n]
+
+    def subpart_index(self, pos):
+        p = np.ascontiguousarray(pos, np.float64)
+        return self.c.fn("subpart_index")(self.h, ptr(p))
+
+    def diffuse_case(self, mol, disp, draws, r_rate_factor=1.0, t_steps=1.0):
+        out = np.zeros(RES_SIZE)
+        d = np.ascontiguousarray(disp, np.float64)
+        dr = np.ascontiguousarray(draws, np.uint32)
+        self.c.fn("diffuse_case")(self.h, _u(mol), ptr(d), ptr(dr), _u(len(dr)), _d(r_rate_factor),
+                                  _d(t_steps), ptr(out))
+        return out
+
+
+def oracle_path() -> Path:
+    return ROOT / "oracle" / "_build" / "libmcell_oracle.so"
+
+
+def ref_path(bits=64) -> Path:
+    return ROOT / "oracle" / "_ref" / f"libmcell_ref{bits}.so"
+
+
+def oracle() -> Checker:
+    return Checker(oracle_path(), "orc")
+
+
+def reference(bits=64) -> Optional[Checker]:
+    p = ref_path(bits)
+    if not p.exists():
+        return None
+    return Checker(p, "ref")
+
+
+# ------------------------------------------------------------------ scenes
+
+def cube_scene(rng: np.random.Generator, n_mol=400, edge_um=1.0, nsub=12, partition_um=1.2,
+               p_rxn=0.0368, classes=None) -> Scene:
+    """Closed reflective cube (the Model API's create_box) with A (0), B (1), C (2)."""
+    lu = conversion.length_unit_um()
+    v, w = geometry.create_box(edge_dimension=edge_um)
+    lay = conversion.partition_layout(v.min(0), v.max(0), partition_dimension_um=partition_um,
+                                      subpartition_dimension_um=partition_um / nsub)
+    verts = v / lu
+    half = edge_um / 2 / lu
+    pos = rng.uniform(-half, half, size=(n_mol, 3))
+    sp = rng.integers(0, 2, size=n_mol).astype(np.uint32)
+    wc = np.zeros((len(w), 3), np.uint8)
+    if classes is not None:
+        wc[:] = classes
+    return Scene(np.array(lay.origin), lay.edge, lay.nsub, conversion.default_rxn_radius_um() / lu,
+                 verts, w, np.array([2.0, 2.0, 1.414213562373095]), wc,
+                 np.array([[0, 1]], np.uint32), np.array([p_rxn]), pos, sp)
+
+
+def sphere_in_cube_scene(rng: np.random.Generator, levels=2, n_mol=400, radius_um=1.0, cube_um=2.5,
+                         nsub=None, transparent_a=True, p_rxn=0.0368) -> Scene:
+    """Icosphere inside a reflective cube; sphere transparent to A (config of the large model)."""
+    lu = conversion.length_unit_um()
+    sv, sw = geometry.create_icosphere(radius_um, levels)
+    bv, bw = geometry.create_box(edge_dimension=cube_um)
+    v, w, obj = geometry.merge_meshes((sv, sw), (bv, bw))
+    lay = conversion.partition_layout(v.min(0), v.max(0), partition_dimension_um=cube_um + 0.2,
+                                      subpartition_dimension_um=0.1)
+    if nsub is not None:
+        lay = conversion.PartitionLayout(lay.origin, lay.edge, nsub)
+    wc = np.zeros((len(w), 3), np.uint8)
+    if transparent_a:
+        wc[obj == 0, 0] = 1
+    half = cube_um / 2 / lu
+    pos = rng.uniform(-half, half, size=(n_mol, 3))
+    sp = rng.integers(0, 2, size=n_mol).astype(np.uint32)
+    return Scene(np.array(lay.origin), lay.edge, lay.nsub, conversion.default_rxn_radius_um() / lu,
+                 v / lu, w, np.array([2.0, 2.0, 1.414213562373095]), wc,
+                 np.array([[0, 1]], np.uint32), np.array([p_rxn]), pos, sp)
+
+
+def random_cases(rng: np.random.Generator, sc: Scene, n_cases: int, scale=2.0, ndraws=64, near_wall_frac=0.3):
+    """Random diffusion cases: (molecule index, displacement, draws). A fraction starts near walls."""
+    cases = []
+    nm = len(sc.mol_species)
+    for _ in range(n_cases):
+        mol = int(rng.integers(0, nm))
+        disp = rng.normal(0.0, scale * 0.7071067811865476, size=3)
+        if rng.random() < near_wall_frac:
+            disp *= rng.uniform(2, 20)
+        draws = rng.integers(0, 2 ** 32, size=ndraws, dtype=np.uint64).astype(np.uint32)
+        cases.append((mol, disp, draws))
+    return cases
