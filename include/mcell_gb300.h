@@ -1,0 +1,125 @@
+/*
+ * mcell_gb300: GB300 (sm_103a) engine for MCell4's volume-molecule
+ * diffuse-react step, behind a C ABI.
+ *
+ * The engine replaces DiffuseReactEvent::step for volume molecules
+ * (src4/diffuse_react_event.cpp:53-64) together with SortMolsBySubpartEvent::step
+ * (src4/sort_mols_by_subpart_event.cpp:62-97) and the per-subpartition reactant
+ * maps (src4/partition.h:354-418). The host World/Scheduler keeps calling one
+ * event per iteration; a GpuDiffuseReactEvent (include/mcell_gb300_event.hpp)
+ * forwards it here.
+ *
+ * Units are MCell4's internal ones: lengths in length_unit (1/sqrt(surface
+ * grid density) um, 0.01 um by default), time in time steps (one per
+ * iteration). Setup conversions (space steps, reaction probabilities,
+ * partition layout) happen on the host before these calls.
+ *
+ * Conventions: every call returns 0 (MCG_OK) or a negative MCG_ERR_* code;
+ * mcg_last_error() gives a message. Handles are not thread-safe; each owns
+ * its CUDA stream. No call falls back to a CPU path.
+ */
+#ifndef MCELL_GB300_H
+#define MCELL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCG_OK 0
+#define MCG_ERR_ARG (-1)          /* invalid argument or call order */
+#define MCG_ERR_CUDA (-2)         /* CUDA runtime error (message has details) */
+#define MCG_ERR_CAPACITY (-3)     /* molecule / product / list capacity exceeded */
+#define MCG_ERR_ESCAPE (-4)       /* a molecule left the partition (diffuse_react_event.cpp:592-612) */
+#define MCG_ERR_WATCHDOG (-5)     /* a bounded device loop gave up (REDO / DDA / resolve rounds) */
+#define MCG_ERR_UNSUPPORTED (-6)  /* model feature outside the GPU path (no fallback) */
+
+#define MCG_PRECISION_FP64 0
+#define MCG_PRECISION_FP32 1
+
+#define MCG_MAX_SPECIES 16
+#define MCG_TRACE_RESULT_SIZE 265 /* doubles per traced case: 9 header + 32 events x 8 */
+
+typedef struct mcg_engine mcg_engine;
+
+/* Replaces the SimulationConfig fields the step reads (src4/simulation_config.h:59-107)
+   plus the partition placement of Partition's ctor (src4/partition.cpp:36-60). */
+typedef struct mcg_config {
+  int precision;                /* MCG_PRECISION_FP64 / MCG_PRECISION_FP32 */
+  double partition_origin[3];   /* internal units */
+  double partition_edge;        /* internal units */
+  uint32_t subparts_per_edge;   /* num_subparts_per_partition_edge (<= 300) */
+  double rxn_radius;            /* rxn_radius_3d, internal units */
+  uint64_t seed;                /* Config.seed */
+  uint64_t capacity;            /* maximum live molecules (0 = 1.5 x first upload) */
+  uint32_t n_species;           /* <= MCG_MAX_SPECIES */
+} mcg_config;
+
+/* Engine lifetime (World::init_simulation creating the event, src4/world.cpp:280-282). */
+int mcg_create(const mcg_config* cfg, mcg_engine** out);
+void mcg_destroy(mcg_engine* e);
+const char* mcg_last_error(const mcg_engine* e);
+
+/* Species: space step per time step in internal units (Species::space_step as
+   set by src/mcell_species.c:270-274); 0 = does not diffuse. */
+int mcg_set_species(mcg_engine* e, uint32_t n, const double* space_step);
+
+/* Static mesh (Partition::finalize_walls, src4/partition.cpp:91; wall constants
+   src4/wall.cpp:281). wall_class[w * n_species + s]: 0 reflective,
+   1 transparent, 2 absorptive for species s at wall w (surface classes,
+   libmcell/api/mcell4_converter.cpp:515-575). */
+int mcg_upload_mesh(mcg_engine* e, uint32_t n_vertices, const double* vertices, uint32_t n_walls,
+                    const uint32_t* walls, const uint8_t* wall_class);
+
+/* Bimolecular vol+vol reaction a+b -> products (-1 = none): max_fixed_p
+   (RxnClass::get_max_fixed_p as used by test_bimolecular, src4/rxn_utils.inl:336). */
+int mcg_add_bimol_rxn(mcg_engine* e, uint32_t a, uint32_t b, double max_fixed_p, int32_t product0,
+                      int32_t product1);
+/* Unimolecular reaction a -> products: k_tot = rate * time_step
+   (time_of_unimol, src4/rxn_utils.inl:721). */
+int mcg_add_unimol_rxn(mcg_engine* e, uint32_t a, double k_tot, int32_t product0, int32_t product1);
+
+/* Volume molecules released before the first iteration (ReleaseEvent::step,
+   src4/release_event.cpp:1255). Their ids are given in call order from 0. */
+int mcg_add_molecules(mcg_engine* e, uint64_t n, const double* pos, const uint32_t* species);
+
+/* Runs n iterations of the diffuse-react step (DiffuseReactEvent::step, once per
+   iteration) without synchronising the host. */
+int mcg_step(mcg_engine* e, uint32_t n_iterations);
+/* Waits for queued work and reports device-side errors. */
+int mcg_sync(mcg_engine* e);
+
+/* Live molecule count per species after the last iteration
+   (replaces counting molecules for MolOrRxnCountEvent, src4/mol_or_rxn_count_event.cpp:707). */
+int mcg_get_counts(mcg_engine* e, uint64_t* counts /* [n_species] */);
+/* Count trajectory: counts after each of the last n iterations run, oldest first
+   ([n * n_species]); n <= iterations run since the last mcg_create. */
+int mcg_get_count_trajectory(mcg_engine* e, uint32_t n, uint64_t* counts);
+/* Copies live molecules out (in subpartition order). Returns the number in *n_out. */
+int mcg_download_molecules(mcg_engine* e, uint64_t cap, double* pos, uint32_t* species, uint64_t* ids,
+                           uint64_t* n_out);
+/* Iterations run, molecule-steps run, and a device status word. */
+int mcg_get_stats(mcg_engine* e, uint64_t* iterations, uint64_t* mol_steps, uint64_t* launches);
+
+/* Per-routine parity harness: one diffusion of a chosen molecule per case with
+   the displacement and the random draws injected, through the same device
+   functions the step uses (ray_trace_vol + the collision loop of
+   diffuse_vol_molecule, src4/diffuse_react_event.cpp:367-780). Molecules
+   must have been added and at least mcg_prepare() called. out: n_cases x
+   MCG_TRACE_RESULT_SIZE doubles (layout in mcell_gb300/csrc/mcg_device.cuh). */
+int mcg_prepare(mcg_engine* e);
+int mcg_trace_cases(mcg_engine* e, uint32_t n_cases, const uint64_t* mol_ids, const double* disp,
+                    const uint32_t* draws, uint32_t draws_per_case, const double* r_rate_factor,
+                    const double* t_steps, double* out);
+
+/* Setup queries for parity tests: wall constants (14 doubles per wall, same
+   layout as the oracle) and the wall lists per subpartition. */
+int mcg_wall_consts(mcg_engine* e, double* out);
+int mcg_walls_in_subparts(mcg_engine* e, uint32_t* counts, uint32_t* list, uint64_t cap, uint64_t* total);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

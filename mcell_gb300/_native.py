@@ -1,0 +1,194 @@
+"""ctypes binding of the engine's C ABI (include/mcell_gb300.h).
+
+The library is built in-tree by mcell_gb300.build into mcell_gb300/_lib/. There is
+no CPU fallback: if the library is missing or cannot be loaded, every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libmcell_gb300.so"
+
+MCG_OK = 0
+ERRORS = {-1: "MCG_ERR_ARG", -2: "MCG_ERR_CUDA", -3: "MCG_ERR_CAPACITY", -4: "MCG_ERR_ESCAPE",
+          -5: "MCG_ERR_WATCHDOG", -6: "MCG_ERR_UNSUPPORTED"}
+PRECISION = {"fp64": 0, "fp32": 1}
+TRACE_RESULT_SIZE = 265
+
+# every entry point declared in include/mcell_gb300.h
+EXPORTS = [
+    "mcg_create", "mcg_destroy", "mcg_last_error", "mcg_set_species", "mcg_upload_mesh", "mcg_add_bimol_rxn",
+    "mcg_add_unimol_rxn", "mcg_add_molecules", "mcg_step", "mcg_sync", "mcg_get_counts",
+    "mcg_get_count_trajectory", "mcg_download_molecules", "mcg_get_stats", "mcg_prepare", "mcg_trace_cases",
+    "mcg_wall_consts", "mcg_walls_in_subparts",
+]
+
+
+class McgConfig(ctypes.Structure):
+    _fields_ = [
+        ("precision", ctypes.c_int),
+        ("partition_origin", ctypes.c_double * 3),
+        ("partition_edge", ctypes.c_double),
+        ("subparts_per_edge", ctypes.c_uint32),
+        ("rxn_radius", ctypes.c_double),
+        ("seed", ctypes.c_uint64),
+        ("capacity", ctypes.c_uint64),
+        ("n_species", ctypes.c_uint32),
+    ]
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: run mcell_gb300.build (nvcc, sm_103a) first")
+        L = ctypes.CDLL(str(LIB_PATH))
+        vp = ctypes.c_void_p
+        L.mcg_create.argtypes = [ctypes.POINTER(McgConfig), ctypes.POINTER(vp)]
+        L.mcg_destroy.argtypes = [vp]
+        L.mcg_destroy.restype = None
+        L.mcg_last_error.argtypes = [vp]
+        L.mcg_last_error.restype = ctypes.c_char_p
+        for name in EXPORTS:
+            getattr(L, name)
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Engine:
+    """One GPU model: thin object over the C ABI (same calls a C++ host makes)."""
+
+    def __init__(self, precision, origin, partition_edge, nsub, rxn_radius, n_species, seed=1, capacity=0):
+        L = lib()
+        cfg = McgConfig()
+        cfg.precision = PRECISION[precision] if isinstance(precision, str) else int(precision)
+        for k in range(3):
+            cfg.partition_origin[k] = float(origin[k])
+        cfg.partition_edge = float(partition_edge)
+        cfg.subparts_per_edge = int(nsub)
+        cfg.rxn_radius = float(rxn_radius)
+        cfg.seed = int(seed)
+        cfg.capacity = int(capacity)
+        cfg.n_species = int(n_species)
+        h = ctypes.c_void_p()
+        rc = L.mcg_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != MCG_OK:
+            raise EngineError(rc, "mcg_create rejected the configuration")
+        self.h = h
+        self.n_species = int(n_species)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mcg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        if rc != MCG_OK:
+            msg = lib().mcg_last_error(self.h)
+            raise EngineError(rc, msg.decode() if msg else "")
+
+    def set_species(self, space_steps):
+        a = np.ascontiguousarray(space_steps, np.float64)
+        self._chk(lib().mcg_set_species(self.h, ctypes.c_uint32(len(a)), _p(a)))
+
+    def upload_mesh(self, verts, walls, wall_class):
+        v = np.ascontiguousarray(verts, np.float64)
+        w = np.ascontiguousarray(walls, np.uint32)
+        c = np.ascontiguousarray(wall_class, np.uint8)
+        self._chk(lib().mcg_upload_mesh(self.h, ctypes.c_uint32(len(v)), _p(v), ctypes.c_uint32(len(w)), _p(w), _p(c)))
+
+    def add_bimol_rxn(self, a, b, p, products=(-1, -1)):
+        pr = list(products) + [-1] * (2 - len(products))
+        self._chk(lib().mcg_add_bimol_rxn(self.h, ctypes.c_uint32(a), ctypes.c_uint32(b), ctypes.c_double(p),
+                                          ctypes.c_int32(pr[0]), ctypes.c_int32(pr[1])))
+
+    def add_unimol_rxn(self, a, k, products=(-1, -1)):
+        pr = list(products) + [-1] * (2 - len(products))
+        self._chk(lib().mcg_add_unimol_rxn(self.h, ctypes.c_uint32(a), ctypes.c_double(k), ctypes.c_int32(pr[0]),
+                                           ctypes.c_int32(pr[1])))
+
+    def add_molecules(self, pos, species):
+        p = np.ascontiguousarray(pos, np.float64)
+        s = np.ascontiguousarray(species, np.uint32)
+        self._chk(lib().mcg_add_molecules(self.h, ctypes.c_uint64(len(s)), _p(p), _p(s)))
+
+    def prepare(self):
+        self._chk(lib().mcg_prepare(self.h))
+
+    def step(self, n=1):
+        self._chk(lib().mcg_step(self.h, ctypes.c_uint32(n)))
+
+    def sync(self):
+        self._chk(lib().mcg_sync(self.h))
+
+    def counts(self):
+        out = np.zeros(self.n_species, np.uint64)
+        self._chk(lib().mcg_get_counts(self.h, _p(out)))
+        return out
+
+    def trajectory(self, n):
+        out = np.zeros((n, self.n_species), np.uint64)
+        self._chk(lib().mcg_get_count_trajectory(self.h, ctypes.c_uint32(n), _p(out)))
+        return out
+
+    def molecules(self, cap=None):
+        n = ctypes.c_uint64()
+        self._chk(lib().mcg_download_molecules(self.h, ctypes.c_uint64(0), None, None, None, ctypes.byref(n)))
+        m = n.value if cap is None else min(cap, n.value)
+        pos = np.zeros((m, 3))
+        sp = np.zeros(m, np.uint32)
+        ids = np.zeros(m, np.uint64)
+        self._chk(lib().mcg_download_molecules(self.h, ctypes.c_uint64(m), _p(pos), _p(sp), _p(ids), ctypes.byref(n)))
+        return pos, sp, ids
+
+    def stats(self):
+        it, ms, ln = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        self._chk(lib().mcg_get_stats(self.h, ctypes.byref(it), ctypes.byref(ms), ctypes.byref(ln)))
+        return it.value, ms.value, ln.value
+
+    def trace_cases(self, ids, disp, draws, r_rate_factor=None, t_steps=None):
+        ids = np.ascontiguousarray(ids, np.uint64)
+        n = len(ids)
+        disp = np.ascontiguousarray(disp, np.float64).reshape(n, 3)
+        draws = np.ascontiguousarray(draws, np.uint32).reshape(n, -1)
+        rrf = np.ascontiguousarray(np.ones(n) if r_rate_factor is None else r_rate_factor, np.float64)
+        tst = np.ascontiguousarray(np.ones(n) if t_steps is None else t_steps, np.float64)
+        out = np.zeros((n, TRACE_RESULT_SIZE))
+        self._chk(lib().mcg_trace_cases(self.h, ctypes.c_uint32(n), _p(ids), _p(disp), _p(draws),
+                                        ctypes.c_uint32(draws.shape[1]), _p(rrf), _p(tst), _p(out)))
+        return out
+
+    def wall_consts(self, nw):
+        out = np.zeros((nw, 14))
+        self._chk(lib().mcg_wall_consts(self.h, _p(out)))
+        return out
+
+    def walls_in_subparts(self, nsub3, cap=1 << 22):
+        counts = np.zeros(nsub3, np.uint32)
+        lst = np.zeros(cap, np.uint32)
+        tot = ctypes.c_uint64()
+        self._chk(lib().mcg_walls_in_subparts(self.h, _p(counts), _p(lst), ctypes.c_uint64(cap), ctypes.byref(tot)))
+        return counts, lst[:tot.value]

@@ -1,0 +1,268 @@
+// C ABI of the engine (declared in include/mcell_gb300.h).
+#include "../../include/mcell_gb300.h"
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mcg_engine.h"
+
+struct mcg_engine {
+  mcg_config cfg;
+  std::string err;
+  mcg::ChemHost chem;
+  bool species_set = false;
+  std::vector<double> verts;
+  std::vector<uint32_t> walls;
+  std::vector<uint8_t> wclass;
+  std::vector<double> pend_pos;
+  std::vector<uint32_t> pend_species;
+  uint64_t next_uid = 0;
+  mcg::DeviceEngine* dev = nullptr;
+};
+
+namespace mcg {
+int status_to_error(uint32_t status, std::string& err) {
+  if (status & (1u << 1)) {
+    err = "a molecule escaped the partition (enlarge the partition or enclose the model in a reflective box)";
+    return MCG_ERR_ESCAPE;
+  }
+  if (status & (1u << 0)) {
+    err = "capacity exceeded (molecules, products or proposals)";
+    return MCG_ERR_CAPACITY;
+  }
+  if (status & (1u << 2)) {
+    err = "a bounded device loop gave up (edge re-tries, wall bounces, reaction rounds or product chain)";
+    return MCG_ERR_WATCHDOG;
+  }
+  return MCG_OK;
+}
+}  // namespace mcg
+
+static int fail(mcg_engine* e, int code, const std::string& msg) {
+  if (e) e->err = msg;
+  return code;
+}
+
+static int prepare(mcg_engine* e) {
+  if (e->dev) return MCG_OK;
+  if (!e->species_set) return fail(e, MCG_ERR_ARG, "mcg_set_species must be called first");
+  if (e->wclass.empty() && !e->walls.empty()) return fail(e, MCG_ERR_ARG, "mesh without wall classes");
+  mcg::HostSetup hs;
+  std::string err;
+  if (mcg::compute_setup(e->cfg.partition_origin, e->cfg.partition_edge, e->cfg.subparts_per_edge, e->cfg.rxn_radius,
+                         (uint32_t)(e->verts.size() / 3), e->verts.data(), (uint32_t)(e->walls.size() / 3),
+                         e->walls.data(), hs, err))
+    return fail(e, MCG_ERR_ARG, err);
+  mcg::DeviceEngine* d = e->cfg.precision == MCG_PRECISION_FP64 ? mcg::make_engine_f64() : mcg::make_engine_f32();
+  uint64_t cap = e->cfg.capacity;
+  if (cap == 0) cap = std::max<uint64_t>(1024, e->pend_species.size() * 3 / 2);
+  int rc = d->init(hs, e->chem, e->wclass, e->cfg.seed, cap, err);
+  if (rc) {
+    delete d;
+    return fail(e, rc, err);
+  }
+  e->dev = d;
+  if (!e->pend_species.empty()) {
+    rc = d->add_molecules(e->pend_species.size(), e->pend_pos.data(), e->pend_species.data(), 0, err);
+    e->pend_pos.clear();
+    e->pend_species.clear();
+    if (rc) return fail(e, rc, err);
+  }
+  return MCG_OK;
+}
+
+extern "C" {
+
+int mcg_create(const mcg_config* cfg, mcg_engine** out) {
+  if (!cfg || !out) return MCG_ERR_ARG;
+  *out = nullptr;
+  if (cfg->precision != MCG_PRECISION_FP64 && cfg->precision != MCG_PRECISION_FP32) return MCG_ERR_ARG;
+  if (cfg->n_species == 0 || cfg->n_species > MCG_MAX_SPECIES) return MCG_ERR_ARG;
+  if (cfg->subparts_per_edge == 0 || cfg->subparts_per_edge > 300) return MCG_ERR_ARG;
+  if (!(cfg->partition_edge > 0) || !(cfg->rxn_radius > 0)) return MCG_ERR_ARG;
+  mcg_engine* e = new mcg_engine();
+  e->cfg = *cfg;
+  e->chem.nsp = cfg->n_species;
+  *out = e;
+  return MCG_OK;
+}
+
+void mcg_destroy(mcg_engine* e) {
+  if (!e) return;
+  delete e->dev;
+  delete e;
+}
+
+const char* mcg_last_error(const mcg_engine* e) { return e ? e->err.c_str() : "null engine"; }
+
+int mcg_set_species(mcg_engine* e, uint32_t n, const double* space_step) {
+  if (!e || !space_step) return MCG_ERR_ARG;
+  if (e->dev) return fail(e, MCG_ERR_ARG, "species must be set before the first step");
+  if (n != e->cfg.n_species) return fail(e, MCG_ERR_ARG, "species count differs from mcg_config.n_species");
+  for (uint32_t i = 0; i < n; i++) {
+    if (!(space_step[i] >= 0)) return fail(e, MCG_ERR_ARG, "space step must be >= 0");
+    e->chem.space_step[i] = space_step[i];
+  }
+  e->species_set = true;
+  return MCG_OK;
+}
+
+int mcg_upload_mesh(mcg_engine* e, uint32_t nv, const double* vertices, uint32_t nw, const uint32_t* walls,
+                    const uint8_t* wall_class) {
+  if (!e || (nv && !vertices) || (nw && (!walls || !wall_class))) return MCG_ERR_ARG;
+  if (e->dev) return fail(e, MCG_ERR_ARG, "the mesh must be uploaded before the first step (static geometry only)");
+  const uint32_t ns = e->cfg.n_species;
+  for (uint64_t k = 0; k < (uint64_t)nw * ns; k++)
+    if (wall_class[k] > 2) return fail(e, MCG_ERR_ARG, "wall class must be 0, 1 or 2");
+  e->verts.assign(vertices, vertices + 3 * (size_t)nv);
+  e->walls.assign(walls, walls + 3 * (size_t)nw);
+  e->wclass.assign(wall_class, wall_class + (size_t)nw * ns);
+  return MCG_OK;
+}
+
+int mcg_add_bimol_rxn(mcg_engine* e, uint32_t a, uint32_t b, double p, int32_t p0, int32_t p1) {
+  if (!e) return MCG_ERR_ARG;
+  const int ns = (int)e->cfg.n_species;
+  if (e->dev) return fail(e, MCG_ERR_ARG, "reactions must be added before the first step");
+  if (a >= (uint32_t)ns || b >= (uint32_t)ns || p0 >= ns || p1 >= ns || p0 < -1 || p1 < -1 || !(p >= 0))
+    return fail(e, MCG_ERR_ARG, "invalid bimolecular reaction");
+  if (e->chem.bimol_p[a][b] >= 0) return fail(e, MCG_ERR_UNSUPPORTED, "one reaction per reactant pair on the GPU path");
+  e->chem.bimol_p[a][b] = e->chem.bimol_p[b][a] = p;
+  e->chem.bimol_prod[a][b][0] = e->chem.bimol_prod[b][a][0] = p0;
+  e->chem.bimol_prod[a][b][1] = e->chem.bimol_prod[b][a][1] = p1;
+  return MCG_OK;
+}
+
+int mcg_add_unimol_rxn(mcg_engine* e, uint32_t a, double k, int32_t p0, int32_t p1) {
+  if (!e) return MCG_ERR_ARG;
+  const int ns = (int)e->cfg.n_species;
+  if (e->dev) return fail(e, MCG_ERR_ARG, "reactions must be added before the first step");
+  if (a >= (uint32_t)ns || p0 >= ns || p1 >= ns || p0 < -1 || p1 < -1 || !(k >= 0))
+    return fail(e, MCG_ERR_ARG, "invalid unimolecular reaction");
+  if (e->chem.unimol_k[a] >= 0) return fail(e, MCG_ERR_UNSUPPORTED, "one unimolecular reaction per species");
+  e->chem.unimol_k[a] = k;
+  e->chem.uni_prod[a][0] = p0;
+  e->chem.uni_prod[a][1] = p1;
+  return MCG_OK;
+}
+
+int mcg_add_molecules(mcg_engine* e, uint64_t n, const double* pos, const uint32_t* species) {
+  if (!e || (n && (!pos || !species))) return MCG_ERR_ARG;
+  for (uint64_t i = 0; i < n; i++)
+    if (species[i] >= e->cfg.n_species) return fail(e, MCG_ERR_ARG, "species index out of range");
+  if (!e->dev) {
+    e->pend_pos.insert(e->pend_pos.end(), pos, pos + 3 * n);
+    e->pend_species.insert(e->pend_species.end(), species, species + n);
+    e->next_uid += n;
+    return MCG_OK;
+  }
+  std::string err;
+  int rc = e->dev->add_molecules(n, pos, species, e->next_uid, err);
+  if (rc) return fail(e, rc, err);
+  e->next_uid += n;
+  return MCG_OK;
+}
+
+int mcg_prepare(mcg_engine* e) {
+  if (!e) return MCG_ERR_ARG;
+  return prepare(e);
+}
+
+int mcg_step(mcg_engine* e, uint32_t n) {
+  if (!e) return MCG_ERR_ARG;
+  int rc = prepare(e);
+  if (rc) return rc;
+  std::string err;
+  rc = e->dev->step(n, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
+int mcg_sync(mcg_engine* e) {
+  if (!e) return MCG_ERR_ARG;
+  if (!e->dev) return MCG_OK;
+  std::string err;
+  int rc = e->dev->sync(err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
+int mcg_get_counts(mcg_engine* e, uint64_t* counts) {
+  if (!e || !counts) return MCG_ERR_ARG;
+  int rc = prepare(e);
+  if (rc) return rc;
+  std::string err;
+  rc = e->dev->counts(counts, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
+int mcg_get_count_trajectory(mcg_engine* e, uint32_t n, uint64_t* counts) {
+  if (!e || !counts || !e->dev) return MCG_ERR_ARG;
+  std::string err;
+  int rc = e->dev->trajectory(n, counts, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
+int mcg_download_molecules(mcg_engine* e, uint64_t cap, double* pos, uint32_t* species, uint64_t* ids,
+                           uint64_t* n_out) {
+  if (!e || !n_out) return MCG_ERR_ARG;
+  int rc = prepare(e);
+  if (rc) return rc;
+  std::string err;
+  rc = e->dev->download(cap, pos, species, ids, n_out, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
+int mcg_get_stats(mcg_engine* e, uint64_t* iterations, uint64_t* mol_steps, uint64_t* launches) {
+  if (!e) return MCG_ERR_ARG;
+  if (!e->dev) {
+    if (iterations) *iterations = 0;
+    if (mol_steps) *mol_steps = 0;
+    if (launches) *launches = 0;
+    return MCG_OK;
+  }
+  e->dev->stats(iterations, mol_steps, launches);
+  return MCG_OK;
+}
+
+int mcg_trace_cases(mcg_engine* e, uint32_t n, const uint64_t* ids, const double* disp, const uint32_t* draws,
+                    uint32_t draws_per_case, const double* rrf, const double* tst, double* out) {
+  if (!e || (n && (!ids || !disp || !rrf || !tst || !out))) return MCG_ERR_ARG;
+  int rc = prepare(e);
+  if (rc) return rc;
+  std::string err;
+  rc = e->dev->trace(n, ids, disp, draws, draws_per_case, rrf, tst, out, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
+int mcg_wall_consts(mcg_engine* e, double* out) {
+  if (!e || !out) return MCG_ERR_ARG;
+  mcg::HostSetup hs;
+  std::string err;
+  if (mcg::compute_setup(e->cfg.partition_origin, e->cfg.partition_edge, e->cfg.subparts_per_edge, e->cfg.rxn_radius,
+                         (uint32_t)(e->verts.size() / 3), e->verts.data(), (uint32_t)(e->walls.size() / 3),
+                         e->walls.data(), hs, err))
+    return fail(e, MCG_ERR_ARG, err);
+  for (uint32_t w = 0; w < hs.nw; w++) {
+    std::memcpy(out + 14 * (size_t)w, &hs.wall[24 * (size_t)w], 13 * sizeof(double));
+    out[14 * (size_t)w + 13] = 0;
+  }
+  return MCG_OK;
+}
+
+int mcg_walls_in_subparts(mcg_engine* e, uint32_t* counts, uint32_t* list, uint64_t cap, uint64_t* total) {
+  if (!e || !counts || !total) return MCG_ERR_ARG;
+  mcg::HostSetup hs;
+  std::string err;
+  if (mcg::compute_setup(e->cfg.partition_origin, e->cfg.partition_edge, e->cfg.subparts_per_edge, e->cfg.rxn_radius,
+                         (uint32_t)(e->verts.size() / 3), e->verts.data(), (uint32_t)(e->walls.size() / 3),
+                         e->walls.data(), hs, err))
+    return fail(e, MCG_ERR_ARG, err);
+  const size_t n3 = hs.wsp_off.size() - 1;
+  for (size_t s = 0; s < n3; s++) counts[s] = hs.wsp_off[s + 1] - hs.wsp_off[s];
+  *total = hs.wsp_list.size();
+  if (list)
+    for (uint64_t k = 0; k < std::min<uint64_t>(cap, hs.wsp_list.size()); k++) list[k] = hs.wsp_list[k];
+  return MCG_OK;
+}
+
+}  // extern "C"

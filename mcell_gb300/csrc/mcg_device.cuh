@@ -1,0 +1,1129 @@
+// Device side of the volume-molecule diffuse-react step.
+//
+// One thread diffuses one molecule for one time step. The per-molecule work
+// restates MCell4's DiffuseReactEvent::diffuse_vol_molecule / ray_trace_vol
+// (src4/diffuse_react_event.cpp:367-780) and the routines they call:
+//   collect_crossed_subparts / collect_neighboring_subparts  collision_utils_subparts.inl:38-300
+//   get_displacement_up_to_partition_boundary                 collision_utils.inl:48-114
+//   get_closest_wall_collision / collide_wall / jump_away_line collision_utils.inl:568-914
+//   collide_mol                                               collision_utils.inl:464-515
+//   reflect_from_wall                                         collision_utils.inl:1711-1747
+//   cross_transparent_wall (non-compartment branch)           diffuse_react_event.cpp:3062-3094
+//   sort_collisions_by_time                                   diffuse_react_event.cpp:341-364
+//   exact_disk                                                exact_disk_utils.inl:840-1145
+//   test_bimolecular / test_intersect / time_of_unimol         rxn_utils.inl:336-414, :593-626, :721-735
+// with the same operation order, so the fp64 instantiation (built with
+// -fmad=false) reproduces the reference's wall hits, subpartitions and reaction
+// decisions exactly for identical inputs.
+//
+// What differs from the reference is the data layout and the parallel
+// schedule: molecules are SoA records sorted by (subpartition, species) at the
+// start of each iteration, partners are read from those sorted ranges (their
+// start-of-iteration positions) instead of per-subpartition hash sets, walls
+// of a subpartition are a CSR list, and reactions are claimed with atomics and
+// resolved deterministically (see mcg_kernels.cuh).
+#pragma once
+
+#include "mcg_math.cuh"
+
+namespace mcg {
+
+constexpr int MAXSP = 16;
+constexpr int MAXC = 16;        // vol-vol collision candidates kept per ray trace (earliest first)
+constexpr int MAXSET = 48;      // subpartitions collected per ray trace for partner tests
+constexpr int MAX_REDO = 256;   // edge/vertex re-tries in one get_closest_wall_collision
+constexpr int MAX_BOUNCES = 4096;
+constexpr uint32_t NONE = 0xFFFFFFFFu;
+
+// device status bits (OR-ed into a status word; the host maps them to MCG_ERR_*)
+constexpr uint32_t ST_CAPACITY = 1u << 0;
+constexpr uint32_t ST_ESCAPE = 1u << 1;
+constexpr uint32_t ST_WATCHDOG = 1u << 2;
+constexpr uint32_t ST_COLL_OVERFLOW = 1u << 3;   // more than MAXC candidates (earliest kept)
+constexpr uint32_t ST_SET_OVERFLOW = 1u << 4;    // more than MAXSET subpartitions
+
+// molecule meta word (w lane of the position record)
+constexpr uint32_t META_SPECIES_MASK = 0xFFu;
+constexpr uint32_t META_SCHEDULE_UNIMOL = 1u << 8;  // MOLECULE_FLAG_SCHEDULE_UNIMOL_RXN
+
+template <typename T>
+struct Eps;
+template <>
+struct Eps<double> {
+  static constexpr double pos = 1e-12;       // POS_EPS (libbng; MCell3 EPS_C)
+  static constexpr double pos_sqrt = 1e-6;   // POS_SQRT_EPS
+  static constexpr double stime = 1e-12;     // STIME_EPS
+};
+template <>
+struct Eps<float> {
+  static constexpr float pos = 1e-6f;
+  static constexpr float pos_sqrt = 1e-3f;
+  static constexpr float stime = 1e-6f;
+};
+constexpr double EPS = 1e-12;  // time EPS (libbng EPS)
+constexpr double TIME_FOREVER = 1e20;
+constexpr double GIGANTIC = 1e140;
+constexpr double MY_PI = 3.14159265358979323846;
+
+template <typename T>
+struct alignas(4 * sizeof(T)) P4 {
+  T x, y, z, w;
+};
+
+__device__ __forceinline__ uint32_t meta_of(const P4<float>& p) { return __float_as_uint(p.w); }
+__device__ __forceinline__ uint32_t meta_of(const P4<double>& p) {
+  return (uint32_t)__double_as_longlong(p.w);
+}
+__device__ __forceinline__ void set_meta(P4<float>& p, uint32_t m) { p.w = __uint_as_float(m); }
+__device__ __forceinline__ void set_meta(P4<double>& p, uint32_t m) {
+  p.w = __longlong_as_double((long long)m);
+}
+
+// species and reaction tables (read-only on the device)
+struct Chem {
+  int nsp;
+  int nuni;
+  double space_step[MAXSP];
+  double unimol_k[MAXSP];       // k_tot per time step, < 0: no unimolecular reaction
+  int uni_prod[MAXSP][2];
+  double bimol_p[MAXSP][MAXSP];  // max_fixed_p, < 0: no reaction
+  int bimol_prod[MAXSP][MAXSP][2];
+  uint32_t partners[MAXSP];      // bit b: species b reacts with this species
+  uint32_t can_volwall[MAXSP];   // has a non-reflective wall class somewhere
+};
+
+template <typename T>
+struct WallFace {
+  V3<T> u, v, v0, v1, v2;
+  T uv1u, uv2u, uv2v;
+};
+
+template <typename T>
+struct Geo {
+  V3<T> origin, opposite;
+  T part_edge, sp_edge, sp_rcp, R;
+  int nsub, nsub2, nsp;
+  const P4<T>* wrej;          // normal xyz, distance to origin
+  const WallFace<T>* wface;
+  const uint32_t* wsp_off;    // CSR: walls per subpartition (ascending wall index)
+  const uint32_t* wsp_list;
+  const uint8_t* wall_class;  // [wall * nsp + species]: 0 reflect, 1 transparent, 2 absorptive
+  const Chem* chem;
+};
+
+// molecules at the start of the iteration, sorted by key = subpart * nsp + species
+template <typename T>
+struct Cells {
+  const P4<T>* pos;
+  const uint64_t* uid;
+  const uint32_t* start;  // [nkeys + 1]
+  const uint8_t* dead;    // optional: partners already used up this iteration
+};
+
+template <typename T>
+struct TraceOut {
+  int status;  // 0 finished, 1 reacted with a partner, 2 absorbed, 3 error
+  V3<T> pos;
+  uint32_t subpart;
+  uint32_t partner;  // index into Cells
+  double t_abs;      // time of the reaction / absorption
+  V3<T> rxn_pos;
+  double elapsed, t_steps;
+  uint32_t err;
+};
+
+// ------------------------------------------------------------------ draws
+
+// production: Philox stream of the molecule-step
+struct PhiloxDraws {
+  Philox ph;
+  __device__ __forceinline__ uint32_t u32() { return ph.next_u32(); }
+  __device__ __forceinline__ bool overrun() const { return false; }
+};
+
+// harness: injected 32-bit draws
+struct InjectedDraws {
+  const uint32_t* d;
+  uint32_t n, used;
+  bool over;
+  __device__ __forceinline__ uint32_t u32() {
+    if (used >= n) {
+      over = true;
+      return 0;
+    }
+    return d[used++];
+  }
+  __device__ __forceinline__ bool overrun() const { return over; }
+};
+
+// rng_dbl: 32-bit draw scaled by 2^-32 (isaac64_dbl32)
+template <class D>
+__device__ __forceinline__ double draw_dbl(D& d) {
+  return (double)d.u32() * (1.0 / 4294967296.0);
+}
+
+// events recorded by the harness (no-op in production)
+struct NoEvents {
+  __device__ __forceinline__ void put(int, uint64_t, int, double, double, double, double, double) {}
+};
+struct EventLog {
+  double* out;  // MCG_TRACE_RESULT_SIZE doubles
+  __device__ void put(int kind, uint64_t index, int side, double t_rel, double t_abs, double x, double y,
+                      double z) {
+    int n = (int)out[6];
+    if (n < 32) {
+      double* e = out + 9 + n * 8;
+      e[0] = kind;
+      e[1] = (double)index;
+      e[2] = side;
+      e[3] = t_rel;
+      e[4] = t_abs;
+      e[5] = x;
+      e[6] = y;
+      e[7] = z;
+    }
+    out[6] = n + 1;
+  }
+};
+
+// ------------------------------------------------------------------ partition helpers
+
+template <typename T>
+__device__ __forceinline__ bool in_partition(const Geo<T>& g, V3<T> p) {
+  return p.x >= g.origin.x && p.y >= g.origin.y && p.z >= g.origin.z && p.x < g.opposite.x &&
+         p.y < g.opposite.y && p.z < g.opposite.z;
+}
+// subpartition 3-D index (Partition::get_subpart_3d_indices). Clamped to the grid:
+// positions a rounding step outside the partition stay addressable.
+template <typename T>
+__device__ __forceinline__ void sub3(const Geo<T>& g, V3<T> p, int& x, int& y, int& z) {
+  V3<T> r = p - g.origin;
+  x = min(max((int)(r.x * g.sp_rcp), 0), g.nsub - 1);
+  y = min(max((int)(r.y * g.sp_rcp), 0), g.nsub - 1);
+  z = min(max((int)(r.z * g.sp_rcp), 0), g.nsub - 1);
+}
+template <typename T>
+__device__ __forceinline__ uint32_t sub_of3(const Geo<T>& g, int x, int y, int z) {
+  return (uint32_t)(x + y * g.nsub + z * g.nsub2);
+}
+template <typename T>
+__device__ __forceinline__ uint32_t subpart_of(const Geo<T>& g, V3<T> p) {
+  int x, y, z;
+  sub3(g, p, x, y, z);
+  return sub_of3(g, x, y, z);
+}
+template <typename T>
+__device__ __forceinline__ V3<T> guard_zero(V3<T> a) {
+  const T tiny = (T)1.17549435082228750797e-38;  // FLT_MIN, as guard_zero_div uses
+  if (a.x == 0) a.x = tiny;
+  if (a.y == 0) a.y = tiny;
+  if (a.z == 0) a.z = tiny;
+  return a;
+}
+template <typename T>
+__device__ __forceinline__ bool distinguishable(T a, T b, T eps) {
+  T c = tabs(a - b);
+  a = tabs(a);
+  if (a < 1) a = 1;
+  b = tabs(b);
+  if (b < a)
+    eps *= a;
+  else
+    eps *= b;
+  return c > eps;
+}
+template <typename T>
+__device__ __forceinline__ T abs_max_2vec(V3<T> a, V3<T> b) {
+  return tmax(tmax(tmax(tabs(a.x), tabs(b.x)), tmax(tabs(a.y), tabs(b.y))), tmax(tabs(a.z), tabs(b.z)));
+}
+
+// get_displacement_up_to_partition_boundary (collision_utils.inl:48-114)
+template <typename T>
+__device__ V3<T> disp_up_to_partition_boundary(const Geo<T>& g, V3<T> pos, V3<T> disp) {
+  V3<T> nz = guard_zero(disp);
+  V3<T> dir = v3<T>(nz.x > 0 ? 1 : 0, nz.y > 0 ? 1 : 0, nz.z > 0 ? 1 : 0);
+  V3<T> edges = g.origin + scale(dir, g.part_edge);
+  V3<T> diff = edges - pos;
+  T hit = 1;
+  if (tabs(diff.x) < Eps<T>::pos || tabs(diff.y) < Eps<T>::pos || tabs(diff.z) < Eps<T>::pos) {
+    return v3<T>(0, 0, 0);
+  }
+  V3<T> t = cdiv(diff, nz);
+  if (t.x >= 0 && t.x < t.y && t.x <= t.z)
+    hit = t.x;
+  else if (t.y >= 0 && t.y <= t.z)
+    hit = t.y;
+  else if (t.z >= 0)
+    hit = t.z;
+  return scale(disp, hit - Eps<T>::stime);
+}
+
+// ------------------------------------------------------------------ subpartition walk
+
+// Visits the subpartitions the segment pos -> pos+disp crosses, in order
+// (collect_crossed_subparts, collision_utils_subparts.inl:127-300). The walk is
+// re-entrant so the wall search can stop early without storing the list.
+template <typename T>
+struct Walk {
+  V3<T> cp, disp, rcp;
+  int cx, cy, cz, ax, ay, az, dx, dy, dz;
+  uint32_t cur, dest;
+  int steps;
+  bool done;
+
+  __device__ void start(const Geo<T>& g, V3<T> pos, uint32_t start_sp, V3<T> d) {
+    disp = d;
+    V3<T> dest_p = pos + d;
+    V3<T> nz = guard_zero(d);
+    dx = nz.x > 0;
+    dy = nz.y > 0;
+    dz = nz.z > 0;
+    cx = (int)(start_sp % g.nsub);
+    cy = (int)((start_sp / g.nsub) % g.nsub);
+    cz = (int)((start_sp / g.nsub2) % g.nsub);
+    int ex, ey, ez;
+    sub3(g, dest_p, ex, ey, ez);
+    dest = sub_of3(g, ex, ey, ez);
+    cur = start_sp;
+    cp = pos;
+    ax = dx ? 1 : -1;
+    ay = dy ? 1 : -1;
+    az = dz ? 1 : -1;
+    rcp = cdiv(v3<T>(1, 1, 1), nz);
+    done = (cur == dest);
+    steps = 0;
+  }
+  // advances to the next crossed subpartition; false when the walk is over
+  __device__ bool next(const Geo<T>& g) {
+    if (done) return false;
+    V3<T> len = v3<T>(g.sp_edge, g.sp_edge, g.sp_edge);
+    V3<T> edges = (g.origin + cmul(v3<T>((T)cx, (T)cy, (T)cz), len)) + cmul(v3<T>((T)dx, (T)dy, (T)dz), len);
+    V3<T> diff = edges - cp;
+    V3<T> t = cmul(diff, rcp);
+    if (t.x < t.y && t.x <= t.z) {
+      cp = cp + scale(disp, t.x);
+      cx += ax;
+      if (cx < 0 || cx >= g.nsub) {
+        done = true;
+        return false;
+      }
+    } else if (t.y <= t.z) {
+      cp = cp + scale(disp, t.y);
+      cy += ay;
+      if (cy < 0 || cy >= g.nsub) {
+        done = true;
+        return false;
+      }
+    } else {
+      cp = cp + scale(disp, t.z);
+      cz += az;
+      if (cz < 0 || cz >= g.nsub) {
+        done = true;
+        return false;
+      }
+    }
+    cur = sub_of3(g, cx, cy, cz);
+    if (cur == dest || ++steps > 3 * g.nsub) done = true;
+    return true;
+  }
+};
+
+struct SubSet {
+  uint32_t s[MAXSET];
+  int n;
+  uint32_t n3;  // number of subpartitions (indices are checked against it)
+  bool overflow;
+  __device__ __forceinline__ void insert(uint32_t v) {
+    if (v >= n3) return;
+    for (int i = 0; i < n; i++)
+      if (s[i] == v) return;
+    if (n < MAXSET)
+      s[n++] = v;
+    else
+      overflow = true;
+  }
+};
+
+// collect_neighboring_subparts (collision_utils_subparts.inl:38-122)
+template <typename T>
+__device__ void collect_neighbors(const Geo<T>& g, V3<T> pos, int ix, int iy, int iz, T r, SubSet& st) {
+  T part_len = g.part_edge;
+  V3<T> rel = pos - g.origin;
+  V3<T> plus = rel + v3<T>(r, r, r);
+  V3<T> minus = rel - v3<T>(r, r, r);
+  V3<T> b = cmul(v3<T>((T)ix, (T)iy, (T)iz), v3<T>(g.sp_edge, g.sp_edge, g.sp_edge));
+  int xd = 0, yd = 0, zd = 0;
+  if (minus.x < b.x && minus.x > (T)0.0) {
+    st.insert(sub_of3(g, ix - 1, iy, iz));
+    xd = -1;
+  } else if (plus.x > b.x + g.sp_edge && plus.x < part_len) {
+    st.insert(sub_of3(g, ix + 1, iy, iz));
+    xd = 1;
+  }
+  if (minus.y < b.y && minus.y > (T)0.0) {
+    st.insert(sub_of3(g, ix, iy - 1, iz));
+    yd = -1;
+  } else if (plus.y > b.y + g.sp_edge && plus.y < part_len) {
+    st.insert(sub_of3(g, ix, iy + 1, iz));
+    yd = 1;
+  }
+  if (minus.z < b.z && minus.z > (T)0.0) {
+    st.insert(sub_of3(g, ix, iy, iz - 1));
+    zd = -1;
+  } else if (plus.z > b.z + g.sp_edge && plus.z < part_len) {
+    st.insert(sub_of3(g, ix, iy, iz + 1));
+    zd = 1;
+  }
+  if (xd && yd) st.insert(sub_of3(g, ix + xd, iy + yd, iz));
+  if (xd && zd) st.insert(sub_of3(g, ix + xd, iy, iz + zd));
+  if (yd && zd) st.insert(sub_of3(g, ix, iy + yd, iz + zd));
+  if (xd && yd && zd) st.insert(sub_of3(g, ix + xd, iy + yd, iz + zd));
+}
+
+// subpartitions whose occupants can collide with the segment: crossed ones and
+// their neighbours within R*sqrt(2) (the molecule half of collect_crossed_subparts)
+template <typename T>
+__device__ void collect_for_molecules(const Geo<T>& g, V3<T> pos, uint32_t sp, V3<T> disp, SubSet& st) {
+  st.n = 0;
+  st.n3 = (uint32_t)g.nsub2 * (uint32_t)g.nsub;
+  const T rn = g.R * (T)1.41421356238;  // POS_SQRT2
+  st.insert(sp);
+  int sx = (int)(sp % g.nsub), sy = (int)((sp / g.nsub) % g.nsub), sz = (int)((sp / g.nsub2) % g.nsub);
+  collect_neighbors(g, pos, sx, sy, sz, rn, st);
+  Walk<T> w;
+  w.start(g, pos, sp, disp);
+  while (w.next(g)) {
+    st.insert(w.cur);
+    collect_neighbors(g, w.cp, w.cx, w.cy, w.cz, rn, st);
+  }
+  V3<T> dest = pos + disp;
+  int ex, ey, ez;
+  sub3(g, dest, ex, ey, ez);
+  collect_neighbors(g, dest, ex, ey, ez, rn, st);
+}
+
+// ------------------------------------------------------------------ walls
+
+enum : int { CT_MISS = 0, CT_REDO = 1, CT_FRONT = 2, CT_BACK = 3 };
+
+// jump_away_line (collision_utils.inl:568-603)
+template <typename T, class D>
+__device__ void jump_away_line(V3<T> p, T k, V3<T> A, V3<T> B, V3<T> n, D& draws, V3<T>& v) {
+  V3<T> e = B - A;
+  T elen2 = dot(e, e);
+  T le_1 = (T)1.0 / sqrt(elen2);
+  e = cmul(e, v3<T>(le_1, le_1, le_1));
+  V3<T> f;
+  f.x = n.y * e.z - n.z * e.y;
+  f.y = n.z * e.x - n.x * e.z;
+  f.z = n.x * e.y - n.y * e.x;
+  T tiny;
+  if (sizeof(T) == 8) {
+    tiny = Eps<T>::pos * (abs_max_2vec(p, v) + (T)1.0) / (k * tmax(tmax(tabs(f.x), tabs(f.y)), tabs(f.z)));
+  } else {
+    tiny = Eps<T>::pos_sqrt;  // fp32 branch of the reference
+  }
+  if ((draws.u32() & 1) == 0) tiny = -tiny;
+  v.x -= tiny * f.x;
+  v.y -= tiny * f.y;
+  v.z -= tiny * f.z;
+}
+
+// collide_wall (collision_utils.inl:629-812)
+template <typename T, class D>
+__device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V3<T>& move, T& ct, V3<T>& cpos) {
+  const P4<T> rj = g.wrej[wi];
+  V3<T> normal = v3<T>(rj.x, rj.y, rj.z);
+  T dp = dot(normal, pos);
+  T dv = dot(normal, move);
+  T dd = dp - rj.w;
+  T d_eps;
+  if (dd > 0) {
+    d_eps = Eps<T>::pos;
+    if (dd < d_eps) d_eps = (T)0.5 * dd;
+    if (dd + dv > d_eps) return CT_MISS;
+  } else {
+    d_eps = -Eps<T>::pos;
+    if (dd > d_eps) d_eps = (T)0.5 * dd;
+    if (dd < 0 && dd + dv < d_eps) return CT_MISS;
+  }
+  T a;
+  if (dd == 0) {
+    if (dv != 0) return CT_MISS;
+    a = (abs_max_2vec(pos, move) + (T)1.0) * Eps<T>::pos;
+    if ((draws.u32() & 1) == 0) a = -a;
+    move = move - cmul(v3<T>(a, a, a), normal);
+    return CT_REDO;
+  }
+  a = (T)1.0 / dv;
+  a *= -dd;
+  ct = a;
+  cpos = pos + scale(move, a);
+  const WallFace<T>& w = g.wface[wi];
+  V3<T> local = cpos - w.v0;
+  T b = dot(local, w.u);
+  T c = dot(local, w.v);
+  T f;
+  if (w.uv2v < 0) {
+    c = -c;
+    f = -w.uv2v;
+  } else {
+    f = w.uv2v;
+  }
+  if (c > 0) {
+    T gg = b * f;
+    T h = c * w.uv2u;
+    if (gg > h) {
+      if (c * w.uv1u + gg < h + w.uv1u * w.uv2v) {
+        return dv > 0 ? CT_BACK : CT_FRONT;
+      } else if (!distinguishable<T>(c * w.uv1u + gg, h + w.uv1u * w.uv2v, Eps<T>::pos)) {
+        jump_away_line(pos, a, w.v1, w.v2, normal, draws, move);
+        return CT_REDO;
+      }
+      return CT_MISS;
+    } else if (!distinguishable<T>(gg, h, Eps<T>::pos)) {
+      jump_away_line(pos, a, w.v2, w.v0, normal, draws, move);
+      return CT_REDO;
+    }
+    return CT_MISS;
+  } else if (!distinguishable<T>(c, (T)0.0, Eps<T>::pos)) {
+    jump_away_line(pos, a, w.v0, w.v1, normal, draws, move);
+    return CT_REDO;
+  }
+  return CT_MISS;
+}
+
+template <typename T>
+struct WallHit {
+  int type;
+  T t;
+  V3<T> pos;
+  uint32_t wall;
+};
+
+// get_closest_wall_collision (collision_utils.inl:819-914). In fp32 the reference
+// also keeps hits that land in another subpartition as tentative ones (:885-893).
+template <typename T, class D>
+__device__ bool closest_wall_collision(const Geo<T>& g, V3<T> pos, uint32_t sp, uint32_t last_hit, D& draws,
+                                       V3<T>& disp, WallHit<T>& closest, WallHit<T>& tentative,
+                                       uint32_t& err) {
+  int redo = 0;
+restart:
+  bool found = false;
+  T closest_t = (T)1e20;
+  const uint32_t b = g.wsp_off[sp], e = g.wsp_off[sp + 1];
+  for (uint32_t k = b; k < e; k++) {
+    uint32_t wi = g.wsp_list[k];
+    if (wi == last_hit) continue;
+    T t;
+    V3<T> cp;
+    int ct = collide_wall(g, pos, wi, draws, disp, t, cp);
+    if (ct == CT_REDO) {
+      if (++redo > MAX_REDO || draws.overrun()) {
+        err |= ST_WATCHDOG;
+        return false;
+      }
+      goto restart;
+    } else if (ct != CT_MISS) {
+      if (subpart_of(g, cp) != sp) {
+        if (sizeof(T) == 4 && t < tentative.t) {
+          tentative.type = ct;
+          tentative.t = t;
+          tentative.pos = cp;
+          tentative.wall = wi;
+        }
+        continue;
+      }
+      if (t < closest_t) {
+        found = true;
+        closest_t = t;
+        closest.type = ct;
+        closest.t = t;
+        closest.pos = cp;
+        closest.wall = wi;
+      }
+    }
+  }
+  return found;
+}
+
+// ------------------------------------------------------------------ collisions with molecules
+
+template <typename T>
+struct VV {
+  T t;
+  uint32_t idx;
+  uint64_t uid;
+  V3<T> pos;
+  double p;
+};
+
+struct CollList;  // fwd
+
+template <typename T>
+struct Colls {
+  VV<T> c[MAXC];
+  int n;
+  bool overflow;
+  // sort_collisions_by_time order: time ascending, equal times by id descending
+  __device__ __forceinline__ static bool before(const VV<T>& a, const VV<T>& b) {
+    if (a.t < b.t) return true;
+    if (a.t > b.t) return false;
+    return a.uid > b.uid;
+  }
+  __device__ void insert(const VV<T>& x) {
+    int i = n;
+    if (n == MAXC) {
+      overflow = true;
+      if (!before(x, c[MAXC - 1])) return;
+      i = MAXC - 1;
+    } else {
+      n++;
+    }
+    while (i > 0 && before(x, c[i - 1])) {
+      c[i] = c[i - 1];
+      i--;
+    }
+    c[i] = x;
+  }
+};
+
+// collide_mol (collision_utils.inl:464-515) against every reacting occupant of the
+// collected subpartitions
+template <typename T>
+__device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos, int species,
+                                       V3<T> disp, const SubSet& st, Colls<T>& out) {
+  const Chem& ch = *g.chem;
+  const uint32_t pmask = ch.partners[species];
+  const T movelen2 = dot(disp, disp);
+  const T sigma2 = g.R * g.R;
+  for (int i = 0; i < st.n; i++) {
+    uint32_t m = pmask;
+    while (m) {
+      int b = __ffs(m) - 1;
+      m &= m - 1;
+      uint32_t key = st.s[i] * (uint32_t)g.nsp + (uint32_t)b;
+      uint32_t j0 = __ldg(cells.start + key), j1 = __ldg(cells.start + key + 1);
+      for (uint32_t j = j0; j < j1; j++) {
+        P4<T> q = cells.pos[j];
+        V3<T> dir = v3<T>(q.x, q.y, q.z) - pos;
+        T d = dot(dir, disp);
+        if (d < 0) continue;
+        if (d > movelen2) continue;
+        T dirlen2 = dot(dir, dir);
+        if (movelen2 * dirlen2 - d * d > movelen2 * sigma2) continue;
+        if (j == self) continue;
+        if (cells.dead && cells.dead[j] == 2) continue;
+        VV<T> c;
+        c.t = d / movelen2;
+        c.pos = pos + scale(disp, c.t);
+        c.idx = j;
+        c.uid = cells.uid[j];
+        c.p = ch.bimol_p[species][b];
+        out.insert(c);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ exact disk
+
+// exd_zetize (exact_disk_utils.inl:54-80)
+template <typename T>
+__device__ T zetize(T y, T x) {
+  if (y >= 0) {
+    if (x >= 0) {
+      if (x < y) return 1 - (T)0.5 * x / y;
+      return (T)0.5 * y / x;
+    }
+    if (-x < y) return 1 - (T)0.5 * x / y;
+    return 2 + (T)0.5 * y / x;
+  }
+  if (x <= 0) {
+    if (y < x) return 3 - (T)0.5 * x / y;
+    return 2 + (T)0.5 * y / x;
+  }
+  if (x < -y) return 3 - (T)0.5 * x / y;
+  return 4 + (T)0.5 * y / x;
+}
+
+template <typename T>
+struct ExV {
+  T u, v, r2, zeta;
+};
+
+constexpr int MAX_DISK_EDGES = 8;
+
+// visible part of the disk when several wall chords occlude it: integrate
+// r(theta)^2 / 2 between consecutive critical angles (chord ends and crossings)
+template <typename T>
+__device__ T sweep_area(const ExV<T>* pa, const ExV<T>* pb, int n, T R2) {
+  T ang[2 * MAX_DISK_EDGES + MAX_DISK_EDGES * (MAX_DISK_EDGES - 1) / 2];
+  int na = 0;
+  for (int i = 0; i < n; i++) {
+    ang[na++] = atan2(pa[i].v, pa[i].u);
+    ang[na++] = atan2(pb[i].v, pb[i].u);
+  }
+  for (int i = 0; i < n; i++) {
+    for (int j = i + 1; j < n; j++) {
+      T d1u = pb[i].u - pa[i].u, d1v = pb[i].v - pa[i].v;
+      T d2u = pb[j].u - pa[j].u, d2v = pb[j].v - pa[j].v;
+      T den = d1u * d2v - d1v * d2u;
+      if (den == 0) continue;
+      T wu = pa[j].u - pa[i].u, wv = pa[j].v - pa[i].v;
+      T t = (wu * d2v - wv * d2u) / den;
+      T s = (wu * d1v - wv * d1u) / den;
+      if (t > 0 && t < 1 && s > 0 && s < 1) ang[na++] = atan2(pa[i].v + t * d1v, pa[i].u + t * d1u);
+    }
+  }
+  for (int i = 1; i < na; i++) {
+    T x = ang[i];
+    int j = i - 1;
+    while (j >= 0 && ang[j] > x) {
+      ang[j + 1] = ang[j];
+      j--;
+    }
+    ang[j + 1] = x;
+  }
+  T area = 0;
+  const T R = sqrt(R2);
+  for (int k = 0; k < na; k++) {
+    T a0 = ang[k];
+    T a1 = (k + 1 < na) ? ang[k + 1] : ang[0] + (T)(2 * MY_PI);
+    if (a1 - a0 <= 0) continue;
+    T am = (T)0.5 * (a0 + a1);
+    T cu = cos(am), cv = sin(am);
+    int best = -1;
+    T best_r = R;
+    for (int i = 0; i < n; i++) {
+      T du = pb[i].u - pa[i].u, dv = pb[i].v - pa[i].v;
+      T den = cu * dv - cv * du;
+      if (den == 0) continue;
+      T r = (pa[i].u * dv - pa[i].v * du) / den;
+      T s = (pa[i].u * cv - pa[i].v * cu) / den;
+      if (r > 0 && s >= 0 && s <= 1 && r < best_r) {
+        best_r = r;
+        best = i;
+      }
+    }
+    if (best < 0) {
+      area += (T)0.5 * R2 * (a1 - a0);
+    } else {
+      T du = pb[best].u - pa[best].u, dv = pb[best].v - pa[best].v;
+      T num = pa[best].u * dv - pa[best].v * du;
+      T r0 = num / (cos(a0) * dv - sin(a0) * du);
+      T r1 = num / (cos(a1) * dv - sin(a1) * du);
+      area += (T)0.5 * r0 * r1 * sin(a1 - a0);
+    }
+  }
+  return area;
+}
+
+// exact_disk (exact_disk_utils.inl:840-1145, use_expanded_list): fraction of the
+// interaction disk around the collision point not occluded by walls, < 0 if a wall
+// separates the molecules
+template <typename T>
+__device__ T exact_disk(const Geo<T>& g, V3<T> loc, V3<T> mv, int moving_species, V3<T> target) {
+  const T R = g.R;
+  const T R2 = R * R;
+  const T m2_i = 1 / dot(mv, mv);
+  V3<T> m, u, v;
+  {
+    // exd_coordize (:94-145)
+    T a = 1 / sqrt(dot(mv, mv));
+    m = cmul(v3<T>(a, a, a), mv);
+    T mx2 = m.x * m.x, my2 = m.y * m.y, mz2 = m.z * m.z;
+    if (mx2 > my2) {
+      if (mx2 > mz2) {
+        if (my2 > mz2) {
+          u = v3<T>(m.y, -m.x, 0); a = 1 - mz2; v = v3<T>(m.z * m.x, m.z * m.y, -a);
+        } else {
+          u = v3<T>(m.z, 0, -m.x); a = 1 - my2; v = v3<T>(-m.y * m.x, a, -m.y * m.z);
+        }
+      } else {
+        u = v3<T>(-m.z, 0, m.x); a = 1 - my2; v = v3<T>(m.y * m.x, -a, m.y * m.z);
+      }
+    } else {
+      if (my2 > mz2) {
+        if (mx2 > mz2) {
+          u = v3<T>(-m.y, m.x, 0); a = 1 - mz2; v = v3<T>(-m.z * m.x, -m.z * m.y, a);
+        } else {
+          u = v3<T>(0, m.z, -m.y); a = 1 - mx2; v = v3<T>(-a, m.x * m.y, m.x * m.z);
+        }
+      } else {
+        u = v3<T>(0, -m.z, m.y); a = 1 - mx2; v = v3<T>(a, -m.x * m.y, -m.x * m.z);
+      }
+    }
+    a = 1 / sqrt(a);
+    u = scale(u, a);
+    v = scale(v, a);
+  }
+  V3<T> L = v3<T>(dot(loc, m), dot(loc, u), dot(loc, v));
+  ExV<T> sm;
+  {
+    // distinguishable_vec3 (src4/defines.h:766)
+    T c = tabs(loc.x), cc, d;
+    d = tabs(loc.y); if (d > c) c = d;
+    d = tabs(loc.z); if (d > c) c = d;
+    d = tabs(target.x); if (d > c) c = d;
+    d = tabs(target.y); if (d > c) c = d;
+    d = tabs(target.z); if (d > c) c = d;
+    cc = tabs(loc.x - target.x);
+    d = tabs(loc.y - target.y); if (d > cc) cc = d;
+    d = tabs(loc.z - target.z); if (d > cc) cc = d;
+    if (c < Eps<T>::pos) c = Eps<T>::pos;
+    if (!(c * Eps<T>::pos < cc)) {
+      sm.u = sm.v = sm.r2 = sm.zeta = 0;
+    } else {
+      V3<T> td = target - loc;
+      sm.u = dot(td, u);
+      sm.v = dot(td, v);
+      sm.r2 = sm.u * sm.u + sm.v * sm.v;
+      sm.zeta = zetize(sm.v, sm.u);
+    }
+  }
+  ExV<T> ea[MAX_DISK_EDGES], eb[MAX_DISK_EDGES];
+  int n_edges = 0;
+  const uint32_t sp = subpart_of(g, loc);
+  const Chem& ch = *g.chem;
+  for (uint32_t k = g.wsp_off[sp]; k < g.wsp_off[sp + 1]; k++) {
+    const uint32_t wi = g.wsp_list[k];
+    const P4<T> rj = g.wrej[wi];
+    V3<T> wn = v3<T>(rj.x, rj.y, rj.z);
+    T l_n = dot(loc, wn);
+    T d = rj.w - l_n;
+    T m_n = dot(mv, wn);
+    if (d * d >= R2 * (1 - m2_i * m_n * m_n)) continue;
+    const WallFace<T>& wf = g.wface[wi];
+    V3<T> wv[3] = {wf.v0, wf.v1, wf.v2};
+    V3<T> llf, urb;
+    llf.x = urb.x = wv[0].x;
+    llf.y = urb.y = wv[0].y;
+    llf.z = urb.z = wv[0].z;
+    if (wv[1].x < llf.x) llf.x = wv[1].x; else if (wv[1].x > urb.x) urb.x = wv[1].x;
+    if (wv[2].x < llf.x) llf.x = wv[2].x; else if (wv[2].x > urb.x) urb.x = wv[2].x;
+    if (wv[1].y < llf.y) llf.y = wv[1].y; else if (wv[1].y > urb.y) urb.y = wv[1].y;
+    if (wv[2].y < llf.y) llf.y = wv[2].y; else if (wv[2].y > urb.y) urb.y = wv[2].y;
+    if (wv[1].z < llf.z) llf.z = wv[1].z; else if (wv[1].z > urb.z) urb.z = wv[1].z;
+    if (wv[2].z < llf.z) llf.z = wv[2].z; else if (wv[2].z > urb.z) urb.z = wv[2].z;
+    T a, b;
+    b = R2 * (1 - mv.x * mv.x * m2_i);
+    a = llf.x - loc.x; if (a > 0 && a * a >= b) continue;
+    a = loc.x - urb.x; if (a > 0 && a * a >= b) continue;
+    b = R2 * (1 - mv.y * mv.y * m2_i);
+    a = llf.y - loc.y; if (a > 0 && a * a >= b) continue;
+    a = loc.y - urb.y; if (a > 0 && a * a >= b) continue;
+    b = R2 * (1 - mv.z * mv.z * m2_i);
+    a = llf.z - loc.z; if (a > 0 && a * a >= b) continue;
+    a = loc.z - urb.z; if (a > 0 && a * a >= b) continue;
+    if (ch.can_volwall[moving_species] && g.wall_class[(size_t)wi * g.nsp + moving_species] == 1) continue;
+    V3<T> p0 = v3<T>(dot(wv[0], m), dot(wv[0], u), dot(wv[0], v)) - L;
+    V3<T> p1 = v3<T>(dot(wv[1], m), dot(wv[1], u), dot(wv[1], v)) - L;
+    V3<T> p2 = v3<T>(dot(wv[2], m), dot(wv[2], u), dot(wv[2], v)) - L;
+    ExV<T> pa, pb;
+    auto isect = [](V3<T> P, V3<T> Q, ExV<T>& o) {
+      T t = P.x / (P.x - Q.x);
+      o.u = P.y + t * (Q.y - P.y);
+      o.v = P.z + t * (Q.z - P.z);
+    };
+    if ((p0.x < 0) == (p1.x < 0)) {
+      if ((p2.x < 0) == (p1.x < 0)) continue;
+      isect(p0, p2, pa);
+      isect(p1, p2, pb);
+    } else if ((p0.x < 0) == (p2.x < 0)) {
+      isect(p0, p1, pa);
+      isect(p2, p1, pb);
+    } else {
+      isect(p1, p0, pa);
+      isect(p2, p0, pb);
+    }
+    pa.r2 = pa.u * pa.u + pa.v * pa.v;
+    pb.r2 = pb.u * pb.u + pb.v * pb.v;
+    if (pa.r2 < Eps<T>::pos * R2 || pb.r2 < Eps<T>::pos * R2) return -1;
+    if (!distinguishable<T>(pa.u * pb.v, pb.u * pa.v, Eps<T>::pos) && (pa.u * pb.u + pa.v * pb.v) < 0) return -1;
+    T ti = 0, si = 1;
+    if (pa.r2 > R2 || pb.r2 > R2) {
+      T pa_pb = pa.u * pb.u + pa.v * pb.v;
+      if (!distinguishable<T>(pa.r2 + pb.r2, 2 * pa_pb, Eps<T>::pos)) {
+        if (sm.r2 < pa.r2 && sm.r2 < pb.r2 && distinguishable<T>(sm.r2, pa.r2, Eps<T>::pos) &&
+            distinguishable<T>(sm.r2, pa.r2, Eps<T>::pos))
+          continue;
+        if (!distinguishable<T>(sm.u * pa.v, sm.v * pa.u, Eps<T>::pos_sqrt) ||
+            !distinguishable<T>(sm.u * pb.v, sm.v * pb.u, Eps<T>::pos_sqrt))
+          return -1;
+        continue;
+      }
+      T ia = 1 / (pa.r2 + pb.r2 - 2 * pa_pb);
+      T ib = (pa_pb - pa.r2) * ia;
+      T ic = (R2 - pa.r2) * ia;
+      T id = ib * ib + ic;
+      if (id <= 0) continue;
+      id = sqrt(id);
+      ti = -ib - id;
+      if (ti >= 1) continue;
+      if (ti < 0) ti = 0;
+      si = -ib + id;
+      if (si <= 0) continue;
+      if (si > 1) si = 1;
+    }
+    ExV<T> qa, qb;
+    if (ti > 0) {
+      qa.u = pa.u + ti * (pb.u - pa.u);
+      qa.v = pa.v + ti * (pb.v - pa.v);
+      qa.r2 = qa.u * qa.u + qa.v * qa.v;
+      qa.zeta = zetize(qa.v, qa.u);
+    } else {
+      qa = pa;
+      qa.zeta = zetize(pa.v, pa.u);
+    }
+    if (si < 1) {
+      qb.u = pa.u + si * (pb.u - pa.u);
+      qb.v = pa.v + si * (pb.v - pa.v);
+      qb.r2 = qb.u * qb.u + qb.v * qb.v;
+      qb.zeta = zetize(qb.v, qb.u);
+    } else {
+      qb = pb;
+      qb.zeta = zetize(pb.v, pb.u);
+    }
+    a = qb.zeta - qa.zeta;
+    if (a < 0) a += 4;
+    if (a >= 2) {
+      ExV<T> t = qa;
+      qa = qb;
+      qb = t;
+      a = 4 - a;
+    }
+    b = sm.zeta - qa.zeta;
+    if (b < 0) b += 4;
+    if (b < a) {
+      T au = qa.u - sm.u, av = qa.v - sm.v, bu = qb.u - sm.u, bv = qb.v - sm.v;
+      T c = au * bv - av * bu;
+      if (c < 0 || !distinguishable<T>(au * bv, av * bu, Eps<T>::pos)) return -1;
+    }
+    if (n_edges < MAX_DISK_EDGES) {
+      ea[n_edges] = qa;
+      eb[n_edges] = qb;
+      n_edges++;
+    }
+  }
+  if (n_edges == 0) return 1;
+  if (n_edges == 1) {
+    T ares = ea[0].u * eb[0].u + ea[0].v * eb[0].v;
+    T bres = ea[0].u * eb[0].v - ea[0].v * eb[0].u;
+    T sres;
+    if (ares <= 0)
+      sres = atan(-ares / bres) + (T)(0.5 * MY_PI);
+    else
+      sres = atan(bres / ares);
+    return ((T)0.5 * bres + R2 * ((T)MY_PI - (T)0.5 * sres)) / ((T)MY_PI * R2);
+  }
+  return sweep_area(ea, eb, n_edges, R2) / ((T)MY_PI * R2);
+}
+
+// ------------------------------------------------------------------ reaction tests
+
+// test_bimolecular (rxn_utils.inl:336-414), single pathway; true if it fires
+template <class D>
+__device__ __forceinline__ bool test_bimolecular(double max_fixed_p, double scaling, D& draws) {
+  double prob;
+  if (max_fixed_p < scaling) {
+    prob = draw_dbl(draws) * scaling;
+    return !(prob >= max_fixed_p);
+  }
+  float max_p = (float)max_fixed_p;
+  if (max_p >= scaling) {
+    (void)draw_dbl(draws);
+    return true;
+  }
+  prob = draw_dbl(draws) * scaling;
+  return !(prob >= max_p);
+}
+
+// test_intersect (rxn_utils.inl:593-626) for an absorptive surface class (rate DBL_GIGANTIC)
+template <class D>
+__device__ __forceinline__ bool test_intersect_absorb(double scaling, D& draws) {
+  const double max_prob = GIGANTIC;
+  double p;
+  if (max_prob > scaling) {
+    p = draw_dbl(draws) * max_prob;
+  } else {
+    p = draw_dbl(draws) * scaling;
+    if (p > max_prob) return false;
+  }
+  if (p > max_prob) return false;
+  (void)draw_dbl(draws);
+  return true;
+}
+
+// time_of_unimol (rxn_utils.inl:721-735)
+template <class D>
+__device__ __forceinline__ double time_of_unimol(double k_tot, D& draws) {
+  double p = draw_dbl(draws);
+  if (k_tot <= 0 || !distinguishable<double>(p, 0.0, EPS)) return TIME_FOREVER;
+  return -log(p) / k_tot;
+}
+
+// ------------------------------------------------------------------ one molecule, one step
+
+// diffuse_vol_molecule from the known displacement on (diffuse_react_event.cpp:450-618):
+// ray trace, sort, collisions in time order, wall interactions; loops while walls are hit.
+template <typename T, class D, class E>
+__device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos, int species,
+                                      V3<T> disp, double r_rate_factor, double t_steps, double start_time, D& draws,
+                                      E& ev, bool allow_vv = true) {
+  TraceOut<T> res;
+  res.status = 0;
+  res.err = 0;
+  res.partner = NONE;
+  res.t_abs = 0;
+  res.rxn_pos = pos;
+  const Chem& ch = *g.chem;
+  const bool can_vol_react = allow_vv && ch.partners[species] != 0;
+  uint32_t sp = subpart_of(g, pos);
+  uint32_t last_hit = NONE;
+  double elapsed = start_time;
+  V3<T> remaining = disp;
+  int bounces = 0;
+  bool was_defunct = false;
+  bool hit_wall;
+  do {
+    // ---- ray_trace_vol (diffuse_react_event.cpp:627-780)
+    hit_wall = false;
+    V3<T> pdisp = remaining;
+    if (!in_partition(g, pos + remaining)) pdisp = disp_up_to_partition_boundary(g, pos, remaining);
+    WallHit<T> hit, tentative;
+    tentative.t = (T)1e20;
+    tentative.type = CT_MISS;
+    bool hit_in_last = false, used_tentative = false;
+    const V3<T> up_to_init = remaining;  // displacement_up_to_wall_collision before the search
+    {
+      Walk<T> w;
+      w.start(g, pos, sp, pdisp);
+      uint32_t cur = sp;
+      for (;;) {
+        if (closest_wall_collision(g, pos, cur, last_hit, draws, remaining, hit, tentative, res.err)) {
+          hit_wall = true;
+          hit_in_last = (cur == w.dest);
+          break;
+        }
+        if (res.err) break;
+        if (!w.next(g)) break;
+        cur = w.cur;
+      }
+      if (!hit_wall && sizeof(T) == 4 && tentative.type != CT_MISS) {
+        hit = tentative;
+        hit_wall = true;
+        used_tentative = true;
+      }
+    }
+    if (res.err) {
+      res.status = 3;
+      break;
+    }
+    Colls<T> colls;
+    colls.n = 0;
+    colls.overflow = false;
+    if (can_vol_react) {
+      SubSet st;
+      st.overflow = false;
+      // ray_trace_vol keeps the set of the first collection unless a wall was hit
+      // before the last crossed subpartition, then re-collects up to the hit
+      V3<T> mdisp = pdisp;
+      if (hit_wall && !hit_in_last) mdisp = used_tentative ? up_to_init : hit.pos - pos;
+      collect_for_molecules(g, pos, sp, mdisp, st);
+      if (st.overflow) res.err |= ST_SET_OVERFLOW;
+      collide_with_occupants(g, cells, self, pos, species, remaining, st, colls);
+      if (colls.overflow) res.err |= ST_COLL_OVERFLOW;
+    }
+    if (!hit_wall) {
+      pos = pos + remaining;
+      sp = subpart_of(g, pos);
+    }
+    // ---- collisions in time order (diffuse_react_event.cpp:450-572)
+    bool wall_done = false;
+    for (int i = 0; i <= colls.n; i++) {
+      bool take_wall;
+      if (i == colls.n) {
+        take_wall = hit_wall;
+      } else {
+        // the wall sorts before a later molecule; equal times keep the molecule first
+        take_wall = hit_wall && hit.t < colls.c[i].t;
+      }
+      if (take_wall) {
+        const int side = hit.type == CT_FRONT ? 1 : 2;
+        const int kind = ch.can_volwall[species] ? g.wall_class[(size_t)hit.wall * g.nsp + species] : 0;
+        const double t_abs = elapsed + t_steps * (double)hit.t;
+        if (kind == 1) {
+          pos = hit.pos;
+          sp = subpart_of(g, pos);
+          double t_smash = (double)hit.t;
+          T f = (T)(1.0 - t_smash);
+          remaining = cmul(remaining, v3<T>(f, f, f));
+          elapsed += t_steps * t_smash;
+          t_steps *= (1.0 - t_smash);
+          if (t_steps < EPS) t_steps = EPS;
+          last_hit = hit.wall;
+          ev.put(2, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
+        } else if (kind == 2 && test_intersect_absorb(r_rate_factor, draws)) {
+          ev.put(3, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
+          was_defunct = true;
+          res.status = 2;
+          res.t_abs = t_abs;
+          res.rxn_pos = hit.pos;
+        } else {
+          // reflect_from_wall (collision_utils.inl:1711-1747)
+          elapsed += t_steps * (double)hit.t;
+          const P4<T> rj = g.wrej[hit.wall];
+          V3<T> n = v3<T>(rj.x, rj.y, rj.z);
+          double t_reflect = (double)hit.t;
+          pos = hit.pos;
+          sp = subpart_of(g, pos);
+          t_steps *= (double)((T)1.0 - (T)t_reflect);
+          last_hit = hit.wall;
+          T rf = (T)-2.0 * dot(remaining, n);
+          if (sizeof(T) == 4 && 1.0 - t_reflect < (double)Eps<T>::pos_sqrt) t_reflect -= (double)Eps<T>::pos_sqrt;
+          T f = (T)(1.0 - t_reflect);
+          remaining = cmul(remaining + cmul(v3<T>(rf, rf, rf), n), v3<T>(f, f, f));
+          ev.put(1, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
+        }
+        wall_done = true;
+        break;
+      }
+      if (i == colls.n) break;
+      const VV<T>& c = colls.c[i];
+      if (c.t < Eps<T>::stime) continue;  // is_immediate_collision
+      const double t_abs = elapsed + t_steps * (double)c.t;
+      P4<T> q = cells.pos[c.idx];
+      T factor = exact_disk(g, c.pos, remaining, species, v3<T>(q.x, q.y, q.z));
+      if (factor < 0) {
+        ev.put(6, c.uid, 0, (double)c.t, t_abs, (double)c.pos.x, (double)c.pos.y, (double)c.pos.z);
+        continue;
+      }
+      double scaling = (double)factor * r_rate_factor;
+      if (!test_bimolecular(c.p, scaling, draws)) {
+        ev.put(4, c.uid, 0, (double)c.t, t_abs, (double)c.pos.x, (double)c.pos.y, (double)c.pos.z);
+        continue;
+      }
+      ev.put(5, c.uid, 0, (double)c.t, t_abs, (double)c.pos.x, (double)c.pos.y, (double)c.pos.z);
+      was_defunct = true;
+      res.status = 1;
+      res.partner = c.idx;
+      res.t_abs = t_abs;
+      res.rxn_pos = c.pos;
+      break;
+    }
+    (void)wall_done;
+    if (draws.overrun() || ++bounces > MAX_BOUNCES) {
+      res.err |= ST_WATCHDOG;
+      res.status = 3;
+      break;
+    }
+  } while (hit_wall && !was_defunct);
+  res.pos = pos;
+  res.subpart = sp;
+  res.elapsed = elapsed;
+  res.t_steps = t_steps;
+  return res;
+}
+
+}  // namespace mcg

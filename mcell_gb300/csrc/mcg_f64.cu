@@ -1,0 +1,7 @@
+// fp64 instantiation of the engine. Built with -fmad=false so that every
+// product and sum is rounded like MCell4's CPU build (no fused multiply-add).
+#include "mcg_engine.cuh"
+
+namespace mcg {
+DeviceEngine* make_engine_f64() { return new DeviceEngineT<double>(); }
+}  // namespace mcg

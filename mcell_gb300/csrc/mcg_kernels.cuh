@@ -1,0 +1,774 @@
+// Kernels of one diffuse-react iteration (templated on the position precision).
+//
+// Schedule of one iteration, all on the engine's stream, no host round trip
+// (so a block of iterations can be captured in a CUDA graph):
+//   k_diffuse      one thread per molecule: unimolecular schedule, displacement,
+//                  ray trace, first firing reaction -> proposal; survivors are
+//                  counted into the (subpartition, species) histogram
+//   k_resolve      a proposal wins if it holds the minimum claim key on both
+//                  molecules; winners kill both reactants and emit products
+//   k_collect_losers / k_reset_claims
+//   k_redo         one CTA re-traces the (rare) losers with used-up partners
+//                  excluded, in rounds, until every proposal is decided
+//   k_products     newborn products diffuse for the rest of the step (twice)
+//   k_scan_*       histogram -> start offsets of the sorted ranges
+//   k_scatter      survivors move into the next iteration's sorted arrays
+//                  (warp-aggregated atomics per key), species are counted
+//   k_end          iteration bookkeeping
+// This replaces MCell4's serial loop over the molecule schedule
+// (DiffuseReactEvent::diffuse_molecules, diffuse_react_event.cpp:67-161), the
+// per-subpartition reactant maps (partition.h:354-418), the sort by subpartition
+// (sort_mols_by_subpart_event.cpp:62-97) and defragmentation
+// (defragmentation_event.cpp:31-116), which the counting sort subsumes.
+#pragma once
+
+#include "mcg_device.cuh"
+
+namespace mcg {
+
+constexpr int TPB = 256;
+constexpr int SCAN_TILE = 2048;
+constexpr int REDO_ROUNDS = 64;
+constexpr uint64_t CLAIM_FREE = ~0ull;
+
+struct Counters {
+  uint32_t n_live;       // molecules in the current sorted arrays
+  uint32_t n_live_next;  // survivors after this iteration
+  uint32_t n_props;      // proposals made in k_diffuse
+  uint32_t n_losers;
+  uint32_t n_prod;       // products created this iteration
+  uint32_t n_prod_done;  // products already diffused
+  uint32_t prod_hi;      // end of the products pass window
+  uint32_t status;       // ST_* bits
+  uint32_t iteration;
+  unsigned long long mol_steps;
+  unsigned long long warn_coll_overflow;
+  unsigned long long warn_set_overflow;
+};
+
+struct Proposal {
+  uint32_t i, partner;
+  uint64_t key;
+  double t_abs;
+  double x, y, z;
+};
+
+template <typename T>
+struct Product {
+  P4<T> pos;       // birth position, then final position (meta in w)
+  double birth;    // time within the iteration
+  uint64_t uid;
+  double tuni;     // unimolecular time relative to the next iteration start
+};
+
+// state of one engine instance as the kernels see it
+template <typename T>
+struct State {
+  Geo<T> g;
+  uint64_t seed;
+  uint32_t cap, prod_cap, prop_cap, nkeys, traj_cap;
+  // current sorted molecules and the next iteration's
+  P4<T>* a_pos;
+  uint64_t* a_uid;
+  T* a_tuni;
+  P4<T>* n_pos;
+  uint64_t* n_uid;
+  T* n_tuni;
+  uint32_t* start;   // [nkeys + 1] of the current arrays
+  uint32_t* nstart;  // [nkeys + 1] of the next arrays
+  uint32_t* counts;  // [nkeys] histogram of the next iteration
+  uint32_t* cursor;  // [nkeys]
+  uint32_t* tile_sum;
+  // this iteration
+  P4<T>* b_pos;      // final positions
+  uint8_t* st;       // 0 survivor, 1 proposer, 2 dead
+  uint64_t* claim;
+  Proposal* props;
+  uint32_t* losers;
+  Proposal* redo_props;
+  Product<T>* prod;
+  uint8_t* pst;      // product status
+  unsigned long long* traj;  // [traj_cap * nsp]
+  Counters* cnt;
+};
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+  // splitmix64 finalizer: a bijection on 64-bit words
+  x ^= x >> 30;
+  x *= 0xbf58476d1ce4e5b9ull;
+  x ^= x >> 27;
+  x *= 0x94d049bb133111ebull;
+  x ^= x >> 31;
+  return x;
+}
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
+
+// histogram add with one atomic per distinct key in the warp
+__device__ __forceinline__ void warp_count(uint32_t* counts, uint32_t key, bool active) {
+  unsigned mask = __ballot_sync(0xffffffffu, active);
+  if (!active) return;
+  unsigned peers = __match_any_sync(mask, key);
+  if ((int)lane_id() == __ffs(peers) - 1) atomicAdd(&counts[key], (uint32_t)__popc(peers));
+}
+
+// Box-Muller pairs from 4 draws -> 3 standard normals
+template <typename T>
+__device__ __forceinline__ V3<T> gauss3(PhiloxDraws& d) {
+  uint32_t a = d.u32(), b = d.u32(), c = d.u32(), e = d.u32();
+  if (sizeof(T) == 8) {
+    double u1 = ((double)a + 0.5) * (1.0 / 4294967296.0), u2 = (double)b * (1.0 / 4294967296.0);
+    double u3 = ((double)c + 0.5) * (1.0 / 4294967296.0), u4 = (double)e * (1.0 / 4294967296.0);
+    double r1 = sqrt(-2.0 * log(u1)), r2 = sqrt(-2.0 * log(u3));
+    double s1, c1, s2, c2;
+    sincospi(2.0 * u2, &s1, &c1);
+    sincospi(2.0 * u4, &s2, &c2);
+    (void)s2;
+    return v3<T>((T)(r1 * c1), (T)(r1 * s1), (T)(r2 * c2));
+  } else {
+    float u1 = ((float)a + 0.5f) * (1.0f / 4294967296.0f), u2 = (float)b * (1.0f / 4294967296.0f);
+    float u3 = ((float)c + 0.5f) * (1.0f / 4294967296.0f), u4 = (float)e * (1.0f / 4294967296.0f);
+    float r1 = sqrtf(-2.0f * logf(u1)), r2 = sqrtf(-2.0f * logf(u3));
+    float s1, c1, s2, c2;
+    sincospif(2.0f * u2, &s1, &c1);
+    sincospif(2.0f * u4, &s2, &c2);
+    (void)s2;
+    return v3<T>((T)(r1 * c1), (T)(r1 * s1), (T)(r2 * c2));
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ uint32_t key_of(const State<T>& s, V3<T> p, uint32_t species) {
+  return subpart_of(s.g, p) * (uint32_t)s.g.nsp + species;
+}
+
+template <typename T>
+__device__ void add_product(const State<T>& s, int species, V3<T> pos, double birth, uint64_t uid) {
+  if (species < 0) return;
+  uint32_t k = atomicAdd(&s.cnt->n_prod, 1u);
+  if (k >= s.prod_cap) {
+    atomicOr(&s.cnt->status, ST_CAPACITY);
+    return;
+  }
+  Product<T> p;
+  p.pos.x = pos.x;
+  p.pos.y = pos.y;
+  p.pos.z = pos.z;
+  set_meta(p.pos, (uint32_t)species | META_SCHEDULE_UNIMOL);
+  p.birth = birth;
+  p.uid = uid;
+  p.tuni = TIME_FOREVER;
+  s.prod[k] = p;
+}
+
+// unimolecular outcome: the molecule is destroyed, products appear at its position
+// (outcome_unimolecular, diffuse_react_event.cpp:2939)
+template <typename T>
+__device__ void unimol_products(const State<T>& s, int species, V3<T> pos, double t, uint64_t uid, uint32_t it) {
+  const Chem& ch = *s.g.chem;
+  for (int k = 0; k < 2; k++) {
+    int ps = ch.uni_prod[species][k];
+    if (ps >= 0) add_product(s, ps, pos, t, mix64(uid ^ ((uint64_t)(it + 1) << 40) ^ (0xA5ull << 32) ^ (uint64_t)k));
+  }
+}
+
+// Outcome of one molecule's step in the main pass. Shared by k_diffuse and k_redo.
+struct StepDecision {
+  int kind;  // 0 survivor, 1 proposal, 2 dead
+};
+
+template <typename T>
+__device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, Proposal* prop_out, uint32_t& err) {
+  const Geo<T>& g = s.g;
+  const Chem& ch = *g.chem;
+  const uint32_t it = s.cnt->iteration;
+  P4<T> rec = s.a_pos[i];
+  const uint64_t uid = s.a_uid[i];
+  uint32_t meta = meta_of(rec);
+  const int species = (int)(meta & META_SPECIES_MASK);
+  double tuni = (double)s.a_tuni[i];
+  V3<T> pos = v3<T>(rec.x, rec.y, rec.z);
+  PhiloxDraws draws;
+  draws.ph.init(s.seed, uid, it, 0);
+  // pick_unimol_rxn_class_and_set_rxn_time (diffuse_react_event.cpp:1731) on first diffusion
+  if (meta & META_SCHEDULE_UNIMOL) {
+    tuni = ch.unimol_k[species] >= 0 ? time_of_unimol(ch.unimol_k[species], draws) : TIME_FOREVER;
+  }
+  if (tuni <= 0.0) {
+    // scheduled at or before the start of the step: react first (diffuse_single_molecule :214-223)
+    unimol_products(s, species, pos, 0.0, uid, it);
+    return 2;
+  }
+  // get_max_time (:164-198) with the barrier at the end of the iteration
+  double max_time = 1.0;
+  if (tuni < max_time) max_time = tuni;
+  // compute_vol_displacement (diffusion_utils.inl:366-432), time_step = 1
+  double steps = 1.0, t_steps = 1.0;
+  if (t_steps > max_time) {
+    t_steps = max_time;
+    steps = max_time;
+  }
+  if (steps < EPS) {
+    steps = EPS;
+    t_steps = EPS;
+  }
+  double scl = ch.space_step[species];
+  double r_rate_factor = 1.0;
+  if (steps != 1.0) {
+    double rate_factor = sqrt(steps);
+    r_rate_factor = 1.0 / rate_factor;
+    scl = rate_factor * ch.space_step[species];
+  }
+  TraceOut<T> r;
+  if (scl != 0.0) {
+    V3<T> gz = gauss3<T>(draws);
+    V3<T> disp = v3<T>((T)(scl * (double)gz.x * 0.70710678118654752440), (T)(scl * (double)gz.y * 0.70710678118654752440),
+                       (T)(scl * (double)gz.z * 0.70710678118654752440));
+    Cells<T> cells;
+    cells.pos = s.a_pos;
+    cells.uid = s.a_uid;
+    cells.start = s.start;
+    cells.dead = dead;
+    NoEvents ev;
+    r = trace_molecule<T>(g, cells, i, pos, species, disp, r_rate_factor, t_steps, 0.0, draws, ev);
+    err |= r.err;
+  } else {
+    r.status = 0;
+    r.pos = pos;
+  }
+  if (r.status == 1) {
+    Proposal p;
+    p.i = i;
+    p.partner = r.partner;
+    float tf = (float)r.t_abs;
+    // earliest reaction wins; the molecule index makes keys unique within the iteration
+    p.key = ((uint64_t)__float_as_uint(tf < 0.f ? 0.f : tf) << 32) | i;
+    p.t_abs = r.t_abs;
+    p.x = (double)r.rxn_pos.x;
+    p.y = (double)r.rxn_pos.y;
+    p.z = (double)r.rxn_pos.z;
+    *prop_out = p;
+    return 1;
+  }
+  if (r.status == 2) return 2;
+  if (max_time < 1.0) {
+    // the unimolecular reaction happens where the molecule stopped
+    unimol_products(s, species, r.pos, tuni, uid, it);
+    return 2;
+  }
+  if (!in_partition(g, r.pos)) {
+    err |= ST_ESCAPE;  // the reference stops with a fatal error; here the molecule is dropped
+    return 2;
+  }
+  P4<T> out;
+  out.x = r.pos.x;
+  out.y = r.pos.y;
+  out.z = r.pos.z;
+  set_meta(out, (uint32_t)species);  // schedule flag consumed
+  s.b_pos[i] = out;
+  if (meta & META_SCHEDULE_UNIMOL) s.a_tuni[i] = (T)tuni;  // keep the drawn time for the scatter
+  return 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_diffuse(State<T> s) {
+  const uint32_t n = s.cnt->n_live;
+  uint32_t err = 0;
+  uint32_t steps = 0;
+  for (uint32_t base = blockIdx.x * TPB; base < n; base += gridDim.x * TPB) {
+    uint32_t i = base + threadIdx.x;
+    bool active = i < n;
+    int kind = 2;
+    uint32_t key = 0;
+    if (active) {
+      Proposal p;
+      kind = run_molecule(s, i, nullptr, &p, err);
+      s.st[i] = (uint8_t)kind;
+      steps++;
+      if (kind == 1) {
+        uint32_t k = atomicAdd(&s.cnt->n_props, 1u);
+        if (k < s.prop_cap) {
+          s.props[k] = p;
+          atomicMin((unsigned long long*)&s.claim[i], (unsigned long long)p.key);
+          atomicMin((unsigned long long*)&s.claim[p.partner], (unsigned long long)p.key);
+        } else {
+          err |= ST_CAPACITY;
+        }
+      } else if (kind == 0) {
+        P4<T> b = s.b_pos[i];
+        key = key_of(s, v3<T>(b.x, b.y, b.z), meta_of(b) & META_SPECIES_MASK);
+      }
+    }
+    warp_count(s.counts, key, active && kind == 0);
+  }
+  if (err) atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
+  if (err & ST_COLL_OVERFLOW) atomicAdd(&s.cnt->warn_coll_overflow, 1ull);
+  if (err & ST_SET_OVERFLOW) atomicAdd(&s.cnt->warn_set_overflow, 1ull);
+  if (steps) atomicAdd(&s.cnt->mol_steps, (unsigned long long)steps);
+}
+
+// a winning proposal: both reactants die, products appear at the collision point
+// (outcome_bimolecular / outcome_products_random, diffuse_react_event.cpp:1833, :2446)
+template <typename T>
+__device__ void commit(const State<T>& s, const Proposal& p) {
+  const Chem& ch = *s.g.chem;
+  const uint32_t it = s.cnt->iteration;
+  s.st[p.i] = 2;
+  if (s.st[p.partner] == 0) {
+    // the partner had finished its own step: take it out of the histogram
+    P4<T> b = s.b_pos[p.partner];
+    atomicSub(&s.counts[key_of(s, v3<T>(b.x, b.y, b.z), meta_of(b) & META_SPECIES_MASK)], 1u);
+  }
+  s.st[p.partner] = 2;
+  const int sa = (int)(meta_of(s.a_pos[p.i]) & META_SPECIES_MASK);
+  const int sb = (int)(meta_of(s.a_pos[p.partner]) & META_SPECIES_MASK);
+  const uint64_t uid = s.a_uid[p.i];
+  for (int k = 0; k < 2; k++) {
+    int ps = ch.bimol_prod[sa][sb][k];
+    if (ps >= 0) {
+      add_product(s, ps, v3<T>((T)p.x, (T)p.y, (T)p.z), p.t_abs,
+                  mix64(uid ^ ((uint64_t)(it + 1) << 40) ^ (0x5Aull << 32) ^ (uint64_t)k));
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_resolve(State<T> s) {
+  uint32_t n = min(s.cnt->n_props, s.prop_cap);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const Proposal p = s.props[k];
+    if (s.claim[p.i] == p.key && s.claim[p.partner] == p.key) commit(s, p);
+  }
+}
+
+template <typename T>
+__global__ void k_collect_losers(State<T> s) {
+  uint32_t n = min(s.cnt->n_props, s.prop_cap);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const Proposal p = s.props[k];
+    if (s.st[p.i] == 1) {
+      uint32_t m = atomicAdd(&s.cnt->n_losers, 1u);
+      s.losers[m] = p.i;  // n_losers <= n_props <= prop_cap
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_reset_claims(State<T> s) {
+  uint32_t n = min(s.cnt->n_props, s.prop_cap);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const Proposal p = s.props[k];
+    s.claim[p.i] = CLAIM_FREE;
+    s.claim[p.partner] = CLAIM_FREE;
+  }
+}
+
+// One CTA re-traces the losers in rounds: a loser's partner was taken by an
+// earlier-keyed reaction, so it replays its own draws (counter-based RNG) with
+// every used-up molecule excluded, and proposes again or finishes.
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_redo(State<T> s) {
+  __shared__ uint32_t n_cur, n_next, n_rp;
+  uint32_t err = 0;
+  if (threadIdx.x == 0) {
+    n_cur = min(s.cnt->n_losers, s.prop_cap);
+  }
+  __syncthreads();
+  uint32_t* cur = s.losers;
+  for (int round = 0; round < REDO_ROUNDS; round++) {
+    if (n_cur == 0) break;
+    if (threadIdx.x == 0) {
+      n_next = 0;
+      n_rp = 0;
+    }
+    __syncthreads();
+    for (uint32_t l = threadIdx.x; l < n_cur; l += blockDim.x) {
+      const uint32_t i = cur[l];
+      Proposal p;
+      int kind = run_molecule(s, i, s.st, &p, err);
+      if (kind == 1) {
+        s.st[i] = 1;
+        uint32_t k = atomicAdd(&n_rp, 1u);
+        s.redo_props[k] = p;
+        atomicMin((unsigned long long*)&s.claim[i], (unsigned long long)p.key);
+        atomicMin((unsigned long long*)&s.claim[p.partner], (unsigned long long)p.key);
+      } else {
+        s.st[i] = (uint8_t)kind;
+        if (kind == 0) {
+          P4<T> b = s.b_pos[i];
+          atomicAdd(&s.counts[key_of(s, v3<T>(b.x, b.y, b.z), meta_of(b) & META_SPECIES_MASK)], 1u);
+        }
+      }
+    }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < n_rp; k += blockDim.x) {
+      const Proposal p = s.redo_props[k];
+      if (s.claim[p.i] == p.key && s.claim[p.partner] == p.key) commit(s, p);
+    }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < n_rp; k += blockDim.x) {
+      const Proposal p = s.redo_props[k];
+      if (s.st[p.i] == 1) {
+        uint32_t m = atomicAdd(&n_next, 1u);
+        s.losers[s.prop_cap + m] = p.i;  // second half of the loser buffer
+      }
+    }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < n_rp; k += blockDim.x) {
+      const Proposal p = s.redo_props[k];
+      s.claim[p.i] = CLAIM_FREE;
+      s.claim[p.partner] = CLAIM_FREE;
+    }
+    for (uint32_t m = threadIdx.x; m < n_next; m += blockDim.x) s.losers[m] = s.losers[s.prop_cap + m];
+    __syncthreads();
+    if (threadIdx.x == 0) n_cur = n_next;
+    __syncthreads();
+  }
+  if (n_cur != 0) {
+    // undecided after the round limit: report and drop them as dead rather than loop on
+    if (threadIdx.x == 0) atomicOr(&s.cnt->status, ST_WATCHDOG);
+    for (uint32_t l = threadIdx.x; l < n_cur; l += blockDim.x) s.st[cur[l]] = 2;
+  }
+  if (err) atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
+}
+
+// Products diffuse the rest of the step from their birth time (the queue of new
+// diffuse actions, diffuse_react_event.cpp:122-129, 2883-2886). Products do not
+// react with other molecules in the step they are born in.
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_products(State<T> s) {
+  const uint32_t b0 = s.cnt->n_prod_done;
+  const uint32_t b1 = s.cnt->prod_hi;
+  const Geo<T>& g = s.g;
+  const Chem& ch = *g.chem;
+  const uint32_t it = s.cnt->iteration;
+  uint32_t err = 0;
+  for (uint32_t base = b0 + blockIdx.x * TPB; base < b1; base += gridDim.x * TPB) {
+    uint32_t k = base + threadIdx.x;
+    bool active = k < b1;
+    uint32_t key = 0;
+    bool survive = false;
+    if (active) {
+      Product<T> p = s.prod[k];
+      const uint32_t meta = meta_of(p.pos);
+      const int species = (int)(meta & META_SPECIES_MASK);
+      PhiloxDraws draws;
+      draws.ph.init(s.seed, p.uid, it, 1);
+      double unimol_time = TIME_FOREVER;
+      if (ch.unimol_k[species] >= 0) unimol_time = p.birth + time_of_unimol(ch.unimol_k[species], draws);
+      double max_time = 1.0 - p.birth;
+      if (unimol_time < p.birth + max_time) max_time = unimol_time - p.birth;
+      V3<T> pos = v3<T>(p.pos.x, p.pos.y, p.pos.z);
+      bool dead = false;
+      if (max_time <= 0.0) {
+        unimol_products(s, species, pos, unimol_time, p.uid, it);
+        dead = true;
+      } else {
+        double steps = 1.0, t_steps = 1.0;
+        if (t_steps > max_time) {
+          t_steps = max_time;
+          steps = max_time;
+        }
+        if (steps < EPS) {
+          steps = EPS;
+          t_steps = EPS;
+        }
+        double scl = ch.space_step[species], r_rate_factor = 1.0;
+        if (steps != 1.0) {
+          double rf = sqrt(steps);
+          r_rate_factor = 1.0 / rf;
+          scl = rf * ch.space_step[species];
+        }
+        if (scl != 0.0) {
+          V3<T> gz = gauss3<T>(draws);
+          V3<T> disp = v3<T>((T)(scl * (double)gz.x * 0.70710678118654752440),
+                             (T)(scl * (double)gz.y * 0.70710678118654752440),
+                             (T)(scl * (double)gz.z * 0.70710678118654752440));
+          Cells<T> cells;
+          cells.pos = s.a_pos;
+          cells.uid = s.a_uid;
+          cells.start = s.start;
+          cells.dead = s.st;
+          NoEvents ev;
+          TraceOut<T> r = trace_molecule<T>(g, cells, NONE, pos, species, disp, r_rate_factor, t_steps, p.birth,
+                                            draws, ev, false);
+          err |= r.err;
+          if (r.status == 2) {
+            dead = true;
+          } else {
+            pos = r.pos;
+          }
+        }
+        if (!dead && unimol_time < 1.0) {
+          unimol_products(s, species, pos, unimol_time, p.uid, it);
+          dead = true;
+        }
+      }
+      if (!dead && !in_partition(g, pos)) {
+        err |= ST_ESCAPE;
+        dead = true;
+      }
+      if (!dead) {
+        p.pos.x = pos.x;
+        p.pos.y = pos.y;
+        p.pos.z = pos.z;
+        set_meta(p.pos, (uint32_t)species);
+        p.tuni = unimol_time - 1.0;
+        s.prod[k] = p;
+        key = key_of(s, pos, (uint32_t)species);
+        survive = true;
+      }
+      s.pst[k] = survive ? 0 : 2;
+    }
+    warp_count(s.counts, key, active && survive);
+  }
+  __syncthreads();
+  if (err) atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
+}
+
+// window of products for the next pass: [done, hi) where hi is a snapshot taken
+// before the pass, so products created during a pass go to the next one
+template <typename T>
+__global__ void k_prod_window(State<T> s) {
+  s.cnt->n_prod_done = s.cnt->prod_hi;
+  s.cnt->prod_hi = min(s.cnt->n_prod, s.prod_cap);
+}
+
+// ---- exclusive scan of the histogram (3 phases over tiles of SCAN_TILE keys)
+
+template <typename T>
+__global__ void k_scan_tiles(State<T> s) {
+  __shared__ uint32_t red[TPB / 32];
+  const uint32_t b = blockIdx.x * SCAN_TILE;
+  uint32_t sum = 0;
+  for (uint32_t k = b + threadIdx.x; k < min(b + SCAN_TILE, s.nkeys); k += TPB) sum += s.counts[k];
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+  if (lane_id() == 0) red[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    uint32_t v = threadIdx.x < TPB / 32 ? red[threadIdx.x] : 0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) s.tile_sum[blockIdx.x] = v;
+  }
+}
+
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t warp_tot[TPB / 32];
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if ((int)lane_id() >= o) x += y;
+  }
+  if (lane_id() == 31) warp_tot[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    uint32_t w = threadIdx.x < TPB / 32 ? warp_tot[threadIdx.x] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if ((int)threadIdx.x >= o) w += y;
+    }
+    if (threadIdx.x < TPB / 32) warp_tot[threadIdx.x] = w;
+  }
+  __syncthreads();
+  uint32_t warp_off = (threadIdx.x >> 5) ? warp_tot[(threadIdx.x >> 5) - 1] : 0;
+  *total = warp_tot[TPB / 32 - 1];
+  __syncthreads();
+  return warp_off + x - v;
+}
+
+template <typename T>
+__global__ void k_scan_top(State<T> s, uint32_t ntiles) {
+  __shared__ uint32_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (uint32_t b = 0; b < ntiles; b += TPB) {
+    uint32_t k = b + threadIdx.x;
+    uint32_t v = k < ntiles ? s.tile_sum[k] : 0;
+    uint32_t tot;
+    uint32_t ex = block_excl_scan(v, &tot);
+    if (k < ntiles) s.tile_sum[k] = carry + ex;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    s.cnt->n_live_next = carry;
+    if (carry > s.cap) atomicOr(&s.cnt->status, ST_CAPACITY);
+  }
+}
+
+template <typename T>
+__global__ void k_scan_apply(State<T> s) {
+  const uint32_t b = blockIdx.x * SCAN_TILE;
+  uint32_t carry = s.tile_sum[blockIdx.x];
+  __shared__ uint32_t sh_carry;
+  for (uint32_t c = 0; c < SCAN_TILE; c += TPB) {
+    uint32_t k = b + c + threadIdx.x;
+    uint32_t v = k < s.nkeys ? s.counts[k] : 0;
+    uint32_t tot;
+    uint32_t ex = block_excl_scan(v, &tot);
+    if (k < s.nkeys) {
+      s.nstart[k] = carry + ex;
+      s.counts[k] = 0;
+      s.cursor[k] = 0;
+    }
+    carry += tot;
+  }
+  (void)sh_carry;
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) s.nstart[s.nkeys] = carry;
+}
+
+// ---- scatter into the next sorted arrays
+
+template <typename T>
+__device__ __forceinline__ void scatter_one(const State<T>& s, bool active, const P4<T>& pos, uint64_t uid, T tuni,
+                                            unsigned long long* sp_count) {
+  uint32_t key = 0;
+  if (active) key = key_of(s, v3<T>(pos.x, pos.y, pos.z), meta_of(pos) & META_SPECIES_MASK);
+  unsigned mask = __ballot_sync(0xffffffffu, active);
+  if (!active) return;
+  unsigned peers = __match_any_sync(mask, key);
+  int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if ((int)lane_id() == leader) base = atomicAdd(&s.cursor[key], (uint32_t)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  uint32_t rank = __popc(peers & ((1u << lane_id()) - 1));
+  uint32_t slot = s.nstart[key] + base + rank;
+  if (slot < s.cap) {
+    s.n_pos[slot] = pos;
+    s.n_uid[slot] = uid;
+    s.n_tuni[slot] = tuni;
+  }
+  atomicAdd(&sp_count[meta_of(pos) & META_SPECIES_MASK], 1ull);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_scatter(State<T> s, int tuni_shift, int count_species) {
+  __shared__ unsigned long long spc[MAXSP];
+  if (threadIdx.x < MAXSP) spc[threadIdx.x] = 0;
+  __syncthreads();
+  const uint32_t n = s.cnt->n_live;
+  for (uint32_t base = blockIdx.x * TPB; base < n; base += gridDim.x * TPB) {
+    uint32_t i = base + threadIdx.x;
+    bool active = i < n && s.st[i] == 0;
+    P4<T> p;
+    uint64_t uid = 0;
+    T tuni = 0;
+    if (active) {
+      p = s.b_pos[i];
+      uid = s.a_uid[i];
+      tuni = s.a_tuni[i] - (T)tuni_shift;
+    }
+    scatter_one(s, active, p, uid, tuni, spc);
+  }
+  const uint32_t np = min(s.cnt->n_prod, s.prod_cap);
+  for (uint32_t base = blockIdx.x * TPB; base < np; base += gridDim.x * TPB) {
+    uint32_t k = base + threadIdx.x;
+    bool active = k < np && k < s.cnt->n_prod_done && s.pst[k] == 0;
+    P4<T> p;
+    uint64_t uid = 0;
+    T tuni = 0;
+    if (active) {
+      Product<T> q = s.prod[k];
+      p = q.pos;
+      uid = q.uid;
+      tuni = (T)q.tuni;
+    }
+    scatter_one(s, active, p, uid, tuni, spc);
+  }
+  __syncthreads();
+  if (count_species && threadIdx.x < s.g.nsp && spc[threadIdx.x]) {
+    const uint32_t row = s.cnt->iteration % s.traj_cap;
+    atomicAdd(&s.traj[(size_t)row * s.g.nsp + threadIdx.x], spc[threadIdx.x]);
+  }
+}
+
+// bookkeeping at the end of an iteration (single thread)
+template <typename T>
+__global__ void k_end(State<T> s) {
+  Counters* c = s.cnt;
+  if (c->n_prod > c->n_prod_done) atomicOr(&c->status, ST_WATCHDOG);  // product chain deeper than the passes
+  c->n_live = min(c->n_live_next, s.cap);
+  c->n_props = 0;
+  c->n_losers = 0;
+  c->n_prod = 0;
+  c->n_prod_done = 0;
+  c->prod_hi = 0;
+  c->iteration += 1;
+  const uint32_t row = c->iteration % s.traj_cap;
+  for (int k = 0; k < s.g.nsp; k++) s.traj[(size_t)row * s.g.nsp + k] = 0;
+}
+
+// ---- uploads: bin freshly added molecules (staged in the product list) into the first arrays
+
+// re-binning (uploads): existing molecules keep their position (b = a, status
+// survivor) and staged ones sit in the product list; both are counted here and
+// moved by k_scatter
+template <typename T>
+__global__ void k_rebin_count(State<T> s, uint32_t n_staged) {
+  const uint32_t n = s.cnt->n_live;
+  for (uint32_t base = blockIdx.x * TPB; base < n; base += gridDim.x * TPB) {
+    uint32_t i = base + threadIdx.x;
+    bool active = i < n;
+    uint32_t key = 0;
+    if (active) {
+      P4<T> p = s.a_pos[i];
+      s.b_pos[i] = p;
+      s.st[i] = 0;
+      key = key_of(s, v3<T>(p.x, p.y, p.z), meta_of(p) & META_SPECIES_MASK);
+    }
+    warp_count(s.counts, key, active);
+  }
+  for (uint32_t base = blockIdx.x * TPB; base < n_staged; base += gridDim.x * TPB) {
+    uint32_t k = base + threadIdx.x;
+    bool active = k < n_staged;
+    uint32_t key = 0;
+    if (active) {
+      P4<T> p = s.prod[k].pos;
+      s.pst[k] = 0;
+      key = key_of(s, v3<T>(p.x, p.y, p.z), meta_of(p) & META_SPECIES_MASK);
+    }
+    warp_count(s.counts, key, active);
+  }
+}
+
+// ---- per-routine parity harness: injected displacement and draws
+
+template <typename T>
+__global__ void k_trace_cases(State<T> s, uint32_t ncases, const uint32_t* idx, const double* disp,
+                              const uint32_t* draws, uint32_t ndraws, const double* rrf, const double* tst,
+                              double* out) {
+  uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncases) return;
+  double* o = out + (size_t)c * 265;
+  for (int k = 0; k < 265; k++) o[k] = 0;
+  const uint32_t i = idx[c];
+  P4<T> rec = s.a_pos[i];
+  const int species = (int)(meta_of(rec) & META_SPECIES_MASK);
+  InjectedDraws d;
+  d.d = draws + (size_t)c * ndraws;
+  d.n = ndraws;
+  d.used = 0;
+  d.over = false;
+  EventLog ev;
+  ev.out = o;
+  Cells<T> cells;
+  cells.pos = s.a_pos;
+  cells.uid = s.a_uid;
+  cells.start = s.start;
+  cells.dead = nullptr;
+  V3<T> dv = v3<T>((T)disp[3 * c], (T)disp[3 * c + 1], (T)disp[3 * c + 2]);
+  TraceOut<T> r = trace_molecule<T>(s.g, cells, i, v3<T>(rec.x, rec.y, rec.z), species, dv, rrf[c], tst[c], 0.0, d, ev);
+  int status = r.status;
+  if (d.over) status = 3;
+  o[0] = status;
+  o[1] = (double)r.pos.x;
+  o[2] = (double)r.pos.y;
+  o[3] = (double)r.pos.z;
+  o[4] = r.subpart;
+  o[5] = d.used;
+  o[7] = r.elapsed;
+  o[8] = r.t_steps;
+}
+
+}  // namespace mcg

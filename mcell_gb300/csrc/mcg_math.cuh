@@ -1,0 +1,114 @@
+// Small vector math and the counter-based RNG shared by all device code.
+//
+// The vector helpers keep MCell4's operation order (glm's dot is
+// (x*x' + y*y') + z*z', cross as in glm::cross); the fp64 translation unit is
+// compiled with -fmad=false so that every result matches the reference's
+// CPU arithmetic bit for bit.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mcg {
+
+template <typename T>
+struct V3 {
+  T x, y, z;
+};
+
+template <typename T>
+__host__ __device__ __forceinline__ V3<T> v3(T x, T y, T z) {
+  V3<T> r;
+  r.x = x;
+  r.y = y;
+  r.z = z;
+  return r;
+}
+template <typename T>
+__host__ __device__ __forceinline__ V3<T> operator+(V3<T> a, V3<T> b) {
+  return v3<T>(a.x + b.x, a.y + b.y, a.z + b.z);
+}
+template <typename T>
+__host__ __device__ __forceinline__ V3<T> operator-(V3<T> a, V3<T> b) {
+  return v3<T>(a.x - b.x, a.y - b.y, a.z - b.z);
+}
+// component-wise product (glm vec * vec)
+template <typename T>
+__host__ __device__ __forceinline__ V3<T> cmul(V3<T> a, V3<T> b) {
+  return v3<T>(a.x * b.x, a.y * b.y, a.z * b.z);
+}
+template <typename T>
+__host__ __device__ __forceinline__ V3<T> cdiv(V3<T> a, V3<T> b) {
+  return v3<T>(a.x / b.x, a.y / b.y, a.z / b.z);
+}
+template <typename T>
+__host__ __device__ __forceinline__ V3<T> scale(V3<T> a, T s) {
+  return v3<T>(a.x * s, a.y * s, a.z * s);
+}
+template <typename T>
+__host__ __device__ __forceinline__ T dot(V3<T> a, V3<T> b) {
+  return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+template <typename T>
+__host__ __device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {
+  return v3<T>(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+template <typename T>
+__host__ __device__ __forceinline__ T tmax(T a, T b) {
+  return a > b ? a : b;
+}
+template <typename T>
+__host__ __device__ __forceinline__ T tabs(T a) {
+  return a < T(0) ? -a : a;
+}
+
+// --------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
+// as 1, 2, 3", SC 2011): a counter-based generator, so every molecule-step owns
+// an independent stream addressed by (molecule id, iteration, phase, block) and
+// any draw can be replayed without storing generator state.
+struct Philox {
+  uint32_t k0, k1;      // key = seed
+  uint32_t c0, c1, c2;  // counter words: id low, id high, iteration
+  uint32_t c3;          // phase << 24 | block
+  uint32_t buf[4];
+  int left;
+
+  __device__ __forceinline__ void init(uint64_t seed, uint64_t id, uint32_t iteration, uint32_t phase) {
+    k0 = (uint32_t)seed;
+    k1 = (uint32_t)(seed >> 32);
+    c0 = (uint32_t)id;
+    c1 = (uint32_t)(id >> 32);
+    c2 = iteration;
+    c3 = phase << 24;
+    left = 0;
+  }
+  __device__ __forceinline__ void block() {
+    uint32_t x0 = c0, x1 = c1, x2 = c2, x3 = c3;
+    uint32_t a = k0, b = k1;
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+      uint32_t hi0 = __umulhi(0xD2511F53u, x0), lo0 = 0xD2511F53u * x0;
+      uint32_t hi1 = __umulhi(0xCD9E8D57u, x2), lo1 = 0xCD9E8D57u * x2;
+      uint32_t y0 = hi1 ^ x1 ^ a, y1 = lo1, y2 = hi0 ^ x3 ^ b, y3 = lo0;
+      x0 = y0;
+      x1 = y1;
+      x2 = y2;
+      x3 = y3;
+      a += 0x9E3779B9u;
+      b += 0xBB67AE85u;
+    }
+    buf[0] = x0;
+    buf[1] = x1;
+    buf[2] = x2;
+    buf[3] = x3;
+    c3++;
+    left = 4;
+  }
+  __device__ __forceinline__ uint32_t next_u32() {
+    if (left == 0) block();
+    return buf[4 - left--];
+  }
+};
+
+}  // namespace mcg

@@ -1,0 +1,142 @@
+#!/usr/bin/env python3
+"""Generates the golden fixtures in tests/golden/ from the reference's own routines.
+
+Needs oracle/_ref/libmcell_ref{64,32}.so, which oracle/ref/build_ref.py compiles
+from the reference sources (only possible where the reference tree exists).
+Every case feeds an injected displacement and injected 32-bit draws to the
+reference's ray_trace_vol / collide_wall / reflect_from_wall / exact_disk /
+test_bimolecular path (driven as diffuse_vol_molecule does) and records the
+result: status, final position and subpartition, draws used, and the event list
+(wall reflections / crossings / absorptions, partners tested / reacted /
+occluded, with times and positions).
+
+Usage: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent.parent))
+
+from tests import harness as H  # noqa: E402
+
+NDRAWS = 24
+
+
+def scenes(rng):
+    out = {}
+    sc = H.cube_scene(rng, n_mol=800, nsub=12, partition_um=1.2, p_rxn=0.0368)
+    out["cube"] = sc
+    sc = H.cube_scene(rng, n_mol=3000, nsub=12, partition_um=1.2, p_rxn=0.6)
+    out["cube_dense"] = sc
+    sc = H.cube_scene(rng, n_mol=600, nsub=12, partition_um=1.2, p_rxn=0.2)
+    wc = np.zeros((12, 3), np.uint8)
+    wc[[2, 8], 0] = 1     # x = +50 face transparent to A
+    wc[[5, 11], 1] = 2    # z = +50 face absorptive for B
+    wc[[0, 6], 0] = 2     # x = -50 face absorptive for A
+    sc.wall_class = wc
+    out["cube_classes"] = sc
+    sc = H.sphere_in_cube_scene(rng, levels=2, n_mol=2500, radius_um=0.5, cube_um=1.2, p_rxn=0.5)
+    out["sphere"] = sc
+    return out
+
+
+def add_edge_molecules(sc: H.Scene):
+    cases = H.edge_cases(sc)
+    extra = [
+        ((50.0, 0.0, 0.0), (0.0, 3.0, 1.0)),    # on the wall plane, moving along it: REDO
+        ((50.0, 3.0, 3.0), (-2.0, 0.5, 0.0)),   # on the wall plane, moving away
+    ]
+    cases = cases + extra
+    n0 = len(sc.mol_species)
+    pos = np.array([c[0] for c in cases])
+    sc.mol_pos = np.concatenate([sc.mol_pos, pos])
+    sc.mol_species = np.concatenate([sc.mol_species, np.zeros(len(cases), np.uint32)])
+    return [(n0 + k, np.array(c[1])) for k, c in enumerate(cases)]
+
+
+def partner_cases(rng, sc: H.Scene, n):
+    """Displacements aimed past a reacting partner: the nearest molecule of a reacting
+    species, passed within 1.2 R, overshooting by 5-60% (exercises collide_mol,
+    exact_disk near walls and test_bimolecular)."""
+    cases = []
+    nm = len(sc.mol_species)
+    react = {}
+    for a, b in np.asarray(sc.rxn_ab).reshape(-1, 2):
+        react.setdefault(int(a), set()).add(int(b))
+        react.setdefault(int(b), set()).add(int(a))
+    for _ in range(n):
+        i = int(rng.integers(0, nm))
+        ok = np.isin(sc.mol_species, list(react.get(int(sc.mol_species[i]), [])))
+        ok[i] = False
+        if not ok.any():
+            continue
+        d = sc.mol_pos - sc.mol_pos[i]
+        dist = np.where(ok, np.linalg.norm(d, axis=1), np.inf)
+        j = int(np.argmin(dist))
+        v = d[j]
+        L = np.linalg.norm(v)
+        u = v / L
+        w = np.cross(u, rng.normal(size=3))
+        w /= np.linalg.norm(w)
+        aim = v + w * rng.uniform(0, 1.2 * sc.rxn_radius)
+        cases.append((i, aim * rng.uniform(1.05, 1.6)))
+    return cases
+
+
+def main():
+    ref64 = H.reference(64)
+    if ref64 is None:
+        raise SystemExit("oracle/_ref/libmcell_ref64.so missing: run python oracle/ref/build_ref.py")
+    rng = np.random.default_rng(20261203)
+    for name, sc in scenes(rng).items():
+        cases = []
+        if name == "cube":
+            cases += add_edge_molecules(sc)
+        cases += [(m, d) for (m, d, _) in H.random_cases(rng, sc, 700, scale=2.0, near_wall_frac=0.4)]
+        cases += partner_cases(rng, sc, 500)
+        h = ref64.scene(sc)
+        mols = np.array([c[0] for c in cases], np.uint32)
+        disps = np.array([c[1] for c in cases], np.float64)
+        draws = rng.integers(0, 2 ** 32, size=(len(cases), NDRAWS), dtype=np.uint64).astype(np.uint32)
+        # a share of cases with draws that make reactions fire (small uniforms)
+        draws[::3, :] = (draws[::3, :] >> 6).astype(np.uint32)
+        res = np.array([h.diffuse_case(int(m), d, dr) for m, d, dr in zip(mols, disps, draws)])
+        nev = int(res[:, 6].max())
+        keep = H.RES_HDR + H.EV_SIZE * max(1, min(nev, H.EV_MAX))
+        info = h.info()
+        wc_ref = h.wall_consts(len(sc.tris))
+        counts, lst = h.walls_in_subparts(sc.nsub ** 3)
+        np.savez_compressed(
+            HERE / f"diffuse_{name}.npz",
+            origin=sc.origin, partition_edge=sc.partition_edge, nsub=sc.nsub, rxn_radius=sc.rxn_radius,
+            verts=sc.verts, tris=sc.tris, space_steps=sc.space_steps, wall_class=sc.wall_class,
+            rxn_ab=sc.rxn_ab, rxn_p=sc.rxn_p, mol_pos=sc.mol_pos, mol_species=sc.mol_species,
+            mols=mols, disps=disps, draws=draws, results=res[:, :keep],
+            info=info, wall_consts=wc_ref, wsp_counts=counts, wsp_list=lst)
+        kinds = np.unique(res[:, H.RES_HDR::H.EV_SIZE][res[:, H.RES_HDR::H.EV_SIZE] > 0], return_counts=True)
+        print(name, len(cases), "cases, event kinds", dict(zip(kinds[0].astype(int).tolist(), kinds[1].tolist())),
+              "status", np.unique(res[:, 0], return_counts=True))
+    # reaction tests on injected uniforms
+    P = np.concatenate([rng.uniform(0, 1, 400), rng.uniform(0, 3, 100), [0.0, 1.0, 2.0, 0.0368]])
+    S = np.concatenate([rng.uniform(0, 1.5, 400), rng.uniform(0, 3, 100), [1.0, 1.0, 1.0, 1.0]])
+    U = rng.integers(0, 2 ** 32, size=len(P), dtype=np.uint64).astype(np.uint32)
+    tb = np.array([ref64.test_bimolecular(p, s, u) for p, s, u in zip(P, S, U)], np.int32)
+    K = rng.uniform(0, 2e-3, 300)
+    Uu = rng.integers(0, 2 ** 32, size=len(K), dtype=np.uint64).astype(np.uint32)
+    Uu[:3] = [0, 1, 2 ** 32 - 1]
+    tu = np.array([ref64.time_of_unimol(k, u) for k, u in zip(K, Uu)])
+    # the reference's ISAAC64 + ziggurat Gaussian stream (distribution reference)
+    import ctypes
+    g = np.zeros(20000)
+    ref64.lib.ref_rng_gauss(ctypes.c_ulonglong(1), ctypes.c_uint(len(g)), H.ptr(g))
+    np.savez_compressed(HERE / "rxn_tests.npz", P=P, S=S, U=U, bimol=tb, K=K, Uu=Uu, unimol=tu, ref_gauss=g)
+    print("rxn tests", (tb >= 0).sum(), "fired of", len(tb))
+
+
+if __name__ == "__main__":
+    main()

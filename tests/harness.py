@@ -204,3 +204,162 @@ def random_cases(rng: np.random.Generator, sc: Scene, n_cases: int, scale=2.0, n
         draws = rng.integers(0, 2 ** 32, size=ndraws, dtype=np.uint64).astype(np.uint32)
         cases.append((mol, disp, draws))
     return cases
+
+
+def engine_from_scene(sc: Scene, precision="fp64", seed=1, capacity=0):
+    """GPU engine holding the scene's mesh, reactions and molecules (ids = scene order)."""
+    from mcell_gb300._native import Engine
+    nsp = len(sc.space_steps)
+    e = Engine(precision, sc.origin, sc.partition_edge, sc.nsub, sc.rxn_radius, nsp, seed=seed, capacity=capacity)
+    e.set_species(sc.space_steps)
+    e.upload_mesh(sc.verts, sc.tris, sc.wall_class.reshape(len(sc.tris), nsp))
+    for (a, b), p in zip(np.asarray(sc.rxn_ab).reshape(-1, 2), sc.rxn_p):
+        e.add_bimol_rxn(int(a), int(b), float(p))
+    e.add_molecules(sc.mol_pos, sc.mol_species)
+    e.prepare()
+    return e
+
+
+def edge_cases(sc: Scene):
+    """Hand-made cases for the closed cube of edge 100 internal units (create_box order):
+    hits on a face diagonal (REDO), a cube vertex, a cube edge, a molecule on a wall
+    plane moving along it and away from it, corner multi-bounces."""
+    P = [
+        ((40.0, 10.0, 10.0), (20.0, 0.0, 0.0)),     # x=+50 face, on the y==z diagonal
+        ((40.0, 40.0, 40.0), (20.0, 20.0, 20.0)),   # straight into the (50,50,50) vertex
+        ((40.0, 40.0, 0.0), (20.0, 20.0, 0.0)),     # into the x=y=50 edge
+        ((-40.0, 5.0, -5.0), (-20.0, 0.0, 0.0)),    # x=-50 face
+        ((0.0, 0.0, 49.0), (0.0, 0.0, 3.0)),        # z=+50 face, perpendicular
+        ((45.0, 45.0, 45.0), (15.0, 12.0, 9.0)),    # corner, several reflections
+        ((-45.0, -45.0, 45.0), (-30.0, -25.0, 20.0)),
+        ((0.0, 0.0, 0.0), (170.0, 130.0, 110.0)),   # long ray, many reflections
+        ((10.0, -20.0, 30.0), (1e-3, 2e-3, -1e-3)), # tiny step
+        ((49.999999, 1.0, 2.0), (0.5, 0.1, 0.0)),   # starts just below the wall
+        ((-30.0, 20.0, 49.0), (0.0, 0.0, 1.0)),     # lands exactly on the wall plane
+    ]
+    return P
+
+
+GOLDEN = ROOT / "tests" / "golden"
+GOLDEN_SCENES = ["cube", "cube_dense", "cube_classes", "sphere"]
+
+
+def load_golden(name):
+    """(Scene, cases dict) of a golden fixture made by tests/golden/make_golden.py."""
+    z = np.load(GOLDEN / f"diffuse_{name}.npz")
+    sc = Scene(z["origin"], float(z["partition_edge"]), int(z["nsub"]), float(z["rxn_radius"]), z["verts"],
+               z["tris"], z["space_steps"], z["wall_class"], z["rxn_ab"], z["rxn_p"], z["mol_pos"],
+               z["mol_species"])
+    return sc, {k: z[k] for k in ("mols", "disps", "draws", "results", "info", "wall_consts", "wsp_counts",
+                                  "wsp_list")}
+
+
+def compare_results(got, want, rel=0.0, label=""):
+    """Compares case results: integer fields exactly; times / positions exactly (rel=0)
+    or within a relative tolerance. Returns the list of mismatching case indices."""
+    bad = []
+    k = want.shape[1]
+    for c in range(len(want)):
+        g, w = got[c, :k], want[c, :k]
+        n = int(w[6])
+        ints = [0, 4, 5, 6] + [RES_HDR + e * EV_SIZE + f for e in range(min(n, EV_MAX)) for f in (0, 1, 2)]
+        if not np.array_equal(g[ints], w[ints]):
+            bad.append(c)
+            continue
+        fl = [i for i in range(k) if i not in ints]
+        if rel == 0.0:
+            ok = np.array_equal(g[fl], w[fl])
+        else:
+            ok = np.allclose(g[fl], w[fl], rtol=rel, atol=rel)
+        if not ok:
+            bad.append(c)
+    return bad
+
+
+# ------------------------------------------------------------------ engines with chemistry
+
+class OracleEngine:
+    def __init__(self, **kw):
+        self.lib = oracle().lib
+        self.lib.orc_engine_new.restype = ctypes.c_void_p
+        self.lib.orc_engine_num_live.restype = ctypes.c_uint64
+        self.lib.orc_engine_mol_steps.restype = ctypes.c_uint64
+        self.lib.orc_engine_molecules.restype = ctypes.c_uint64
+        self.keep = []
+        d = OrcDesc()
+        for k, v in kw.items():
+            if isinstance(v, np.ndarray):
+                self.keep.append(v)
+                setattr(d, k, v.ctypes.data_as(ctypes.c_void_p))
+            else:
+                setattr(d, k, v)
+        self.d = d
+        self.h = ctypes.c_void_p(self.lib.orc_engine_new(ctypes.byref(d)))
+        self.nsp = kw["nspecies"]
+
+    def run(self, n):
+        out = np.zeros((n, self.nsp), np.uint64)
+        rc = self.lib.orc_engine_run(self.h, ctypes.c_uint(n), ptr(out))
+        assert rc == 0
+        return out
+
+    def molecules(self):
+        n = self.lib.orc_engine_num_live(self.h)
+        pos = np.zeros((n, 3))
+        sp = np.zeros(n, np.uint32)
+        self.lib.orc_engine_molecules(self.h, ctypes.c_uint64(n), ptr(pos), ptr(sp))
+        return pos, sp
+
+    def __del__(self):
+        self.lib.orc_engine_free(self.h)
+
+
+vp = ctypes.c_void_p
+
+
+class OrcDesc(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_double * 3), ("partition_edge", ctypes.c_double), ("nsub", ctypes.c_uint),
+                ("rxn_radius", ctypes.c_double), ("nv", ctypes.c_uint), ("verts", vp), ("nw", ctypes.c_uint),
+                ("tris", vp), ("nspecies", ctypes.c_uint), ("space_steps", vp), ("wall_class", vp),
+                ("nbimol", ctypes.c_uint), ("bimol_reactants", vp), ("bimol_p", vp), ("bimol_products", vp),
+                ("nunimol", ctypes.c_uint), ("unimol_reactant", vp), ("unimol_k", vp), ("unimol_products", vp),
+                ("nmol", ctypes.c_uint), ("mol_pos", vp), ("mol_species", vp), ("seed", ctypes.c_uint64)]
+
+
+def make_oracle_engine(sc: Scene, bimol=(), unimol=(), seed=1):
+    """bimol: [(a, b, p, (p0, p1))], unimol: [(a, k, (p0, p1))]"""
+    nsp = len(sc.space_steps)
+    kw = dict(origin=(ctypes.c_double * 3)(*sc.origin), partition_edge=sc.partition_edge, nsub=sc.nsub,
+              rxn_radius=sc.rxn_radius, nv=len(sc.verts), verts=np.ascontiguousarray(sc.verts, np.float64),
+              nw=len(sc.tris), tris=np.ascontiguousarray(sc.tris, np.uint32), nspecies=nsp,
+              space_steps=np.ascontiguousarray(sc.space_steps, np.float64),
+              wall_class=np.ascontiguousarray(sc.wall_class, np.uint8),
+              nbimol=len(bimol),
+              bimol_reactants=np.array([[b[0], b[1]] for b in bimol] or [[0, 0]], np.uint32),
+              bimol_p=np.array([b[2] for b in bimol] or [0.0]),
+              bimol_products=np.array([list(b[3]) for b in bimol] or [[-1, -1]], np.int32),
+              nunimol=len(unimol),
+              unimol_reactant=np.array([u[0] for u in unimol] or [0], np.uint32),
+              unimol_k=np.array([u[1] for u in unimol] or [0.0]),
+              unimol_products=np.array([list(u[2]) for u in unimol] or [[-1, -1]], np.int32),
+              nmol=len(sc.mol_species), mol_pos=np.ascontiguousarray(sc.mol_pos, np.float64),
+              mol_species=np.ascontiguousarray(sc.mol_species, np.uint32), seed=seed)
+    return OracleEngine(**kw)
+
+
+
+
+def make_gpu_engine(sc: Scene, precision="fp64", bimol=(), unimol=(), seed=1, capacity=0):
+    """GPU engine with explicit chemistry: bimol [(a, b, p, (p0, p1))], unimol [(a, k, (p0, p1))]."""
+    from mcell_gb300._native import Engine
+    nsp = len(sc.space_steps)
+    e = Engine(precision, sc.origin, sc.partition_edge, sc.nsub, sc.rxn_radius, nsp, seed=seed, capacity=capacity)
+    e.set_species(sc.space_steps)
+    e.upload_mesh(sc.verts, sc.tris, np.asarray(sc.wall_class).reshape(len(sc.tris), nsp))
+    for a, b, p, pr in bimol:
+        e.add_bimol_rxn(a, b, p, pr)
+    for a, k, pr in unimol:
+        e.add_unimol_rxn(a, k, pr)
+    e.add_molecules(sc.mol_pos, sc.mol_species)
+    e.prepare()
+    return e

@@ -1,0 +1,70 @@
+"""CPU tests of the drop-in boundary: the library builds, loads and exports every
+entry point include/mcell_gb300.h declares; host-side argument checks work
+without a GPU; and the product path fails loudly (no CPU fallback) when no
+device is present."""
+import re
+
+import numpy as np
+import pytest
+
+from tests import harness as H
+from mcell_gb300 import _native
+
+
+def declared_symbols():
+    text = (H.ROOT / "include" / "mcell_gb300.h").read_text()
+    return sorted(set(re.findall(r"\b(mcg_[a-z_]+)\s*\(", text)))
+
+
+def test_header_and_binding_agree():
+    assert declared_symbols() == sorted(_native.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol():
+    L = _native.lib()
+    for name in declared_symbols():
+        assert hasattr(L, name), name
+
+
+def test_config_validation():
+    with pytest.raises(_native.EngineError):
+        _native.Engine("fp64", (0, 0, 0), 100.0, 0, 0.56, 3)        # no subpartitions
+    with pytest.raises(_native.EngineError):
+        _native.Engine("fp64", (0, 0, 0), 100.0, 301, 0.56, 3)      # over MAX_SUBPARTS_PER_PARTITION
+    with pytest.raises(_native.EngineError):
+        _native.Engine("fp64", (0, 0, 0), 100.0, 10, 0.56, 17)      # too many species
+    e = _native.Engine("fp64", (-60, -60, -60), 120.0, 12, 0.5642, 3)
+    with pytest.raises(_native.EngineError):
+        e.set_species([2.0, 2.0])                                   # count mismatch
+    e.set_species([2.0, 2.0, 1.41])
+    with pytest.raises(_native.EngineError):
+        e.add_bimol_rxn(0, 5, 0.1)                                  # bad species
+    e.add_bimol_rxn(0, 1, 0.0368, (2, -1))
+    with pytest.raises(_native.EngineError):
+        e.add_bimol_rxn(1, 0, 0.1)                                  # second class for the same pair
+    with pytest.raises(_native.EngineError):
+        e.add_molecules(np.zeros((1, 3)), np.array([7]))
+
+
+def test_host_setup_matches_oracle_without_gpu():
+    """Wall constants and wall lists come from host code and must equal the oracle's
+    (which equal the reference's, see test_oracle)."""
+    for name in H.GOLDEN_SCENES:
+        sc, g = H.load_golden(name)
+        nsp = len(sc.space_steps)
+        e = _native.Engine("fp64", sc.origin, sc.partition_edge, sc.nsub, sc.rxn_radius, nsp)
+        e.set_species(sc.space_steps)
+        e.upload_mesh(sc.verts, sc.tris, sc.wall_class.reshape(len(sc.tris), nsp))
+        assert np.array_equal(e.wall_consts(len(sc.tris)), g["wall_consts"]), name
+        counts, lst = e.walls_in_subparts(sc.nsub ** 3)
+        assert np.array_equal(counts, g["wsp_counts"]) and np.array_equal(lst, g["wsp_list"]), name
+
+
+def test_fails_loudly_without_device():
+    import torch  # only to ask whether a device exists
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    sc = H.cube_scene(np.random.default_rng(0), n_mol=10)
+    with pytest.raises(_native.EngineError) as ei:
+        H.engine_from_scene(sc)
+    assert ei.value.code == -2  # MCG_ERR_CUDA, no silent fallback

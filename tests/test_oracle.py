@@ -1,0 +1,99 @@
+"""CPU tests: the oracle port against the reference's own routines.
+
+1. against the golden fixtures (made from the reference routines by
+   tests/golden/make_golden.py; these run everywhere),
+2. against the reference routines directly on fresh random cases (only where
+   oracle/_ref was built from the reference sources),
+3. the oracle's serial engine against closed forms (diffusion, unimolecular
+   decay, conservation), which also pins the rate -> probability conversion.
+"""
+import numpy as np
+import pytest
+
+from tests import harness as H
+from mcell_gb300 import conversion
+
+
+@pytest.mark.parametrize("name", H.GOLDEN_SCENES)
+def test_oracle_matches_golden(name):
+    sc, g = H.load_golden(name)
+    orc = H.oracle().scene(sc)
+    assert np.array_equal(orc.info(), g["info"])
+    assert np.array_equal(orc.wall_consts(len(sc.tris)), g["wall_consts"]), "wall constants differ"
+    counts, lst = orc.walls_in_subparts(sc.nsub ** 3)
+    assert np.array_equal(counts, g["wsp_counts"]) and np.array_equal(lst, g["wsp_list"]), "wall binning differs"
+    got = np.array([orc.diffuse_case(int(m), d, dr) for m, d, dr in zip(g["mols"], g["disps"], g["draws"])])
+    bad = H.compare_results(got, g["results"], rel=0.0)
+    # exact_disk with 2+ occluding edges uses an angular sweep here, so allow 1e-9 there
+    bad = [c for c in bad if H.compare_results(got[c:c + 1], g["results"][c:c + 1], rel=1e-9)]
+    assert not bad, f"{len(bad)} cases differ, first {bad[:5]}"
+
+
+def test_reaction_tests_match_golden():
+    z = np.load(H.GOLDEN / "rxn_tests.npz")
+    orc = H.oracle()
+    tb = np.array([orc.test_bimolecular(p, s, u) for p, s, u in zip(z["P"], z["S"], z["U"])])
+    # the reference returns the pathway (0) or PATHWAY_INDEX_NO_RXN (< 0)
+    assert np.array_equal(tb >= 0, z["bimol"] >= 0)
+    tu = np.array([orc.time_of_unimol(k, u) for k, u in zip(z["K"], z["Uu"])])
+    assert np.array_equal(tu, z["unimol"])
+
+
+REF = H.reference(64)
+
+
+@pytest.mark.skipif(REF is None, reason="reference routines not built here (no reference sources)")
+@pytest.mark.parametrize("seed", [11, 12])
+def test_oracle_matches_reference_random(seed):
+    rng = np.random.default_rng(seed)
+    for sc in [H.cube_scene(rng, n_mol=1500, p_rxn=0.3),
+               H.sphere_in_cube_scene(rng, levels=3, n_mol=2000, radius_um=0.6, cube_um=1.5, p_rxn=0.3)]:
+        o, r = H.oracle().scene(sc), REF.scene(sc)
+        assert np.array_equal(o.wall_consts(len(sc.tris)), r.wall_consts(len(sc.tris)))
+        n3 = sc.nsub ** 3
+        co, lo = o.walls_in_subparts(n3)
+        cr, lr = r.walls_in_subparts(n3)
+        assert np.array_equal(co, cr) and np.array_equal(lo, lr)
+        bad = 0
+        for m, d, dr in H.random_cases(rng, sc, 800, scale=3.0, near_wall_frac=0.5):
+            a, b = o.diffuse_case(m, d, dr), r.diffuse_case(m, d, dr)
+            if not np.array_equal(a, b) and H.compare_results(a[None], b[None], rel=1e-9):
+                bad += 1
+        assert bad == 0
+
+
+# ---------------------------------------------------------------- serial engine closed forms
+
+def test_oracle_engine_conserves_and_confines():
+    rng = np.random.default_rng(3)
+    sc = H.cube_scene(rng, n_mol=500)
+    e = H.make_oracle_engine(sc)
+    counts = e.run(50)
+    assert (counts.sum(1) == 500).all()
+    pos, _ = e.molecules()
+    assert (np.abs(pos) <= 50).all()
+
+
+def test_oracle_engine_unimolecular_decay():
+    rng = np.random.default_rng(4)
+    sc = H.cube_scene(rng, n_mol=4000)
+    sc.mol_species[:] = 2
+    k = 1e-2
+    e = H.make_oracle_engine(sc, unimol=[(2, k, (-1, -1))])
+    counts = e.run(100)
+    n = counts[:, 2].astype(float)
+    t = np.arange(1, 101)
+    expect = 4000 * np.exp(-k * t)
+    assert np.all(np.abs(n - expect) < 5 * np.sqrt(expect * (1 - np.exp(-k * t))) + 1)
+
+
+def test_space_step_and_probability_conversions():
+    lu = conversion.length_unit_um()
+    assert lu == 0.01
+    assert abs(conversion.space_step(1e-6, 1e-6, lu) - 2.0) < 1e-12
+    R = conversion.default_rxn_radius_um()
+    p = conversion.bimol_probability(1e8, 2.0, 2.0, R, 1e-6, lu)
+    assert abs(p - 0.0368) < 5e-4
+    lay = conversion.partition_layout([-0.5] * 3, [0.5] * 3, partition_dimension_um=1.2,
+                                      subpartition_dimension_um=0.1)
+    assert lay.nsub == 12 and abs(lay.edge - 120) < 1e-9 and abs(lay.origin[0] + 60) < 1e-9
