@@ -1,0 +1,314 @@
+#!/usr/bin/env python3
+"""Benchmark of the volume-molecule diffuse-react step on one GB300.
+
+Workload (one step = one iteration of the whole model): an icosphere of radius
+1 um with 20,480 triangles, transparent to A and reflective to B and C, centred
+in a reflective 2.5 um cube (20,492 walls); 1,000,000 molecules, A:B 1:1
+uniform in the cube; D = 1e-6 cm^2/s (C: 5e-7); A + B -> C at 1e8 M^-1 s^-1;
+C -> 0 at 1e3 s^-1; dt = 1 us; fp32 positions; subpartitions of 0.1 um.
+Synthetic, seeded inputs (no dataset exists for this configuration).
+
+Metric: molecule-steps/s = live volume molecules at the start of each step,
+summed over the timed steps, over the device time of those steps.
+  value  device time (CUDA events on the engine's stream) per step, with the L2
+         flushed (a 512 MB write) before every timed step
+  e2e    the same metric through the C ABI with host buffers: the molecule
+         upload from host memory and, every step, mcg_step + a device-to-host
+         read of the species counts, timed on the host
+Arms:
+  default            the CUDA engine (mcell_gb300)
+  --impl reference   the reference algorithm on the host cores: the oracle's
+                     serial engine (a restatement of MCell4's step; the
+                     reference itself cannot be built), one seeded process per
+                     core as MCell4 is single-threaded
+Multi-GPU: replicas only (independent models per rank, no collectives).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "molecule-steps/s @1M mols,20k tris; batched/served vs plain GPU; p50/p99 latency"
+UNIT = "molecule-steps/s"
+ALG_BYTES_PER_MOL_STEP = 32  # read a 16 B record + write a 16 B record
+
+
+def _rank_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ---------------------------------------------------------------- CPU (oracle) leg
+
+def _cpu_worker(args):
+    n_mol, iters, seed = args
+    from mcell_gb300 import workloads
+    from oracle.oracle_py import oracle_engine_for_model
+
+    m = workloads.sphere_in_cube(n_mol=n_mol, seed=seed)
+    e = oracle_engine_for_model(m, seed=seed)
+    t0 = time.perf_counter()
+    e.run(iters)
+    dt = time.perf_counter() - t0
+    steps = e.lib.orc_engine_mol_steps(e.h)
+    return steps, dt
+
+
+def cpu_measure(procs, n_mol, iters, pool=None):
+    """Aggregate mol-steps/s of `procs` independent seeded processes (spawned)."""
+    args = [(n_mol, iters, 1000 + k) for k in range(procs)]
+    if pool is None:
+        with mp.get_context("spawn").Pool(procs) as p:
+            res = p.map(_cpu_worker, args)
+    else:
+        res = pool.map(_cpu_worker, args)
+    rate = sum(s / dt for s, dt in res)
+    return rate, res
+
+
+def _ensure_oracle_built():
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+
+
+# ---------------------------------------------------------------- clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.idx = gpu_index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        mx = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- GPU leg
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic_per_mol_step():
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("k_diffuse_dram_bytes_per_mol_step")
+    return None
+
+
+def run_gpu(args, rank, world):
+    import numpy as np
+    import torch
+
+    from mcell_gb300 import workloads
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    # replicas: every rank simulates its own seeded model
+    model = workloads.sphere_in_cube(n_mol=args.n_mol, seed=1 + rank)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    e = workloads.engine_for(model, "fp32", seed=7 + rank)
+    e.set_options(use_graphs=True, profile=True)
+    for _ in range(args.warmup):
+        e.step(1)
+    e.sync()
+    e.profile()
+    _, ms0, l0 = e.stats()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    prof = np.zeros(6)
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            flush.zero_()  # L2 flush between timed steps (legacy stream, ordered before the engine stream)
+            e.step(1)
+            e.sync()
+            prof += e.profile()
+    torch.cuda.synchronize()
+    _, ms1, l1 = e.stats()
+    clocks = clk.summary()
+    mol_steps = ms1 - ms0
+    iter_ms = prof[0]
+    t = torch.tensor([iter_ms], dtype=torch.float64, device="cuda")
+    steps_t = torch.tensor([float(mol_steps)], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(steps_t, op=torch.distributed.ReduceOp.SUM)
+    value = steps_t.item() / (t.item() / 1e3)
+    diffuse_ms_per_launch = prof[1] / args.steps
+    mols_per_launch = mol_steps / args.steps
+    achieved = ALG_BYTES_PER_MOL_STEP * mols_per_launch / (diffuse_ms_per_launch / 1e3) / 1e9
+    peak, peak_kind = _peaks()
+    tpm = _traffic_per_mol_step()
+    # graph-replay throughput without flushes (steady state, informative)
+    e.set_options(use_graphs=True, profile=False)
+    e.sync()
+    _, a0, _ = e.stats()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e.step(args.steps if args.steps % 2 == 0 else args.steps + 1)
+    e.sync()
+    graph_s = time.perf_counter() - t0
+    _, a1, _ = e.stats()
+    graph_rate = (a1 - a0) / graph_s
+    e.close()
+
+    # end to end through the C ABI, host buffers in and out
+    e2 = workloads.engine_for(model, "fp32", seed=7 + rank, with_molecules=False)
+    pos = np.ascontiguousarray(model.pos, np.float64)
+    sp = np.ascontiguousarray(model.species, np.uint32)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2.add_molecules(pos, sp)
+    counts = None
+    for _ in range(args.steps):
+        e2.step(1)
+        counts = e2.counts()
+    e2_s = time.perf_counter() - t0
+    _, e2_steps, _ = e2.stats()
+    e2.close()
+    e2e_t = torch.tensor([e2_s], dtype=torch.float64, device="cuda")
+    e2e_n = torch.tensor([float(e2_steps)], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(e2e_n, op=torch.distributed.ReduceOp.SUM)
+    h2d = pos.nbytes + sp.nbytes
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t.item() / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded uniform release; icosphere + cube mesh generated)",
+        "config": {"workload": "sphere_in_cube: icosphere r=1um 20480 tris transparent to A in a 2.5um "
+                               "reflective cube, 1M molecules A:B 1:1, A+B->C 1e8/M/s, C->0 1e3/s, dt=1us",
+                   "molecules": args.n_mol, "walls": int(len(model.walls)), "subparts_per_edge": int(model.nsub),
+                   "precision": "fp32 positions", "parallelism": f"replicas x{world}",
+                   "l2": "flushed (512 MB write) before every timed step"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "kernel": "k_diffuse",
+                     "algorithmic_bytes_per_mol_step": ALG_BYTES_PER_MOL_STEP,
+                     "traffic": (tpm * mols_per_launch) if tpm else None},
+        "e2e": {"value": e2e_n.item() / e2e_t.item(), "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
+                "d2h_bytes_per_step": 8 * model.n_species},
+        "gpu_launches": int(l1 - l0),
+        "clocks": clocks,
+        "kernel_ms_per_step": {"diffuse": prof[1] / args.steps, "reactions": prof[2] / args.steps,
+                               "products": prof[3] / args.steps, "sort": prof[4] / args.steps},
+        "graph_replay_value": graph_rate,
+        "final_counts": [int(x) for x in counts] if counts is not None else None,
+    }
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n-mol", type=int, default=1_000_000)
+    ap.add_argument("--cpu-procs", type=int, default=0, help="CPU processes (0 = all host cores)")
+    ap.add_argument("--cpu-iters", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, _ = _rank_env()
+    procs = args.cpu_procs or os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        _ensure_oracle_built()
+        # each step: one iteration of the full model on every host core (independent seeds)
+        with mp.get_context("spawn").Pool(procs) as pool:
+            rate_w, _ = cpu_measure(procs, args.n_mol, 1, pool)  # warm-up pass (setup + first iteration)
+            t_all, steps_all = 0.0, 0
+            for _ in range(max(1, min(args.steps, 3))):
+                r, res = cpu_measure(procs, args.n_mol, args.cpu_iters, pool)
+                steps_all += sum(s for s, _ in res)
+                t_all += max(dt for _, dt in res)
+        value = steps_all / t_all
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "sphere_in_cube, 1M molecules (see the GPU arm)", "molecules": args.n_mol},
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
+                                 "sample": f"{procs} processes x {args.cpu_iters} iterations of the 1M-molecule model "
+                                           f"per step, up to 3 steps"},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    # our arm: CPU baseline first (spawned processes, before any GPU call)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        _ensure_oracle_built()
+        rate, res = cpu_measure(procs, args.n_mol, args.cpu_iters)
+        cpu = {"value": rate, "unit": UNIT, "cores": procs, "kind": "port",
+               "sample": f"{procs} independent seeded processes x {args.cpu_iters} iterations of the "
+                         f"1M-molecule model (oracle serial engine, fp64)"}
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    line = run_gpu(args, rank, world)
+    if rank == 0:
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -103,6 +103,14 @@ int mcg_download_molecules(mcg_engine* e, uint64_t cap, double* pos, uint32_t* s
 /* Iterations run, molecule-steps run, and a device status word. */
 int mcg_get_stats(mcg_engine* e, uint64_t* iterations, uint64_t* mol_steps, uint64_t* launches);
 
+/* Execution options: use_graphs (replay blocks of two iterations from CUDA graphs,
+   default on) and profile (record CUDA events around the kernel groups of each
+   iteration; implies no graphs). */
+int mcg_set_options(mcg_engine* e, int use_graphs, int profile);
+/* Profile since the last call: out[0] iteration ms, [1] diffuse kernel ms, [2] reaction
+   resolution ms, [3] products ms, [4] sort (scan + scatter) ms, [5] iterations profiled. */
+int mcg_get_profile(mcg_engine* e, double* out);
+
 /* Per-routine parity harness: one diffusion of a chosen molecule per case with
    the displacement and the random draws injected, through the same device
    functions the step uses (ray_trace_vol + the collision loop of

@@ -24,7 +24,7 @@ EXPORTS = [
     "mcg_create", "mcg_destroy", "mcg_last_error", "mcg_set_species", "mcg_upload_mesh", "mcg_add_bimol_rxn",
     "mcg_add_unimol_rxn", "mcg_add_molecules", "mcg_step", "mcg_sync", "mcg_get_counts",
     "mcg_get_count_trajectory", "mcg_download_molecules", "mcg_get_stats", "mcg_prepare", "mcg_trace_cases",
-    "mcg_wall_consts", "mcg_walls_in_subparts",
+    "mcg_wall_consts", "mcg_walls_in_subparts", "mcg_set_options", "mcg_get_profile",
 ]
 
 
@@ -168,6 +168,15 @@ class Engine:
         it, ms, ln = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
         self._chk(lib().mcg_get_stats(self.h, ctypes.byref(it), ctypes.byref(ms), ctypes.byref(ln)))
         return it.value, ms.value, ln.value
+
+    def set_options(self, use_graphs=True, profile=False):
+        self._chk(lib().mcg_set_options(self.h, ctypes.c_int(int(use_graphs)), ctypes.c_int(int(profile))))
+
+    def profile(self):
+        """ms since the last call: iteration, diffuse, reactions, products, sort; iterations profiled"""
+        out = np.zeros(6)
+        self._chk(lib().mcg_get_profile(self.h, _p(out)))
+        return out
 
     def trace_cases(self, ids, disp, draws, r_rate_factor=None, t_steps=None):
         ids = np.ascontiguousarray(ids, np.uint64)

@@ -224,6 +224,21 @@ int mcg_get_stats(mcg_engine* e, uint64_t* iterations, uint64_t* mol_steps, uint
   return MCG_OK;
 }
 
+int mcg_set_options(mcg_engine* e, int use_graphs, int profile) {
+  if (!e) return MCG_ERR_ARG;
+  int rc = prepare(e);
+  if (rc) return rc;
+  e->dev->set_options(use_graphs, profile);
+  return MCG_OK;
+}
+
+int mcg_get_profile(mcg_engine* e, double* out) {
+  if (!e || !out || !e->dev) return MCG_ERR_ARG;
+  std::string err;
+  int rc = e->dev->profile(out, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
 int mcg_trace_cases(mcg_engine* e, uint32_t n, const uint64_t* ids, const double* disp, const uint32_t* draws,
                     uint32_t draws_per_case, const double* rrf, const double* tst, double* out) {
   if (!e || (n && (!ids || !disp || !rrf || !tst || !out))) return MCG_ERR_ARG;

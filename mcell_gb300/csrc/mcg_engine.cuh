@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cstring>
 #include <unordered_map>
 
@@ -197,7 +198,7 @@ class DeviceEngineT : public DeviceEngine {
     }
     uint32_t done = 0;
     while (done < n) {
-      if (n - done >= 2 && use_graphs_) {
+      if (n - done >= 2 && use_graphs_ && !profile_) {
         cudaGraphExec_t& ge = graph_[parity_];
         if (!ge) {
           if (capture(parity_, err)) return -2;
@@ -206,7 +207,7 @@ class DeviceEngineT : public DeviceEngine {
         launches_ += 2 * kernels_per_iteration_;
         done += 2;  // two iterations return to the same parity
       } else {
-        launch_iteration(state(parity_));
+        launch_iteration(state(parity_), profile_);
         MCG_CUDA(cudaGetLastError());
         parity_ ^= 1;
         done += 1;
@@ -225,6 +226,14 @@ class DeviceEngineT : public DeviceEngine {
   int counts(uint64_t* out, std::string& err) override {
     int rc = sync(err);
     if (rc) return rc;
+    if (cnt_.iteration > 0) {
+      // species counts of the last finished iteration, accumulated by k_scatter
+      const uint64_t row = (cnt_.iteration - 1) % traj_cap_;
+      std::vector<unsigned long long> h(nsp_);
+      MCG_CUDA(cudaMemcpy(h.data(), d_traj_ + row * nsp_, sizeof(unsigned long long) * nsp_, cudaMemcpyDeviceToHost));
+      for (uint32_t a = 0; a < nsp_; a++) out[a] = h[a];
+      return 0;
+    }
     std::vector<uint32_t> st(nkeys_ + 1);
     MCG_CUDA(cudaMemcpy(st.data(), state(parity_).start, sizeof(uint32_t) * (nkeys_ + 1), cudaMemcpyDeviceToHost));
     for (uint32_t a = 0; a < nsp_; a++) out[a] = 0;
@@ -325,6 +334,33 @@ class DeviceEngineT : public DeviceEngine {
     cudaFree(d_tst);
     cudaFree(d_out);
     cudaFree(d_draws);
+    return 0;
+  }
+
+  void set_options(int use_graphs, int profile) override {
+    use_graphs_ = use_graphs != 0;
+    profile_ = profile != 0;
+  }
+
+  int profile(double* out, std::string& err) override {
+    MCG_CUDA(cudaStreamSynchronize(stream_));
+    for (int k = 0; k < 6; k++) out[k] = 0;
+    for (auto& ev : prof_) {
+      float ms;
+      MCG_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[4]));
+      out[0] += ms;
+      MCG_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+      out[1] += ms;
+      MCG_CUDA(cudaEventElapsedTime(&ms, ev[1], ev[2]));
+      out[2] += ms;
+      MCG_CUDA(cudaEventElapsedTime(&ms, ev[2], ev[3]));
+      out[3] += ms;
+      MCG_CUDA(cudaEventElapsedTime(&ms, ev[3], ev[4]));
+      out[4] += ms;
+      for (int k = 0; k < 5; k++) cudaEventDestroy(ev[k]);
+    }
+    out[5] = (double)prof_.size();
+    prof_.clear();
     return 0;
   }
 
@@ -441,24 +477,37 @@ class DeviceEngineT : public DeviceEngine {
     return s;
   }
 
-  void launch_iteration(const State<T>& s) {
+  // records an event on the engine stream when profiling (not during graph capture)
+  void mark(int k, bool prof) {
+    if (!prof) return;
+    if (k == 0) prof_.emplace_back();
+    cudaEventCreate(&prof_.back()[k]);
+    cudaEventRecord(prof_.back()[k], stream_);
+  }
+
+  void launch_iteration(const State<T>& s, bool prof = false) {
     const unsigned g = grid(cap_);
     const unsigned gs = (unsigned)std::max(1, sms_);
+    mark(0, prof);
     k_diffuse<T><<<g, TPB, 0, stream_>>>(s);
+    mark(1, prof);
     k_resolve<T><<<gs, TPB, 0, stream_>>>(s);
     k_collect_losers<T><<<gs, TPB, 0, stream_>>>(s);
     k_reset_claims<T><<<gs, TPB, 0, stream_>>>(s);
     k_redo<T><<<1, TPB, 0, stream_>>>(s);
+    mark(2, prof);
     k_prod_window<T><<<1, 1, 0, stream_>>>(s);
     k_products<T><<<gs, TPB, 0, stream_>>>(s);
     k_prod_window<T><<<1, 1, 0, stream_>>>(s);
     k_products<T><<<gs, TPB, 0, stream_>>>(s);
     k_prod_window<T><<<1, 1, 0, stream_>>>(s);
+    mark(3, prof);
     k_scan_tiles<T><<<ntiles_, TPB, 0, stream_>>>(s);
     k_scan_top<T><<<1, TPB, 0, stream_>>>(s, ntiles_);
     k_scan_apply<T><<<ntiles_, TPB, 0, stream_>>>(s);
     k_scatter<T><<<g, TPB, 0, stream_>>>(s, 1, 1);
     k_end<T><<<1, 1, 0, stream_>>>(s);
+    mark(4, prof);
     launches_ += kernels_per_iteration_;
   }
 
@@ -517,6 +566,8 @@ class DeviceEngineT : public DeviceEngine {
   int sms_ = 1;
   int parity_ = 0;
   bool use_graphs_ = true;
+  bool profile_ = false;
+  std::vector<std::array<cudaEvent_t, 5>> prof_;
   cudaGraphExec_t graph_[2] = {nullptr, nullptr};
   uint32_t nsp_ = 0, nw_ = 0, nkeys_ = 0, ntiles_ = 0, traj_cap_ = 65536;
   uint64_t cap_ = 0, iterations_ = 0, launches_ = 0;

@@ -30,8 +30,8 @@ def test_fp64_matches_reference_golden(name):
     sc, g = H.load_golden(name)
     e = H.engine_from_scene(sc, "fp64")
     got = _trace(e, sc, g["mols"], g["disps"], g["draws"])
-    bad = H.compare_results(got, g["results"], rel=0.0)
-    hard = [c for c in bad if H.compare_results(got[c:c + 1], g["results"][c:c + 1], rel=1e-9)]
+    bad = H.compare_results(got, g["results"], rel=0.0, scene=sc)
+    hard = [c for c in bad if H.compare_results(got[c:c + 1], g["results"][c:c + 1], rel=1e-9, scene=sc)]
     assert not hard, f"{len(hard)} of {len(got)} cases differ from the reference routines: {hard[:5]}"
     assert len(bad) <= len(got) // 100
 
@@ -50,8 +50,8 @@ def test_fp64_matches_oracle_random(seed):
         got = _trace(e, sc, mols, disps, draws)
         orc = H.oracle().scene(sc)
         want = np.array([orc.diffuse_case(m, d, dr) for m, d, dr in zip(mols, disps, draws)])
-        bad = H.compare_results(got, want, rel=0.0)
-        hard = [c for c in bad if H.compare_results(got[c:c + 1], want[c:c + 1], rel=1e-9)]
+        bad = H.compare_results(got, want, rel=0.0, scene=sc)
+        hard = [c for c in bad if H.compare_results(got[c:c + 1], want[c:c + 1], rel=1e-9, scene=sc)]
         assert not hard, f"{len(hard)} cases differ: {hard[:5]}"
 
 

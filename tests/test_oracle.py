@@ -23,9 +23,9 @@ def test_oracle_matches_golden(name):
     counts, lst = orc.walls_in_subparts(sc.nsub ** 3)
     assert np.array_equal(counts, g["wsp_counts"]) and np.array_equal(lst, g["wsp_list"]), "wall binning differs"
     got = np.array([orc.diffuse_case(int(m), d, dr) for m, d, dr in zip(g["mols"], g["disps"], g["draws"])])
-    bad = H.compare_results(got, g["results"], rel=0.0)
+    bad = H.compare_results(got, g["results"], rel=0.0, scene=sc)
     # exact_disk with 2+ occluding edges uses an angular sweep here, so allow 1e-9 there
-    bad = [c for c in bad if H.compare_results(got[c:c + 1], g["results"][c:c + 1], rel=1e-9)]
+    bad = [c for c in bad if H.compare_results(got[c:c + 1], g["results"][c:c + 1], rel=1e-9, scene=sc)]
     assert not bad, f"{len(bad)} cases differ, first {bad[:5]}"
 
 
@@ -57,7 +57,7 @@ def test_oracle_matches_reference_random(seed):
         bad = 0
         for m, d, dr in H.random_cases(rng, sc, 800, scale=3.0, near_wall_frac=0.5):
             a, b = o.diffuse_case(m, d, dr), r.diffuse_case(m, d, dr)
-            if not np.array_equal(a, b) and H.compare_results(a[None], b[None], rel=1e-9):
+            if not np.array_equal(a, b) and H.compare_results(a[None], b[None], rel=1e-9, scene=sc):
                 bad += 1
         assert bad == 0
 
