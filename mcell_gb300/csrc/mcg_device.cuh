@@ -1084,6 +1084,22 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
           if (sizeof(T) == 4 && 1.0 - t_reflect < (double)Eps<T>::pos_sqrt) t_reflect -= (double)Eps<T>::pos_sqrt;
           T f = (T)(1.0 - t_reflect);
           remaining = cmul(remaining + cmul(v3<T>(rf, rf, rf), n), v3<T>(f, f, f));
+          if (sizeof(T) == 4) {
+            // fp32 tie-break in fp64: the rounded reflection point must stay on the side the
+            // molecule came from, else a coplanar neighbour triangle can reflect it outwards.
+            // Push it back by a few ulps of its coordinates (~1 pm at 1 um).
+            const double side = hit.type == CT_FRONT ? 1.0 : -1.0;
+            const double ddn = (double)pos.x * (double)rj.x + (double)pos.y * (double)rj.y +
+                               (double)pos.z * (double)rj.z - (double)rj.w;
+            const double margin =
+                8.0 * 1.1920928955078125e-07 *
+                (double)tmax(tmax(tabs(pos.x), tabs(pos.y)), tmax(tabs(pos.z), (T)1));
+            if (ddn * side < margin) {
+              const T push = (T)(side * (margin - ddn * side));
+              pos = pos + scale(n, push);
+              sp = subpart_of(g, pos);
+            }
+          }
           ev.put(1, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
         }
         wall_done = true;
