@@ -111,6 +111,11 @@ int mcg_set_options(mcg_engine* e, int use_graphs, int profile);
    resolution ms, [3] products ms, [4] sort (scan + scatter) ms, [5] iterations profiled. */
 int mcg_get_profile(mcg_engine* e, double* out);
 
+/* Molecules that left the partition (MCG_ERR_ESCAPE): total in *n and up to
+   min(cap, 8) records of 12 doubles: id, species, iteration, start xyz,
+   displacement xyz, final xyz. */
+int mcg_get_escapes(mcg_engine* e, uint32_t cap, double* out, uint32_t* n);
+
 /* Per-routine parity harness: one diffusion of a chosen molecule per case with
    the displacement and the random draws injected, through the same device
    functions the step uses (ray_trace_vol + the collision loop of

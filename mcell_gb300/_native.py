@@ -25,6 +25,7 @@ EXPORTS = [
     "mcg_add_unimol_rxn", "mcg_add_molecules", "mcg_step", "mcg_sync", "mcg_get_counts",
     "mcg_get_count_trajectory", "mcg_download_molecules", "mcg_get_stats", "mcg_prepare", "mcg_trace_cases",
     "mcg_wall_consts", "mcg_walls_in_subparts", "mcg_set_options", "mcg_get_profile",
+    "mcg_get_escapes",
 ]
 
 
@@ -177,6 +178,13 @@ class Engine:
         out = np.zeros(6)
         self._chk(lib().mcg_get_profile(self.h, _p(out)))
         return out
+
+    def escapes(self):
+        out = np.zeros((8, 12))
+        n = ctypes.c_uint32()
+        rc = lib().mcg_get_escapes(self.h, ctypes.c_uint32(8), _p(out), ctypes.byref(n))
+        self._chk(rc)
+        return n.value, out[:min(8, n.value)]
 
     def trace_cases(self, ids, disp, draws, r_rate_factor=None, t_steps=None):
         ids = np.ascontiguousarray(ids, np.uint64)

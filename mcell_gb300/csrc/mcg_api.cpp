@@ -239,6 +239,13 @@ int mcg_get_profile(mcg_engine* e, double* out) {
   return rc ? fail(e, rc, err) : MCG_OK;
 }
 
+int mcg_get_escapes(mcg_engine* e, uint32_t cap, double* out, uint32_t* n) {
+  if (!e || !n || (cap && !out) || !e->dev) return MCG_ERR_ARG;
+  std::string err;
+  int rc = e->dev->escapes(out, cap, n, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
 int mcg_trace_cases(mcg_engine* e, uint32_t n, const uint64_t* ids, const double* disp, const uint32_t* draws,
                     uint32_t draws_per_case, const double* rrf, const double* tst, double* out) {
   if (!e || (n && (!ids || !disp || !rrf || !tst || !out))) return MCG_ERR_ARG;

@@ -429,6 +429,29 @@ __device__ void jump_away_line(V3<T> p, T k, V3<T> A, V3<T> B, V3<T> n, D& draws
   v.z -= tiny * f.z;
 }
 
+enum : int { PT_MISS = 0, PT_PARALLEL = 1, PT_HIT = 2 };
+
+// plane part of collide_wall (collision_utils.inl:659-716): start and end on the same
+// side (with the POS_EPS band) is a miss, a move inside the plane is re-tried,
+// otherwise a = time of the crossing
+template <typename S>
+__device__ __forceinline__ int plane_test(S dd, S dv, S eps, S& a) {
+  S d_eps;
+  if (dd > 0) {
+    d_eps = eps;
+    if (dd < d_eps) d_eps = (S)0.5 * dd;
+    if (dd + dv > d_eps) return PT_MISS;
+  } else {
+    d_eps = -eps;
+    if (dd > d_eps) d_eps = (S)0.5 * dd;
+    if (dd < 0 && dd + dv < d_eps) return PT_MISS;
+  }
+  if (dd == 0) return dv != 0 ? PT_MISS : PT_PARALLEL;
+  a = (S)1.0 / dv;
+  a *= -dd;
+  return PT_HIT;
+}
+
 // collide_wall (collision_utils.inl:629-812)
 template <typename T, class D>
 __device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V3<T>& move, T& ct, V3<T>& cpos) {
@@ -437,26 +460,31 @@ __device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V
   T dp = dot(normal, pos);
   T dv = dot(normal, move);
   T dd = dp - rj.w;
-  T d_eps;
-  if (dd > 0) {
-    d_eps = Eps<T>::pos;
-    if (dd < d_eps) d_eps = (T)0.5 * dd;
-    if (dd + dv > d_eps) return CT_MISS;
-  } else {
-    d_eps = -Eps<T>::pos;
-    if (dd > d_eps) d_eps = (T)0.5 * dd;
-    if (dd < 0 && dd + dv < d_eps) return CT_MISS;
-  }
   T a;
-  if (dd == 0) {
-    if (dv != 0) return CT_MISS;
+  int pt;
+  if (sizeof(T) == 4 && tabs(dd) < (T)1e-2) {
+    // fp32 tie-break: near the plane the fp32 side test can have the wrong sign (its
+    // error grows with the coordinates), letting a molecule moving outwards pass a
+    // reflective wall. The float plane and position are exact in fp64, so the side
+    // test is redone there.
+    const double ddd = ((double)normal.x * (double)pos.x + (double)normal.y * (double)pos.y +
+                        (double)normal.z * (double)pos.z) - (double)rj.w;
+    const double dvd = (double)normal.x * (double)move.x + (double)normal.y * (double)move.y +
+                       (double)normal.z * (double)move.z;
+    double ad = 0;
+    pt = plane_test<double>(ddd, dvd, (double)Eps<T>::pos, ad);
+    a = (T)ad;
+    dv = (T)dvd;
+  } else {
+    pt = plane_test<T>(dd, dv, Eps<T>::pos, a);
+  }
+  if (pt == PT_MISS) return CT_MISS;
+  if (pt == PT_PARALLEL) {
     a = (abs_max_2vec(pos, move) + (T)1.0) * Eps<T>::pos;
     if ((draws.u32() & 1) == 0) a = -a;
     move = move - cmul(v3<T>(a, a, a), normal);
     return CT_REDO;
   }
-  a = (T)1.0 / dv;
-  a *= -dd;
   ct = a;
   cpos = pos + scale(move, a);
   const WallFace<T>& w = g.wface[wi];

@@ -364,6 +364,15 @@ class DeviceEngineT : public DeviceEngine {
     return 0;
   }
 
+  int escapes(double* out, uint32_t cap, uint32_t* n, std::string& err) override {
+    MCG_CUDA(cudaStreamSynchronize(stream_));
+    if (read_counters(err)) return -2;
+    *n = cnt_.n_esc;
+    for (uint32_t k = 0; k < std::min<uint32_t>(std::min<uint32_t>(cap, cnt_.n_esc), 8); k++)
+      for (int q = 0; q < 12; q++) out[k * 12 + q] = cnt_.esc[k][q];
+    return 0;
+  }
+
   void stats(uint64_t* iterations, uint64_t* mol_steps, uint64_t* launches) override {
     std::string e;
     sync(e);

@@ -44,6 +44,9 @@ struct Counters {
   unsigned long long mol_steps;
   unsigned long long warn_coll_overflow;
   unsigned long long warn_set_overflow;
+  // first escapes (diagnostics): uid, species, iteration, start xyz, displacement xyz, final xyz
+  uint32_t n_esc;
+  double esc[8][12];
 };
 
 struct Proposal {
@@ -220,9 +223,10 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
     scl = rate_factor * ch.space_step[species];
   }
   TraceOut<T> r;
+  V3<T> disp = v3<T>(0, 0, 0);
   if (scl != 0.0) {
     V3<T> gz = gauss3<T>(draws);
-    V3<T> disp = v3<T>((T)(scl * (double)gz.x * 0.70710678118654752440), (T)(scl * (double)gz.y * 0.70710678118654752440),
+    disp = v3<T>((T)(scl * (double)gz.x * 0.70710678118654752440), (T)(scl * (double)gz.y * 0.70710678118654752440),
                        (T)(scl * (double)gz.z * 0.70710678118654752440));
     Cells<T> cells;
     cells.pos = s.a_pos;
@@ -258,6 +262,13 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   }
   if (!in_partition(g, r.pos)) {
     err |= ST_ESCAPE;  // the reference stops with a fatal error; here the molecule is dropped
+    uint32_t k = atomicAdd(&s.cnt->n_esc, 1u);
+    if (k < 8) {
+      const double rec_[12] = {(double)uid, (double)species, (double)it, (double)pos.x, (double)pos.y, (double)pos.z,
+                               (double)disp.x, (double)disp.y, (double)disp.z, (double)r.pos.x, (double)r.pos.y,
+                               (double)r.pos.z};
+      for (int q = 0; q < 12; q++) s.cnt->esc[k][q] = rec_[q];
+    }
     return 2;
   }
   P4<T> out;
