@@ -521,6 +521,21 @@ __device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V
   return CT_MISS;
 }
 
+// fp32 tie-break in fp64: puts `pos` on the given side (+1 front, -1 back) of the
+// wall plane by a margin of a few ulps of its coordinates (~1 pm at 1 um) when
+// rounding left it on the plane or on the other side. Returns true if it moved.
+template <typename T>
+__device__ bool keep_side(const P4<T>& rj, double side, V3<T>& pos) {
+  const double ddn = ((double)pos.x * (double)rj.x + (double)pos.y * (double)rj.y + (double)pos.z * (double)rj.z) -
+                     (double)rj.w;
+  const double margin =
+      8.0 * 1.1920928955078125e-07 * (double)tmax(tmax(tabs(pos.x), tabs(pos.y)), tmax(tabs(pos.z), (T)1));
+  if (ddn * side >= margin) return false;
+  const T push = (T)(side * (margin - ddn * side));
+  pos = pos + scale(v3<T>(rj.x, rj.y, rj.z), push);
+  return true;
+}
+
 template <typename T>
 struct WallHit {
   int type;
@@ -1091,6 +1106,10 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
           t_steps *= (1.0 - t_smash);
           if (t_steps < EPS) t_steps = EPS;
           last_hit = hit.wall;
+          // fp32: make sure the crossing point lies on the far side, else the neighbouring
+          // triangle of the crossed edge is hit again at t ~ 0 and re-tried without end
+          if (sizeof(T) == 4 && keep_side(g.wrej[hit.wall], hit.type == CT_FRONT ? -1.0 : 1.0, pos))
+            sp = subpart_of(g, pos);
           ev.put(2, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
         } else if (kind == 2 && test_intersect_absorb(r_rate_factor, draws)) {
           ev.put(3, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
@@ -1112,22 +1131,9 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
           if (sizeof(T) == 4 && 1.0 - t_reflect < (double)Eps<T>::pos_sqrt) t_reflect -= (double)Eps<T>::pos_sqrt;
           T f = (T)(1.0 - t_reflect);
           remaining = cmul(remaining + cmul(v3<T>(rf, rf, rf), n), v3<T>(f, f, f));
-          if (sizeof(T) == 4) {
-            // fp32 tie-break in fp64: the rounded reflection point must stay on the side the
-            // molecule came from, else a coplanar neighbour triangle can reflect it outwards.
-            // Push it back by a few ulps of its coordinates (~1 pm at 1 um).
-            const double side = hit.type == CT_FRONT ? 1.0 : -1.0;
-            const double ddn = (double)pos.x * (double)rj.x + (double)pos.y * (double)rj.y +
-                               (double)pos.z * (double)rj.z - (double)rj.w;
-            const double margin =
-                8.0 * 1.1920928955078125e-07 *
-                (double)tmax(tmax(tabs(pos.x), tabs(pos.y)), tmax(tabs(pos.z), (T)1));
-            if (ddn * side < margin) {
-              const T push = (T)(side * (margin - ddn * side));
-              pos = pos + scale(n, push);
-              sp = subpart_of(g, pos);
-            }
-          }
+          // fp32: the rounded reflection point must stay on the side the molecule came
+          // from, else a coplanar neighbour triangle can reflect it outwards
+          if (sizeof(T) == 4 && keep_side(rj, hit.type == CT_FRONT ? 1.0 : -1.0, pos)) sp = subpart_of(g, pos);
           ev.put(1, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
         }
         wall_done = true;

@@ -260,15 +260,19 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
     unimol_products(s, species, r.pos, tuni, uid, it);
     return 2;
   }
-  if (!in_partition(g, r.pos)) {
-    err |= ST_ESCAPE;  // the reference stops with a fatal error; here the molecule is dropped
+  const bool escaped = !in_partition(g, r.pos);
+  if (escaped || (r.err & ST_WATCHDOG)) {
+    // anomaly log for the host: kind 1 escape, 2 watchdog (field 1 = species + 1000 * kind)
     uint32_t k = atomicAdd(&s.cnt->n_esc, 1u);
     if (k < 8) {
-      const double rec_[12] = {(double)uid, (double)species, (double)it, (double)pos.x, (double)pos.y, (double)pos.z,
-                               (double)disp.x, (double)disp.y, (double)disp.z, (double)r.pos.x, (double)r.pos.y,
-                               (double)r.pos.z};
+      const double rec_[12] = {(double)uid, (double)species + 1000.0 * (escaped ? 1 : 2), (double)it,
+                               (double)pos.x, (double)pos.y, (double)pos.z, (double)disp.x, (double)disp.y,
+                               (double)disp.z, (double)r.pos.x, (double)r.pos.y, (double)r.pos.z};
       for (int q = 0; q < 12; q++) s.cnt->esc[k][q] = rec_[q];
     }
+  }
+  if (escaped) {
+    err |= ST_ESCAPE;  // the reference stops with a fatal error; here the molecule is dropped
     return 2;
   }
   P4<T> out;
