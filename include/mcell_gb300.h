@@ -116,6 +116,12 @@ int mcg_get_profile(mcg_engine* e, double* out);
    displacement xyz, final xyz. */
 int mcg_get_escapes(mcg_engine* e, uint32_t cap, double* out, uint32_t* n);
 
+/* Diagnostics: log every step of one molecule (by id) into a ring of the last 64
+   iterations; each record is 271 doubles: the trace result layout of
+   mcg_trace_cases (slot 5 holds the iteration), then start xyz and displacement xyz. */
+int mcg_debug_molecule(mcg_engine* e, uint64_t id);
+int mcg_get_debug_log(mcg_engine* e, double* out /* [64 * 271] */);
+
 /* Per-routine parity harness: one diffusion of a chosen molecule per case with
    the displacement and the random draws injected, through the same device
    functions the step uses (ray_trace_vol + the collision loop of

@@ -25,7 +25,7 @@ EXPORTS = [
     "mcg_add_unimol_rxn", "mcg_add_molecules", "mcg_step", "mcg_sync", "mcg_get_counts",
     "mcg_get_count_trajectory", "mcg_download_molecules", "mcg_get_stats", "mcg_prepare", "mcg_trace_cases",
     "mcg_wall_consts", "mcg_walls_in_subparts", "mcg_set_options", "mcg_get_profile",
-    "mcg_get_escapes",
+    "mcg_get_escapes", "mcg_debug_molecule", "mcg_get_debug_log",
 ]
 
 
@@ -185,6 +185,14 @@ class Engine:
         rc = lib().mcg_get_escapes(self.h, ctypes.c_uint32(8), _p(out), ctypes.byref(n))
         self._chk(rc)
         return n.value, out[:min(8, n.value)]
+
+    def debug_molecule(self, uid):
+        self._chk(lib().mcg_debug_molecule(self.h, ctypes.c_uint64(uid)))
+
+    def debug_log(self):
+        out = np.zeros((64, 271))
+        self._chk(lib().mcg_get_debug_log(self.h, _p(out)))
+        return out
 
     def trace_cases(self, ids, disp, draws, r_rate_factor=None, t_steps=None):
         ids = np.ascontiguousarray(ids, np.uint64)

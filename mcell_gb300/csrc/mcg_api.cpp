@@ -239,6 +239,22 @@ int mcg_get_profile(mcg_engine* e, double* out) {
   return rc ? fail(e, rc, err) : MCG_OK;
 }
 
+int mcg_debug_molecule(mcg_engine* e, uint64_t id) {
+  if (!e) return MCG_ERR_ARG;
+  int rc = prepare(e);
+  if (rc) return rc;
+  std::string err;
+  rc = e->dev->debug_molecule(id, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
+int mcg_get_debug_log(mcg_engine* e, double* out) {
+  if (!e || !out || !e->dev) return MCG_ERR_ARG;
+  std::string err;
+  int rc = e->dev->debug_log(out, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
 int mcg_get_escapes(mcg_engine* e, uint32_t cap, double* out, uint32_t* n) {
   if (!e || !n || (cap && !out) || !e->dev) return MCG_ERR_ARG;
   std::string err;

@@ -166,6 +166,27 @@ __device__ __forceinline__ double draw_dbl(D& d) {
 struct NoEvents {
   __device__ __forceinline__ void put(int, uint64_t, int, double, double, double, double, double) {}
 };
+// events of one chosen molecule in production runs (diagnostics), null = off
+struct MaybeEvents {
+  double* out;
+  __device__ __forceinline__ void put(int kind, uint64_t index, int side, double t_rel, double t_abs, double x,
+                                      double y, double z) {
+    if (!out) return;
+    int n = (int)out[6];
+    if (n < 32) {
+      double* e = out + 9 + n * 8;
+      e[0] = kind;
+      e[1] = (double)index;
+      e[2] = side;
+      e[3] = t_rel;
+      e[4] = t_abs;
+      e[5] = x;
+      e[6] = y;
+      e[7] = z;
+    }
+    out[6] = n + 1;
+  }
+};
 struct EventLog {
   double* out;  // MCG_TRACE_RESULT_SIZE doubles
   __device__ void put(int kind, uint64_t index, int side, double t_rel, double t_abs, double x, double y,

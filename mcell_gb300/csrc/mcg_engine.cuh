@@ -98,6 +98,8 @@ class DeviceEngineT : public DeviceEngine {
     MCG_CUDA(cudaMemcpy(d_chem_, &c, sizeof(Chem), cudaMemcpyHostToDevice));
     g.chem = d_chem_;
     base_.seed = seed;
+    base_.debug_uid = ~0ull;
+    base_.debug_log = nullptr;
     nkeys_ = (uint32_t)((uint64_t)hs.nsub * hs.nsub * hs.nsub * ch.nsp);
     base_.nkeys = nkeys_;
     ntiles_ = (nkeys_ + SCAN_TILE - 1) / SCAN_TILE;
@@ -364,6 +366,27 @@ class DeviceEngineT : public DeviceEngine {
     return 0;
   }
 
+  int debug_molecule(uint64_t uid, std::string& err) override {
+    if (!d_debug_) {
+      MCG_CUDA(cudaMalloc(&d_debug_, sizeof(double) * 64 * 271));
+    }
+    MCG_CUDA(cudaMemset(d_debug_, 0, sizeof(double) * 64 * 271));
+    base_.debug_uid = uid;
+    base_.debug_log = d_debug_;
+    invalidate_graphs();
+    return 0;
+  }
+
+  int debug_log(double* out, std::string& err) override {
+    MCG_CUDA(cudaStreamSynchronize(stream_));
+    if (!d_debug_) {
+      err = "no molecule is being logged";
+      return -1;
+    }
+    MCG_CUDA(cudaMemcpy(out, d_debug_, sizeof(double) * 64 * 271, cudaMemcpyDeviceToHost));
+    return 0;
+  }
+
   int escapes(double* out, uint32_t cap, uint32_t* n, std::string& err) override {
     MCG_CUDA(cudaStreamSynchronize(stream_));
     if (read_counters(err)) return -2;
@@ -561,6 +584,7 @@ class DeviceEngineT : public DeviceEngine {
     cudaFree(d_tile_);
     cudaFree(d_traj_);
     cudaFree(d_cnt_);
+    cudaFree(d_debug_);
     cudaFree(d_chem_);
     cudaFree(d_wrej_);
     cudaFree(d_wface_);
@@ -596,6 +620,7 @@ class DeviceEngineT : public DeviceEngine {
   uint32_t *d_counts_ = nullptr, *d_cursor_ = nullptr, *d_tile_ = nullptr;
   unsigned long long* d_traj_ = nullptr;
   Counters* d_cnt_ = nullptr;
+  double* d_debug_ = nullptr;
   Chem* d_chem_ = nullptr;
   P4<T>* d_wrej_ = nullptr;
   WallFace<T>* d_wface_ = nullptr;

@@ -46,6 +46,8 @@ class DeviceEngine {
   virtual void stats(uint64_t* iterations, uint64_t* mol_steps, uint64_t* launches) = 0;
   virtual void set_options(int use_graphs, int profile) = 0;
   virtual int profile(double* out, std::string& err) = 0;
+  virtual int debug_molecule(uint64_t uid, std::string& err) = 0;
+  virtual int debug_log(double* out, std::string& err) = 0;
   virtual int escapes(double* out, uint32_t cap, uint32_t* n, std::string& err) = 0;
 };
 

@@ -69,6 +69,8 @@ template <typename T>
 struct State {
   Geo<T> g;
   uint64_t seed;
+  uint64_t debug_uid;  // molecule whose steps are logged into debug_log (diagnostics)
+  double* debug_log;   // [64 iterations][271] or null
   uint32_t cap, prod_cap, prop_cap, nkeys, traj_cap;
   // current sorted molecules and the next iteration's
   P4<T>* a_pos;
@@ -233,8 +235,28 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
     cells.uid = s.a_uid;
     cells.start = s.start;
     cells.dead = dead;
-    NoEvents ev;
+    MaybeEvents ev;
+    ev.out = nullptr;
+    if (uid == s.debug_uid && s.debug_log) {
+      // per-iteration record of one chosen molecule: 9 + 32*8 result doubles, start xyz, displacement xyz
+      ev.out = s.debug_log + (size_t)(it % 64) * 271;
+      for (int q = 0; q < 271; q++) ev.out[q] = 0;
+      ev.out[265] = (double)pos.x;
+      ev.out[266] = (double)pos.y;
+      ev.out[267] = (double)pos.z;
+      ev.out[268] = (double)disp.x;
+      ev.out[269] = (double)disp.y;
+      ev.out[270] = (double)disp.z;
+    }
     r = trace_molecule<T>(g, cells, i, pos, species, disp, r_rate_factor, t_steps, 0.0, draws, ev);
+    if (ev.out) {
+      ev.out[0] = r.status;
+      ev.out[1] = (double)r.pos.x;
+      ev.out[2] = (double)r.pos.y;
+      ev.out[3] = (double)r.pos.z;
+      ev.out[4] = r.subpart;
+      ev.out[5] = it;
+    }
     err |= r.err;
   } else {
     r.status = 0;
