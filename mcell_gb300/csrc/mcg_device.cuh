@@ -545,13 +545,15 @@ __device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V
 // fp32 tie-break in fp64: puts `pos` on the given side (+1 front, -1 back) of the
 // wall plane by a margin of a few ulps of its coordinates (~1 pm at 1 um) when
 // rounding left it on the plane or on the other side. Returns true if it moved.
+// With near_only, only a position within the margin of the plane is moved.
 template <typename T>
-__device__ bool keep_side(const P4<T>& rj, double side, V3<T>& pos) {
+__device__ bool keep_side(const P4<T>& rj, double side, V3<T>& pos, bool near_only = false) {
   const double ddn = ((double)pos.x * (double)rj.x + (double)pos.y * (double)rj.y + (double)pos.z * (double)rj.z) -
                      (double)rj.w;
   const double margin =
       8.0 * 1.1920928955078125e-07 * (double)tmax(tmax(tabs(pos.x), tabs(pos.y)), tmax(tabs(pos.z), (T)1));
   if (ddn * side >= margin) return false;
+  if (near_only && (ddn >= margin || ddn <= -margin)) return false;
   const T push = (T)(side * (margin - ddn * side));
   pos = pos + scale(v3<T>(rj.x, rj.y, rj.z), push);
   return true;
@@ -1100,8 +1102,22 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
       if (colls.overflow) res.err |= ST_COLL_OVERFLOW;
     }
     if (!hit_wall) {
+      const V3<T> seg_start = pos;
       pos = pos + remaining;
       sp = subpart_of(g, pos);
+      if (sizeof(T) == 4) {
+        // fp32: a segment that crossed no wall may still end on a wall plane after
+        // rounding; a later step starting exactly on the plane would then pass the wall
+        // (collide_wall treats "starts on the plane" as a miss). Keep it on the side it
+        // came from.
+        for (uint32_t k = g.wsp_off[sp]; k < g.wsp_off[sp + 1]; k++) {
+          const P4<T> rj = g.wrej[g.wsp_list[k]];
+          const double d0 = ((double)seg_start.x * (double)rj.x + (double)seg_start.y * (double)rj.y +
+                             (double)seg_start.z * (double)rj.z) - (double)rj.w;
+          keep_side(rj, d0 >= 0 ? 1.0 : -1.0, pos, true);
+        }
+        sp = subpart_of(g, pos);
+      }
     }
     // ---- collisions in time order (diffuse_react_event.cpp:450-572)
     bool wall_done = false;

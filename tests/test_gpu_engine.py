@@ -162,3 +162,18 @@ def test_ensemble_matches_oracle(precision):
     print(f"C after {n_iter} it: gpu {g.mean():.1f} +- {g.std(ddof=1):.1f}, oracle {c.mean():.1f} +- "
           f"{c.std(ddof=1):.1f}, se {se:.1f}")
     assert abs(g.mean() - c.mean()) < 3 * se + 1e-9
+
+
+def test_fp32_large_model_stays_confined():
+    """1M molecules in fp32 around the 20,480-triangle sphere: fp32 rounding must not let
+    any molecule through the reflective cube (the fp64 tie-breaks of the precision form)."""
+    from mcell_gb300 import workloads
+    m = workloads.sphere_in_cube(n_mol=1_000_000)
+    e = workloads.engine_for(m, "fp32", seed=7)
+    for _ in range(6):
+        e.step(20)
+        e.sync()  # raises MCG_ERR_ESCAPE on a leak
+    pos, sp, ids = e.molecules()
+    assert (np.abs(pos) <= 125.0).all()
+    c = e.counts()
+    assert c[0] == c[1] and c[0] + c[2] <= 500000
