@@ -103,6 +103,7 @@ struct Geo {
   V3<T> origin, opposite;
   T part_edge, sp_edge, sp_rcp, R;
   int nsub, nsub2, nsp;
+  uint32_t oct_shift;         // 3: occupants binned per subpartition octant, 0: per subpartition
   const P4<T>* wrej;          // normal xyz, distance to origin
   const WallFace<T>* wface;
   const uint32_t* wsp_off;    // CSR: walls per subpartition (ascending wall index)
@@ -615,16 +616,14 @@ restart:
 
 // ------------------------------------------------------------------ collisions with molecules
 
+// one vol-vol collision candidate: relative time and index of the partner; the
+// collision point (pos + t * disp), the partner id and the reaction are looked up
+// again when the candidate is processed
 template <typename T>
 struct VV {
   T t;
   uint32_t idx;
-  uint64_t uid;
-  V3<T> pos;
-  double p;
 };
-
-struct CollList;  // fwd
 
 template <typename T>
 struct Colls {
@@ -632,27 +631,43 @@ struct Colls {
   int n;
   bool overflow;
   // sort_collisions_by_time order: time ascending, equal times by id descending
-  __device__ __forceinline__ static bool before(const VV<T>& a, const VV<T>& b) {
+  __device__ __forceinline__ static bool before(const VV<T>& a, const VV<T>& b, const uint64_t* uid) {
     if (a.t < b.t) return true;
     if (a.t > b.t) return false;
-    return a.uid > b.uid;
+    return uid[a.idx] > uid[b.idx];
   }
-  __device__ void insert(const VV<T>& x) {
+  __device__ void insert(const VV<T>& x, const uint64_t* uid) {
     int i = n;
     if (n == MAXC) {
       overflow = true;
-      if (!before(x, c[MAXC - 1])) return;
+      if (!before(x, c[MAXC - 1], uid)) return;
       i = MAXC - 1;
     } else {
       n++;
     }
-    while (i > 0 && before(x, c[i - 1])) {
+    while (i > 0 && before(x, c[i - 1], uid)) {
       c[i] = c[i - 1];
       i--;
     }
     c[i] = x;
   }
 };
+
+// Occupants of a subpartition are binned by octant (key = ((subpart * 8 + octant) *
+// n_species + species)). A partner can only satisfy collide_mol if it lies within R
+// of the segment, i.e. inside the segment's bounding box grown by R, so octants
+// outside that box are skipped: an exact filter (with a rounding margin) that does
+// not change which partners are found.
+template <typename T>
+__device__ __forceinline__ uint32_t octant_of(const Geo<T>& g, V3<T> p, int ix, int iy, int iz) {
+  V3<T> r = p - g.origin;
+  const T half = (T)0.5;
+  uint32_t o = 0;
+  if (r.x * g.sp_rcp - (T)ix >= half) o |= 1;
+  if (r.y * g.sp_rcp - (T)iy >= half) o |= 2;
+  if (r.z * g.sp_rcp - (T)iz >= half) o |= 4;
+  return o;
+}
 
 // collide_mol (collision_utils.inl:464-515) against every reacting occupant of the
 // collected subpartitions
@@ -663,30 +678,46 @@ __device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, u
   const uint32_t pmask = ch.partners[species];
   const T movelen2 = dot(disp, disp);
   const T sigma2 = g.R * g.R;
+  // segment box grown by R plus a margin that covers rounding in the octant test
+  const V3<T> e = pos + disp;
+  const T mg = g.R * (T)1.01 + g.sp_edge * (T)1e-3;
+  const V3<T> lo = v3<T>(min(pos.x, e.x) - mg, min(pos.y, e.y) - mg, min(pos.z, e.z) - mg);
+  const V3<T> hi = v3<T>(max(pos.x, e.x) + mg, max(pos.y, e.y) + mg, max(pos.z, e.z) + mg);
+  const T h = g.sp_edge * (T)0.5;
   for (int i = 0; i < st.n; i++) {
-    uint32_t m = pmask;
-    while (m) {
-      int b = __ffs(m) - 1;
-      m &= m - 1;
-      uint32_t key = st.s[i] * (uint32_t)g.nsp + (uint32_t)b;
-      uint32_t j0 = __ldg(cells.start + key), j1 = __ldg(cells.start + key + 1);
-      for (uint32_t j = j0; j < j1; j++) {
-        P4<T> q = cells.pos[j];
-        V3<T> dir = v3<T>(q.x, q.y, q.z) - pos;
-        T d = dot(dir, disp);
-        if (d < 0) continue;
-        if (d > movelen2) continue;
-        T dirlen2 = dot(dir, dir);
-        if (movelen2 * dirlen2 - d * d > movelen2 * sigma2) continue;
-        if (j == self) continue;
-        if (cells.dead && cells.dead[j] == 2) continue;
-        VV<T> c;
-        c.t = d / movelen2;
-        c.pos = pos + scale(disp, c.t);
-        c.idx = j;
-        c.uid = cells.uid[j];
-        c.p = ch.bimol_p[species][b];
-        out.insert(c);
+    const uint32_t sp = st.s[i];
+    const int ix = (int)(sp % g.nsub), iy = (int)((sp / g.nsub) % g.nsub), iz = (int)(sp / g.nsub2);
+    const V3<T> llf = g.origin + cmul(v3<T>((T)ix, (T)iy, (T)iz), v3<T>(g.sp_edge, g.sp_edge, g.sp_edge));
+    // octant ranges overlapping the box, per axis: bit 0 = lower half, bit 1 = upper half
+    const uint32_t ax = (lo.x < llf.x + h ? 1u : 0u) | (hi.x >= llf.x + h ? 2u : 0u);
+    const uint32_t ay = (lo.y < llf.y + h ? 1u : 0u) | (hi.y >= llf.y + h ? 2u : 0u);
+    const uint32_t az = (lo.z < llf.z + h ? 1u : 0u) | (hi.z >= llf.z + h ? 2u : 0u);
+    const uint32_t noct = 1u << g.oct_shift;
+    for (uint32_t o = 0; o < noct; o++) {
+      if (noct == 8 &&
+          (!((ax >> (o & 1)) & 1) || !((ay >> ((o >> 1) & 1)) & 1) || !((az >> ((o >> 2) & 1)) & 1)))
+        continue;
+      uint32_t m = pmask;
+      while (m) {
+        const int b = __ffs(m) - 1;
+        m &= m - 1;
+        const uint32_t key = ((sp << g.oct_shift) | o) * (uint32_t)g.nsp + (uint32_t)b;
+        const uint32_t j0 = __ldg(cells.start + key), j1 = __ldg(cells.start + key + 1);
+        for (uint32_t j = j0; j < j1; j++) {
+          const P4<T> q = cells.pos[j];
+          const V3<T> dir = v3<T>(q.x, q.y, q.z) - pos;
+          const T d = dot(dir, disp);
+          if (d < 0) continue;
+          if (d > movelen2) continue;
+          const T dirlen2 = dot(dir, dir);
+          if (movelen2 * dirlen2 - d * d > movelen2 * sigma2) continue;
+          if (j == self) continue;
+          if (cells.dead && cells.dead[j] == 2) continue;
+          VV<T> c;
+          c.t = d / movelen2;
+          c.idx = j;
+          out.insert(c, cells.uid);
+        }
       }
     }
   }
@@ -1101,6 +1132,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
       collide_with_occupants(g, cells, self, pos, species, remaining, st, colls);
       if (colls.overflow) res.err |= ST_COLL_OVERFLOW;
     }
+    const V3<T> pos_at_start = pos;  // collision points are measured from here
     if (!hit_wall) {
       const V3<T> seg_start = pos;
       pos = pos + remaining;
@@ -1177,26 +1209,28 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
         break;
       }
       if (i == colls.n) break;
-      const VV<T>& c = colls.c[i];
+      const VV<T> c = colls.c[i];
       if (c.t < Eps<T>::stime) continue;  // is_immediate_collision
       const double t_abs = elapsed + t_steps * (double)c.t;
-      P4<T> q = cells.pos[c.idx];
-      T factor = exact_disk(g, c.pos, remaining, species, v3<T>(q.x, q.y, q.z));
+      const P4<T> q = cells.pos[c.idx];
+      const uint64_t cuid = cells.uid[c.idx];
+      const V3<T> cpos = pos_at_start + scale(remaining, c.t);  // collide_mol's rel_collision_pos
+      const T factor = exact_disk(g, cpos, remaining, species, v3<T>(q.x, q.y, q.z));
       if (factor < 0) {
-        ev.put(6, c.uid, 0, (double)c.t, t_abs, (double)c.pos.x, (double)c.pos.y, (double)c.pos.z);
+        ev.put(6, cuid, 0, (double)c.t, t_abs, (double)cpos.x, (double)cpos.y, (double)cpos.z);
         continue;
       }
       double scaling = (double)factor * r_rate_factor;
-      if (!test_bimolecular(c.p, scaling, draws)) {
-        ev.put(4, c.uid, 0, (double)c.t, t_abs, (double)c.pos.x, (double)c.pos.y, (double)c.pos.z);
+      if (!test_bimolecular(ch.bimol_p[species][meta_of(q) & META_SPECIES_MASK], scaling, draws)) {
+        ev.put(4, cuid, 0, (double)c.t, t_abs, (double)cpos.x, (double)cpos.y, (double)cpos.z);
         continue;
       }
-      ev.put(5, c.uid, 0, (double)c.t, t_abs, (double)c.pos.x, (double)c.pos.y, (double)c.pos.z);
+      ev.put(5, cuid, 0, (double)c.t, t_abs, (double)cpos.x, (double)cpos.y, (double)cpos.z);
       was_defunct = true;
       res.status = 1;
       res.partner = c.idx;
       res.t_abs = t_abs;
-      res.rxn_pos = c.pos;
+      res.rxn_pos = cpos;
       break;
     }
     (void)wall_done;

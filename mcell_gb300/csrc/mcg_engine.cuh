@@ -36,6 +36,12 @@ class DeviceEngineT : public DeviceEngine {
     int dev = 0;
     MCG_CUDA(cudaGetDevice(&dev));
     MCG_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
+    {
+      // k_diffuse runs persistent warps: exactly as many blocks as can be resident
+      int bps = 1;
+      MCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_diffuse<T>, TPB, 0));
+      diffuse_grid_ = std::max(1, bps) * sms_;
+    }
     nsp_ = ch.nsp;
     nw_ = hs.nw;
     // geometry
@@ -100,7 +106,12 @@ class DeviceEngineT : public DeviceEngine {
     base_.seed = seed;
     base_.debug_uid = ~0ull;
     base_.debug_log = nullptr;
-    nkeys_ = (uint32_t)((uint64_t)hs.nsub * hs.nsub * hs.nsub * ch.nsp);
+    {
+      // occupants are binned per subpartition octant while the key space stays small
+      const uint64_t base_keys = (uint64_t)hs.nsub * hs.nsub * hs.nsub * ch.nsp;
+      g.oct_shift = base_keys * 8 <= (1ull << 26) ? 3 : 0;
+      nkeys_ = (uint32_t)(base_keys << g.oct_shift);
+    }
     base_.nkeys = nkeys_;
     ntiles_ = (nkeys_ + SCAN_TILE - 1) / SCAN_TILE;
     base_.traj_cap = traj_cap_;
@@ -521,7 +532,7 @@ class DeviceEngineT : public DeviceEngine {
     const unsigned g = grid(cap_);
     const unsigned gs = (unsigned)std::max(1, sms_);
     mark(0, prof);
-    k_diffuse<T><<<g, TPB, 0, stream_>>>(s);
+    k_diffuse<T><<<diffuse_grid_, TPB, 0, stream_>>>(s);
     mark(1, prof);
     k_resolve<T><<<gs, TPB, 0, stream_>>>(s);
     k_collect_losers<T><<<gs, TPB, 0, stream_>>>(s);
@@ -597,6 +608,7 @@ class DeviceEngineT : public DeviceEngine {
   State<T> base_{};
   cudaStream_t stream_ = nullptr;
   int sms_ = 1;
+  int diffuse_grid_ = 1;
   int parity_ = 0;
   bool use_graphs_ = true;
   bool profile_ = false;

@@ -39,6 +39,7 @@ struct Counters {
   uint32_t n_prod;       // products created this iteration
   uint32_t n_prod_done;  // products already diffused
   uint32_t prod_hi;      // end of the products pass window
+  uint32_t work;         // next molecule handed to a k_diffuse warp
   uint32_t status;       // ST_* bits
   uint32_t iteration;
   unsigned long long mol_steps;
@@ -142,9 +143,14 @@ __device__ __forceinline__ V3<T> gauss3(PhiloxDraws& d) {
   }
 }
 
+// sort key: (subpartition, octant within it, species)
 template <typename T>
 __device__ __forceinline__ uint32_t key_of(const State<T>& s, V3<T> p, uint32_t species) {
-  return subpart_of(s.g, p) * (uint32_t)s.g.nsp + species;
+  int x, y, z;
+  sub3(s.g, p, x, y, z);
+  const uint32_t sp = sub_of3(s.g, x, y, z);
+  const uint32_t oct = s.g.oct_shift ? octant_of(s.g, p, x, y, z) : 0u;
+  return ((sp << s.g.oct_shift) | oct) * (uint32_t)s.g.nsp + species;
 }
 
 template <typename T>
@@ -312,8 +318,14 @@ __global__ void __launch_bounds__(TPB) k_diffuse(State<T> s) {
   const uint32_t n = s.cnt->n_live;
   uint32_t err = 0;
   uint32_t steps = 0;
-  for (uint32_t base = blockIdx.x * TPB; base < n; base += gridDim.x * TPB) {
-    uint32_t i = base + threadIdx.x;
+  // persistent warps: each warp takes the next 32 molecules (in sorted order) until
+  // none are left, so long-running warps near walls do not leave SMs idle at the end
+  for (;;) {
+    uint32_t base = 0;
+    if (lane_id() == 0) base = atomicAdd(&s.cnt->work, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) break;
+    uint32_t i = base + lane_id();
     bool active = i < n;
     int kind = 2;
     uint32_t key = 0;
@@ -731,6 +743,7 @@ __global__ void k_end(State<T> s) {
   c->n_prod = 0;
   c->n_prod_done = 0;
   c->prod_hi = 0;
+  c->work = 0;
   c->iteration += 1;
   const uint32_t row = c->iteration % s.traj_cap;
   for (int k = 0; k < s.g.nsp; k++) s.traj[(size_t)row * s.g.nsp + k] = 0;
