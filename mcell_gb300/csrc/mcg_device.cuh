@@ -754,7 +754,7 @@ constexpr int MAX_DISK_EDGES = 8;
 // visible part of the disk when several wall chords occlude it: integrate
 // r(theta)^2 / 2 between consecutive critical angles (chord ends and crossings)
 template <typename T>
-__device__ T sweep_area(const ExV<T>* pa, const ExV<T>* pb, int n, T R2) {
+__device__ __noinline__ T sweep_area(const ExV<T>* pa, const ExV<T>* pb, int n, T R2) {
   T ang[2 * MAX_DISK_EDGES + MAX_DISK_EDGES * (MAX_DISK_EDGES - 1) / 2];
   int na = 0;
   for (int i = 0; i < n; i++) {
@@ -819,8 +819,10 @@ __device__ T sweep_area(const ExV<T>* pa, const ExV<T>* pb, int n, T R2) {
 // exact_disk (exact_disk_utils.inl:840-1145, use_expanded_list): fraction of the
 // interaction disk around the collision point not occluded by walls, < 0 if a wall
 // separates the molecules
+// (kept out of line: it runs for a small fraction of collisions and would bloat the
+// hot loop's code)
 template <typename T>
-__device__ T exact_disk(const Geo<T>& g, V3<T> loc, V3<T> mv, int moving_species, V3<T> target) {
+__device__ __noinline__ T exact_disk(const Geo<T>& g, V3<T> loc, V3<T> mv, int moving_species, V3<T> target) {
   const T R = g.R;
   const T R2 = R * R;
   const T m2_i = 1 / dot(mv, mv);
@@ -1144,6 +1146,9 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
         // came from.
         for (uint32_t k = g.wsp_off[sp]; k < g.wsp_off[sp + 1]; k++) {
           const P4<T> rj = g.wrej[g.wsp_list[k]];
+          // cheap fp32 screen first; the fp64 side test only for end points near the plane
+          const T d1 = dot(v3<T>(rj.x, rj.y, rj.z), pos) - rj.w;
+          if (tabs(d1) > (T)1e-2) continue;
           const double d0 = ((double)seg_start.x * (double)rj.x + (double)seg_start.y * (double)rj.y +
                              (double)seg_start.z * (double)rj.z) - (double)rj.w;
           keep_side(rj, d0 >= 0 ? 1.0 : -1.0, pos, true);
