@@ -107,7 +107,7 @@ struct Geo {
   const P4<T>* wrej;          // normal xyz, distance to origin
   const WallFace<T>* wface;
   const uint32_t* wsp_off;    // CSR: walls per subpartition (ascending wall index)
-  const uint32_t* wsp_list;
+  const uint32_t* wsp_list;   // entries: wall index << 8 | mask of the subpartition octants it reaches
   const uint8_t* wall_class;  // [wall * nsp + species]: 0 reflect, 1 transparent, 2 absorptive
   const Chem* chem;
 };
@@ -233,6 +233,30 @@ __device__ __forceinline__ uint32_t subpart_of(const Geo<T>& g, V3<T> p) {
   int x, y, z;
   sub3(g, p, x, y, z);
   return sub_of3(g, x, y, z);
+}
+// octants (bit o: x half o&1, y half o&2, z half o&4) of subpartition sp that the box
+// [lo, hi] overlaps
+template <typename T>
+__device__ __forceinline__ uint32_t octants_touched(const Geo<T>& g, uint32_t sp, V3<T> lo, V3<T> hi) {
+  const int ix = (int)(sp % g.nsub), iy = (int)((sp / g.nsub) % g.nsub), iz = (int)(sp / g.nsub2);
+  const T h = g.sp_edge * (T)0.5;
+  const V3<T> mid = g.origin + cmul(v3<T>((T)ix, (T)iy, (T)iz), v3<T>(g.sp_edge, g.sp_edge, g.sp_edge)) +
+                    v3<T>(h, h, h);
+  const uint32_t ax = (lo.x < mid.x ? 1u : 0u) | (hi.x >= mid.x ? 2u : 0u);
+  const uint32_t ay = (lo.y < mid.y ? 1u : 0u) | (hi.y >= mid.y ? 2u : 0u);
+  const uint32_t az = (lo.z < mid.z ? 1u : 0u) | (hi.z >= mid.z ? 2u : 0u);
+  // expand the per-axis half sets into the 8 octant bits
+  const uint32_t mx = (ax & 1 ? 0x55u : 0u) | (ax & 2 ? 0xAAu : 0u);
+  const uint32_t my = (ay & 1 ? 0x33u : 0u) | (ay & 2 ? 0xCCu : 0u);
+  const uint32_t mz = (az & 1 ? 0x0Fu : 0u) | (az & 2 ? 0xF0u : 0u);
+  return mx & my & mz;
+}
+// box around the segment p -> p + d, grown by m in each direction
+template <typename T>
+__device__ __forceinline__ void seg_box(V3<T> p, V3<T> d, T m, V3<T>& lo, V3<T>& hi) {
+  const V3<T> e = p + d;
+  lo = v3<T>(min(p.x, e.x) - m, min(p.y, e.y) - m, min(p.z, e.z) - m);
+  hi = v3<T>(max(p.x, e.x) + m, max(p.y, e.y) + m, max(p.z, e.z) + m);
 }
 template <typename T>
 __device__ __forceinline__ V3<T> guard_zero(V3<T> a) {
@@ -578,9 +602,19 @@ __device__ bool closest_wall_collision(const Geo<T>& g, V3<T> pos, uint32_t sp, 
 restart:
   bool found = false;
   T closest_t = (T)1e20;
+  // A wall can only be hit (or re-tried at an edge) where it meets the segment, so walls
+  // that reach none of the octants the segment's box touches are skipped. The only
+  // case this leaves out is a ray lying exactly in the plane of a wall it never
+  // reaches (collide_wall's dd == 0 && dv == 0 re-try), which needs a displacement
+  // with an exactly zero component.
+  V3<T> lo, hi;
+  seg_box(pos, disp, g.sp_edge * (T)1e-3, lo, hi);
+  const uint32_t om = octants_touched(g, sp, lo, hi);
   const uint32_t b = g.wsp_off[sp], e = g.wsp_off[sp + 1];
   for (uint32_t k = b; k < e; k++) {
-    uint32_t wi = g.wsp_list[k];
+    const uint32_t ent = g.wsp_list[k];
+    if (!(ent & om)) continue;
+    const uint32_t wi = ent >> 8;
     if (wi == last_hit) continue;
     T t;
     V3<T> cp;
@@ -885,8 +919,14 @@ __device__ __noinline__ T exact_disk(const Geo<T>& g, V3<T> loc, V3<T> mv, int m
   int n_edges = 0;
   const uint32_t sp = subpart_of(g, loc);
   const Chem& ch = *g.chem;
+  // only walls reaching the octants within R of the collision point can occlude the disk
+  V3<T> blo, bhi;
+  seg_box(loc, v3<T>(0, 0, 0), R * (T)1.01 + g.sp_edge * (T)1e-3, blo, bhi);
+  const uint32_t om = octants_touched(g, sp, blo, bhi);
   for (uint32_t k = g.wsp_off[sp]; k < g.wsp_off[sp + 1]; k++) {
-    const uint32_t wi = g.wsp_list[k];
+    const uint32_t ent = g.wsp_list[k];
+    if (!(ent & om)) continue;
+    const uint32_t wi = ent >> 8;
     const P4<T> rj = g.wrej[wi];
     V3<T> wn = v3<T>(rj.x, rj.y, rj.z);
     T l_n = dot(loc, wn);
@@ -1144,8 +1184,13 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
         // rounding; a later step starting exactly on the plane would then pass the wall
         // (collide_wall treats "starts on the plane" as a miss). Keep it on the side it
         // came from.
+        V3<T> glo, ghi;
+        seg_box(pos, v3<T>(0, 0, 0), (T)2e-2, glo, ghi);
+        const uint32_t gm = octants_touched(g, sp, glo, ghi);
         for (uint32_t k = g.wsp_off[sp]; k < g.wsp_off[sp + 1]; k++) {
-          const P4<T> rj = g.wrej[g.wsp_list[k]];
+          const uint32_t ent = g.wsp_list[k];
+          if (!(ent & gm)) continue;
+          const P4<T> rj = g.wrej[ent >> 8];
           // cheap fp32 screen first; the fp64 side test only for end points near the plane
           const T d1 = dot(v3<T>(rj.x, rj.y, rj.z), pos) - rj.w;
           if (tabs(d1) > (T)1e-2) continue;

@@ -72,8 +72,11 @@ class DeviceEngineT : public DeviceEngine {
       face[w].v1 = v3<T>((T)o[16], (T)o[17], (T)o[18]);
       face[w].v2 = v3<T>((T)o[19], (T)o[20], (T)o[21]);
     }
+    // wall list entries on the device: wall index << 8 | octant mask
+    std::vector<uint32_t> ent(std::max<size_t>(hs.wsp_list.size(), 1), 0);
+    for (size_t k = 0; k < hs.wsp_list.size(); k++) ent[k] = (hs.wsp_list[k] << 8) | hs.wsp_mask[k];
     if (alloc_copy(&d_wrej_, rej, err) || alloc_copy(&d_wface_, face, err) || alloc_copy(&d_wsp_off_, hs.wsp_off, err) ||
-        alloc_copy(&d_wsp_list_, hs.wsp_list.empty() ? std::vector<uint32_t>(1, 0) : hs.wsp_list, err) ||
+        alloc_copy(&d_wsp_list_, ent, err) ||
         alloc_copy(&d_wclass_, wall_class.empty() ? std::vector<uint8_t>(1, 0) : wall_class, err))
       return -2;
     g.wrej = d_wrej_;

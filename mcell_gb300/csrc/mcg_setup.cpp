@@ -169,6 +169,7 @@ int compute_setup(const double* origin, double partition_edge, uint32_t nsub, do
   }
   Grid g{d3(origin[0], origin[1], origin[2]), hs.sp_edge, hs.sp_rcp, hs.part_edge, rxn_radius, (int)nsub};
   std::vector<std::vector<uint32_t>> lists((size_t)nsub * nsub * nsub);
+  std::vector<std::vector<uint8_t>> masks((size_t)nsub * nsub * nsub);
   for (uint32_t w = 0; w < nw; w++) {
     D3 v0 = V[tris[3 * w]], v1 = V[tris[3 * w + 1]], v2 = V[tris[3 * w + 2]];
     double* o = &hs.wall[(size_t)w * 24];
@@ -229,7 +230,17 @@ int compute_setup(const double* origin, double partition_edge, uint32_t nsub, do
           D3 sl = g.origin + mulc(d3(x, y, z), e3);
           D3 su = sl + e3;
           if (wall_in_box(vert, n, dist, sl - l3, su + l3)) {
-            lists[(size_t)x + (size_t)y * nsub + (size_t)z * nsub * nsub].push_back(w);
+            const size_t s = (size_t)x + (size_t)y * nsub + (size_t)z * nsub * nsub;
+            lists[s].push_back(w);
+            // octants of this subpartition the wall reaches (same leeway)
+            const double h = 0.5 * hs.sp_edge;
+            uint8_t mask = 0;
+            for (int o = 0; o < 8; o++) {
+              D3 ol = sl + d3((o & 1) ? h : 0.0, (o & 2) ? h : 0.0, (o & 4) ? h : 0.0);
+              D3 ou = ol + d3(h, h, h);
+              if (wall_in_box(vert, n, dist, ol - l3, ou + l3)) mask |= (uint8_t)(1u << o);
+            }
+            masks[s].push_back(mask ? mask : (uint8_t)0xFF);
           }
         }
   }
@@ -237,8 +248,15 @@ int compute_setup(const double* origin, double partition_edge, uint32_t nsub, do
   hs.wsp_off.assign(n3 + 1, 0);
   for (size_t s = 0; s < n3; s++) hs.wsp_off[s + 1] = hs.wsp_off[s] + (uint32_t)lists[s].size();
   hs.wsp_list.resize(hs.wsp_off[n3]);
-  for (size_t s = 0; s < n3; s++)
+  hs.wsp_mask.resize(hs.wsp_off[n3]);
+  for (size_t s = 0; s < n3; s++) {
     std::copy(lists[s].begin(), lists[s].end(), hs.wsp_list.begin() + hs.wsp_off[s]);
+    std::copy(masks[s].begin(), masks[s].end(), hs.wsp_mask.begin() + hs.wsp_off[s]);
+  }
+  if (nw >= (1u << 24)) {
+    err = "more than 16,777,215 walls";
+    return -1;
+  }
   return 0;
 }
 
