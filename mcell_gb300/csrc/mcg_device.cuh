@@ -708,37 +708,52 @@ __device__ __forceinline__ uint32_t octant_of(const Geo<T>& g, V3<T> p, int ix, 
 template <typename T>
 __device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos, int species,
                                        V3<T> disp, const SubSet& st, Colls<T>& out) {
+  // The lanes of a warp that reach this point together scan their occupant ranges
+  // cooperatively: one subpartition at a time (the lowest pending one of any lane), the
+  // union of the octant and species ranges the participating lanes want, every
+  // occupant loaded once for the warp and tested by each lane that wants it. Each lane
+  // still tests exactly its own candidates; only the loop structure is shared, which
+  // removes most of the divergence of per-lane loops over different ranges.
   const Chem& ch = *g.chem;
   const uint32_t pmask = ch.partners[species];
   const T movelen2 = dot(disp, disp);
   const T sigma2 = g.R * g.R;
   // segment box grown by R plus a margin that covers rounding in the octant test
-  const V3<T> e = pos + disp;
-  const T mg = g.R * (T)1.01 + g.sp_edge * (T)1e-3;
-  const V3<T> lo = v3<T>(min(pos.x, e.x) - mg, min(pos.y, e.y) - mg, min(pos.z, e.z) - mg);
-  const V3<T> hi = v3<T>(max(pos.x, e.x) + mg, max(pos.y, e.y) + mg, max(pos.z, e.z) + mg);
-  const T h = g.sp_edge * (T)0.5;
-  for (int i = 0; i < st.n; i++) {
-    const uint32_t sp = st.s[i];
-    const int ix = (int)(sp % g.nsub), iy = (int)((sp / g.nsub) % g.nsub), iz = (int)(sp / g.nsub2);
-    const V3<T> llf = g.origin + cmul(v3<T>((T)ix, (T)iy, (T)iz), v3<T>(g.sp_edge, g.sp_edge, g.sp_edge));
-    // octant ranges overlapping the box, per axis: bit 0 = lower half, bit 1 = upper half
-    const uint32_t ax = (lo.x < llf.x + h ? 1u : 0u) | (hi.x >= llf.x + h ? 2u : 0u);
-    const uint32_t ay = (lo.y < llf.y + h ? 1u : 0u) | (hi.y >= llf.y + h ? 2u : 0u);
-    const uint32_t az = (lo.z < llf.z + h ? 1u : 0u) | (hi.z >= llf.z + h ? 2u : 0u);
-    const uint32_t noct = 1u << g.oct_shift;
-    for (uint32_t o = 0; o < noct; o++) {
-      if (noct == 8 &&
-          (!((ax >> (o & 1)) & 1) || !((ay >> ((o >> 1) & 1)) & 1) || !((az >> ((o >> 2) & 1)) & 1)))
-        continue;
-      uint32_t m = pmask;
-      while (m) {
-        const int b = __ffs(m) - 1;
-        m &= m - 1;
-        const uint32_t key = ((sp << g.oct_shift) | o) * (uint32_t)g.nsp + (uint32_t)b;
+  V3<T> lo, hi;
+  seg_box(pos, disp, g.R * (T)1.01 + g.sp_edge * (T)1e-3, lo, hi);
+  const unsigned wmask = __activemask();
+  const uint32_t noct_mask = g.oct_shift ? 0xFFu : 0x1u;
+  // bit i set: st.s[i] still to be scanned by this lane
+  uint64_t pending = st.n >= 64 ? ~0ull : ((1ull << st.n) - 1ull);
+  for (;;) {
+    const bool has = pending != 0;
+    const unsigned pend = __ballot_sync(wmask, has);
+    if (!pend) break;
+    const int leader = __ffs(pend) - 1;
+    const uint32_t sp = __shfl_sync(wmask, has ? st.s[__ffsll((long long)pending) - 1] : 0u, leader);
+    bool mine = false;
+    for (uint64_t pp = pending; pp; pp &= pp - 1) {
+      const int q = __ffsll((long long)pp) - 1;
+      if (st.s[q] == sp) {
+        pending &= ~(1ull << q);
+        mine = true;
+        break;
+      }
+    }
+    const uint32_t om = mine ? (g.oct_shift ? octants_touched(g, sp, lo, hi) : 1u) & noct_mask : 0u;
+    const uint32_t pm = mine ? pmask : 0u;
+    const uint32_t uom = __reduce_or_sync(wmask, om);
+    const uint32_t upm = __reduce_or_sync(wmask, pm);
+    for (uint32_t oo = uom; oo; oo &= oo - 1) {
+      const uint32_t o = (uint32_t)(__ffs(oo) - 1);
+      for (uint32_t mm = upm; mm; mm &= mm - 1) {
+        const uint32_t b = (uint32_t)(__ffs(mm) - 1);
+        const bool want = ((om >> o) & 1u) && ((pm >> b) & 1u);
+        const uint32_t key = ((sp << g.oct_shift) | o) * (uint32_t)g.nsp + b;
         const uint32_t j0 = __ldg(cells.start + key), j1 = __ldg(cells.start + key + 1);
         for (uint32_t j = j0; j < j1; j++) {
           const P4<T> q = cells.pos[j];
+          if (!want) continue;
           const V3<T> dir = v3<T>(q.x, q.y, q.z) - pos;
           const T d = dot(dir, disp);
           if (d < 0) continue;

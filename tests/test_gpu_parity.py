@@ -32,6 +32,12 @@ def test_fp64_matches_reference_golden(name):
     got = _trace(e, sc, g["mols"], g["disps"], g["draws"])
     bad = H.compare_results(got, g["results"], rel=0.0, scene=sc)
     hard = [c for c in bad if H.compare_results(got[c:c + 1], g["results"][c:c + 1], rel=1e-9, scene=sc)]
+    for c in hard[:3]:
+        w = g["results"][c]
+        n = int(w[6])
+        print("case", c, "mol", g["mols"][c], "disp", g["disps"][c])
+        print(" want", w[:9], w[9:9 + 8 * min(n, 4)].reshape(-1, 8))
+        print(" got ", got[c, :9], got[c, 9:9 + 8 * min(int(got[c, 6]), 4)].reshape(-1, 8))
     assert not hard, f"{len(hard)} of {len(got)} cases differ from the reference routines: {hard[:5]}"
     assert len(bad) <= len(got) // 100
 
