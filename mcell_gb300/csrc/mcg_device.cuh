@@ -603,13 +603,16 @@ restart:
   bool found = false;
   T closest_t = (T)1e20;
   // A wall can only be hit (or re-tried at an edge) where it meets the segment, so walls
-  // that reach none of the octants the segment's box touches are skipped. The only
-  // case this leaves out is a ray lying exactly in the plane of a wall it never
-  // reaches (collide_wall's dd == 0 && dv == 0 re-try), which needs a displacement
-  // with an exactly zero component.
+  // that reach none of the octants the segment's box touches are skipped. The one
+  // exception is collide_wall's re-try of a move lying exactly in a wall's plane
+  // (dd == 0 && dv == 0), which happens wherever the triangle is; it needs a move
+  // exactly perpendicular to the wall normal.
+  // A move with an exactly zero component (e.g. nothing left after a reflection at
+  // t = 1, or an axis-aligned injected move) is not filtered, so that re-try stays.
   V3<T> lo, hi;
   seg_box(pos, disp, g.sp_edge * (T)1e-3, lo, hi);
-  const uint32_t om = octants_touched(g, sp, lo, hi);
+  const uint32_t om =
+      (disp.x == 0 || disp.y == 0 || disp.z == 0) ? 0xFFu : octants_touched(g, sp, lo, hi);
   const uint32_t b = g.wsp_off[sp], e = g.wsp_off[sp + 1];
   for (uint32_t k = b; k < e; k++) {
     const uint32_t ent = g.wsp_list[k];
@@ -708,52 +711,34 @@ __device__ __forceinline__ uint32_t octant_of(const Geo<T>& g, V3<T> p, int ix, 
 template <typename T>
 __device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos, int species,
                                        V3<T> disp, const SubSet& st, Colls<T>& out) {
-  // The lanes of a warp that reach this point together scan their occupant ranges
-  // cooperatively: one subpartition at a time (the lowest pending one of any lane), the
-  // union of the octant and species ranges the participating lanes want, every
-  // occupant loaded once for the warp and tested by each lane that wants it. Each lane
-  // still tests exactly its own candidates; only the loop structure is shared, which
-  // removes most of the divergence of per-lane loops over different ranges.
   const Chem& ch = *g.chem;
   const uint32_t pmask = ch.partners[species];
   const T movelen2 = dot(disp, disp);
   const T sigma2 = g.R * g.R;
   // segment box grown by R plus a margin that covers rounding in the octant test
-  V3<T> lo, hi;
-  seg_box(pos, disp, g.R * (T)1.01 + g.sp_edge * (T)1e-3, lo, hi);
-  const unsigned wmask = __activemask();
-  const uint32_t noct_mask = g.oct_shift ? 0xFFu : 0x1u;
-  // bit i set: st.s[i] still to be scanned by this lane
-  uint64_t pending = st.n >= 64 ? ~0ull : ((1ull << st.n) - 1ull);
-  for (;;) {
-    const bool has = pending != 0;
-    const unsigned pend = __ballot_sync(wmask, has);
-    if (!pend) break;
-    const int leader = __ffs(pend) - 1;
-    const uint32_t sp = __shfl_sync(wmask, has ? st.s[__ffsll((long long)pending) - 1] : 0u, leader);
-    bool mine = false;
-    for (uint64_t pp = pending; pp; pp &= pp - 1) {
-      const int q = __ffsll((long long)pp) - 1;
-      if (st.s[q] == sp) {
-        pending &= ~(1ull << q);
-        mine = true;
-        break;
-      }
-    }
-    const uint32_t om = mine ? (g.oct_shift ? octants_touched(g, sp, lo, hi) : 1u) & noct_mask : 0u;
-    const uint32_t pm = mine ? pmask : 0u;
-    const uint32_t uom = __reduce_or_sync(wmask, om);
-    const uint32_t upm = __reduce_or_sync(wmask, pm);
-    for (uint32_t oo = uom; oo; oo &= oo - 1) {
-      const uint32_t o = (uint32_t)(__ffs(oo) - 1);
-      for (uint32_t mm = upm; mm; mm &= mm - 1) {
-        const uint32_t b = (uint32_t)(__ffs(mm) - 1);
-        const bool want = ((om >> o) & 1u) && ((pm >> b) & 1u);
-        const uint32_t key = ((sp << g.oct_shift) | o) * (uint32_t)g.nsp + b;
-        const uint32_t j0 = __ldg(cells.start + key), j1 = __ldg(cells.start + key + 1);
+  const V3<T> e = pos + disp;
+  const T mg = g.R * (T)1.01 + g.sp_edge * (T)1e-3;
+  const V3<T> lo = v3<T>(min(pos.x, e.x) - mg, min(pos.y, e.y) - mg, min(pos.z, e.z) - mg);
+  const V3<T> hi = v3<T>(max(pos.x, e.x) + mg, max(pos.y, e.y) + mg, max(pos.z, e.z) + mg);
+  for (int i = 0; i < st.n; i++) {
+    const uint32_t sp = st.s[i];
+    const uint32_t om = g.oct_shift ? octants_touched(g, sp, lo, hi) : 1u;
+    uint32_t m = pmask;
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      // the octants of (subpartition, species) are consecutive keys: load their starts
+      // together (independent loads, one or two cache lines), then scan the wanted ones
+      const uint32_t base = (sp * (uint32_t)g.nsp + (uint32_t)b) << g.oct_shift;
+      uint32_t s9[9];
+      const uint32_t noct = 1u << g.oct_shift;
+#pragma unroll
+      for (int o = 0; o < 9; o++) s9[o] = (o <= (int)noct) ? __ldg(cells.start + base + o) : 0u;
+      for (uint32_t oo = om; oo; oo &= oo - 1) {
+        const uint32_t o = (uint32_t)(__ffs(oo) - 1);
+        const uint32_t j0 = s9[o], j1 = s9[o + 1];
         for (uint32_t j = j0; j < j1; j++) {
           const P4<T> q = cells.pos[j];
-          if (!want) continue;
           const V3<T> dir = v3<T>(q.x, q.y, q.z) - pos;
           const T d = dot(dir, disp);
           if (d < 0) continue;

@@ -253,7 +253,7 @@ class DeviceEngineT : public DeviceEngine {
     std::vector<uint32_t> st(nkeys_ + 1);
     MCG_CUDA(cudaMemcpy(st.data(), state(parity_).start, sizeof(uint32_t) * (nkeys_ + 1), cudaMemcpyDeviceToHost));
     for (uint32_t a = 0; a < nsp_; a++) out[a] = 0;
-    for (uint32_t k = 0; k < nkeys_; k++) out[k % nsp_] += st[k + 1] - st[k];
+    for (uint32_t k = 0; k < nkeys_; k++) out[(k >> base_.g.oct_shift) % nsp_] += st[k + 1] - st[k];
     return 0;
   }
 

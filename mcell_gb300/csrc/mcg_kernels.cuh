@@ -27,6 +27,10 @@
 namespace mcg {
 
 constexpr int TPB = 256;
+// resident blocks of k_diffuse the register allocation must allow (occupancy vs spills)
+#ifndef MCG_DIFFUSE_MIN_BLOCKS
+#define MCG_DIFFUSE_MIN_BLOCKS 2
+#endif
 constexpr int SCAN_TILE = 2048;
 constexpr int REDO_ROUNDS = 64;
 constexpr uint64_t CLAIM_FREE = ~0ull;
@@ -143,14 +147,14 @@ __device__ __forceinline__ V3<T> gauss3(PhiloxDraws& d) {
   }
 }
 
-// sort key: (subpartition, octant within it, species)
+// sort key: (subpartition, species, octant within the subpartition)
 template <typename T>
 __device__ __forceinline__ uint32_t key_of(const State<T>& s, V3<T> p, uint32_t species) {
   int x, y, z;
   sub3(s.g, p, x, y, z);
   const uint32_t sp = sub_of3(s.g, x, y, z);
   const uint32_t oct = s.g.oct_shift ? octant_of(s.g, p, x, y, z) : 0u;
-  return ((sp << s.g.oct_shift) | oct) * (uint32_t)s.g.nsp + species;
+  return ((sp * (uint32_t)s.g.nsp + species) << s.g.oct_shift) | oct;
 }
 
 template <typename T>
@@ -314,7 +318,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(TPB) k_diffuse(State<T> s) {
+__global__ void __launch_bounds__(TPB, MCG_DIFFUSE_MIN_BLOCKS) k_diffuse(State<T> s) {
   const uint32_t n = s.cnt->n_live;
   uint32_t err = 0;
   uint32_t steps = 0;
