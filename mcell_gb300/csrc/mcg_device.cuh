@@ -737,20 +737,29 @@ __device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, u
       for (uint32_t oo = om; oo; oo &= oo - 1) {
         const uint32_t o = (uint32_t)(__ffs(oo) - 1);
         const uint32_t j0 = s9[o], j1 = s9[o + 1];
-        for (uint32_t j = j0; j < j1; j++) {
-          const P4<T> q = cells.pos[j];
-          const V3<T> dir = v3<T>(q.x, q.y, q.z) - pos;
-          const T d = dot(dir, disp);
-          if (d < 0) continue;
-          if (d > movelen2) continue;
-          const T dirlen2 = dot(dir, dir);
-          if (movelen2 * dirlen2 - d * d > movelen2 * sigma2) continue;
-          if (j == self) continue;
-          if (cells.dead && cells.dead[j] == 2) continue;
-          VV<T> c;
-          c.t = d / movelen2;
-          c.idx = j;
-          out.insert(c, cells.uid);
+        // four occupants per round: their loads are issued together (latency overlap)
+        for (uint32_t j4 = j0; j4 < j1; j4 += 4) {
+          P4<T> q4[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+            if (j4 + u < j1) q4[u] = cells.pos[j4 + u];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const uint32_t j = j4 + u;
+            if (j >= j1) break;
+            const V3<T> dir = v3<T>(q4[u].x, q4[u].y, q4[u].z) - pos;
+            const T d = dot(dir, disp);
+            if (d < 0) continue;
+            if (d > movelen2) continue;
+            const T dirlen2 = dot(dir, dir);
+            if (movelen2 * dirlen2 - d * d > movelen2 * sigma2) continue;
+            if (j == self) continue;
+            if (cells.dead && cells.dead[j] == 2) continue;
+            VV<T> c;
+            c.t = d / movelen2;
+            c.idx = j;
+            out.insert(c, cells.uid);
+          }
         }
       }
     }
