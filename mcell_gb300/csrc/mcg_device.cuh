@@ -26,6 +26,11 @@
 
 #include "mcg_math.cuh"
 
+// occupants whose positions one thread loads together in the partner scan
+#ifndef MCG_OCC_BATCH
+#define MCG_OCC_BATCH 1
+#endif
+
 namespace mcg {
 
 constexpr int MAXSP = 16;
@@ -737,14 +742,14 @@ __device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, u
       for (uint32_t oo = om; oo; oo &= oo - 1) {
         const uint32_t o = (uint32_t)(__ffs(oo) - 1);
         const uint32_t j0 = s9[o], j1 = s9[o + 1];
-        // four occupants per round: their loads are issued together (latency overlap)
-        for (uint32_t j4 = j0; j4 < j1; j4 += 4) {
-          P4<T> q4[4];
+        // MCG_OCC_BATCH occupants per round: their loads are issued together (latency overlap)
+        for (uint32_t j4 = j0; j4 < j1; j4 += MCG_OCC_BATCH) {
+          P4<T> q4[MCG_OCC_BATCH];
 #pragma unroll
-          for (int u = 0; u < 4; u++)
+          for (int u = 0; u < MCG_OCC_BATCH; u++)
             if (j4 + u < j1) q4[u] = cells.pos[j4 + u];
 #pragma unroll
-          for (int u = 0; u < 4; u++) {
+          for (int u = 0; u < MCG_OCC_BATCH; u++) {
             const uint32_t j = j4 + u;
             if (j >= j1) break;
             const V3<T> dir = v3<T>(q4[u].x, q4[u].y, q4[u].z) - pos;

@@ -29,7 +29,7 @@ namespace mcg {
 constexpr int TPB = 256;
 // resident blocks of k_diffuse the register allocation must allow (occupancy vs spills)
 #ifndef MCG_DIFFUSE_MIN_BLOCKS
-#define MCG_DIFFUSE_MIN_BLOCKS 4
+#define MCG_DIFFUSE_MIN_BLOCKS 6
 #endif
 constexpr int SCAN_TILE = 2048;
 constexpr int REDO_ROUNDS = 64;
