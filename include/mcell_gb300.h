@@ -133,6 +133,28 @@ int mcg_trace_cases(mcg_engine* e, uint32_t n_cases, const uint64_t* mol_ids, co
                     const uint32_t* draws, uint32_t draws_per_case, const double* r_rate_factor,
                     const double* t_steps, double* out);
 
+/* mcg_trace_cases without device allocation. It has no counterpart in the
+   reference: it exists for callers that must not allocate device memory while
+   they check a model, for example a loop that keeps other engines running on
+   the same device (cudaFree waits for the whole device and would stall them)
+   or a process whose device memory is fully committed to resident models (an
+   allocation could fail half-way). Inputs, results and the id lookup use one
+   fixed scratch array per device, built into the library (about 0.6 MB).
+   Limits: n_cases <= MCG_TRACE_STATIC_MAX_CASES and
+   n_cases * draws_per_case <= MCG_TRACE_STATIC_MAX_DRAWS; larger requests
+   return MCG_ERR_ARG without running anything. The engine must be prepared
+   (mcg_prepare) with no molecules pending, else MCG_ERR_ARG. The first call on
+   each device looks up the scratch's device address; make that first call
+   before any CUDA stream capture begins. All handles of a process on one
+   device share the one scratch: calls that overlap in time (from several
+   threads) race on it and must be serialised by the caller. Same arguments,
+   results and errors as mcg_trace_cases. */
+#define MCG_TRACE_STATIC_MAX_CASES 256
+#define MCG_TRACE_STATIC_MAX_DRAWS 16384
+int mcg_trace_cases_static(mcg_engine* e, uint32_t n_cases, const uint64_t* mol_ids, const double* disp,
+                           const uint32_t* draws, uint32_t draws_per_case, const double* r_rate_factor,
+                           const double* t_steps, double* out);
+
 /* Setup queries for parity tests: wall constants (14 doubles per wall, same
    layout as the oracle) and the wall lists per subpartition. */
 int mcg_wall_consts(mcg_engine* e, double* out);

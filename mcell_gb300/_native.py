@@ -25,7 +25,7 @@ EXPORTS = [
     "mcg_add_unimol_rxn", "mcg_add_molecules", "mcg_step", "mcg_sync", "mcg_get_counts",
     "mcg_get_count_trajectory", "mcg_download_molecules", "mcg_get_stats", "mcg_prepare", "mcg_trace_cases",
     "mcg_wall_consts", "mcg_walls_in_subparts", "mcg_set_options", "mcg_get_profile",
-    "mcg_get_escapes", "mcg_debug_molecule", "mcg_get_debug_log",
+    "mcg_get_escapes", "mcg_debug_molecule", "mcg_get_debug_log", "mcg_trace_cases_static",
 ]
 
 
@@ -204,6 +204,19 @@ class Engine:
         out = np.zeros((n, TRACE_RESULT_SIZE))
         self._chk(lib().mcg_trace_cases(self.h, ctypes.c_uint32(n), _p(ids), _p(disp), _p(draws),
                                         ctypes.c_uint32(draws.shape[1]), _p(rrf), _p(tst), _p(out)))
+        return out
+
+    def trace_cases_static(self, ids, disp, draws, r_rate_factor=None, t_steps=None):
+        """trace_cases through mcg_trace_cases_static (fixed device scratch, no allocation)."""
+        ids = np.ascontiguousarray(ids, np.uint64)
+        n = len(ids)
+        disp = np.ascontiguousarray(disp, np.float64).reshape(n, 3)
+        draws = np.ascontiguousarray(draws, np.uint32).reshape(n, -1)
+        rrf = np.ascontiguousarray(np.ones(n) if r_rate_factor is None else r_rate_factor, np.float64)
+        tst = np.ascontiguousarray(np.ones(n) if t_steps is None else t_steps, np.float64)
+        out = np.zeros((n, TRACE_RESULT_SIZE))
+        self._chk(lib().mcg_trace_cases_static(self.h, ctypes.c_uint32(n), _p(ids), _p(disp), _p(draws),
+                                               ctypes.c_uint32(draws.shape[1]), _p(rrf), _p(tst), _p(out)))
         return out
 
     def wall_consts(self, nw):

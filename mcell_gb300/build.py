@@ -38,6 +38,7 @@ def _units():
     return [
         ("mcg_f64.cu", dev + ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
         ("mcg_f32.cu", dev),
+        ("mcg_trace_static.cu", dev),
         ("mcg_setup.cpp", ["-x", "c++"] + host),
         ("mcg_api.cpp", ["-x", "c++"] + host),
     ]

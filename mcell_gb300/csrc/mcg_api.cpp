@@ -272,6 +272,26 @@ int mcg_trace_cases(mcg_engine* e, uint32_t n, const uint64_t* ids, const double
   return rc ? fail(e, rc, err) : MCG_OK;
 }
 
+int mcg_trace_cases_static(mcg_engine* e, uint32_t n, const uint64_t* ids, const double* disp,
+                           const uint32_t* draws, uint32_t draws_per_case, const double* rrf, const double* tst,
+                           double* out) {
+  if (!e || (n && (!ids || !disp || !rrf || !tst || !out))) return MCG_ERR_ARG;
+  // preparing would allocate: this entry point only runs on an engine that is ready
+  if (!e->dev || !e->pend_species.empty())
+    return fail(e, MCG_ERR_ARG, "mcg_trace_cases_static: call mcg_prepare first (no molecules may be pending)");
+  if (n > MCG_TRACE_STATIC_MAX_CASES)
+    return fail(e, MCG_ERR_ARG, "mcg_trace_cases_static: n_cases " + std::to_string(n) + " exceeds the maximum " +
+                                    std::to_string(MCG_TRACE_STATIC_MAX_CASES));
+  if ((uint64_t)n * draws_per_case > MCG_TRACE_STATIC_MAX_DRAWS)
+    return fail(e, MCG_ERR_ARG, "mcg_trace_cases_static: n_cases x draws_per_case " +
+                                    std::to_string((uint64_t)n * draws_per_case) + " exceeds the maximum " +
+                                    std::to_string(MCG_TRACE_STATIC_MAX_DRAWS));
+  if (n && draws_per_case && !draws) return MCG_ERR_ARG;
+  std::string err;
+  int rc = e->dev->trace_static(n, ids, disp, draws, draws_per_case, rrf, tst, out, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
 int mcg_wall_consts(mcg_engine* e, double* out) {
   if (!e || !out) return MCG_ERR_ARG;
   mcg::HostSetup hs;

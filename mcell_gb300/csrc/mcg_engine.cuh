@@ -12,6 +12,7 @@
 
 #include "mcg_engine.h"
 #include "mcg_kernels.cuh"
+#include "mcg_trace_static.h"
 
 namespace mcg {
 
@@ -350,6 +351,48 @@ class DeviceEngineT : public DeviceEngine {
     cudaFree(d_tst);
     cudaFree(d_out);
     cudaFree(d_draws);
+    return 0;
+  }
+
+  int trace_static(uint32_t nc, const uint64_t* ids, const double* disp, const uint32_t* draws, uint32_t ndraws,
+                   const double* rrf, const double* tst, double* out, std::string& err) override {
+    int rc = sync(err);
+    if (rc) return rc;
+    unsigned char* sc = nullptr;
+    rc = trace_static_scratch(&sc, err);
+    if (rc) return rc;
+    if (nc == 0) return 0;
+    using L = TraceStaticLayout;
+    uint64_t* d_ids = reinterpret_cast<uint64_t*>(sc + L::ids);
+    uint32_t* d_idx = reinterpret_cast<uint32_t*>(sc + L::idx);
+    double* d_disp = reinterpret_cast<double*>(sc + L::disp);
+    double* d_rrf = reinterpret_cast<double*>(sc + L::rrf);
+    double* d_tst = reinterpret_cast<double*>(sc + L::tst);
+    uint32_t* d_draws = reinterpret_cast<uint32_t*>(sc + L::draws);
+    double* d_out = reinterpret_cast<double*>(sc + L::out);
+    State<T> s = state(parity_);
+    // molecule ids -> positions in the current (sorted) arrays, on the device
+    MCG_CUDA(cudaMemcpyAsync(d_ids, ids, sizeof(uint64_t) * nc, cudaMemcpyHostToDevice, stream_));
+    MCG_CUDA(cudaMemsetAsync(d_idx, 0xFF, sizeof(uint32_t) * nc, stream_));
+    MCG_CUDA(launch_find_ids(s.a_uid, cnt_.n_live, d_ids, nc, d_idx, stream_));
+    uint32_t idx[MCG_TRACE_STATIC_MAX_CASES];
+    MCG_CUDA(cudaMemcpyAsync(idx, d_idx, sizeof(uint32_t) * nc, cudaMemcpyDeviceToHost, stream_));
+    MCG_CUDA(cudaStreamSynchronize(stream_));
+    for (uint32_t c = 0; c < nc; c++)
+      if (idx[c] == NONE) {
+        err = "traced molecule id is not live";
+        return -1;
+      }
+    MCG_CUDA(cudaMemcpyAsync(d_disp, disp, sizeof(double) * 3 * nc, cudaMemcpyHostToDevice, stream_));
+    MCG_CUDA(cudaMemcpyAsync(d_rrf, rrf, sizeof(double) * nc, cudaMemcpyHostToDevice, stream_));
+    MCG_CUDA(cudaMemcpyAsync(d_tst, tst, sizeof(double) * nc, cudaMemcpyHostToDevice, stream_));
+    if (ndraws)
+      MCG_CUDA(cudaMemcpyAsync(d_draws, draws, sizeof(uint32_t) * ndraws * nc, cudaMemcpyHostToDevice, stream_));
+    k_trace_cases<T><<<(nc + 127) / 128, 128, 0, stream_>>>(s, nc, d_idx, d_disp, d_draws, ndraws, d_rrf, d_tst, d_out);
+    launches_ += cnt_.n_live ? 2 : 1;
+    MCG_CUDA(cudaGetLastError());
+    MCG_CUDA(cudaMemcpyAsync(out, d_out, sizeof(double) * MCG_TRACE_RESULT_SIZE * nc, cudaMemcpyDeviceToHost, stream_));
+    MCG_CUDA(cudaStreamSynchronize(stream_));
     return 0;
   }
 

@@ -43,6 +43,9 @@ class DeviceEngine {
                        std::string& err) = 0;
   virtual int trace(uint32_t n, const uint64_t* ids, const double* disp, const uint32_t* draws, uint32_t ndraws,
                     const double* rrf, const double* tst, double* out, std::string& err) = 0;
+  // trace() on the fixed scratch of mcg_trace_static.cu (no device allocation)
+  virtual int trace_static(uint32_t n, const uint64_t* ids, const double* disp, const uint32_t* draws,
+                           uint32_t ndraws, const double* rrf, const double* tst, double* out, std::string& err) = 0;
   virtual void stats(uint64_t* iterations, uint64_t* mol_steps, uint64_t* launches) = 0;
   virtual void set_options(int use_graphs, int profile) = 0;
   virtual int profile(double* out, std::string& err) = 0;
