@@ -155,6 +155,60 @@ int mcg_trace_cases_static(mcg_engine* e, uint32_t n_cases, const uint64_t* mol_
                            const uint32_t* draws, uint32_t draws_per_case, const double* r_rate_factor,
                            const double* t_steps, double* out);
 
+/* ---- Batching: many independent models (replicas) advanced together.
+   The reference runs one model per process; these calls have no counterpart
+   there. Each replica is described by an mcg_engine handle that was set up
+   with the calls above but never prepared or stepped (mcg_create,
+   mcg_set_species, mcg_upload_mesh, mcg_add_*_rxn, mcg_add_molecules); the
+   batch copies the description, so the handle may be destroyed afterwards.
+   All replicas' molecules live in one set of device arrays: every kernel of an
+   iteration runs once over all of them (one persistent diffuse kernel per
+   iteration), and blocks of iterations replay from CUDA graphs. A replica's
+   random stream depends only on its own seed, molecule ids and iteration
+   count, so its results are the same alone and in any mix. */
+typedef struct mcg_batch mcg_batch;
+
+typedef struct mcg_batch_config {
+  int precision;          /* MCG_PRECISION_FP64 / MCG_PRECISION_FP32 */
+  uint32_t n_species;     /* species of every replica (<= MCG_MAX_SPECIES) */
+  uint32_t max_replicas;  /* replica slots (<= 65536) */
+  uint64_t capacity;      /* molecules over all replicas (0 = grow as needed) */
+  int autotune;           /* 1: subpartitions per edge chosen per replica from its density and mesh
+                             (a cost model; never finer than the model asks), and the resident
+                             blocks of the diffuse kernel timed on the first iterations */
+} mcg_batch_config;
+
+/* On MCG_ERR_CUDA (no usable device) *out still receives a handle whose only
+   uses are mcg_batch_last_error and mcg_batch_destroy. */
+int mcg_batch_create(const mcg_batch_config* cfg, mcg_batch** out);
+void mcg_batch_destroy(mcg_batch* b);
+const char* mcg_batch_last_error(const mcg_batch* b);
+/* Adds n models as replicas; replica k runs n_iterations[k] iterations and then
+   freezes (0 = until removed). Slots are written to replica_ids. */
+int mcg_batch_add(mcg_batch* b, uint32_t n, mcg_engine* const* models, const uint32_t* n_iterations,
+                  uint32_t* replica_ids);
+/* Frees replica slots; their molecules are dropped. */
+int mcg_batch_remove(mcg_batch* b, uint32_t n, const uint32_t* replica_ids);
+/* Runs n iterations of every running replica. */
+int mcg_batch_step(mcg_batch* b, uint32_t n_iterations);
+int mcg_batch_sync(mcg_batch* b);
+/* Iterations a replica has run and the subpartitions per edge it runs with. */
+int mcg_batch_replica_info(mcg_batch* b, uint32_t replica, uint64_t* iterations_done, uint32_t* subparts_per_edge);
+int mcg_batch_get_counts(mcg_batch* b, uint32_t replica, uint64_t* counts);
+int mcg_batch_get_count_trajectory(mcg_batch* b, uint32_t replica, uint32_t n, uint64_t* counts);
+int mcg_batch_download_molecules(mcg_batch* b, uint32_t replica, uint64_t cap, double* pos, uint32_t* species,
+                                 uint64_t* ids, uint64_t* n_out);
+int mcg_batch_get_stats(mcg_batch* b, uint64_t* iterations, uint64_t* mol_steps, uint64_t* launches);
+int mcg_batch_set_options(mcg_batch* b, int use_graphs, int profile);
+int mcg_batch_get_profile(mcg_batch* b, double* out);
+/* Device bytes held by the batch, and the resident blocks per SM the diffuse
+   kernel runs with (the autotuner's choice, or the maximum). */
+int mcg_batch_get_memory(mcg_batch* b, uint64_t* device_bytes);
+int mcg_batch_get_tuning(mcg_batch* b, int* diffuse_blocks_per_sm);
+/* The autotuner's subpartition choice for a model (host only, no device):
+   subpartitions per edge and whether occupants are binned per octant. */
+int mcg_autotune_subparts(const mcg_engine* model, uint32_t* subparts_per_edge, int* octants);
+
 /* Setup queries for parity tests: wall constants (14 doubles per wall, same
    layout as the oracle) and the wall lists per subpartition. */
 int mcg_wall_consts(mcg_engine* e, double* out);

@@ -26,6 +26,11 @@ EXPORTS = [
     "mcg_get_count_trajectory", "mcg_download_molecules", "mcg_get_stats", "mcg_prepare", "mcg_trace_cases",
     "mcg_wall_consts", "mcg_walls_in_subparts", "mcg_set_options", "mcg_get_profile",
     "mcg_get_escapes", "mcg_debug_molecule", "mcg_get_debug_log", "mcg_trace_cases_static",
+    "mcg_batch_create", "mcg_batch_destroy", "mcg_batch_last_error", "mcg_batch_add", "mcg_batch_remove",
+    "mcg_batch_step", "mcg_batch_sync", "mcg_batch_replica_info", "mcg_batch_get_counts",
+    "mcg_batch_get_count_trajectory", "mcg_batch_download_molecules", "mcg_batch_get_stats",
+    "mcg_batch_set_options", "mcg_batch_get_profile", "mcg_batch_get_memory", "mcg_batch_get_tuning",
+    "mcg_autotune_subparts",
 ]
 
 
@@ -39,6 +44,16 @@ class McgConfig(ctypes.Structure):
         ("seed", ctypes.c_uint64),
         ("capacity", ctypes.c_uint64),
         ("n_species", ctypes.c_uint32),
+    ]
+
+
+class McgBatchConfig(ctypes.Structure):
+    _fields_ = [
+        ("precision", ctypes.c_int),
+        ("n_species", ctypes.c_uint32),
+        ("max_replicas", ctypes.c_uint32),
+        ("capacity", ctypes.c_uint64),
+        ("autotune", ctypes.c_int),
     ]
 
 
@@ -63,6 +78,11 @@ def lib():
         L.mcg_destroy.restype = None
         L.mcg_last_error.argtypes = [vp]
         L.mcg_last_error.restype = ctypes.c_char_p
+        L.mcg_batch_create.argtypes = [ctypes.POINTER(McgBatchConfig), ctypes.POINTER(vp)]
+        L.mcg_batch_destroy.argtypes = [vp]
+        L.mcg_batch_destroy.restype = None
+        L.mcg_batch_last_error.argtypes = [vp]
+        L.mcg_batch_last_error.restype = ctypes.c_char_p
         for name in EXPORTS:
             getattr(L, name)
         _lib = L
@@ -206,6 +226,13 @@ class Engine:
                                         ctypes.c_uint32(draws.shape[1]), _p(rrf), _p(tst), _p(out)))
         return out
 
+    def autotune_subparts(self):
+        """The batch autotuner's (subpartitions per edge, octant bins) for this model."""
+        n = ctypes.c_uint32()
+        o = ctypes.c_int()
+        self._chk(lib().mcg_autotune_subparts(self.h, ctypes.byref(n), ctypes.byref(o)))
+        return n.value, bool(o.value)
+
     def trace_cases_static(self, ids, disp, draws, r_rate_factor=None, t_steps=None):
         """trace_cases through mcg_trace_cases_static (fixed device scratch, no allocation)."""
         ids = np.ascontiguousarray(ids, np.uint64)
@@ -230,3 +257,112 @@ class Engine:
         tot = ctypes.c_uint64()
         self._chk(lib().mcg_walls_in_subparts(self.h, _p(counts), _p(lst), ctypes.c_uint64(cap), ctypes.byref(tot)))
         return counts, lst[:tot.value]
+
+
+class Batch:
+    """Many models advanced together as replicas of one device engine (mcg_batch_*).
+
+    Models are unprepared Engine objects (set up, never stepped); the batch
+    copies them, so they may be closed after add()."""
+
+    def __init__(self, precision, n_species, max_replicas, capacity=0, autotune=False):
+        L = lib()
+        cfg = McgBatchConfig()
+        cfg.precision = PRECISION[precision] if isinstance(precision, str) else int(precision)
+        cfg.n_species = int(n_species)
+        cfg.max_replicas = int(max_replicas)
+        cfg.capacity = int(capacity)
+        cfg.autotune = 1 if autotune else 0
+        h = ctypes.c_void_p()
+        rc = L.mcg_batch_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != MCG_OK:
+            msg = L.mcg_batch_last_error(h) if h.value else b"mcg_batch_create rejected the configuration"
+            if h.value:
+                L.mcg_batch_destroy(h)
+            raise EngineError(rc, msg.decode() if msg else "")
+        self.h = h
+        self.n_species = int(n_species)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mcg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        if rc != MCG_OK:
+            msg = lib().mcg_batch_last_error(self.h)
+            raise EngineError(rc, msg.decode() if msg else "")
+
+    def add(self, models, n_iterations=None):
+        n = len(models)
+        arr = (ctypes.c_void_p * n)(*[m.h.value for m in models])
+        its = np.ascontiguousarray(np.zeros(n) if n_iterations is None else n_iterations, np.uint32)
+        ids = np.zeros(n, np.uint32)
+        self._chk(lib().mcg_batch_add(self.h, ctypes.c_uint32(n), arr, _p(its), _p(ids)))
+        return ids
+
+    def remove(self, ids):
+        ids = np.ascontiguousarray(ids, np.uint32)
+        self._chk(lib().mcg_batch_remove(self.h, ctypes.c_uint32(len(ids)), _p(ids)))
+
+    def step(self, n=1):
+        self._chk(lib().mcg_batch_step(self.h, ctypes.c_uint32(n)))
+
+    def sync(self):
+        self._chk(lib().mcg_batch_sync(self.h))
+
+    def replica_info(self, rep):
+        done = ctypes.c_uint64()
+        nsub = ctypes.c_uint32()
+        self._chk(lib().mcg_batch_replica_info(self.h, ctypes.c_uint32(rep), ctypes.byref(done), ctypes.byref(nsub)))
+        return done.value, nsub.value
+
+    def counts(self, rep):
+        out = np.zeros(self.n_species, np.uint64)
+        self._chk(lib().mcg_batch_get_counts(self.h, ctypes.c_uint32(rep), _p(out)))
+        return out
+
+    def trajectory(self, rep, n):
+        out = np.zeros((n, self.n_species), np.uint64)
+        self._chk(lib().mcg_batch_get_count_trajectory(self.h, ctypes.c_uint32(rep), ctypes.c_uint32(n), _p(out)))
+        return out
+
+    def molecules(self, rep):
+        n = ctypes.c_uint64()
+        self._chk(lib().mcg_batch_download_molecules(self.h, ctypes.c_uint32(rep), ctypes.c_uint64(0), None, None,
+                                                     None, ctypes.byref(n)))
+        pos = np.zeros((n.value, 3))
+        sp = np.zeros(n.value, np.uint32)
+        ids = np.zeros(n.value, np.uint64)
+        self._chk(lib().mcg_batch_download_molecules(self.h, ctypes.c_uint32(rep), ctypes.c_uint64(n.value), _p(pos),
+                                                     _p(sp), _p(ids), ctypes.byref(n)))
+        return pos, sp, ids
+
+    def stats(self):
+        it, ms, la = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        self._chk(lib().mcg_batch_get_stats(self.h, ctypes.byref(it), ctypes.byref(ms), ctypes.byref(la)))
+        return it.value, ms.value, la.value
+
+    def set_options(self, use_graphs=True, profile=False):
+        self._chk(lib().mcg_batch_set_options(self.h, int(use_graphs), int(profile)))
+
+    def profile(self):
+        out = np.zeros(6)
+        self._chk(lib().mcg_batch_get_profile(self.h, _p(out)))
+        return out
+
+    def device_bytes(self):
+        b = ctypes.c_uint64()
+        self._chk(lib().mcg_batch_get_memory(self.h, ctypes.byref(b)))
+        return b.value
+
+    def diffuse_blocks_per_sm(self):
+        v = ctypes.c_int()
+        self._chk(lib().mcg_batch_get_tuning(self.h, ctypes.byref(v)))
+        return v.value

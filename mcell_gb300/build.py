@@ -4,7 +4,9 @@ Translation units are compiled in parallel:
   mcg_f64.cu    fp64 engine, -fmad=false (bit-identical rounding to the reference's CPU build)
   mcg_f32.cu    fp32 engine (fused multiply-add allowed; checked against the fp64 oracle)
   mcg_setup.cpp host setup (wall constants, wall binning), -ffp-contract=off
-  mcg_api.cpp   C ABI
+  mcg_api.cpp   C ABI (single models)
+  mcg_batch.cpp C ABI of batches (replicas) and the batch autotuner
+  mcg_trace_static.cu  fixed device scratch of mcg_trace_cases_static
 Usage: python -m mcell_gb300.build [--force] [-v]
 """
 from __future__ import annotations
@@ -41,6 +43,7 @@ def _units():
         ("mcg_trace_static.cu", dev),
         ("mcg_setup.cpp", ["-x", "c++"] + host),
         ("mcg_api.cpp", ["-x", "c++"] + host),
+        ("mcg_batch.cpp", ["-x", "c++"] + host),
     ]
 
 

@@ -5,21 +5,7 @@
 #include <string>
 #include <vector>
 
-#include "mcg_engine.h"
-
-struct mcg_engine {
-  mcg_config cfg;
-  std::string err;
-  mcg::ChemHost chem;
-  bool species_set = false;
-  std::vector<double> verts;
-  std::vector<uint32_t> walls;
-  std::vector<uint8_t> wclass;
-  std::vector<double> pend_pos;
-  std::vector<uint32_t> pend_species;
-  uint64_t next_uid = 0;
-  mcg::DeviceEngine* dev = nullptr;
-};
+#include "mcg_model.h"
 
 namespace mcg {
 int status_to_error(uint32_t status, std::string& err) {
@@ -57,18 +43,29 @@ static int prepare(mcg_engine* e) {
   mcg::DeviceEngine* d = e->cfg.precision == MCG_PRECISION_FP64 ? mcg::make_engine_f64() : mcg::make_engine_f32();
   uint64_t cap = e->cfg.capacity;
   if (cap == 0) cap = std::max<uint64_t>(1024, e->pend_species.size() * 3 / 2);
-  int rc = d->init(hs, e->chem, e->wclass, e->cfg.seed, cap, err);
+  int rc = d->create(e->cfg.n_species, 1, cap, err);
+  if (rc) {
+    delete d;
+    return fail(e, rc, err);
+  }
+  // the model is replica 0 of a one-replica engine
+  mcg::ReplicaSpec sp;
+  sp.hs = &hs;
+  sp.chem = &e->chem;
+  sp.wall_class = &e->wclass;
+  sp.seed = e->cfg.seed;
+  sp.n_mol = e->pend_species.size();
+  sp.pos = e->pend_pos.data();
+  sp.species = e->pend_species.data();
+  uint32_t rep = 0;
+  rc = d->add_replicas(&sp, 1, &rep, err);
+  e->pend_pos.clear();
+  e->pend_species.clear();
   if (rc) {
     delete d;
     return fail(e, rc, err);
   }
   e->dev = d;
-  if (!e->pend_species.empty()) {
-    rc = d->add_molecules(e->pend_species.size(), e->pend_pos.data(), e->pend_species.data(), 0, err);
-    e->pend_pos.clear();
-    e->pend_species.clear();
-    if (rc) return fail(e, rc, err);
-  }
   return MCG_OK;
 }
 
@@ -158,7 +155,7 @@ int mcg_add_molecules(mcg_engine* e, uint64_t n, const double* pos, const uint32
     return MCG_OK;
   }
   std::string err;
-  int rc = e->dev->add_molecules(n, pos, species, e->next_uid, err);
+  int rc = e->dev->add_molecules(0, n, pos, species, e->next_uid, err);
   if (rc) return fail(e, rc, err);
   e->next_uid += n;
   return MCG_OK;
@@ -191,14 +188,14 @@ int mcg_get_counts(mcg_engine* e, uint64_t* counts) {
   int rc = prepare(e);
   if (rc) return rc;
   std::string err;
-  rc = e->dev->counts(counts, err);
+  rc = e->dev->counts(0, counts, err);
   return rc ? fail(e, rc, err) : MCG_OK;
 }
 
 int mcg_get_count_trajectory(mcg_engine* e, uint32_t n, uint64_t* counts) {
   if (!e || !counts || !e->dev) return MCG_ERR_ARG;
   std::string err;
-  int rc = e->dev->trajectory(n, counts, err);
+  int rc = e->dev->trajectory(0, n, counts, err);
   return rc ? fail(e, rc, err) : MCG_OK;
 }
 
@@ -208,7 +205,7 @@ int mcg_download_molecules(mcg_engine* e, uint64_t cap, double* pos, uint32_t* s
   int rc = prepare(e);
   if (rc) return rc;
   std::string err;
-  rc = e->dev->download(cap, pos, species, ids, n_out, err);
+  rc = e->dev->download(0, cap, pos, species, ids, n_out, err);
   return rc ? fail(e, rc, err) : MCG_OK;
 }
 

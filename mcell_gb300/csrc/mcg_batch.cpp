@@ -1,0 +1,300 @@
+// C ABI of batches (declared in include/mcell_gb300.h): many independent models
+// as replicas of one device engine, plus the batch autotuner.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mcg_model.h"
+
+struct mcg_batch {
+  mcg_batch_config cfg;
+  std::string err;
+  mcg::DeviceEngine* dev = nullptr;
+  std::vector<uint32_t> nsub;  // subpartitions per edge of each replica slot
+  bool tune_pending = false;
+  int diffuse_blocks = 0;
+};
+
+namespace {
+
+int bfail(mcg_batch* b, int code, const std::string& msg) {
+  if (b) b->err = msg;
+  return code;
+}
+
+// Autotuner, part 1: subpartitions per edge of one replica from a cost model of
+// the per-molecule work of an iteration, in units of one partner test:
+//   partner tests    density/2 * edge^3 * (0.35 with octant bins, else 1) * 1.3
+//   wall tests       3 * (wall-subpartition incidences / subpartitions) * 0.35
+//   key-space sweep  0.07 * sort keys / molecules (scan and scatter touch every key)
+// The incidence count of a mesh grows as (1 + triangle extent / edge)^2 per wall.
+// Candidates run from the model's own subpartition edge (never finer) to the
+// whole partition as one subpartition, with edges of at least 4 reaction radii.
+uint32_t choose_subparts(const mcg_engine* m, bool* octants) {
+  const double L = m->cfg.partition_edge;
+  const uint32_t n_user = m->cfg.subparts_per_edge;
+  const double N = std::max<double>(1.0, (double)m->pend_species.size());
+  const double rho = N / (L * L * L);
+  const uint32_t nsp = m->cfg.n_species;
+  const size_t nw = m->walls.size() / 3;
+  double ext = 0;
+  for (size_t w = 0; w < nw; w++) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int k = 0; k < 3; k++) {
+      const double* v = &m->verts[3 * (size_t)m->walls[3 * w + k]];
+      for (int a = 0; a < 3; a++) {
+        lo[a] = std::min(lo[a], v[a]);
+        hi[a] = std::max(hi[a], v[a]);
+      }
+    }
+    ext += std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+  }
+  if (nw) ext /= (double)nw;
+  uint32_t best_n = n_user;
+  bool best_oct = true;
+  double best = 1e300;
+  for (uint32_t n = n_user; n >= 1; n--) {
+    const double e = L / n;
+    if (e < 4.0 * m->cfg.rxn_radius && n != n_user) continue;
+    const double n3 = (double)n * n * n;
+    const double inc = (double)nw * (1.0 + ext / e) * (1.0 + ext / e);
+    for (int oct = 1; oct >= 0; oct--) {
+      const double keys = nsp * n3 * (oct ? 8.0 : 1.0);
+      if (oct && keys > (double)(1u << 26)) continue;
+      const double cost = 0.5 * rho * e * e * e * (oct ? 0.35 : 1.0) * 1.3 + 3.0 * (inc / n3) * 0.35 + 0.07 * keys / N;
+      if (cost < best) {
+        best = cost;
+        best_n = n;
+        best_oct = oct != 0;
+      }
+    }
+  }
+  *octants = best_oct;
+  return best_n;
+}
+
+// Autotuner, part 2: resident blocks per SM of the persistent diffuse kernel,
+// timed on the first iterations (two per candidate, CUDA events around the
+// kernel). The simulation advances meanwhile; the grid shape does not change
+// results.
+int tune_diffuse(mcg_batch* b, uint32_t* used, uint32_t budget, std::string& err) {
+  const int mx = b->dev->max_diffuse_blocks_per_sm();
+  std::vector<int> cand;
+  for (int c : {mx, mx - 1, mx - 2, (mx * 2) / 3, mx / 2, 2})
+    if (c >= 1 && c <= mx && std::find(cand.begin(), cand.end(), c) == cand.end()) cand.push_back(c);
+  if (budget < 2 * cand.size()) return 0;  // not enough iterations yet: tune on a later call
+  b->dev->set_options(0, 1);
+  double prof[6];
+  if (b->dev->profile(prof, err)) return -2;  // discard earlier records
+  double best = 1e300;
+  int best_c = mx;
+  for (int c : cand) {
+    int rc = b->dev->set_diffuse_blocks_per_sm(c, err);
+    if (!rc) rc = b->dev->step(2, err);
+    if (!rc) rc = b->dev->profile(prof, err);
+    if (rc) return rc;
+    *used += 2;
+    if (prof[1] < best) {
+      best = prof[1];
+      best_c = c;
+    }
+  }
+  b->dev->set_options(1, 0);
+  int rc = b->dev->set_diffuse_blocks_per_sm(best_c, err);
+  if (rc) return rc;
+  b->diffuse_blocks = best_c;
+  b->tune_pending = false;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mcg_batch_create(const mcg_batch_config* cfg, mcg_batch** out) {
+  if (!cfg || !out) return MCG_ERR_ARG;
+  *out = nullptr;
+  if (cfg->precision != MCG_PRECISION_FP64 && cfg->precision != MCG_PRECISION_FP32) return MCG_ERR_ARG;
+  if (cfg->n_species == 0 || cfg->n_species > MCG_MAX_SPECIES) return MCG_ERR_ARG;
+  if (cfg->max_replicas == 0 || cfg->max_replicas > 65536) return MCG_ERR_ARG;
+  mcg_batch* b = new mcg_batch();
+  b->cfg = *cfg;
+  b->dev = cfg->precision == MCG_PRECISION_FP64 ? mcg::make_engine_f64() : mcg::make_engine_f32();
+  std::string err;
+  int rc = b->dev->create(cfg->n_species, cfg->max_replicas, cfg->capacity, err);
+  if (rc) {
+    delete b->dev;
+    b->dev = nullptr;
+    *out = b;  // the message stays readable through mcg_batch_last_error
+    b->err = err;
+    return rc;
+  }
+  b->nsub.assign(cfg->max_replicas, 0);
+  b->tune_pending = cfg->autotune != 0;
+  b->diffuse_blocks = b->dev->max_diffuse_blocks_per_sm();
+  *out = b;
+  return MCG_OK;
+}
+
+void mcg_batch_destroy(mcg_batch* b) {
+  if (!b) return;
+  delete b->dev;
+  delete b;
+}
+
+const char* mcg_batch_last_error(const mcg_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int mcg_batch_add(mcg_batch* b, uint32_t n, mcg_engine* const* models, const uint32_t* n_iterations,
+                  uint32_t* ids) {
+  if (!b || (n && (!models || !ids))) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  std::vector<mcg::HostSetup> hs(n);
+  std::vector<mcg::ReplicaSpec> specs(n);
+  std::vector<uint32_t> nsub(n);
+  for (uint32_t k = 0; k < n; k++) {
+    const mcg_engine* m = models[k];
+    if (!m) return bfail(b, MCG_ERR_ARG, "null model");
+    if (m->dev) return bfail(b, MCG_ERR_ARG, "a model added to a batch must not have been prepared or stepped");
+    if (m->cfg.n_species != b->cfg.n_species) return bfail(b, MCG_ERR_ARG, "model species count differs from the batch");
+    if (!m->species_set) return bfail(b, MCG_ERR_ARG, "model without mcg_set_species");
+    if (m->wclass.empty() && !m->walls.empty()) return bfail(b, MCG_ERR_ARG, "mesh without wall classes");
+    bool oct = true;
+    nsub[k] = b->cfg.autotune ? choose_subparts(m, &oct) : m->cfg.subparts_per_edge;
+    std::string err;
+    if (mcg::compute_setup(m->cfg.partition_origin, m->cfg.partition_edge, nsub[k], m->cfg.rxn_radius,
+                           (uint32_t)(m->verts.size() / 3), m->verts.data(), (uint32_t)(m->walls.size() / 3),
+                           m->walls.data(), hs[k], err))
+      return bfail(b, MCG_ERR_ARG, err);
+    mcg::ReplicaSpec& sp = specs[k];
+    sp.hs = &hs[k];
+    sp.chem = &m->chem;
+    sp.wall_class = &m->wclass;
+    sp.seed = m->cfg.seed;
+    sp.n_mol = m->pend_species.size();
+    sp.pos = m->pend_pos.data();
+    sp.species = m->pend_species.data();
+    sp.n_iterations = n_iterations ? n_iterations[k] : 0;
+    sp.octants = oct;
+  }
+  std::string err;
+  int rc = b->dev->add_replicas(specs.data(), n, ids, err);
+  if (rc) return bfail(b, rc, err);
+  for (uint32_t k = 0; k < n; k++) b->nsub[ids[k]] = nsub[k];
+  return MCG_OK;
+}
+
+int mcg_batch_remove(mcg_batch* b, uint32_t n, const uint32_t* ids) {
+  if (!b || (n && !ids)) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  std::string err;
+  int rc = b->dev->remove_replicas(ids, n, err);
+  if (rc) return bfail(b, rc, err);
+  for (uint32_t k = 0; k < n; k++) b->nsub[ids[k]] = 0;
+  return MCG_OK;
+}
+
+int mcg_batch_step(mcg_batch* b, uint32_t n) {
+  if (!b) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  std::string err;
+  uint32_t used = 0;
+  if (b->tune_pending) {
+    int rc = tune_diffuse(b, &used, n, err);
+    if (rc) return bfail(b, rc, err);
+  }
+  if (n > used) {
+    int rc = b->dev->step(n - used, err);
+    if (rc) return bfail(b, rc, err);
+  }
+  return MCG_OK;
+}
+
+int mcg_batch_sync(mcg_batch* b) {
+  if (!b) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  std::string err;
+  int rc = b->dev->sync(err);
+  return rc ? bfail(b, rc, err) : MCG_OK;
+}
+
+int mcg_batch_replica_info(mcg_batch* b, uint32_t rep, uint64_t* done, uint32_t* nsub) {
+  if (!b || !done) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  std::string err;
+  int rc = b->dev->replica_iterations(rep, done, err);
+  if (rc) return bfail(b, rc, err);
+  if (nsub) *nsub = b->nsub[rep];
+  return MCG_OK;
+}
+
+int mcg_batch_get_counts(mcg_batch* b, uint32_t rep, uint64_t* counts) {
+  if (!b || !counts) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  std::string err;
+  int rc = b->dev->counts(rep, counts, err);
+  return rc ? bfail(b, rc, err) : MCG_OK;
+}
+
+int mcg_batch_get_count_trajectory(mcg_batch* b, uint32_t rep, uint32_t n, uint64_t* counts) {
+  if (!b || (n && !counts)) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  std::string err;
+  int rc = b->dev->trajectory(rep, n, counts, err);
+  return rc ? bfail(b, rc, err) : MCG_OK;
+}
+
+int mcg_batch_download_molecules(mcg_batch* b, uint32_t rep, uint64_t cap, double* pos, uint32_t* species,
+                                 uint64_t* ids, uint64_t* n_out) {
+  if (!b || !n_out) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  std::string err;
+  int rc = b->dev->download(rep, cap, pos, species, ids, n_out, err);
+  return rc ? bfail(b, rc, err) : MCG_OK;
+}
+
+int mcg_batch_get_stats(mcg_batch* b, uint64_t* iterations, uint64_t* mol_steps, uint64_t* launches) {
+  if (!b) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  b->dev->stats(iterations, mol_steps, launches);
+  return MCG_OK;
+}
+
+int mcg_batch_set_options(mcg_batch* b, int use_graphs, int profile) {
+  if (!b) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  b->dev->set_options(use_graphs, profile);
+  return MCG_OK;
+}
+
+int mcg_batch_get_profile(mcg_batch* b, double* out) {
+  if (!b || !out) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  std::string err;
+  int rc = b->dev->profile(out, err);
+  return rc ? bfail(b, rc, err) : MCG_OK;
+}
+
+int mcg_batch_get_memory(mcg_batch* b, uint64_t* bytes) {
+  if (!b || !bytes) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  *bytes = b->dev->device_bytes();
+  return MCG_OK;
+}
+
+int mcg_autotune_subparts(const mcg_engine* m, uint32_t* nsub, int* octants) {
+  if (!m || !nsub || !octants) return MCG_ERR_ARG;
+  bool oct = true;
+  *nsub = choose_subparts(m, &oct);
+  *octants = oct ? 1 : 0;
+  return MCG_OK;
+}
+
+int mcg_batch_get_tuning(mcg_batch* b, int* blocks) {
+  if (!b || !blocks) return MCG_ERR_ARG;
+  *blocks = b->diffuse_blocks;
+  return MCG_OK;
+}
+
+}  // extern "C"

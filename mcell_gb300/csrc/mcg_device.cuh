@@ -47,9 +47,19 @@ constexpr uint32_t ST_WATCHDOG = 1u << 2;
 constexpr uint32_t ST_COLL_OVERFLOW = 1u << 3;   // more than MAXC candidates (earliest kept)
 constexpr uint32_t ST_SET_OVERFLOW = 1u << 4;    // more than MAXSET subpartitions
 
-// molecule meta word (w lane of the position record)
+// molecule meta word (w lane of the position record): species in bits 0-7, the
+// schedule flag in bit 8, the replica (model) the molecule belongs to in bits 16-31
 constexpr uint32_t META_SPECIES_MASK = 0xFFu;
 constexpr uint32_t META_SCHEDULE_UNIMOL = 1u << 8;  // MOLECULE_FLAG_SCHEDULE_UNIMOL_RXN
+constexpr uint32_t META_REP_SHIFT = 16;
+constexpr uint32_t MAX_REPLICAS = 1u << 16;
+__host__ __device__ __forceinline__ uint32_t make_meta(uint32_t species, uint32_t rep, uint32_t flags = 0) {
+  return species | flags | (rep << META_REP_SHIFT);
+}
+__host__ __device__ __forceinline__ uint32_t meta_rep(uint32_t m) { return m >> META_REP_SHIFT; }
+
+// replica modes: advancing, frozen (finished, kept until collected), dropped at the next sort
+constexpr uint32_t REP_RUN = 0, REP_FROZEN = 1, REP_DROP = 2;
 
 template <typename T>
 struct Eps;
@@ -103,12 +113,23 @@ struct WallFace {
   T uv1u, uv2u, uv2v;
 };
 
+// One replica (independent model) as the kernels see it: its partition grid,
+// walls, reaction tables, random stream and place in the shared sort-key space.
+// The engine keeps one per replica in a device table; a molecule finds its own
+// through the replica index in its meta word.
 template <typename T>
 struct Geo {
   V3<T> origin, opposite;
   T part_edge, sp_edge, sp_rcp, R;
   int nsub, nsub2, nsp;
+  uint32_t n3;                // subpartitions (nsub^3)
   uint32_t oct_shift;         // 3: occupants binned per subpartition octant, 0: per subpartition
+  uint32_t kbase;             // first sort key of the replica; keys are (species, subpartition, octant)
+  uint32_t rep;               // replica index
+  uint32_t it0;               // engine iteration at which the replica's own iteration 0 runs
+  uint32_t mode;              // REP_RUN / REP_FROZEN / REP_DROP
+  uint32_t it_end;            // engine iteration from which the replica is frozen (its iteration budget)
+  uint64_t seed;              // Config.seed of the replica
   const P4<T>* wrej;          // normal xyz, distance to origin
   const WallFace<T>* wface;
   const uint32_t* wsp_off;    // CSR: walls per subpartition (ascending wall index)
@@ -117,7 +138,7 @@ struct Geo {
   const Chem* chem;
 };
 
-// molecules at the start of the iteration, sorted by key = subpart * nsp + species
+// molecules at the start of the iteration, sorted by key (replica, species, subpartition, octant)
 template <typename T>
 struct Cells {
   const P4<T>* pos;
@@ -734,7 +755,7 @@ __device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, u
       m &= m - 1;
       // the octants of (subpartition, species) are consecutive keys: load their starts
       // together (independent loads, one or two cache lines), then scan the wanted ones
-      const uint32_t base = (sp * (uint32_t)g.nsp + (uint32_t)b) << g.oct_shift;
+      const uint32_t base = g.kbase + (((uint32_t)b * g.n3 + sp) << g.oct_shift);
       uint32_t s9[9];
       const uint32_t noct = 1u << g.oct_shift;
 #pragma unroll

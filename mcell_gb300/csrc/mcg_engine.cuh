@@ -1,12 +1,17 @@
-// Device engine for one model (templated on the position precision). Owns all
-// device memory of the model and one CUDA stream; iterations run without host
-// synchronisation, blocks of two iterations are replayed from CUDA graphs.
+// Device engine (templated on the position precision). Owns all device memory
+// and one CUDA stream. It holds a table of replicas — independent models, each
+// with its own mesh, partition grid, reactions, seed and iteration budget — whose
+// molecules share one set of sorted arrays, so every kernel of an iteration
+// covers all replicas. Iterations run without host synchronisation; blocks of
+// two iterations are replayed from CUDA graphs. Adding or removing replicas
+// re-sorts the molecules once (the key space is laid out again).
 #pragma once
 
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <array>
+#include <climits>
 #include <cstring>
 #include <unordered_map>
 
@@ -30,186 +35,128 @@ class DeviceEngineT : public DeviceEngine {
  public:
   ~DeviceEngineT() override { release(); }
 
-  int init(const HostSetup& hs, const ChemHost& ch, const std::vector<uint8_t>& wall_class, uint64_t seed,
-           uint64_t capacity, std::string& err) override {
+  int create(uint32_t nsp, uint32_t max_rep, uint64_t capacity, std::string& err) override {
+    if (nsp == 0 || nsp > (uint32_t)MAXSP || max_rep == 0 || max_rep > MAX_REPLICAS) {
+      err = "invalid species count or replica slots";
+      return -1;
+    }
     // a blocking stream: setup copies on the legacy default stream are ordered before its kernels
     MCG_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamDefault));
     int dev = 0;
     MCG_CUDA(cudaGetDevice(&dev));
     MCG_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
     {
-      // k_diffuse runs persistent warps: exactly as many blocks as can be resident
+      // k_diffuse runs persistent warps: as many blocks as can be resident
       int bps = 1;
       MCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_diffuse<T>, TPB, 0));
-      diffuse_grid_ = std::max(1, bps) * sms_;
+      bps_max_ = std::max(1, bps);
+      diffuse_grid_ = bps_max_ * sms_;
     }
-    nsp_ = ch.nsp;
-    nw_ = hs.nw;
-    // geometry
-    Geo<T>& g = base_.g;
-    g.origin = v3<T>((T)hs.origin[0], (T)hs.origin[1], (T)hs.origin[2]);
-    g.opposite = v3<T>((T)hs.opposite[0], (T)hs.opposite[1], (T)hs.opposite[2]);
-    g.part_edge = (T)hs.part_edge;
-    g.sp_edge = (T)hs.sp_edge;
-    g.sp_rcp = (T)hs.sp_rcp;
-    g.R = (T)hs.R;
-    g.nsub = (int)hs.nsub;
-    g.nsub2 = (int)(hs.nsub * hs.nsub);
-    g.nsp = (int)ch.nsp;
-    std::vector<P4<T>> rej(std::max<uint32_t>(nw_, 1));
-    std::vector<WallFace<T>> face(std::max<uint32_t>(nw_, 1));
-    for (uint32_t w = 0; w < nw_; w++) {
-      const double* o = &hs.wall[(size_t)w * 24];
-      rej[w].x = (T)o[0];
-      rej[w].y = (T)o[1];
-      rej[w].z = (T)o[2];
-      rej[w].w = (T)o[3];
-      face[w].u = v3<T>((T)o[4], (T)o[5], (T)o[6]);
-      face[w].v = v3<T>((T)o[7], (T)o[8], (T)o[9]);
-      face[w].uv1u = (T)o[10];
-      face[w].uv2u = (T)o[11];
-      face[w].uv2v = (T)o[12];
-      face[w].v0 = v3<T>((T)o[13], (T)o[14], (T)o[15]);
-      face[w].v1 = v3<T>((T)o[16], (T)o[17], (T)o[18]);
-      face[w].v2 = v3<T>((T)o[19], (T)o[20], (T)o[21]);
+    nsp_ = nsp;
+    max_rep_ = max_rep;
+    reps_.assign(max_rep, Rep());
+    geos_h_.assign(max_rep, Geo<T>{});
+    for (uint32_t r = 0; r < max_rep; r++) {
+      geos_h_[r].mode = REP_DROP;  // free slot: no keys, no molecules
+      geos_h_[r].nsp = (int)nsp;
+      geos_h_[r].rep = r;
     }
-    // wall list entries on the device: wall index << 8 | octant mask
-    std::vector<uint32_t> ent(std::max<size_t>(hs.wsp_list.size(), 1), 0);
-    for (size_t k = 0; k < hs.wsp_list.size(); k++) ent[k] = (hs.wsp_list[k] << 8) | hs.wsp_mask[k];
-    if (alloc_copy(&d_wrej_, rej, err) || alloc_copy(&d_wface_, face, err) || alloc_copy(&d_wsp_off_, hs.wsp_off, err) ||
-        alloc_copy(&d_wsp_list_, ent, err) ||
-        alloc_copy(&d_wclass_, wall_class.empty() ? std::vector<uint8_t>(1, 0) : wall_class, err))
-      return -2;
-    g.wrej = d_wrej_;
-    g.wface = d_wface_;
-    g.wsp_off = d_wsp_off_;
-    g.wsp_list = d_wsp_list_;
-    g.wall_class = d_wclass_;
-    // chemistry
-    Chem c;
-    std::memset(&c, 0, sizeof(c));
-    c.nsp = (int)ch.nsp;
-    for (int a = 0; a < MAXSP; a++) {
-      c.space_step[a] = ch.space_step[a];
-      c.unimol_k[a] = ch.unimol_k[a];
-      c.uni_prod[a][0] = ch.uni_prod[a][0];
-      c.uni_prod[a][1] = ch.uni_prod[a][1];
-      for (int b = 0; b < MAXSP; b++) {
-        c.bimol_p[a][b] = ch.bimol_p[a][b];
-        c.bimol_prod[a][b][0] = ch.bimol_prod[a][b][0];
-        c.bimol_prod[a][b][1] = ch.bimol_prod[a][b][1];
-        if (ch.bimol_p[a][b] >= 0) c.partners[a] |= 1u << b;
-      }
-    }
-    for (uint32_t w = 0; w < nw_; w++)
-      for (uint32_t a = 0; a < ch.nsp; a++)
-        if (wall_class[(size_t)w * ch.nsp + a]) c.can_volwall[a] = 1;
-    MCG_CUDA(cudaMalloc(&d_chem_, sizeof(Chem)));
-    MCG_CUDA(cudaMemcpy(d_chem_, &c, sizeof(Chem), cudaMemcpyHostToDevice));
-    g.chem = d_chem_;
-    base_.seed = seed;
-    base_.debug_uid = ~0ull;
-    base_.debug_log = nullptr;
-    {
-      // occupants are binned per subpartition octant while the key space stays small
-      const uint64_t base_keys = (uint64_t)hs.nsub * hs.nsub * hs.nsub * ch.nsp;
-      g.oct_shift = base_keys * 8 <= (1ull << 26) ? 3 : 0;
-      nkeys_ = (uint32_t)(base_keys << g.oct_shift);
-    }
-    base_.nkeys = nkeys_;
-    ntiles_ = (nkeys_ + SCAN_TILE - 1) / SCAN_TILE;
-    base_.traj_cap = traj_cap_;
+    MCG_CUDA(cudaMalloc(&d_geos_, sizeof(Geo<T>) * max_rep));
+    MCG_CUDA(cudaMemcpy(d_geos_, geos_h_.data(), sizeof(Geo<T>) * max_rep, cudaMemcpyHostToDevice));
+    // count trajectory ring: [row][replica][species], at most 64 MB
+    const uint64_t row_bytes = sizeof(unsigned long long) * (uint64_t)max_rep * nsp;
+    traj_cap_ = (uint32_t)std::max<uint64_t>(64, std::min<uint64_t>(65536, (64ull << 20) / row_bytes));
+    MCG_CUDA(cudaMalloc(&d_traj_, row_bytes * traj_cap_));
+    MCG_CUDA(cudaMemset(d_traj_, 0, row_bytes * traj_cap_));
     MCG_CUDA(cudaMalloc(&d_cnt_, sizeof(Counters)));
     MCG_CUDA(cudaMemset(d_cnt_, 0, sizeof(Counters)));
-    base_.cnt = d_cnt_;
-    for (int k = 0; k < 2; k++) {
-      MCG_CUDA(cudaMalloc(&d_start_[k], sizeof(uint32_t) * (nkeys_ + 1)));
-      MCG_CUDA(cudaMemset(d_start_[k], 0, sizeof(uint32_t) * (nkeys_ + 1)));
-    }
-    MCG_CUDA(cudaMalloc(&d_counts_, sizeof(uint32_t) * nkeys_));
-    MCG_CUDA(cudaMemset(d_counts_, 0, sizeof(uint32_t) * nkeys_));
-    MCG_CUDA(cudaMalloc(&d_cursor_, sizeof(uint32_t) * nkeys_));
-    MCG_CUDA(cudaMemset(d_cursor_, 0, sizeof(uint32_t) * nkeys_));
-    MCG_CUDA(cudaMalloc(&d_tile_, sizeof(uint32_t) * (ntiles_ + 1)));
-    MCG_CUDA(cudaMalloc(&d_traj_, sizeof(unsigned long long) * traj_cap_ * nsp_));
-    MCG_CUDA(cudaMemset(d_traj_, 0, sizeof(unsigned long long) * traj_cap_ * nsp_));
-    base_.start = d_start_[0];
-    base_.nstart = d_start_[1];
-    base_.counts = d_counts_;
-    base_.cursor = d_cursor_;
-    base_.tile_sum = d_tile_;
+    base_.geos = d_geos_;
+    base_.n_rep = max_rep;
+    base_.nsp = (int)nsp;
+    base_.traj_cap = traj_cap_;
     base_.traj = d_traj_;
-    if (capacity) {
-      if (ensure_capacity(capacity, err)) return -2;
-    }
+    base_.cnt = d_cnt_;
+    base_.debug_uid = ~0ull;
+    base_.debug_log = nullptr;
+    if (capacity && ensure_capacity(capacity, err)) return -2;
     return 0;
   }
 
-  int add_molecules(uint64_t n, const double* pos, const uint32_t* species, uint64_t uid0, std::string& err) override {
+  int add_replicas(const ReplicaSpec* specs, uint32_t n, uint32_t* out_reps, std::string& err) override {
     if (n == 0) return 0;
-    uint64_t live = 0;
     if (read_counters(err)) return -2;
-    live = cnt_.n_live;
-    if (live + n > 0xFFFFFFF0ull) {
-      err = "too many molecules for 32-bit indices";
+    std::vector<uint32_t> slots;
+    for (uint32_t r = 0; r < max_rep_ && slots.size() < n; r++)
+      if (!reps_[r].used) slots.push_back(r);
+    if (slots.size() < n) {
+      err = "no free replica slot";
       return -3;
     }
-    if (live + n > cap_ && ensure_capacity(std::max<uint64_t>((live + n) * 3 / 2, 1024), err)) return -2;
-    if (n > base_.prod_cap && ensure_prod(n, err)) return -2;
-    std::vector<Product<T>> stage(n);
-    for (uint64_t i = 0; i < n; i++) {
-      if (species[i] >= nsp_) {
-        err = "species index out of range";
+    uint64_t n_new = 0;
+    for (uint32_t k = 0; k < n; k++) n_new += specs[k].n_mol;
+    std::vector<Product<T>> stage;
+    stage.reserve(n_new);
+    for (uint32_t k = 0; k < n; k++) {
+      const ReplicaSpec& sp = specs[k];
+      const uint32_t r = slots[k];
+      int rc = upload_replica(sp, r, err);
+      if (rc) {
+        for (uint32_t j = 0; j <= k; j++) free_replica(slots[j]);
+        return rc;
+      }
+      rc = stage_molecules(r, sp.n_mol, sp.pos, sp.species, 0, stage, err);
+      if (rc) {
+        for (uint32_t j = 0; j <= k; j++) free_replica(slots[j]);
+        return rc;
+      }
+      reps_[r].next_uid = sp.n_mol;
+      out_reps[k] = r;
+    }
+    int rc = layout_keys(err);
+    if (rc) return rc;
+    return rebin(stage, err);
+  }
+
+  int remove_replicas(const uint32_t* reps, uint32_t n, std::string& err) override {
+    if (n == 0) return 0;
+    for (uint32_t k = 0; k < n; k++)
+      if (reps[k] >= max_rep_ || !reps_[reps[k]].used) {
+        err = "no such replica";
         return -1;
       }
-      stage[i].pos.x = (T)pos[3 * i];
-      stage[i].pos.y = (T)pos[3 * i + 1];
-      stage[i].pos.z = (T)pos[3 * i + 2];
-      uint32_t meta = species[i] | META_SCHEDULE_UNIMOL;
-      std::memcpy(&stage[i].pos.w, &meta, sizeof(meta));
-      if (sizeof(T) == 8) {
-        uint64_t m64 = meta;
-        std::memcpy(&stage[i].pos.w, &m64, sizeof(m64));
-      }
-      stage[i].birth = 0;
-      stage[i].uid = uid0 + i;
-      stage[i].tuni = TIME_FOREVER;
-      const double* p = pos + 3 * i;
-      if (!(p[0] >= origin_d(0) && p[1] >= origin_d(1) && p[2] >= origin_d(2) && p[0] < opp_d(0) && p[1] < opp_d(1) &&
-            p[2] < opp_d(2))) {
-        err = "molecule outside the partition";
-        return -4;
-      }
+    int rc = sync(err);
+    if (rc) return rc;
+    for (uint32_t k = 0; k < n; k++) {
+      geos_h_[reps[k]].mode = REP_DROP;  // its molecules leave with the re-binning below
+      reps_[reps[k]].used = false;
     }
-    MCG_CUDA(cudaMemcpyAsync(base_.prod, stage.data(), sizeof(Product<T>) * n, cudaMemcpyHostToDevice, stream_));
-    // counters: staged molecules sit in the product list, already "diffused"
-    Counters c = cnt_;
-    c.n_prod = (uint32_t)n;
-    c.n_prod_done = (uint32_t)n;
-    c.prod_hi = (uint32_t)n;
-    MCG_CUDA(cudaMemcpyAsync(d_cnt_, &c, sizeof(Counters), cudaMemcpyHostToDevice, stream_));
-    State<T> s = state(parity_);
-    k_rebin_count<T><<<grid(live + n), TPB, 0, stream_>>>(s, (uint32_t)n);
-    k_scan_tiles<T><<<ntiles_, TPB, 0, stream_>>>(s);
-    k_scan_top<T><<<1, TPB, 0, stream_>>>(s, ntiles_);
-    k_scan_apply<T><<<ntiles_, TPB, 0, stream_>>>(s);
-    k_scatter<T><<<grid(live + n), TPB, 0, stream_>>>(s, 0, 0);
-    launches_ += 5;
-    MCG_CUDA(cudaGetLastError());
-    MCG_CUDA(cudaStreamSynchronize(stream_));
+    rc = layout_keys(err);
+    if (rc) return rc;
+    std::vector<Product<T>> none;
+    rc = rebin(none, err);
+    if (rc) return rc;
+    for (uint32_t k = 0; k < n; k++) free_replica(reps[k]);
+    return 0;
+  }
+
+  int add_molecules(uint32_t rep, uint64_t n, const double* pos, const uint32_t* species, uint64_t uid0,
+                    std::string& err) override {
+    if (n == 0) return 0;
+    if (rep >= max_rep_ || !reps_[rep].used) {
+      err = "no such replica";
+      return -1;
+    }
+    std::vector<Product<T>> stage;
+    stage.reserve(n);
+    int rc = stage_molecules(rep, n, pos, species, uid0, stage, err);
+    if (rc) return rc;
+    reps_[rep].next_uid = std::max<uint64_t>(reps_[rep].next_uid, uid0 + n);
     if (read_counters(err)) return -2;
-    Counters c2 = cnt_;
-    c2.n_live = std::min<uint32_t>(c2.n_live_next, (uint32_t)cap_);
-    c2.n_prod = c2.n_prod_done = c2.prod_hi = 0;
-    MCG_CUDA(cudaMemcpy(d_cnt_, &c2, sizeof(Counters), cudaMemcpyHostToDevice));
-    parity_ ^= 1;  // the staged arrays became the current ones
-    cnt_ = c2;
-    invalidate_graphs();
-    return status_to_error(c2.status, err);
+    return rebin(stage, err);
   }
 
   int step(uint32_t n, std::string& err) override {
-    if (cap_ == 0) {
+    if (nkeys_ == 0 || cap_ == 0) {
       err = "no molecules";
       return -1;
     }
@@ -240,71 +187,119 @@ class DeviceEngineT : public DeviceEngine {
     return status_to_error(cnt_.status, err);
   }
 
-  int counts(uint64_t* out, std::string& err) override {
+  int counts(uint32_t rep, uint64_t* out, std::string& err) override {
     int rc = sync(err);
     if (rc) return rc;
-    if (cnt_.iteration > 0) {
-      // species counts of the last finished iteration, accumulated by k_scatter
+    if (rep >= max_rep_ || !reps_[rep].used) {
+      err = "no such replica";
+      return -1;
+    }
+    const Geo<T>& g = geos_h_[rep];
+    if (cnt_.iteration > g.it0) {
+      // species counts of the last finished iteration (k_end)
       const uint64_t row = (cnt_.iteration - 1) % traj_cap_;
       std::vector<unsigned long long> h(nsp_);
-      MCG_CUDA(cudaMemcpy(h.data(), d_traj_ + row * nsp_, sizeof(unsigned long long) * nsp_, cudaMemcpyDeviceToHost));
+      MCG_CUDA(cudaMemcpy(h.data(), d_traj_ + (row * max_rep_ + rep) * nsp_, sizeof(unsigned long long) * nsp_,
+                          cudaMemcpyDeviceToHost));
       for (uint32_t a = 0; a < nsp_; a++) out[a] = h[a];
       return 0;
     }
-    std::vector<uint32_t> st(nkeys_ + 1);
-    MCG_CUDA(cudaMemcpy(st.data(), state(parity_).start, sizeof(uint32_t) * (nkeys_ + 1), cudaMemcpyDeviceToHost));
-    for (uint32_t a = 0; a < nsp_; a++) out[a] = 0;
-    for (uint32_t k = 0; k < nkeys_; k++) out[(k >> base_.g.oct_shift) % nsp_] += st[k + 1] - st[k];
+    // before the replica's first iteration: from the start offsets of its key ranges
+    const uint32_t span = g.n3 << g.oct_shift;
+    const uint32_t* st = state(parity_).start;
+    for (uint32_t a = 0; a < nsp_; a++) {
+      uint32_t lo = 0, hi = 0;
+      MCG_CUDA(cudaMemcpy(&lo, st + g.kbase + a * span, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+      MCG_CUDA(cudaMemcpy(&hi, st + g.kbase + (a + 1) * span, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+      out[a] = hi - lo;
+    }
     return 0;
   }
 
-  int trajectory(uint32_t n, uint64_t* out, std::string& err) override {
+  int trajectory(uint32_t rep, uint32_t n, uint64_t* out, std::string& err) override {
     int rc = sync(err);
     if (rc) return rc;
-    if (n > iterations_ || n > traj_cap_ - 1) {
+    if (rep >= max_rep_ || !reps_[rep].used) {
+      err = "no such replica";
+      return -1;
+    }
+    const uint64_t ran = cnt_.iteration - geos_h_[rep].it0;
+    if (n > ran || n > traj_cap_ - 1) {
       err = "trajectory longer than the iterations run or the ring";
       return -1;
     }
-    std::vector<unsigned long long> h((size_t)traj_cap_ * nsp_);
-    MCG_CUDA(cudaMemcpy(h.data(), d_traj_, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
     const uint64_t last = cnt_.iteration;  // rows 0..iteration-1 hold finished iterations
-    for (uint32_t k = 0; k < n; k++) {
-      uint64_t it = last - n + k;
-      for (uint32_t a = 0; a < nsp_; a++) out[(size_t)k * nsp_ + a] = h[(it % traj_cap_) * nsp_ + a];
+    std::vector<unsigned long long> h((size_t)n * nsp_);
+    uint32_t k = 0;
+    while (k < n) {
+      const uint64_t row = (last - n + k) % traj_cap_;
+      const uint32_t rows = (uint32_t)std::min<uint64_t>(n - k, traj_cap_ - row);
+      MCG_CUDA(cudaMemcpy2D(h.data() + (size_t)k * nsp_, sizeof(unsigned long long) * nsp_,
+                            d_traj_ + (row * max_rep_ + rep) * nsp_, sizeof(unsigned long long) * nsp_ * max_rep_,
+                            sizeof(unsigned long long) * nsp_, rows, cudaMemcpyDeviceToHost));
+      k += rows;
     }
+    for (size_t q = 0; q < h.size(); q++) out[q] = h[q];
     return 0;
   }
 
-  int download(uint64_t capn, double* pos, uint32_t* species, uint64_t* ids, uint64_t* n_out,
+  int download(uint32_t rep, uint64_t capn, double* pos, uint32_t* species, uint64_t* ids, uint64_t* n_out,
                std::string& err) override {
     int rc = sync(err);
     if (rc) return rc;
-    const uint32_t n = cnt_.n_live;
+    if (rep >= max_rep_ || !reps_[rep].used) {
+      err = "no such replica";
+      return -1;
+    }
+    const Geo<T>& g = geos_h_[rep];
+    State<T> s = state(parity_);
+    uint32_t lo = 0, hi = 0;
+    MCG_CUDA(cudaMemcpy(&lo, s.start + g.kbase, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    MCG_CUDA(cudaMemcpy(&hi, s.start + g.kbase + nsp_ * (g.n3 << g.oct_shift), sizeof(uint32_t),
+                        cudaMemcpyDeviceToHost));
+    const uint32_t n = hi - lo;
     *n_out = n;
     if (n == 0) return 0;
-    State<T> s = state(parity_);
     std::vector<P4<T>> p(n);
     std::vector<uint64_t> u(n);
-    MCG_CUDA(cudaMemcpy(p.data(), s.a_pos, sizeof(P4<T>) * n, cudaMemcpyDeviceToHost));
-    MCG_CUDA(cudaMemcpy(u.data(), s.a_uid, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
+    MCG_CUDA(cudaMemcpy(p.data(), s.a_pos + lo, sizeof(P4<T>) * n, cudaMemcpyDeviceToHost));
+    MCG_CUDA(cudaMemcpy(u.data(), s.a_uid + lo, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
     for (uint64_t i = 0; i < std::min<uint64_t>(n, capn); i++) {
       if (pos) {
         pos[3 * i] = (double)p[i].x;
         pos[3 * i + 1] = (double)p[i].y;
         pos[3 * i + 2] = (double)p[i].z;
       }
-      uint32_t meta;
-      if (sizeof(T) == 8) {
-        uint64_t m64;
-        std::memcpy(&m64, &p[i].w, 8);
-        meta = (uint32_t)m64;
-      } else {
-        std::memcpy(&meta, &p[i].w, 4);
-      }
-      if (species) species[i] = meta & META_SPECIES_MASK;
+      if (species) species[i] = host_meta(p[i]) & META_SPECIES_MASK;
       if (ids) ids[i] = u[i];
     }
     return 0;
+  }
+
+  int replica_iterations(uint32_t rep, uint64_t* done, std::string& err) override {
+    int rc = sync(err);
+    if (rc) return rc;
+    if (rep >= max_rep_ || !reps_[rep].used) {
+      err = "no such replica";
+      return -1;
+    }
+    const Geo<T>& g = geos_h_[rep];
+    *done = std::min<uint64_t>(cnt_.iteration, g.it_end) - g.it0;
+    return 0;
+  }
+
+  uint64_t replica_bytes(uint32_t rep) override {
+    if (rep >= max_rep_ || !reps_[rep].used) return 0;
+    return reps_[rep].bytes + (uint64_t)reps_[rep].span * 16;
+  }
+
+  uint64_t device_bytes() override {
+    uint64_t b = (uint64_t)cap_ * (2 * (sizeof(P4<T>) + 8 + sizeof(T)) + sizeof(P4<T>) + 1 + 8);
+    b += (uint64_t)base_.prop_cap * (2 * sizeof(Proposal) + 8) + (uint64_t)base_.prod_cap * (sizeof(Product<T>) + 1);
+    b += (uint64_t)key_alloc_ * 16 + (uint64_t)traj_cap_ * max_rep_ * nsp_ * 8;
+    for (uint32_t r = 0; r < max_rep_; r++)
+      if (reps_[r].used) b += reps_[r].bytes;
+    return b;
   }
 
   int trace(uint32_t nc, const uint64_t* ids, const double* disp, const uint32_t* draws, uint32_t ndraws,
@@ -401,6 +396,18 @@ class DeviceEngineT : public DeviceEngine {
     profile_ = profile != 0;
   }
 
+  int set_diffuse_blocks_per_sm(int blocks, std::string& err) override {
+    if (blocks < 0 || blocks > bps_max_) {
+      err = "diffuse blocks per SM out of range";
+      return -1;
+    }
+    diffuse_grid_ = (blocks ? blocks : bps_max_) * sms_;
+    invalidate_graphs();
+    return 0;
+  }
+
+  int max_diffuse_blocks_per_sm() override { return bps_max_; }
+
   int profile(double* out, std::string& err) override {
     MCG_CUDA(cudaStreamSynchronize(stream_));
     for (int k = 0; k < 6; k++) out[k] = 0;
@@ -464,14 +471,267 @@ class DeviceEngineT : public DeviceEngine {
   static constexpr int kernels_per_iteration_ = 15;
 
  private:
+  // host view of one replica slot
+  struct Rep {
+    bool used = false;
+    uint32_t span = 0;      // sort keys: nsp * n3 << oct_shift
+    uint64_t bytes = 0;     // device bytes of its mesh, wall lists and tables
+    uint64_t next_uid = 0;  // next molecule id for uploads
+    P4<T>* wrej = nullptr;
+    WallFace<T>* wface = nullptr;
+    uint32_t* wsp_off = nullptr;
+    uint32_t* wsp_list = nullptr;
+    uint8_t* wclass = nullptr;
+    Chem* chem = nullptr;
+  };
+
+  static uint32_t host_meta(const P4<T>& p) {
+    if (sizeof(T) == 8) {
+      uint64_t m64;
+      std::memcpy(&m64, &p.w, 8);
+      return (uint32_t)m64;
+    }
+    uint32_t m;
+    std::memcpy(&m, &p.w, 4);
+    return m;
+  }
+
+  static void put_meta(P4<T>& p, uint32_t meta) {
+    if (sizeof(T) == 8) {
+      uint64_t m64 = meta;
+      std::memcpy(&p.w, &m64, 8);
+    } else {
+      std::memcpy(&p.w, &meta, 4);
+    }
+  }
+
   template <typename V>
-  int alloc_copy(V** d, const std::vector<V>& h, std::string& err) {
-    MCG_CUDA(cudaMalloc((void**)d, sizeof(V) * std::max<size_t>(h.size(), 1)));
+  int alloc_copy(V** d, const std::vector<V>& h, uint64_t& bytes, std::string& err) {
+    const size_t sz = sizeof(V) * std::max<size_t>(h.size(), 1);
+    MCG_CUDA(cudaMalloc((void**)d, sz));
+    bytes += sz;
     if (!h.empty()) MCG_CUDA(cudaMemcpy(*d, h.data(), sizeof(V) * h.size(), cudaMemcpyHostToDevice));
     return 0;
   }
-  double origin_d(int k) const { return (double)(&base_.g.origin.x)[k]; }
-  double opp_d(int k) const { return (double)(&base_.g.opposite.x)[k]; }
+
+  // device copies of one model's walls, wall lists and reaction tables; its Geo entry
+  int upload_replica(const ReplicaSpec& sp, uint32_t r, std::string& err) {
+    const HostSetup& hs = *sp.hs;
+    const ChemHost& ch = *sp.chem;
+    const std::vector<uint8_t>& wall_class = *sp.wall_class;
+    Rep& R = reps_[r];
+    R = Rep();
+    Geo<T> g{};
+    g.origin = v3<T>((T)hs.origin[0], (T)hs.origin[1], (T)hs.origin[2]);
+    g.opposite = v3<T>((T)hs.opposite[0], (T)hs.opposite[1], (T)hs.opposite[2]);
+    g.part_edge = (T)hs.part_edge;
+    g.sp_edge = (T)hs.sp_edge;
+    g.sp_rcp = (T)hs.sp_rcp;
+    g.R = (T)hs.R;
+    g.nsub = (int)hs.nsub;
+    g.nsub2 = (int)(hs.nsub * hs.nsub);
+    g.nsp = (int)nsp_;
+    g.n3 = hs.nsub * hs.nsub * hs.nsub;
+    const uint64_t base_keys = (uint64_t)g.n3 * nsp_;
+    // occupants are binned per subpartition octant while the key space stays small
+    g.oct_shift = (sp.octants && base_keys * 8 <= (1ull << 26)) ? 3 : 0;
+    if ((base_keys << g.oct_shift) >= (1ull << 31)) {
+      err = "subpartition grid too large";
+      return -1;
+    }
+    g.rep = r;
+    g.it0 = cnt_.iteration;
+    g.it_end = sp.n_iterations ? cnt_.iteration + sp.n_iterations : UINT_MAX;
+    g.mode = REP_RUN;
+    g.seed = sp.seed;
+    const uint32_t nw = hs.nw;
+    std::vector<P4<T>> rej(std::max<uint32_t>(nw, 1));
+    std::vector<WallFace<T>> face(std::max<uint32_t>(nw, 1));
+    for (uint32_t w = 0; w < nw; w++) {
+      const double* o = &hs.wall[(size_t)w * 24];
+      rej[w].x = (T)o[0];
+      rej[w].y = (T)o[1];
+      rej[w].z = (T)o[2];
+      rej[w].w = (T)o[3];
+      face[w].u = v3<T>((T)o[4], (T)o[5], (T)o[6]);
+      face[w].v = v3<T>((T)o[7], (T)o[8], (T)o[9]);
+      face[w].uv1u = (T)o[10];
+      face[w].uv2u = (T)o[11];
+      face[w].uv2v = (T)o[12];
+      face[w].v0 = v3<T>((T)o[13], (T)o[14], (T)o[15]);
+      face[w].v1 = v3<T>((T)o[16], (T)o[17], (T)o[18]);
+      face[w].v2 = v3<T>((T)o[19], (T)o[20], (T)o[21]);
+    }
+    // wall list entries on the device: wall index << 8 | octant mask
+    std::vector<uint32_t> ent(std::max<size_t>(hs.wsp_list.size(), 1), 0);
+    for (size_t k = 0; k < hs.wsp_list.size(); k++) ent[k] = (hs.wsp_list[k] << 8) | hs.wsp_mask[k];
+    Chem c;
+    std::memset(&c, 0, sizeof(c));
+    c.nsp = (int)ch.nsp;
+    for (int a = 0; a < MAXSP; a++) {
+      c.space_step[a] = ch.space_step[a];
+      c.unimol_k[a] = ch.unimol_k[a];
+      c.uni_prod[a][0] = ch.uni_prod[a][0];
+      c.uni_prod[a][1] = ch.uni_prod[a][1];
+      for (int b = 0; b < MAXSP; b++) {
+        c.bimol_p[a][b] = ch.bimol_p[a][b];
+        c.bimol_prod[a][b][0] = ch.bimol_prod[a][b][0];
+        c.bimol_prod[a][b][1] = ch.bimol_prod[a][b][1];
+        if (ch.bimol_p[a][b] >= 0) c.partners[a] |= 1u << b;
+      }
+    }
+    for (uint32_t w = 0; w < nw; w++)
+      for (uint32_t a = 0; a < ch.nsp; a++)
+        if (wall_class[(size_t)w * ch.nsp + a]) c.can_volwall[a] = 1;
+    R.used = true;  // from here on free_replica() releases what was allocated
+    if (alloc_copy(&R.wrej, rej, R.bytes, err) || alloc_copy(&R.wface, face, R.bytes, err) ||
+        alloc_copy(&R.wsp_off, hs.wsp_off, R.bytes, err) || alloc_copy(&R.wsp_list, ent, R.bytes, err) ||
+        alloc_copy(&R.wclass, wall_class.empty() ? std::vector<uint8_t>(1, 0) : wall_class, R.bytes, err) ||
+        alloc_copy(&R.chem, std::vector<Chem>(1, c), R.bytes, err))
+      return -2;
+    g.wrej = R.wrej;
+    g.wface = R.wface;
+    g.wsp_off = R.wsp_off;
+    g.wsp_list = R.wsp_list;
+    g.wall_class = R.wclass;
+    g.chem = R.chem;
+    R.span = (uint32_t)(base_keys << g.oct_shift);
+    geos_h_[r] = g;
+    return 0;
+  }
+
+  void free_replica(uint32_t r) {
+    Rep& R = reps_[r];
+    cudaFree(R.wrej);
+    cudaFree(R.wface);
+    cudaFree(R.wsp_off);
+    cudaFree(R.wsp_list);
+    cudaFree(R.wclass);
+    cudaFree(R.chem);
+    R = Rep();
+    Geo<T> g{};
+    g.mode = REP_DROP;
+    g.nsp = (int)nsp_;
+    g.rep = r;
+    geos_h_[r] = g;
+  }
+
+  // molecules of replica r into the staging list (checked against its partition)
+  int stage_molecules(uint32_t r, uint64_t n, const double* pos, const uint32_t* species, uint64_t uid0,
+                      std::vector<Product<T>>& stage, std::string& err) {
+    const Geo<T>& g = geos_h_[r];
+    const double o[3] = {(double)g.origin.x, (double)g.origin.y, (double)g.origin.z};
+    const double q[3] = {(double)g.opposite.x, (double)g.opposite.y, (double)g.opposite.z};
+    for (uint64_t i = 0; i < n; i++) {
+      if (species[i] >= nsp_) {
+        err = "species index out of range";
+        return -1;
+      }
+      const double* p = pos + 3 * i;
+      if (!(p[0] >= o[0] && p[1] >= o[1] && p[2] >= o[2] && p[0] < q[0] && p[1] < q[1] && p[2] < q[2])) {
+        err = "molecule outside the partition";
+        return -4;
+      }
+      Product<T> m;
+      m.pos.x = (T)p[0];
+      m.pos.y = (T)p[1];
+      m.pos.z = (T)p[2];
+      put_meta(m.pos, make_meta(species[i], r, META_SCHEDULE_UNIMOL));
+      m.birth = 0;
+      m.uid = uid0 + i;
+      m.tuni = TIME_FOREVER;
+      stage.push_back(m);
+    }
+    return 0;
+  }
+
+  // key ranges of the used replicas in slot order; grows the key arrays when needed
+  int layout_keys(std::string& err) {
+    uint64_t k = 0;
+    for (uint32_t r = 0; r < max_rep_; r++) {
+      geos_h_[r].kbase = (uint32_t)k;
+      if (reps_[r].used) k += reps_[r].span;
+    }
+    if (k >= 0xFFFFFFF0ull) {
+      err = "sort key space of the replicas exceeds 32 bits";
+      return -3;
+    }
+    nkeys_ = (uint32_t)k;
+    if (nkeys_ > key_alloc_) {
+      const uint64_t na = std::max<uint64_t>(nkeys_, (uint64_t)key_alloc_ * 5 / 4);
+      for (int p = 0; p < 2; p++) {
+        cudaFree(d_start_[p]);
+        d_start_[p] = nullptr;
+      }
+      cudaFree(d_counts_);
+      cudaFree(d_cursor_);
+      cudaFree(d_tile_);
+      d_counts_ = d_cursor_ = d_tile_ = nullptr;
+      key_alloc_ = 0;
+      for (int p = 0; p < 2; p++) {
+        MCG_CUDA(cudaMalloc(&d_start_[p], sizeof(uint32_t) * (na + 1)));
+        MCG_CUDA(cudaMemset(d_start_[p], 0, sizeof(uint32_t) * (na + 1)));
+      }
+      MCG_CUDA(cudaMalloc(&d_counts_, sizeof(uint32_t) * na));
+      MCG_CUDA(cudaMemset(d_counts_, 0, sizeof(uint32_t) * na));
+      MCG_CUDA(cudaMalloc(&d_cursor_, sizeof(uint32_t) * na));
+      MCG_CUDA(cudaMemset(d_cursor_, 0, sizeof(uint32_t) * na));
+      MCG_CUDA(cudaMalloc(&d_tile_, sizeof(uint32_t) * ((na + SCAN_TILE - 1) / SCAN_TILE + 1)));
+      key_alloc_ = (uint32_t)na;
+    }
+    base_.nkeys = nkeys_;
+    ntiles_ = (nkeys_ + SCAN_TILE - 1) / SCAN_TILE;
+    MCG_CUDA(cudaMemcpy(d_geos_, geos_h_.data(), sizeof(Geo<T>) * max_rep_, cudaMemcpyHostToDevice));
+    invalidate_graphs();
+    return 0;
+  }
+
+  // re-sorts the live molecules plus the staged ones into the other sorted arrays
+  // (molecules of dropped replicas are left out); counters must be fresh
+  int rebin(const std::vector<Product<T>>& stage, std::string& err) {
+    const uint64_t n = stage.size();
+    const uint64_t live = cnt_.n_live;
+    if (live + n > 0xFFFFFFF0ull) {
+      err = "too many molecules for 32-bit indices";
+      return -3;
+    }
+    if (live + n > cap_ && ensure_capacity(std::max<uint64_t>((live + n) * 3 / 2, 1024), err)) return -2;
+    if (n > base_.prod_cap && ensure_prod(n, err)) return -2;
+    if (nkeys_ == 0) {
+      // no replica left: nothing to sort
+      Counters c = cnt_;
+      c.n_live = 0;
+      MCG_CUDA(cudaMemcpy(d_cnt_, &c, sizeof(Counters), cudaMemcpyHostToDevice));
+      cnt_ = c;
+      return 0;
+    }
+    if (n) MCG_CUDA(cudaMemcpyAsync(base_.prod, stage.data(), sizeof(Product<T>) * n, cudaMemcpyHostToDevice, stream_));
+    // staged molecules sit in the product list, already "diffused"
+    Counters c = cnt_;
+    c.n_prod = (uint32_t)n;
+    c.n_prod_done = (uint32_t)n;
+    c.prod_hi = (uint32_t)n;
+    MCG_CUDA(cudaMemcpyAsync(d_cnt_, &c, sizeof(Counters), cudaMemcpyHostToDevice, stream_));
+    State<T> s = state(parity_);
+    k_rebin_count<T><<<grid(live + n), TPB, 0, stream_>>>(s, (uint32_t)n);
+    k_scan_tiles<T><<<ntiles_, TPB, 0, stream_>>>(s);
+    k_scan_top<T><<<1, TPB, 0, stream_>>>(s, ntiles_);
+    k_scan_apply<T><<<ntiles_, TPB, 0, stream_>>>(s);
+    k_scatter<T><<<grid(live + n), TPB, 0, stream_>>>(s, 0);
+    launches_ += 5;
+    MCG_CUDA(cudaGetLastError());
+    MCG_CUDA(cudaStreamSynchronize(stream_));
+    if (read_counters(err)) return -2;
+    Counters c2 = cnt_;
+    c2.n_live = std::min<uint32_t>(c2.n_live_next, (uint32_t)cap_);
+    c2.n_prod = c2.n_prod_done = c2.prod_hi = 0;
+    MCG_CUDA(cudaMemcpy(d_cnt_, &c2, sizeof(Counters), cudaMemcpyHostToDevice));
+    parity_ ^= 1;  // the re-binned arrays became the current ones
+    cnt_ = c2;
+    invalidate_graphs();
+    return status_to_error(c2.status, err);
+  }
+
   unsigned grid(uint64_t n) const {
     uint64_t b = (n + TPB - 1) / TPB;
     uint64_t mx = (uint64_t)sms_ * 8;
@@ -555,6 +815,9 @@ class DeviceEngineT : public DeviceEngine {
     s.n_tuni = tuni_[parity ^ 1];
     s.start = d_start_[parity];
     s.nstart = d_start_[parity ^ 1];
+    s.counts = d_counts_;
+    s.cursor = d_cursor_;
+    s.tile_sum = d_tile_;
     s.b_pos = d_b_pos_;
     s.st = d_st_;
     s.claim = d_claim_;
@@ -594,8 +857,8 @@ class DeviceEngineT : public DeviceEngine {
     k_scan_tiles<T><<<ntiles_, TPB, 0, stream_>>>(s);
     k_scan_top<T><<<1, TPB, 0, stream_>>>(s, ntiles_);
     k_scan_apply<T><<<ntiles_, TPB, 0, stream_>>>(s);
-    k_scatter<T><<<g, TPB, 0, stream_>>>(s, 1, 1);
-    k_end<T><<<1, 1, 0, stream_>>>(s);
+    k_scatter<T><<<g, TPB, 0, stream_>>>(s, 1);
+    k_end<T><<<1, TPB, 0, stream_>>>(s);
     mark(4, prof);
     launches_ += kernels_per_iteration_;
   }
@@ -622,6 +885,8 @@ class DeviceEngineT : public DeviceEngine {
 
   void release() {
     invalidate_graphs();
+    for (uint32_t r = 0; r < reps_.size(); r++)
+      if (reps_[r].used) free_replica(r);
     for (int k = 0; k < 2; k++) {
       cudaFree(pos_[k]);
       cudaFree(uid_[k]);
@@ -642,27 +907,26 @@ class DeviceEngineT : public DeviceEngine {
     cudaFree(d_traj_);
     cudaFree(d_cnt_);
     cudaFree(d_debug_);
-    cudaFree(d_chem_);
-    cudaFree(d_wrej_);
-    cudaFree(d_wface_);
-    cudaFree(d_wsp_off_);
-    cudaFree(d_wsp_list_);
-    cudaFree(d_wclass_);
+    cudaFree(d_geos_);
     if (stream_) cudaStreamDestroy(stream_);
   }
 
   State<T> base_{};
   cudaStream_t stream_ = nullptr;
   int sms_ = 1;
+  int bps_max_ = 1;
   int diffuse_grid_ = 1;
   int parity_ = 0;
   bool use_graphs_ = true;
   bool profile_ = false;
   std::vector<std::array<cudaEvent_t, 5>> prof_;
   cudaGraphExec_t graph_[2] = {nullptr, nullptr};
-  uint32_t nsp_ = 0, nw_ = 0, nkeys_ = 0, ntiles_ = 0, traj_cap_ = 65536;
+  uint32_t nsp_ = 0, max_rep_ = 0, nkeys_ = 0, key_alloc_ = 0, ntiles_ = 0, traj_cap_ = 65536;
   uint64_t cap_ = 0, iterations_ = 0, launches_ = 0;
   Counters cnt_{};
+  std::vector<Rep> reps_;
+  std::vector<Geo<T>> geos_h_;
+  Geo<T>* d_geos_ = nullptr;
   P4<T>* pos_[2] = {nullptr, nullptr};
   uint64_t* uid_[2] = {nullptr, nullptr};
   T* tuni_[2] = {nullptr, nullptr};
@@ -679,11 +943,6 @@ class DeviceEngineT : public DeviceEngine {
   unsigned long long* d_traj_ = nullptr;
   Counters* d_cnt_ = nullptr;
   double* d_debug_ = nullptr;
-  Chem* d_chem_ = nullptr;
-  P4<T>* d_wrej_ = nullptr;
-  WallFace<T>* d_wface_ = nullptr;
-  uint32_t *d_wsp_off_ = nullptr, *d_wsp_list_ = nullptr;
-  uint8_t* d_wclass_ = nullptr;
 };
 
 }  // namespace mcg

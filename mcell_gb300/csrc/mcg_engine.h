@@ -1,4 +1,9 @@
 // Device engine interface shared by the fp64 and fp32 translation units and the C ABI.
+//
+// One engine holds any number of replicas (independent models: own mesh,
+// partition grid, reactions, seed and molecules) in one set of device arrays;
+// every kernel of an iteration covers all of them. The plain C ABI drives an
+// engine with a single replica (slot 0).
 #pragma once
 
 #include <cstdint>
@@ -28,19 +33,41 @@ struct ChemHost {
   }
 };
 
+// one model to add as a replica
+struct ReplicaSpec {
+  const HostSetup* hs = nullptr;
+  const ChemHost* chem = nullptr;
+  const std::vector<uint8_t>* wall_class = nullptr;  // [wall][species]
+  uint64_t seed = 1;
+  uint64_t n_mol = 0;
+  const double* pos = nullptr;       // [n_mol][3]
+  const uint32_t* species = nullptr;  // [n_mol]
+  uint32_t n_iterations = 0;         // iterations to run, then the replica freezes; 0 = unlimited
+  bool octants = true;               // bin occupants per subpartition octant when the key space allows
+};
+
 class DeviceEngine {
  public:
   virtual ~DeviceEngine() {}
-  virtual int init(const HostSetup& hs, const ChemHost& chem, const std::vector<uint8_t>& wall_class, uint64_t seed,
-                   uint64_t capacity, std::string& err) = 0;
-  virtual int add_molecules(uint64_t n, const double* pos, const uint32_t* species, uint64_t uid0,
+  // engine with max_replicas replica slots of nsp species each
+  virtual int create(uint32_t nsp, uint32_t max_replicas, uint64_t capacity, std::string& err) = 0;
+  // adds replicas (one re-sort of all molecules); slots written to reps[]
+  virtual int add_replicas(const ReplicaSpec* specs, uint32_t n, uint32_t* reps, std::string& err) = 0;
+  // frees replica slots; their molecules leave with one re-sort
+  virtual int remove_replicas(const uint32_t* reps, uint32_t n, std::string& err) = 0;
+  virtual int add_molecules(uint32_t rep, uint64_t n, const double* pos, const uint32_t* species, uint64_t uid0,
                             std::string& err) = 0;
   virtual int step(uint32_t n, std::string& err) = 0;
   virtual int sync(std::string& err) = 0;
-  virtual int counts(uint64_t* out, std::string& err) = 0;
-  virtual int trajectory(uint32_t n, uint64_t* out, std::string& err) = 0;
-  virtual int download(uint64_t cap, double* pos, uint32_t* species, uint64_t* ids, uint64_t* n_out,
+  virtual int counts(uint32_t rep, uint64_t* out, std::string& err) = 0;
+  virtual int trajectory(uint32_t rep, uint32_t n, uint64_t* out, std::string& err) = 0;
+  virtual int download(uint32_t rep, uint64_t cap, double* pos, uint32_t* species, uint64_t* ids, uint64_t* n_out,
                        std::string& err) = 0;
+  // iterations the replica has run (it freezes after its n_iterations)
+  virtual int replica_iterations(uint32_t rep, uint64_t* done, std::string& err) = 0;
+  // device bytes held for the replica (mesh, grid, its share of the molecule arrays)
+  virtual uint64_t replica_bytes(uint32_t rep) = 0;
+  virtual uint64_t device_bytes() = 0;
   virtual int trace(uint32_t n, const uint64_t* ids, const double* disp, const uint32_t* draws, uint32_t ndraws,
                     const double* rrf, const double* tst, double* out, std::string& err) = 0;
   // trace() on the fixed scratch of mcg_trace_static.cu (no device allocation)
@@ -48,6 +75,9 @@ class DeviceEngine {
                            uint32_t ndraws, const double* rrf, const double* tst, double* out, std::string& err) = 0;
   virtual void stats(uint64_t* iterations, uint64_t* mol_steps, uint64_t* launches) = 0;
   virtual void set_options(int use_graphs, int profile) = 0;
+  // diffuse-kernel shape: resident blocks per SM of the persistent grid (0 = as many as fit)
+  virtual int set_diffuse_blocks_per_sm(int blocks, std::string& err) = 0;
+  virtual int max_diffuse_blocks_per_sm() = 0;
   virtual int profile(double* out, std::string& err) = 0;
   virtual int debug_molecule(uint64_t uid, std::string& err) = 0;
   virtual int debug_log(double* out, std::string& err) = 0;

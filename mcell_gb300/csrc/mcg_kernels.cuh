@@ -72,8 +72,9 @@ struct Product {
 // state of one engine instance as the kernels see it
 template <typename T>
 struct State {
-  Geo<T> g;
-  uint64_t seed;
+  const Geo<T>* __restrict__ geos;  // [n_rep] replica table
+  uint32_t n_rep;                   // replica slots (used or free)
+  int nsp;                          // species per replica
   uint64_t debug_uid;  // molecule whose steps are logged into debug_log (diagnostics)
   double* debug_log;   // [64 iterations][271] or null
   uint32_t cap, prod_cap, prop_cap, nkeys, traj_cap;
@@ -98,7 +99,7 @@ struct State {
   Proposal* redo_props;
   Product<T>* prod;
   uint8_t* pst;      // product status
-  unsigned long long* traj;  // [traj_cap * nsp]
+  unsigned long long* traj;  // [traj_cap][n_rep][nsp] species counts after each iteration
   Counters* cnt;
 };
 
@@ -147,18 +148,32 @@ __device__ __forceinline__ V3<T> gauss3(PhiloxDraws& d) {
   }
 }
 
-// sort key: (subpartition, species, octant within the subpartition)
+// sort key: (replica, species, subpartition, octant within the subpartition). The
+// species-major order inside a replica makes each (replica, species) one contiguous
+// key range, so species counts are differences of two scan offsets.
 template <typename T>
-__device__ __forceinline__ uint32_t key_of(const State<T>& s, V3<T> p, uint32_t species) {
+__device__ __forceinline__ uint32_t key_of(const Geo<T>& g, V3<T> p, uint32_t species) {
   int x, y, z;
-  sub3(s.g, p, x, y, z);
-  const uint32_t sp = sub_of3(s.g, x, y, z);
-  const uint32_t oct = s.g.oct_shift ? octant_of(s.g, p, x, y, z) : 0u;
-  return ((sp * (uint32_t)s.g.nsp + species) << s.g.oct_shift) | oct;
+  sub3(g, p, x, y, z);
+  const uint32_t sp = sub_of3(g, x, y, z);
+  const uint32_t oct = g.oct_shift ? octant_of(g, p, x, y, z) : 0u;
+  return g.kbase + (((species * g.n3 + sp) << g.oct_shift) | oct);
 }
 
 template <typename T>
-__device__ void add_product(const State<T>& s, int species, V3<T> pos, double birth, uint64_t uid) {
+__device__ __forceinline__ const Geo<T>& geo_of(const State<T>& s, uint32_t meta) {
+  return s.geos[meta_rep(meta)];
+}
+
+// key of a record from its own meta word
+template <typename T>
+__device__ __forceinline__ uint32_t key_of_rec(const State<T>& s, const P4<T>& b) {
+  const uint32_t m = meta_of(b);
+  return key_of(geo_of(s, m), v3<T>(b.x, b.y, b.z), m & META_SPECIES_MASK);
+}
+
+template <typename T>
+__device__ void add_product(const State<T>& s, int species, uint32_t rep, V3<T> pos, double birth, uint64_t uid) {
   if (species < 0) return;
   uint32_t k = atomicAdd(&s.cnt->n_prod, 1u);
   if (k >= s.prod_cap) {
@@ -169,7 +184,7 @@ __device__ void add_product(const State<T>& s, int species, V3<T> pos, double bi
   p.pos.x = pos.x;
   p.pos.y = pos.y;
   p.pos.z = pos.z;
-  set_meta(p.pos, (uint32_t)species | META_SCHEDULE_UNIMOL);
+  set_meta(p.pos, make_meta((uint32_t)species, rep, META_SCHEDULE_UNIMOL));
   p.birth = birth;
   p.uid = uid;
   p.tuni = TIME_FOREVER;
@@ -177,13 +192,15 @@ __device__ void add_product(const State<T>& s, int species, V3<T> pos, double bi
 }
 
 // unimolecular outcome: the molecule is destroyed, products appear at its position
-// (outcome_unimolecular, diffuse_react_event.cpp:2939)
+// (outcome_unimolecular, diffuse_react_event.cpp:2939). it: the replica's own iteration.
 template <typename T>
-__device__ void unimol_products(const State<T>& s, int species, V3<T> pos, double t, uint64_t uid, uint32_t it) {
-  const Chem& ch = *s.g.chem;
+__device__ void unimol_products(const State<T>& s, const Geo<T>& g, int species, V3<T> pos, double t, uint64_t uid,
+                                uint32_t it) {
+  const Chem& ch = *g.chem;
   for (int k = 0; k < 2; k++) {
     int ps = ch.uni_prod[species][k];
-    if (ps >= 0) add_product(s, ps, pos, t, mix64(uid ^ ((uint64_t)(it + 1) << 40) ^ (0xA5ull << 32) ^ (uint64_t)k));
+    if (ps >= 0)
+      add_product(s, ps, g.rep, pos, t, mix64(uid ^ ((uint64_t)(it + 1) << 40) ^ (0xA5ull << 32) ^ (uint64_t)k));
   }
 }
 
@@ -192,26 +209,33 @@ struct StepDecision {
   int kind;  // 0 survivor, 1 proposal, 2 dead
 };
 
+// returns 0 survivor, 1 proposal, 2 dead, 3 survivor of a frozen replica (not stepped)
 template <typename T>
 __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, Proposal* prop_out, uint32_t& err) {
-  const Geo<T>& g = s.g;
-  const Chem& ch = *g.chem;
-  const uint32_t it = s.cnt->iteration;
   P4<T> rec = s.a_pos[i];
-  const uint64_t uid = s.a_uid[i];
   uint32_t meta = meta_of(rec);
+  const Geo<T>& g = geo_of(s, meta);
+  const uint32_t mode = (g.mode == REP_RUN && s.cnt->iteration >= g.it_end) ? REP_FROZEN : g.mode;
+  if (mode != REP_RUN) {
+    if (mode == REP_DROP) return 2;
+    s.b_pos[i] = rec;  // frozen: stays as it is until the replica is collected
+    return 3;
+  }
+  const Chem& ch = *g.chem;
+  const uint32_t it = s.cnt->iteration - g.it0;  // the replica's own iteration
+  const uint64_t uid = s.a_uid[i];
   const int species = (int)(meta & META_SPECIES_MASK);
   double tuni = (double)s.a_tuni[i];
   V3<T> pos = v3<T>(rec.x, rec.y, rec.z);
   PhiloxDraws draws;
-  draws.ph.init(s.seed, uid, it, 0);
+  draws.ph.init(g.seed, uid, it, 0);
   // pick_unimol_rxn_class_and_set_rxn_time (diffuse_react_event.cpp:1731) on first diffusion
   if (meta & META_SCHEDULE_UNIMOL) {
     tuni = ch.unimol_k[species] >= 0 ? time_of_unimol(ch.unimol_k[species], draws) : TIME_FOREVER;
   }
   if (tuni <= 0.0) {
     // scheduled at or before the start of the step: react first (diffuse_single_molecule :214-223)
-    unimol_products(s, species, pos, 0.0, uid, it);
+    unimol_products(s, g, species, pos, 0.0, uid, it);
     return 2;
   }
   // get_max_time (:164-198) with the barrier at the end of the iteration
@@ -289,7 +313,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   if (r.status == 2) return 2;
   if (max_time < 1.0) {
     // the unimolecular reaction happens where the molecule stopped
-    unimol_products(s, species, r.pos, tuni, uid, it);
+    unimol_products(s, g, species, r.pos, tuni, uid, it);
     return 2;
   }
   const bool escaped = !in_partition(g, r.pos);
@@ -311,7 +335,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   out.x = r.pos.x;
   out.y = r.pos.y;
   out.z = r.pos.z;
-  set_meta(out, (uint32_t)species);  // schedule flag consumed
+  set_meta(out, make_meta((uint32_t)species, g.rep));  // schedule flag consumed
   s.b_pos[i] = out;
   if (meta & META_SCHEDULE_UNIMOL) s.a_tuni[i] = (T)tuni;  // keep the drawn time for the scatter
   return 0;
@@ -336,8 +360,11 @@ __global__ void __launch_bounds__(TPB, MCG_DIFFUSE_MIN_BLOCKS) k_diffuse(State<T
     if (active) {
       Proposal p;
       kind = run_molecule(s, i, nullptr, &p, err);
+      if (kind == 3)
+        kind = 0;  // frozen replica: kept, not stepped
+      else
+        steps++;
       s.st[i] = (uint8_t)kind;
-      steps++;
       if (kind == 1) {
         uint32_t k = atomicAdd(&s.cnt->n_props, 1u);
         if (k < s.prop_cap) {
@@ -348,8 +375,7 @@ __global__ void __launch_bounds__(TPB, MCG_DIFFUSE_MIN_BLOCKS) k_diffuse(State<T
           err |= ST_CAPACITY;
         }
       } else if (kind == 0) {
-        P4<T> b = s.b_pos[i];
-        key = key_of(s, v3<T>(b.x, b.y, b.z), meta_of(b) & META_SPECIES_MASK);
+        key = key_of_rec(s, s.b_pos[i]);
       }
     }
     warp_count(s.counts, key, active && kind == 0);
@@ -364,22 +390,23 @@ __global__ void __launch_bounds__(TPB, MCG_DIFFUSE_MIN_BLOCKS) k_diffuse(State<T
 // (outcome_bimolecular / outcome_products_random, diffuse_react_event.cpp:1833, :2446)
 template <typename T>
 __device__ void commit(const State<T>& s, const Proposal& p) {
-  const Chem& ch = *s.g.chem;
-  const uint32_t it = s.cnt->iteration;
+  const uint32_t ma = meta_of(s.a_pos[p.i]);
+  const Geo<T>& g = geo_of(s, ma);
+  const Chem& ch = *g.chem;
+  const uint32_t it = s.cnt->iteration - g.it0;
   s.st[p.i] = 2;
   if (s.st[p.partner] == 0) {
     // the partner had finished its own step: take it out of the histogram
-    P4<T> b = s.b_pos[p.partner];
-    atomicSub(&s.counts[key_of(s, v3<T>(b.x, b.y, b.z), meta_of(b) & META_SPECIES_MASK)], 1u);
+    atomicSub(&s.counts[key_of_rec(s, s.b_pos[p.partner])], 1u);
   }
   s.st[p.partner] = 2;
-  const int sa = (int)(meta_of(s.a_pos[p.i]) & META_SPECIES_MASK);
+  const int sa = (int)(ma & META_SPECIES_MASK);
   const int sb = (int)(meta_of(s.a_pos[p.partner]) & META_SPECIES_MASK);
   const uint64_t uid = s.a_uid[p.i];
   for (int k = 0; k < 2; k++) {
     int ps = ch.bimol_prod[sa][sb][k];
     if (ps >= 0) {
-      add_product(s, ps, v3<T>((T)p.x, (T)p.y, (T)p.z), p.t_abs,
+      add_product(s, ps, g.rep, v3<T>((T)p.x, (T)p.y, (T)p.z), p.t_abs,
                   mix64(uid ^ ((uint64_t)(it + 1) << 40) ^ (0x5Aull << 32) ^ (uint64_t)k));
     }
   }
@@ -447,9 +474,9 @@ __global__ void __launch_bounds__(TPB) k_redo(State<T> s) {
         atomicMin((unsigned long long*)&s.claim[p.partner], (unsigned long long)p.key);
       } else {
         s.st[i] = (uint8_t)kind;
-        if (kind == 0) {
-          P4<T> b = s.b_pos[i];
-          atomicAdd(&s.counts[key_of(s, v3<T>(b.x, b.y, b.z), meta_of(b) & META_SPECIES_MASK)], 1u);
+        if (kind == 0 || kind == 3) {
+          s.st[i] = 0;
+          atomicAdd(&s.counts[key_of_rec(s, s.b_pos[i])], 1u);
         }
       }
     }
@@ -492,9 +519,7 @@ template <typename T>
 __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
   const uint32_t b0 = s.cnt->n_prod_done;
   const uint32_t b1 = s.cnt->prod_hi;
-  const Geo<T>& g = s.g;
-  const Chem& ch = *g.chem;
-  const uint32_t it = s.cnt->iteration;
+  const uint32_t it_engine = s.cnt->iteration;
   uint32_t err = 0;
   for (uint32_t base = b0 + blockIdx.x * TPB; base < b1; base += gridDim.x * TPB) {
     uint32_t k = base + threadIdx.x;
@@ -505,8 +530,11 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
       Product<T> p = s.prod[k];
       const uint32_t meta = meta_of(p.pos);
       const int species = (int)(meta & META_SPECIES_MASK);
+      const Geo<T>& g = geo_of(s, meta);
+      const Chem& ch = *g.chem;
+      const uint32_t it = it_engine - g.it0;
       PhiloxDraws draws;
-      draws.ph.init(s.seed, p.uid, it, 1);
+      draws.ph.init(g.seed, p.uid, it, 1);
       double unimol_time = TIME_FOREVER;
       if (ch.unimol_k[species] >= 0) unimol_time = p.birth + time_of_unimol(ch.unimol_k[species], draws);
       double max_time = 1.0 - p.birth;
@@ -514,7 +542,7 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
       V3<T> pos = v3<T>(p.pos.x, p.pos.y, p.pos.z);
       bool dead = false;
       if (max_time <= 0.0) {
-        unimol_products(s, species, pos, unimol_time, p.uid, it);
+        unimol_products(s, g, species, pos, unimol_time, p.uid, it);
         dead = true;
       } else {
         double steps = 1.0, t_steps = 1.0;
@@ -553,7 +581,7 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
           }
         }
         if (!dead && unimol_time < 1.0) {
-          unimol_products(s, species, pos, unimol_time, p.uid, it);
+          unimol_products(s, g, species, pos, unimol_time, p.uid, it);
           dead = true;
         }
       }
@@ -565,10 +593,10 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
         p.pos.x = pos.x;
         p.pos.y = pos.y;
         p.pos.z = pos.z;
-        set_meta(p.pos, (uint32_t)species);
+        set_meta(p.pos, make_meta((uint32_t)species, g.rep));
         p.tuni = unimol_time - 1.0;
         s.prod[k] = p;
-        key = key_of(s, pos, (uint32_t)species);
+        key = key_of(g, pos, (uint32_t)species);
         survive = true;
       }
       s.pst[k] = survive ? 0 : 2;
@@ -674,10 +702,9 @@ __global__ void k_scan_apply(State<T> s) {
 // ---- scatter into the next sorted arrays
 
 template <typename T>
-__device__ __forceinline__ void scatter_one(const State<T>& s, bool active, const P4<T>& pos, uint64_t uid, T tuni,
-                                            unsigned long long* sp_count) {
+__device__ __forceinline__ void scatter_one(const State<T>& s, bool active, const P4<T>& pos, uint64_t uid, T tuni) {
   uint32_t key = 0;
-  if (active) key = key_of(s, v3<T>(pos.x, pos.y, pos.z), meta_of(pos) & META_SPECIES_MASK);
+  if (active) key = key_of_rec(s, pos);
   unsigned mask = __ballot_sync(0xffffffffu, active);
   if (!active) return;
   unsigned peers = __match_any_sync(mask, key);
@@ -692,14 +719,10 @@ __device__ __forceinline__ void scatter_one(const State<T>& s, bool active, cons
     s.n_uid[slot] = uid;
     s.n_tuni[slot] = tuni;
   }
-  atomicAdd(&sp_count[meta_of(pos) & META_SPECIES_MASK], 1ull);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(TPB) k_scatter(State<T> s, int tuni_shift, int count_species) {
-  __shared__ unsigned long long spc[MAXSP];
-  if (threadIdx.x < MAXSP) spc[threadIdx.x] = 0;
-  __syncthreads();
+__global__ void __launch_bounds__(TPB) k_scatter(State<T> s, int tuni_shift) {
   const uint32_t n = s.cnt->n_live;
   for (uint32_t base = blockIdx.x * TPB; base < n; base += gridDim.x * TPB) {
     uint32_t i = base + threadIdx.x;
@@ -712,7 +735,7 @@ __global__ void __launch_bounds__(TPB) k_scatter(State<T> s, int tuni_shift, int
       uid = s.a_uid[i];
       tuni = s.a_tuni[i] - (T)tuni_shift;
     }
-    scatter_one(s, active, p, uid, tuni, spc);
+    scatter_one(s, active, p, uid, tuni);
   }
   const uint32_t np = min(s.cnt->n_prod, s.prod_cap);
   for (uint32_t base = blockIdx.x * TPB; base < np; base += gridDim.x * TPB) {
@@ -727,19 +750,33 @@ __global__ void __launch_bounds__(TPB) k_scatter(State<T> s, int tuni_shift, int
       uid = q.uid;
       tuni = (T)q.tuni;
     }
-    scatter_one(s, active, p, uid, tuni, spc);
-  }
-  __syncthreads();
-  if (count_species && threadIdx.x < s.g.nsp && spc[threadIdx.x]) {
-    const uint32_t row = s.cnt->iteration % s.traj_cap;
-    atomicAdd(&s.traj[(size_t)row * s.g.nsp + threadIdx.x], spc[threadIdx.x]);
+    scatter_one(s, active, p, uid, tuni);
   }
 }
 
-// bookkeeping at the end of an iteration (single thread)
+// species counts of every replica after the sort: each (replica, species) is one
+// contiguous key range of the next arrays, so its count is a difference of two
+// start offsets
+template <typename T>
+__device__ void count_species(const State<T>& s, uint32_t row) {
+  const uint32_t nq = s.n_rep * (uint32_t)s.nsp;
+  for (uint32_t q = threadIdx.x; q < nq; q += blockDim.x) {
+    const Geo<T>& g = s.geos[q / (uint32_t)s.nsp];
+    const uint32_t a = q % (uint32_t)s.nsp;
+    const uint32_t span = g.n3 << g.oct_shift;
+    const uint32_t k0 = g.kbase + a * span;
+    s.traj[(size_t)row * nq + q] = g.mode == REP_DROP ? 0ull : (unsigned long long)(s.nstart[k0 + span] - s.nstart[k0]);
+  }
+}
+
+// bookkeeping at the end of an iteration (one block)
 template <typename T>
 __global__ void k_end(State<T> s) {
   Counters* c = s.cnt;
+  const uint32_t it = c->iteration;
+  count_species(s, it % s.traj_cap);
+  __syncthreads();
+  if (threadIdx.x != 0) return;
   if (c->n_prod > c->n_prod_done) atomicOr(&c->status, ST_WATCHDOG);  // product chain deeper than the passes
   c->n_live = min(c->n_live_next, s.cap);
   c->n_props = 0;
@@ -748,9 +785,7 @@ __global__ void k_end(State<T> s) {
   c->n_prod_done = 0;
   c->prod_hi = 0;
   c->work = 0;
-  c->iteration += 1;
-  const uint32_t row = c->iteration % s.traj_cap;
-  for (int k = 0; k < s.g.nsp; k++) s.traj[(size_t)row * s.g.nsp + k] = 0;
+  c->iteration = it + 1;
 }
 
 // ---- uploads: bin freshly added molecules (staged in the product list) into the first arrays
@@ -768,8 +803,10 @@ __global__ void k_rebin_count(State<T> s, uint32_t n_staged) {
     if (active) {
       P4<T> p = s.a_pos[i];
       s.b_pos[i] = p;
-      s.st[i] = 0;
-      key = key_of(s, v3<T>(p.x, p.y, p.z), meta_of(p) & META_SPECIES_MASK);
+      // molecules of a dropped replica leave with this re-binning
+      active = geo_of(s, meta_of(p)).mode != REP_DROP;
+      s.st[i] = active ? 0 : 2;
+      if (active) key = key_of_rec(s, p);
     }
     warp_count(s.counts, key, active);
   }
@@ -780,7 +817,7 @@ __global__ void k_rebin_count(State<T> s, uint32_t n_staged) {
     if (active) {
       P4<T> p = s.prod[k].pos;
       s.pst[k] = 0;
-      key = key_of(s, v3<T>(p.x, p.y, p.z), meta_of(p) & META_SPECIES_MASK);
+      key = key_of_rec(s, p);
     }
     warp_count(s.counts, key, active);
   }
@@ -799,6 +836,7 @@ __global__ void k_trace_cases(State<T> s, uint32_t ncases, const uint32_t* idx, 
   const uint32_t i = idx[c];
   P4<T> rec = s.a_pos[i];
   const int species = (int)(meta_of(rec) & META_SPECIES_MASK);
+  const Geo<T>& g = geo_of(s, meta_of(rec));
   InjectedDraws d;
   d.d = draws + (size_t)c * ndraws;
   d.n = ndraws;
@@ -812,7 +850,7 @@ __global__ void k_trace_cases(State<T> s, uint32_t ncases, const uint32_t* idx, 
   cells.start = s.start;
   cells.dead = nullptr;
   V3<T> dv = v3<T>((T)disp[3 * c], (T)disp[3 * c + 1], (T)disp[3 * c + 2]);
-  TraceOut<T> r = trace_molecule<T>(s.g, cells, i, v3<T>(rec.x, rec.y, rec.z), species, dv, rrf[c], tst[c], 0.0, d, ev);
+  TraceOut<T> r = trace_molecule<T>(g, cells, i, v3<T>(rec.x, rec.y, rec.z), species, dv, rrf[c], tst[c], 0.0, d, ev);
   int status = r.status;
   if (d.over) status = 3;
   o[0] = status;

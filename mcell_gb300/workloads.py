@@ -7,6 +7,9 @@ and parameters of the configurations (no public dataset is involved):
 - closed_cube: a reflective 1 um cube (the Model API's create_box) with A and B
   uniformly inside, D_A = D_B = 1e-6 cm^2/s, C with 5e-7, A + B -> C at
   1e8 M^-1 s^-1, dt = 1 us, subpartitions of 0.1 um.
+- replica_models: the batching / serving distribution of independent models
+  (cubes of 0.5-3 um, optional icospheres of level 2-5, 1k-200k molecules,
+  k from 1e6 to 1e9 M^-1 s^-1).
 - sphere_in_cube: an icosphere of radius 1 um (20,480 triangles at 5 subdivision
   levels) transparent to A and reflective to B and C, centred in a reflective
   2.5 um cube; A and B 1:1 uniformly in the cube; A + B -> C at 1e8 M^-1 s^-1,
@@ -91,8 +94,46 @@ def sphere_in_cube(n_mol=1_000_000, seed=1, levels=5, radius_um=1.0, cube_um=2.5
                  pos, sp, dt)
 
 
-def engine_for(model: Model, precision="fp32", seed=1, capacity=0, with_molecules=True):
-    """A prepared GPU engine holding the model (molecules optional)."""
+def replica_models(n_replicas=256, seed=7, n_range=(1_000, 200_000), edge_range_um=(0.5, 3.0),
+                   k_range=(1e6, 1e9), levels=(2, 5), sphere_fraction=0.5, dt=1e-6):
+    """Independent models for batching and serving: reflective cubes of edge
+    log-uniform in edge_range_um, half of them (sphere_fraction) holding an
+    icosphere of radius 0.4 x edge and level uniform in levels (transparent to A,
+    reflective to B and C); molecule counts log-uniform in n_range (A:B 1:1,
+    uniform in the cube); A + B -> C with k log-uniform in k_range M^-1 s^-1,
+    C -> 0 at 1e3 s^-1; D = 1e-6 cm^2/s (C: 5e-7); subpartitions of 0.1 um."""
+    lu = conversion.length_unit_um()
+    R_um = conversion.default_rxn_radius_um()
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(n_replicas):
+        edge = float(np.exp(rng.uniform(np.log(edge_range_um[0]), np.log(edge_range_um[1]))))
+        n_mol = int(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1]))))
+        k = float(np.exp(rng.uniform(np.log(k_range[0]), np.log(k_range[1]))))
+        bv, bw = geometry.create_box(edge_dimension=edge)
+        if rng.uniform() < sphere_fraction:
+            level = int(rng.integers(levels[0], levels[1] + 1))
+            sv, sw = geometry.create_icosphere(0.4 * edge, level)
+            v, w, obj = geometry.merge_meshes((sv, sw), (bv, bw))
+            wc = np.zeros((len(w), 3), np.uint8)
+            wc[obj == 0, 0] = 1
+        else:
+            v, w = bv, bw
+            wc = np.zeros((len(w), 3), np.uint8)
+        lay = conversion.partition_layout(v.min(0), v.max(0), partition_dimension_um=edge + 0.1,
+                                          subpartition_dimension_um=0.1)
+        steps, bimol, unimol = _chemistry(dt, lu, R_um, k_bimol=k, k_unimol=1e3)
+        half = edge / 2 / lu
+        pos = rng.uniform(-half, half, size=(n_mol, 3))
+        sp = (np.arange(n_mol) % 2).astype(np.uint32)
+        out.append(Model(f"replica{r}", lay.origin, lay.edge, lay.nsub, R_um / lu, v / lu, w, wc, steps, bimol,
+                         unimol, pos, sp, dt))
+    return out
+
+
+def model_handle(model: Model, precision="fp32", seed=1, capacity=0, with_molecules=True):
+    """An engine handle holding the model's description, not yet prepared (the
+    form a batch takes models in)."""
     from ._native import Engine
 
     e = Engine(precision, model.origin, model.partition_edge, model.nsub, model.rxn_radius, model.n_species,
@@ -105,5 +146,11 @@ def engine_for(model: Model, precision="fp32", seed=1, capacity=0, with_molecule
         e.add_unimol_rxn(a, k, pr)
     if with_molecules:
         e.add_molecules(model.pos, model.species)
+    return e
+
+
+def engine_for(model: Model, precision="fp32", seed=1, capacity=0, with_molecules=True):
+    """A prepared GPU engine holding the model (molecules optional)."""
+    e = model_handle(model, precision, seed, capacity, with_molecules)
     e.prepare()
     return e

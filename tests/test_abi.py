@@ -68,3 +68,28 @@ def test_fails_loudly_without_device():
     with pytest.raises(_native.EngineError) as ei:
         H.engine_from_scene(sc)
     assert ei.value.code == -2  # MCG_ERR_CUDA, no silent fallback
+
+
+def test_batch_config_validation_and_no_fallback():
+    with pytest.raises(_native.EngineError) as ei:
+        _native.Batch("fp32", 3, 0)                                 # no replica slots
+    assert ei.value.code == -1
+    with pytest.raises(_native.EngineError):
+        _native.Batch("fp32", 17, 4)                                # too many species
+    import torch
+    if torch.cuda.is_available():
+        return
+    with pytest.raises(_native.EngineError) as ei:
+        _native.Batch("fp32", 3, 4)
+    assert ei.value.code == -2  # MCG_ERR_CUDA: a batch needs the device, no CPU path
+
+
+def test_batch_subpartition_autotuner_choices():
+    """The cost model keeps the dense 1M-molecule model's grid and coarsens sparse replicas."""
+    from mcell_gb300 import workloads as W
+    dense = W.sphere_in_cube(n_mol=1_000_000)
+    n, octants = W.model_handle(dense).autotune_subparts()
+    assert n == dense.nsub and octants
+    sparse = W.replica_models(1, seed=1, n_range=(1000, 1001), edge_range_um=(3.0, 3.0), sphere_fraction=0.0)[0]
+    n, octants = W.model_handle(sparse).autotune_subparts()
+    assert n <= sparse.nsub // 2 and not octants
