@@ -250,6 +250,70 @@ def run_gpu(args, rank, world):
     return line
 
 
+# ---------------------------------------------------------------- batching form
+
+def run_batching(args):
+    """Independent replicas (the batching distribution of workloads.replica_models)
+    for args.batch_iters iterations: all in one batch (one launch per kernel per
+    iteration, CUDA graphs, autotuned) against the same models run one after
+    another on the plain engine (graphs on). Both fp32. Times are host wall
+    clock around step + sync of the whole job; model upload is reported apart."""
+    import torch
+
+    from mcell_gb300 import _native
+    from mcell_gb300 import workloads as W
+
+    models = W.replica_models(args.batch_replicas, seed=7)
+    iters = args.batch_iters
+    n_mol = sum(len(m.species) for m in models)
+    # batched
+    t0 = time.perf_counter()
+    b = _native.Batch("fp32", 3, len(models), autotune=True)
+    hs = [W.model_handle(m, "fp32", seed=1000 + k) for k, m in enumerate(models)]
+    ids = b.add(hs)
+    for h in hs:
+        h.close()
+    b.sync()
+    setup_b = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.step(iters)
+    b.sync()
+    job_b = time.perf_counter() - t0
+    _, steps_b, launches_b = b.stats()
+    finals_b = [b.counts(r) for r in ids]
+    blocks = b.diffuse_blocks_per_sm()
+    mem_b = b.device_bytes()
+    b.close()
+    # plain engine, one model after another
+    job_p, setup_p, steps_p = 0.0, 0.0, 0
+    for k, m in enumerate(models):
+        t0 = time.perf_counter()
+        e = W.engine_for(m, "fp32", seed=1000 + k)
+        e.sync()
+        t1 = time.perf_counter()
+        e.step(iters)
+        e.sync()
+        t2 = time.perf_counter()
+        _, st, _ = e.stats()
+        steps_p += st
+        setup_p += t1 - t0
+        job_p += t2 - t1
+        e.close()
+    return {
+        "workload": f"{len(models)} replicas: cubes 0.5-3 um (log-uniform), half with an icosphere (level 2-5, "
+                    f"r = 0.4 edge, transparent to A), 1k-200k molecules (log-uniform, {n_mol} in total), "
+                    f"A+B->C k 1e6-1e9 /M/s (log-uniform), C->0 1e3/s, dt 1 us, fp32, {iters} iterations",
+        "batched": {"job_s": job_b, "setup_s": setup_b, "replicas_per_hour": 3600.0 * len(models) / job_b,
+                    "molecule_steps_per_s": steps_b / job_b, "diffuse_blocks_per_sm": blocks,
+                    "device_bytes": mem_b, "launches": launches_b},
+        "plain_sequential": {"job_s": job_p, "setup_s": setup_p, "replicas_per_hour": 3600.0 * len(models) / job_p,
+                             "molecule_steps_per_s": steps_p / job_p},
+        "speedup_replicas_per_hour": job_p / job_b,
+        "final_counts_replica0": [int(x) for x in finals_b[0]],
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -260,6 +324,9 @@ def main():
     ap.add_argument("--cpu-procs", type=int, default=0, help="CPU processes (0 = all host cores)")
     ap.add_argument("--cpu-iters", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batching measurement")
+    ap.add_argument("--batch-replicas", type=int, default=256)
+    ap.add_argument("--batch-iters", type=int, default=1000)
     args = ap.parse_args()
     rank, world, _ = _rank_env()
     procs = args.cpu_procs or os.cpu_count() or 1
@@ -300,6 +367,8 @@ def main():
         import torch
         torch.distributed.init_process_group("nccl")
     line = run_gpu(args, rank, world)
+    if rank == 0 and not args.no_batch:
+        line["batching"] = run_batching(args)
     if rank == 0:
         if cpu:
             line["cpu_baseline"] = cpu
