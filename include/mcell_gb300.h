@@ -205,9 +205,66 @@ int mcg_batch_get_profile(mcg_batch* b, double* out);
    kernel runs with (the autotuner's choice, or the maximum). */
 int mcg_batch_get_memory(mcg_batch* b, uint64_t* device_bytes);
 int mcg_batch_get_tuning(mcg_batch* b, int* diffuse_blocks_per_sm);
+/* As mcg_get_escapes, with a 13th double per record: the replica. */
+int mcg_batch_get_escapes(mcg_batch* b, uint32_t cap, double* out, uint32_t* n);
 /* The autotuner's subpartition choice for a model (host only, no device):
    subpartitions per edge and whether occupants are binned per octant. */
 int mcg_autotune_subparts(const mcg_engine* model, uint32_t* subparts_per_edge, int* octants);
+
+/* ---- Serving: simulation requests that arrive at any time, continuously
+   batched on one device (no counterpart in the reference). A worker thread
+   owns a batch; between blocks of iterations it admits queued requests, first
+   come first served, as replica slots and the device-memory budget allow, runs
+   every admitted request in the same kernels, and collects the requests that
+   reached their iteration count. A request's molecules, mesh and partition stay
+   resident on the device from admission to its last iteration. Results (the
+   species-count trajectory) are the same as the model run alone. The model
+   handle is copied at submission and may be destroyed afterwards. */
+typedef struct mcg_server mcg_server;
+
+typedef struct mcg_server_config {
+  int precision;              /* MCG_PRECISION_FP64 / MCG_PRECISION_FP32 */
+  uint32_t n_species;         /* species of every request */
+  uint32_t max_slots;         /* requests on the device at once (<= 65536) */
+  uint64_t hbm_budget_bytes;  /* device memory the admitted requests may hold (estimated per request) */
+  int autotune;               /* as mcg_batch_config.autotune */
+} mcg_server_config;
+
+#define MCG_REQ_QUEUED 0
+#define MCG_REQ_RUNNING 1
+#define MCG_REQ_DONE 2
+#define MCG_REQ_CANCELLED 3
+#define MCG_REQ_FAILED 4
+
+typedef struct mcg_serve_stats {
+  uint64_t queued, running, completed;
+  uint64_t mol_steps;       /* molecule-steps run by the server */
+  uint64_t reserved_bytes;  /* budget held by running requests */
+  double busy_seconds;      /* wall time spent in blocks of iterations */
+  int failed;               /* 1 after a device error (every open request failed) */
+} mcg_serve_stats;
+
+/* On MCG_ERR_CUDA *out still receives a handle for mcg_serve_last_error /
+   mcg_serve_destroy. */
+int mcg_serve_create(const mcg_server_config* cfg, mcg_server** out);
+/* Stops the worker (open requests are abandoned) and frees everything. */
+void mcg_serve_destroy(mcg_server* s);
+const char* mcg_serve_last_error(const mcg_server* s);
+int mcg_serve_submit(mcg_server* s, const mcg_engine* model, uint32_t n_iterations, uint64_t* ticket);
+/* State of a request and seconds from submission to its result (or until now). */
+int mcg_serve_poll(mcg_server* s, uint64_t ticket, int* state, double* seconds);
+/* Blocks until the request is no longer queued or running, or timeout_s passes. */
+int mcg_serve_wait(mcg_server* s, uint64_t ticket, double timeout_s, int* state);
+/* Result of a finished request: counts after its last iteration ([n_species]) and
+   its count trajectory (up to cap_rows rows of n_species, one per iteration);
+   *n_rows = its iteration count. */
+int mcg_serve_result(mcg_server* s, uint64_t ticket, uint64_t* final_counts, uint32_t cap_rows, uint64_t* trajectory,
+                     uint32_t* n_rows);
+/* Queued requests leave the queue; running ones stop at the end of the current block. */
+int mcg_serve_cancel(mcg_server* s, uint64_t ticket);
+/* Forgets a finished, cancelled or failed request (frees its host result). */
+int mcg_serve_release(mcg_server* s, uint64_t ticket);
+int mcg_serve_get_stats(mcg_server* s, mcg_serve_stats* out);
 
 /* Setup queries for parity tests: wall constants (14 doubles per wall, same
    layout as the oracle) and the wall lists per subpartition. */

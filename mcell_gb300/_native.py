@@ -30,7 +30,9 @@ EXPORTS = [
     "mcg_batch_step", "mcg_batch_sync", "mcg_batch_replica_info", "mcg_batch_get_counts",
     "mcg_batch_get_count_trajectory", "mcg_batch_download_molecules", "mcg_batch_get_stats",
     "mcg_batch_set_options", "mcg_batch_get_profile", "mcg_batch_get_memory", "mcg_batch_get_tuning",
-    "mcg_autotune_subparts",
+    "mcg_autotune_subparts", "mcg_batch_get_escapes",
+    "mcg_serve_create", "mcg_serve_destroy", "mcg_serve_last_error", "mcg_serve_submit", "mcg_serve_poll",
+    "mcg_serve_wait", "mcg_serve_result", "mcg_serve_cancel", "mcg_serve_release", "mcg_serve_get_stats",
 ]
 
 
@@ -55,6 +57,31 @@ class McgBatchConfig(ctypes.Structure):
         ("capacity", ctypes.c_uint64),
         ("autotune", ctypes.c_int),
     ]
+
+
+class McgServerConfig(ctypes.Structure):
+    _fields_ = [
+        ("precision", ctypes.c_int),
+        ("n_species", ctypes.c_uint32),
+        ("max_slots", ctypes.c_uint32),
+        ("hbm_budget_bytes", ctypes.c_uint64),
+        ("autotune", ctypes.c_int),
+    ]
+
+
+class McgServeStats(ctypes.Structure):
+    _fields_ = [
+        ("queued", ctypes.c_uint64),
+        ("running", ctypes.c_uint64),
+        ("completed", ctypes.c_uint64),
+        ("mol_steps", ctypes.c_uint64),
+        ("reserved_bytes", ctypes.c_uint64),
+        ("busy_seconds", ctypes.c_double),
+        ("failed", ctypes.c_int),
+    ]
+
+
+REQ_STATES = {0: "queued", 1: "running", 2: "done", 3: "cancelled", 4: "failed"}
 
 
 class EngineError(RuntimeError):
@@ -83,6 +110,12 @@ def lib():
         L.mcg_batch_destroy.restype = None
         L.mcg_batch_last_error.argtypes = [vp]
         L.mcg_batch_last_error.restype = ctypes.c_char_p
+        L.mcg_serve_create.argtypes = [ctypes.POINTER(McgServerConfig), ctypes.POINTER(vp)]
+        L.mcg_serve_destroy.argtypes = [vp]
+        L.mcg_serve_destroy.restype = None
+        L.mcg_serve_last_error.argtypes = [vp]
+        L.mcg_serve_last_error.restype = ctypes.c_char_p
+        L.mcg_serve_wait.argtypes = [vp, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
         for name in EXPORTS:
             getattr(L, name)
         _lib = L
@@ -362,7 +395,92 @@ class Batch:
         self._chk(lib().mcg_batch_get_memory(self.h, ctypes.byref(b)))
         return b.value
 
+    def escapes(self):
+        """Molecules that left their partition: rows of uid, species + 1000 * kind, iteration, start xyz,
+        displacement xyz, final xyz, replica (kind 1 escape, 2 watchdog)."""
+        out = np.zeros((8, 13))
+        n = ctypes.c_uint32()
+        self._chk(lib().mcg_batch_get_escapes(self.h, ctypes.c_uint32(8), _p(out), ctypes.byref(n)))
+        return out[:min(n.value, 8)], n.value
+
     def diffuse_blocks_per_sm(self):
         v = ctypes.c_int()
         self._chk(lib().mcg_batch_get_tuning(self.h, ctypes.byref(v)))
         return v.value
+
+
+class Server:
+    """Serving loop (mcg_serve_*): requests are continuously batched on the device
+    by a worker thread inside the library. Models are unprepared Engine objects,
+    copied at submission."""
+
+    def __init__(self, precision, n_species, max_slots=256, hbm_budget_bytes=150 << 30, autotune=True):
+        L = lib()
+        cfg = McgServerConfig()
+        cfg.precision = PRECISION[precision] if isinstance(precision, str) else int(precision)
+        cfg.n_species = int(n_species)
+        cfg.max_slots = int(max_slots)
+        cfg.hbm_budget_bytes = int(hbm_budget_bytes)
+        cfg.autotune = 1 if autotune else 0
+        h = ctypes.c_void_p()
+        rc = L.mcg_serve_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != MCG_OK:
+            msg = L.mcg_serve_last_error(h) if h.value else b"mcg_serve_create rejected the configuration"
+            if h.value:
+                L.mcg_serve_destroy(h)
+            raise EngineError(rc, msg.decode() if msg else "")
+        self.h = h
+        self.n_species = int(n_species)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mcg_serve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        if rc != MCG_OK:
+            msg = lib().mcg_serve_last_error(self.h)
+            raise EngineError(rc, msg.decode() if msg else "")
+
+    def submit(self, model, n_iterations):
+        t = ctypes.c_uint64()
+        self._chk(lib().mcg_serve_submit(self.h, model.h, ctypes.c_uint32(n_iterations), ctypes.byref(t)))
+        return t.value
+
+    def poll(self, ticket):
+        st = ctypes.c_int()
+        sec = ctypes.c_double()
+        self._chk(lib().mcg_serve_poll(self.h, ctypes.c_uint64(ticket), ctypes.byref(st), ctypes.byref(sec)))
+        return REQ_STATES[st.value], sec.value
+
+    def wait(self, ticket, timeout_s=600.0):
+        st = ctypes.c_int()
+        self._chk(lib().mcg_serve_wait(self.h, ctypes.c_uint64(ticket), ctypes.c_double(timeout_s), ctypes.byref(st)))
+        return REQ_STATES[st.value]
+
+    def result(self, ticket):
+        n = ctypes.c_uint32()
+        self._chk(lib().mcg_serve_result(self.h, ctypes.c_uint64(ticket), None, ctypes.c_uint32(0), None,
+                                         ctypes.byref(n)))
+        traj = np.zeros((n.value, self.n_species), np.uint64)
+        final = np.zeros(self.n_species, np.uint64)
+        self._chk(lib().mcg_serve_result(self.h, ctypes.c_uint64(ticket), _p(final), ctypes.c_uint32(n.value),
+                                         _p(traj), ctypes.byref(n)))
+        return final, traj
+
+    def cancel(self, ticket):
+        self._chk(lib().mcg_serve_cancel(self.h, ctypes.c_uint64(ticket)))
+
+    def release(self, ticket):
+        self._chk(lib().mcg_serve_release(self.h, ctypes.c_uint64(ticket)))
+
+    def stats(self):
+        st = McgServeStats()
+        self._chk(lib().mcg_serve_get_stats(self.h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in McgServeStats._fields_}

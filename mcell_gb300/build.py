@@ -6,6 +6,7 @@ Translation units are compiled in parallel:
   mcg_setup.cpp host setup (wall constants, wall binning), -ffp-contract=off
   mcg_api.cpp   C ABI (single models)
   mcg_batch.cpp C ABI of batches (replicas) and the batch autotuner
+  mcg_serve.cpp C ABI of the serving loop (continuous batching on a worker thread)
   mcg_trace_static.cu  fixed device scratch of mcg_trace_cases_static
 Usage: python -m mcell_gb300.build [--force] [-v]
 """
@@ -44,6 +45,7 @@ def _units():
         ("mcg_setup.cpp", ["-x", "c++"] + host),
         ("mcg_api.cpp", ["-x", "c++"] + host),
         ("mcg_batch.cpp", ["-x", "c++"] + host),
+        ("mcg_serve.cpp", ["-x", "c++"] + host),
     ]
 
 
@@ -77,7 +79,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=len(units)) as ex:
         list(ex.map(compile_one, units))
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nv, "-shared", ARCH, "-o", str(tmp)] + [str(o) for o in objs]
+    cmd = [nv, "-shared", ARCH, "-o", str(tmp)] + [str(o) for o in objs] + ["-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode:
         sys.stderr.write(r.stdout + r.stderr)

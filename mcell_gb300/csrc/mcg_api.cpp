@@ -1,6 +1,7 @@
 // C ABI of the engine (declared in include/mcell_gb300.h).
 #include "../../include/mcell_gb300.h"
 
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -255,8 +256,12 @@ int mcg_get_debug_log(mcg_engine* e, double* out) {
 int mcg_get_escapes(mcg_engine* e, uint32_t cap, double* out, uint32_t* n) {
   if (!e || !n || (cap && !out) || !e->dev) return MCG_ERR_ARG;
   std::string err;
-  int rc = e->dev->escapes(out, cap, n, err);
-  return rc ? fail(e, rc, err) : MCG_OK;
+  double rec[8 * 13];
+  int rc = e->dev->escapes(rec, 8, n, err);
+  if (rc) return fail(e, rc, err);
+  for (uint32_t k = 0; k < std::min<uint32_t>(std::min<uint32_t>(cap, *n), 8); k++)
+    std::memcpy(out + 12 * k, rec + 13 * k, 12 * sizeof(double));  // the replica field is always 0 here
+  return MCG_OK;
 }
 
 int mcg_trace_cases(mcg_engine* e, uint32_t n, const uint64_t* ids, const double* disp, const uint32_t* draws,

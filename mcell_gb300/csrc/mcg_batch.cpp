@@ -6,16 +6,7 @@
 #include <string>
 #include <vector>
 
-#include "mcg_model.h"
-
-struct mcg_batch {
-  mcg_batch_config cfg;
-  std::string err;
-  mcg::DeviceEngine* dev = nullptr;
-  std::vector<uint32_t> nsub;  // subpartitions per edge of each replica slot
-  bool tune_pending = false;
-  int diffuse_blocks = 0;
-};
+#include "mcg_batch.h"
 
 namespace {
 
@@ -280,6 +271,17 @@ int mcg_batch_get_memory(mcg_batch* b, uint64_t* bytes) {
   if (!b || !bytes) return MCG_ERR_ARG;
   if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
   *bytes = b->dev->device_bytes();
+  return MCG_OK;
+}
+
+int mcg_batch_get_escapes(mcg_batch* b, uint32_t cap, double* out, uint32_t* n) {
+  if (!b || !n || (cap && !out)) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  std::string err;
+  double rec[8 * 13];
+  int rc = b->dev->escapes(rec, 8, n, err);
+  if (rc) return bfail(b, rc, err);
+  std::memcpy(out, rec, sizeof(double) * 13 * std::min<uint32_t>(std::min<uint32_t>(cap, *n), 8));
   return MCG_OK;
 }
 

@@ -456,7 +456,7 @@ class DeviceEngineT : public DeviceEngine {
     if (read_counters(err)) return -2;
     *n = cnt_.n_esc;
     for (uint32_t k = 0; k < std::min<uint32_t>(std::min<uint32_t>(cap, cnt_.n_esc), 8); k++)
-      for (int q = 0; q < 12; q++) out[k * 12 + q] = cnt_.esc[k][q];
+      for (int q = 0; q < 13; q++) out[k * 13 + q] = cnt_.esc[k][q];
     return 0;
   }
 

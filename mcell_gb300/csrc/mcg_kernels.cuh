@@ -49,9 +49,9 @@ struct Counters {
   unsigned long long mol_steps;
   unsigned long long warn_coll_overflow;
   unsigned long long warn_set_overflow;
-  // first escapes (diagnostics): uid, species, iteration, start xyz, displacement xyz, final xyz
+  // first escapes (diagnostics): uid, species, iteration, start xyz, displacement xyz, final xyz, replica
   uint32_t n_esc;
-  double esc[8][12];
+  double esc[8][13];
 };
 
 struct Proposal {
@@ -325,6 +325,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
                                (double)pos.x, (double)pos.y, (double)pos.z, (double)disp.x, (double)disp.y,
                                (double)disp.z, (double)r.pos.x, (double)r.pos.y, (double)r.pos.z};
       for (int q = 0; q < 12; q++) s.cnt->esc[k][q] = rec_[q];
+      s.cnt->esc[k][12] = (double)g.rep;
     }
   }
   if (escaped) {

@@ -93,3 +93,15 @@ def test_batch_subpartition_autotuner_choices():
     sparse = W.replica_models(1, seed=1, n_range=(1000, 1001), edge_range_um=(3.0, 3.0), sphere_fraction=0.0)[0]
     n, octants = W.model_handle(sparse).autotune_subparts()
     assert n <= sparse.nsub // 2 and not octants
+
+
+def test_server_needs_the_device():
+    with pytest.raises(_native.EngineError) as ei:
+        _native.Server("fp32", 3, max_slots=0)
+    assert ei.value.code == -1
+    import torch
+    if torch.cuda.is_available():
+        return
+    with pytest.raises(_native.EngineError) as ei:
+        _native.Server("fp32", 3, max_slots=4)
+    assert ei.value.code == -2
