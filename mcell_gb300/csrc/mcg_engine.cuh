@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <array>
 #include <climits>
+#include <cmath>
 #include <cstring>
 #include <unordered_map>
 
@@ -483,7 +484,39 @@ class DeviceEngineT : public DeviceEngine {
     uint32_t* wsp_list = nullptr;
     uint8_t* wclass = nullptr;
     Chem* chem = nullptr;
+    // host copies for placing fp32 molecules: wall planes (n xyz, d), walls per
+    // subpartition, and the grid
+    std::vector<double> planes;
+    std::vector<uint32_t> h_wsp_off, h_wsp_list;
+    double origin[3] = {0, 0, 0}, sp_rcp = 1;
+    uint32_t nsub = 1;
   };
+
+  // Rounding a position to fp32 can put a molecule that lies within a few ulps of
+  // a wall on the plane or behind it, from where it would leave without a hit.
+  // Such molecules are moved along the wall normal to 1e-4 internal units (or 8
+  // ulps of the coordinates, if larger) from the plane, on their own side, before
+  // rounding; the walls checked are those listed for the molecule's subpartition
+  // (every wall within the reaction radius of it).
+  void place_fp32(const Rep& R, double* p) const {
+    if (sizeof(T) != 4 || R.planes.empty()) return;
+    int ix[3];
+    for (int a = 0; a < 3; a++) {
+      ix[a] = (int)((p[a] - R.origin[a]) * R.sp_rcp);
+      ix[a] = std::min(std::max(ix[a], 0), (int)R.nsub - 1);
+    }
+    const size_t sp = (size_t)ix[0] + (size_t)ix[1] * R.nsub + (size_t)ix[2] * R.nsub * R.nsub;
+    const double mag = std::max(std::fabs(p[0]), std::max(std::fabs(p[1]), std::fabs(p[2])));
+    const double margin = std::max(1e-4, 8.0 * mag * 1.1920928955078125e-07);
+    for (int pass = 0; pass < 2; pass++)
+      for (uint32_t k = R.h_wsp_off[sp]; k < R.h_wsp_off[sp + 1]; k++) {
+        const double* pl = &R.planes[4 * (size_t)R.h_wsp_list[k]];
+        const double dd = pl[0] * p[0] + pl[1] * p[1] + pl[2] * p[2] - pl[3];
+        if (std::fabs(dd) >= margin) continue;
+        const double shift = (dd >= 0 ? margin : -margin) - dd;
+        for (int a = 0; a < 3; a++) p[a] += shift * pl[a];
+      }
+  }
 
   static uint32_t host_meta(const P4<T>& p) {
     if (sizeof(T) == 8) {
@@ -596,6 +629,16 @@ class DeviceEngineT : public DeviceEngine {
     g.wall_class = R.wclass;
     g.chem = R.chem;
     R.span = (uint32_t)(base_keys << g.oct_shift);
+    if (sizeof(T) == 4) {
+      R.planes.resize(4 * (size_t)nw);
+      for (uint32_t w = 0; w < nw; w++)
+        for (int k = 0; k < 4; k++) R.planes[4 * (size_t)w + k] = hs.wall[(size_t)w * 24 + k];
+      R.h_wsp_off = hs.wsp_off;
+      R.h_wsp_list = hs.wsp_list;
+      for (int a = 0; a < 3; a++) R.origin[a] = hs.origin[a];
+      R.sp_rcp = hs.sp_rcp;
+      R.nsub = hs.nsub;
+    }
     geos_h_[r] = g;
     return 0;
   }
@@ -627,11 +670,12 @@ class DeviceEngineT : public DeviceEngine {
         err = "species index out of range";
         return -1;
       }
-      const double* p = pos + 3 * i;
+      double p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
       if (!(p[0] >= o[0] && p[1] >= o[1] && p[2] >= o[2] && p[0] < q[0] && p[1] < q[1] && p[2] < q[2])) {
         err = "molecule outside the partition";
         return -4;
       }
+      place_fp32(reps_[r], p);
       Product<T> m;
       m.pos.x = (T)p[0];
       m.pos.y = (T)p[1];

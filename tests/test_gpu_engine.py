@@ -177,3 +177,34 @@ def test_fp32_large_model_stays_confined():
     assert (np.abs(pos) <= 125.0).all()
     c = e.counts()
     assert c[0] == c[1] and c[0] + c[2] <= 500000
+
+
+def test_fp32_molecules_released_on_walls_stay_inside():
+    """Molecules released within 1e-8 internal units of the cube's faces, edges
+    and corners: rounded to fp32 they would sit on a face plane (or behind it)
+    and leave without a hit; the upload moves them to 1e-4 inside first."""
+    from mcell_gb300 import conversion, geometry, workloads
+    from mcell_gb300.workloads import Model, _chemistry
+    lu = conversion.length_unit_um()
+    edge = 0.8991  # a face coordinate (44.955...) that is not an fp32 number
+    v, w = geometry.create_box(edge_dimension=edge)
+    lay = conversion.partition_layout(v.min(0), v.max(0), partition_dimension_um=edge + 0.1,
+                                      subpartition_dimension_um=0.1)
+    steps, bimol, unimol = _chemistry(1e-6, lu, conversion.default_rxn_radius_um())
+    h = edge / 2 / lu
+    rng = np.random.default_rng(3)
+    n = 6000
+    pos = rng.uniform(-h, h, size=(n, 3))
+    axis = rng.integers(0, 3, size=n)
+    sign = rng.choice([-1.0, 1.0], size=n)
+    inset = rng.uniform(0, 1e-8, size=n)
+    pos[np.arange(n), axis] = sign * (h - inset)
+    pos[:200] = sign[:200, None] * (h - inset[:200, None])  # corners
+    sp = (np.arange(n) % 2).astype(np.uint32)
+    m = Model("faces", lay.origin, lay.edge, lay.nsub, conversion.default_rxn_radius_um() / lu, v / lu, w,
+              np.zeros((len(w), 3), np.uint8), steps, [], [], pos, sp, 1e-6)
+    e = workloads.engine_for(m, "fp32", seed=11)
+    e.step(40)
+    e.sync()  # raises MCG_ERR_ESCAPE on a leak
+    p, _, _ = e.molecules()
+    assert len(p) == n and (np.abs(p) <= float(np.float32(h))).all()
