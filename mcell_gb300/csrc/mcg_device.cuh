@@ -524,6 +524,34 @@ __device__ __forceinline__ int plane_test(S dd, S dv, S eps, S& a) {
   return PT_HIT;
 }
 
+// in-triangle part of collide_wall (collision_utils.inl:718-810) at a plane crossing
+// with coordinates b (along unit_u) and c (along unit_v) from vertex 0: outside,
+// inside, or within eps of the edge v1-v2 / v2-v0 / v0-v1 (a re-try)
+enum : int { TRI_OUT = 0, TRI_IN = 1, TRI_E12 = 2, TRI_E20 = 3, TRI_E01 = 4 };
+template <typename S>
+__device__ __forceinline__ int tri_test(S b, S c, S uv1u, S uv2u, S uv2v, S eps) {
+  S f;
+  if (uv2v < 0) {
+    c = -c;
+    f = -uv2v;
+  } else {
+    f = uv2v;
+  }
+  if (c > 0) {
+    S gg = b * f;
+    S h = c * uv2u;
+    if (gg > h) {
+      if (c * uv1u + gg < h + uv1u * uv2v) return TRI_IN;
+      if (!distinguishable<S>(c * uv1u + gg, h + uv1u * uv2v, eps)) return TRI_E12;
+      return TRI_OUT;
+    }
+    if (!distinguishable<S>(gg, h, eps)) return TRI_E20;
+    return TRI_OUT;
+  }
+  if (!distinguishable<S>(c, (S)0.0, eps)) return TRI_E01;
+  return TRI_OUT;
+}
+
 // collide_wall (collision_utils.inl:629-812)
 template <typename T, class D>
 __device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V3<T>& move, T& ct, V3<T>& cpos) {
@@ -561,36 +589,40 @@ __device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V
   cpos = pos + scale(move, a);
   const WallFace<T>& w = g.wface[wi];
   V3<T> local = cpos - w.v0;
-  T b = dot(local, w.u);
-  T c = dot(local, w.v);
-  T f;
-  if (w.uv2v < 0) {
-    c = -c;
-    f = -w.uv2v;
-  } else {
-    f = w.uv2v;
-  }
-  if (c > 0) {
-    T gg = b * f;
-    T h = c * w.uv2u;
-    if (gg > h) {
-      if (c * w.uv1u + gg < h + w.uv1u * w.uv2v) {
-        return dv > 0 ? CT_BACK : CT_FRONT;
-      } else if (!distinguishable<T>(c * w.uv1u + gg, h + w.uv1u * w.uv2v, Eps<T>::pos)) {
-        jump_away_line(pos, a, w.v1, w.v2, normal, draws, move);
-        return CT_REDO;
-      }
-      return CT_MISS;
-    } else if (!distinguishable<T>(gg, h, Eps<T>::pos)) {
-      jump_away_line(pos, a, w.v2, w.v0, normal, draws, move);
-      return CT_REDO;
+  int tr = tri_test<T>(dot(local, w.u), dot(local, w.v), w.uv1u, w.uv2u, w.uv2v, Eps<T>::pos);
+  if (sizeof(T) == 4 && tr >= TRI_E12) {
+    // fp32 tie-break near an edge or vertex: the float test is within its own
+    // rounding there (a molecule released on a face diagonal would re-try until the
+    // watchdog), so the crossing and the in-triangle test are redone in fp64 on the
+    // exact float inputs, with the fp64 band; only a crossing within that band of
+    // the edge is re-tried.
+    const double nx = normal.x, ny = normal.y, nz = normal.z;
+    const double px = pos.x, py = pos.y, pz = pos.z, mx = move.x, my = move.y, mz = move.z;
+    const double ddd = (nx * px + ny * py + nz * pz) - (double)rj.w;
+    const double dvd = nx * mx + ny * my + nz * mz;
+    double ad = 0;
+    const int ptd = plane_test<double>(ddd, dvd, Eps<double>::pos, ad);
+    if (ptd == PT_MISS) return CT_MISS;
+    if (ptd == PT_HIT) {
+      const double cx = px + mx * ad, cy = py + my * ad, cz = pz + mz * ad;
+      const double lx = cx - (double)w.v0.x, ly = cy - (double)w.v0.y, lz = cz - (double)w.v0.z;
+      const double bd = lx * (double)w.u.x + ly * (double)w.u.y + lz * (double)w.u.z;
+      const double cd = lx * (double)w.v.x + ly * (double)w.v.y + lz * (double)w.v.z;
+      tr = tri_test<double>(bd, cd, (double)w.uv1u, (double)w.uv2u, (double)w.uv2v, Eps<double>::pos);
+      ct = (T)ad;
+      cpos = v3<T>((T)cx, (T)cy, (T)cz);
+      dv = (T)dvd;
     }
-    return CT_MISS;
-  } else if (!distinguishable<T>(c, (T)0.0, Eps<T>::pos)) {
-    jump_away_line(pos, a, w.v0, w.v1, normal, draws, move);
-    return CT_REDO;
   }
-  return CT_MISS;
+  if (tr == TRI_IN) return dv > 0 ? CT_BACK : CT_FRONT;
+  if (tr == TRI_OUT) return CT_MISS;
+  if (tr == TRI_E12)
+    jump_away_line(pos, ct, w.v1, w.v2, normal, draws, move);
+  else if (tr == TRI_E20)
+    jump_away_line(pos, ct, w.v2, w.v0, normal, draws, move);
+  else
+    jump_away_line(pos, ct, w.v0, w.v1, normal, draws, move);
+  return CT_REDO;
 }
 
 // fp32 tie-break in fp64: puts `pos` on the given side (+1 front, -1 back) of the
