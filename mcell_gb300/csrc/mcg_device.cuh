@@ -136,6 +136,9 @@ struct Geo {
   const uint32_t* wsp_list;   // entries: wall index << 8 | mask of the subpartition octants it reaches
   const uint8_t* wall_class;  // [wall * nsp + species]: 0 reflect, 1 transparent, 2 absorptive
   const Chem* chem;
+  // fp32 engines: the wall constants in fp64 for the tie-breaks, 16 per wall (normal
+  // xyz, d, unit_u xyz, unit_v xyz, v0 xyz, uv_vert1_u, uv_vert2 u v); null in fp64
+  const double* w64;
 };
 
 // molecules at the start of the iteration, sorted by key (replica, species, subpartition, octant)
@@ -562,15 +565,14 @@ __device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V
   T dd = dp - rj.w;
   T a;
   int pt;
+  const double* w64 = (sizeof(T) == 4) ? g.w64 + 16 * (size_t)wi : nullptr;
   if (sizeof(T) == 4 && tabs(dd) < (T)1e-2) {
     // fp32 tie-break: near the plane the fp32 side test can have the wrong sign (its
     // error grows with the coordinates), letting a molecule moving outwards pass a
-    // reflective wall. The float plane and position are exact in fp64, so the side
-    // test is redone there.
-    const double ddd = ((double)normal.x * (double)pos.x + (double)normal.y * (double)pos.y +
-                        (double)normal.z * (double)pos.z) - (double)rj.w;
-    const double dvd = (double)normal.x * (double)move.x + (double)normal.y * (double)move.y +
-                       (double)normal.z * (double)move.z;
+    // reflective wall. The side test is redone in fp64 with the fp64 plane (the float
+    // position is exact in fp64).
+    const double ddd = (w64[0] * (double)pos.x + w64[1] * (double)pos.y + w64[2] * (double)pos.z) - w64[3];
+    const double dvd = w64[0] * (double)move.x + w64[1] * (double)move.y + w64[2] * (double)move.z;
     double ad = 0;
     pt = plane_test<double>(ddd, dvd, (double)Eps<T>::pos, ad);
     a = (T)ad;
@@ -592,23 +594,23 @@ __device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V
   int tr = tri_test<T>(dot(local, w.u), dot(local, w.v), w.uv1u, w.uv2u, w.uv2v, Eps<T>::pos);
   if (sizeof(T) == 4 && tr >= TRI_E12) {
     // fp32 tie-break near an edge or vertex: the float test is within its own
-    // rounding there (a molecule released on a face diagonal would re-try until the
-    // watchdog), so the crossing and the in-triangle test are redone in fp64 on the
-    // exact float inputs, with the fp64 band; only a crossing within that band of
+    // rounding there, and the float constants of two triangles sharing an edge do
+    // not meet exactly (a ray can pass between them, or re-try at a face diagonal
+    // until the watchdog). The crossing and the in-triangle test are redone in fp64
+    // with the fp64 wall constants and band; only a crossing within that band of
     // the edge is re-tried.
-    const double nx = normal.x, ny = normal.y, nz = normal.z;
     const double px = pos.x, py = pos.y, pz = pos.z, mx = move.x, my = move.y, mz = move.z;
-    const double ddd = (nx * px + ny * py + nz * pz) - (double)rj.w;
-    const double dvd = nx * mx + ny * my + nz * mz;
+    const double ddd = (w64[0] * px + w64[1] * py + w64[2] * pz) - w64[3];
+    const double dvd = w64[0] * mx + w64[1] * my + w64[2] * mz;
     double ad = 0;
     const int ptd = plane_test<double>(ddd, dvd, Eps<double>::pos, ad);
     if (ptd == PT_MISS) return CT_MISS;
     if (ptd == PT_HIT) {
       const double cx = px + mx * ad, cy = py + my * ad, cz = pz + mz * ad;
-      const double lx = cx - (double)w.v0.x, ly = cy - (double)w.v0.y, lz = cz - (double)w.v0.z;
-      const double bd = lx * (double)w.u.x + ly * (double)w.u.y + lz * (double)w.u.z;
-      const double cd = lx * (double)w.v.x + ly * (double)w.v.y + lz * (double)w.v.z;
-      tr = tri_test<double>(bd, cd, (double)w.uv1u, (double)w.uv2u, (double)w.uv2v, Eps<double>::pos);
+      const double lx = cx - w64[10], ly = cy - w64[11], lz = cz - w64[12];
+      const double bd = lx * w64[4] + ly * w64[5] + lz * w64[6];
+      const double cd = lx * w64[7] + ly * w64[8] + lz * w64[9];
+      tr = tri_test<double>(bd, cd, w64[13], w64[14], w64[15], Eps<double>::pos);
       ct = (T)ad;
       cpos = v3<T>((T)cx, (T)cy, (T)cz);
       dv = (T)dvd;

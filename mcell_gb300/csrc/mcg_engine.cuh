@@ -484,6 +484,7 @@ class DeviceEngineT : public DeviceEngine {
     uint32_t* wsp_list = nullptr;
     uint8_t* wclass = nullptr;
     Chem* chem = nullptr;
+    double* w64 = nullptr;  // fp32 engines: fp64 wall constants for the tie-breaks
     // host copies for placing fp32 molecules: wall planes (n xyz, d), walls per
     // subpartition, and the grid
     std::vector<double> planes;
@@ -628,6 +629,23 @@ class DeviceEngineT : public DeviceEngine {
     g.wsp_list = R.wsp_list;
     g.wall_class = R.wclass;
     g.chem = R.chem;
+    g.w64 = nullptr;
+    if (sizeof(T) == 4) {
+      std::vector<double> w64(16 * (size_t)std::max<uint32_t>(nw, 1), 0.0);
+      for (uint32_t w = 0; w < nw; w++) {
+        const double* o = &hs.wall[(size_t)w * 24];
+        double* q = &w64[16 * (size_t)w];
+        for (int k = 0; k < 10; k++) q[k] = o[k];  // normal, d, unit_u, unit_v
+        q[10] = o[13];                               // v0
+        q[11] = o[14];
+        q[12] = o[15];
+        q[13] = o[10];                               // uv_vert1_u, uv_vert2 u v
+        q[14] = o[11];
+        q[15] = o[12];
+      }
+      if (alloc_copy(&R.w64, w64, R.bytes, err)) return -2;
+      g.w64 = R.w64;
+    }
     R.span = (uint32_t)(base_keys << g.oct_shift);
     if (sizeof(T) == 4) {
       R.planes.resize(4 * (size_t)nw);
@@ -651,6 +669,7 @@ class DeviceEngineT : public DeviceEngine {
     cudaFree(R.wsp_list);
     cudaFree(R.wclass);
     cudaFree(R.chem);
+    cudaFree(R.w64);
     R = Rep();
     Geo<T> g{};
     g.mode = REP_DROP;
