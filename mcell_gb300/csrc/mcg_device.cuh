@@ -644,6 +644,28 @@ __device__ bool keep_side(const P4<T>& rj, double side, V3<T>& pos, bool near_on
   return true;
 }
 
+// fp32: moves `pos` off any wall plane of subpartition sp that it lies on (within
+// keep_side's margin) to the side `ref` is on; `skip` is left alone. The point
+// reached a rounded position on a segment from `ref` that crossed none of these
+// walls (except `skip`).
+template <typename T>
+__device__ __noinline__ void guard_sides(const Geo<T>& g, uint32_t sp, V3<T>& pos, V3<T> ref, uint32_t skip) {
+  V3<T> glo, ghi;
+  seg_box(pos, v3<T>(0, 0, 0), (T)2e-2, glo, ghi);
+  const uint32_t gm = octants_touched(g, sp, glo, ghi);
+  for (uint32_t k = g.wsp_off[sp]; k < g.wsp_off[sp + 1]; k++) {
+    const uint32_t ent = g.wsp_list[k];
+    if (!(ent & gm) || (ent >> 8) == skip) continue;
+    const P4<T> rj = g.wrej[ent >> 8];
+    // cheap fp32 screen first; the fp64 side test only for points near the plane
+    const T d1 = dot(v3<T>(rj.x, rj.y, rj.z), pos) - rj.w;
+    if (tabs(d1) > (T)1e-2) continue;
+    const double d0 = ((double)ref.x * (double)rj.x + (double)ref.y * (double)rj.y + (double)ref.z * (double)rj.z) -
+                      (double)rj.w;
+    keep_side(rj, d0 >= 0 ? 1.0 : -1.0, pos, true);
+  }
+}
+
 template <typename T>
 struct WallHit {
   int type;
@@ -1253,20 +1275,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
         // rounding; a later step starting exactly on the plane would then pass the wall
         // (collide_wall treats "starts on the plane" as a miss). Keep it on the side it
         // came from.
-        V3<T> glo, ghi;
-        seg_box(pos, v3<T>(0, 0, 0), (T)2e-2, glo, ghi);
-        const uint32_t gm = octants_touched(g, sp, glo, ghi);
-        for (uint32_t k = g.wsp_off[sp]; k < g.wsp_off[sp + 1]; k++) {
-          const uint32_t ent = g.wsp_list[k];
-          if (!(ent & gm)) continue;
-          const P4<T> rj = g.wrej[ent >> 8];
-          // cheap fp32 screen first; the fp64 side test only for end points near the plane
-          const T d1 = dot(v3<T>(rj.x, rj.y, rj.z), pos) - rj.w;
-          if (tabs(d1) > (T)1e-2) continue;
-          const double d0 = ((double)seg_start.x * (double)rj.x + (double)seg_start.y * (double)rj.y +
-                             (double)seg_start.z * (double)rj.z) - (double)rj.w;
-          keep_side(rj, d0 >= 0 ? 1.0 : -1.0, pos, true);
-        }
+        guard_sides(g, sp, pos, seg_start, NONE);
         sp = subpart_of(g, pos);
       }
     }
@@ -1296,8 +1305,11 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
           last_hit = hit.wall;
           // fp32: make sure the crossing point lies on the far side, else the neighbouring
           // triangle of the crossed edge is hit again at t ~ 0 and re-tried without end
-          if (sizeof(T) == 4 && keep_side(g.wrej[hit.wall], hit.type == CT_FRONT ? -1.0 : 1.0, pos))
+          if (sizeof(T) == 4) {
+            keep_side(g.wrej[hit.wall], hit.type == CT_FRONT ? -1.0 : 1.0, pos);
+            guard_sides(g, sp, pos, pos_at_start, hit.wall);  // every other plane: the side it came from
             sp = subpart_of(g, pos);
+          }
           ev.put(2, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
         } else if (kind == 2 && test_intersect_absorb(r_rate_factor, draws)) {
           ev.put(3, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
@@ -1321,7 +1333,13 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
           remaining = cmul(remaining + cmul(v3<T>(rf, rf, rf), n), v3<T>(f, f, f));
           // fp32: the rounded reflection point must stay on the side the molecule came
           // from, else a coplanar neighbour triangle can reflect it outwards
-          if (sizeof(T) == 4 && keep_side(rj, hit.type == CT_FRONT ? 1.0 : -1.0, pos)) sp = subpart_of(g, pos);
+          // (and on the side it came from of every other plane it lies on: a hit on the
+          // edge of two faces rounds onto both planes)
+          if (sizeof(T) == 4) {
+            keep_side(rj, hit.type == CT_FRONT ? 1.0 : -1.0, pos);
+            guard_sides(g, sp, pos, pos_at_start, hit.wall);
+            sp = subpart_of(g, pos);
+          }
           ev.put(1, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
         }
         wall_done = true;
