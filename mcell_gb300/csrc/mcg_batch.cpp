@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "mcg_batch.h"
@@ -15,46 +16,105 @@ int bfail(mcg_batch* b, int code, const std::string& msg) {
   return code;
 }
 
-// Autotuner, part 1: subpartitions per edge of one replica from a cost model of
-// the per-molecule work of an iteration, in units of one partner test:
-//   partner tests    density/2 * edge^3 * (0.35 with octant bins, else 1) * 1.3
-//   wall tests       3 * (wall-subpartition incidences / subpartitions) * 0.35
-//   key-space sweep  0.07 * sort keys / molecules (scan and scatter touch every key)
-// The incidence count of a mesh grows as (1 + triangle extent / edge)^2 per wall.
-// Candidates run from the model's own subpartition edge (never finer) to the
-// whole partition as one subpartition, with edges of at least 4 reaction radii.
+// Autotuner, part 1: subpartitions per edge of one replica, from a cost model of
+// the per-molecule work of an iteration, in units of one partner test, evaluated
+// on a sample of the model's molecules (e = subpartition edge, d = mean absolute
+// displacement per axis, R = reaction radius):
+//   partner tests     local partner density * volume scanned: with octant bins
+//                     prod(e/2 + d + 2R), without prod(e + d + 2R*sqrt(2))
+//   subpartitions     3.6 per subpartition collected, prod(1 + (d + 2R*sqrt(2))/e)
+//   wall tests        2 * walls listed for the molecule's
+//                     subpartition (walls binned by bounding box grown by R)
+//   key-space sweep   0.07 * sort keys / molecules (scan and scatter touch every key)
+// The constants were fitted to measured k_diffuse times of the 1M-molecule sphere
+// model and of batch replicas at several grids. Candidates run over a geometric
+// ladder around the model's own count, with edges of at least 4 reaction radii
+// (the converter needs 2*sqrt(2)): dense meshes get finer subpartitions, sparse
+// models coarser ones.
 uint32_t choose_subparts(const mcg_engine* m, bool* octants) {
   const double L = m->cfg.partition_edge;
+  const double* O = m->cfg.partition_origin;
   const uint32_t n_user = m->cfg.subparts_per_edge;
-  const double N = std::max<double>(1.0, (double)m->pend_species.size());
-  const double rho = N / (L * L * L);
+  const size_t N = m->pend_species.size();
   const uint32_t nsp = m->cfg.n_species;
+  const double R = m->cfg.rxn_radius;
   const size_t nw = m->walls.size() / 3;
-  double ext = 0;
+  if (N == 0) {
+    *octants = true;
+    return n_user;
+  }
+  // sampled molecules and triangle boxes (grown by R, the binning leeway)
+  double d = 0;  // mean absolute displacement per axis: space_step / sqrt(2) * sqrt(2 / pi)
+  for (uint32_t a = 0; a < nsp; a++) d = std::max(d, 0.5641896 * m->chem.space_step[a]);
+  const size_t stride = std::max<size_t>(1, N / 8192);
+  std::vector<const double*> smp;
+  for (size_t i = 0; i < N; i += stride) smp.push_back(&m->pend_pos[3 * i]);
+  const double S = (double)smp.size();
+  std::vector<double> box(6 * nw);
   for (size_t w = 0; w < nw; w++) {
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    double* bx = &box[6 * w];
+    for (int a = 0; a < 3; a++) {
+      bx[a] = 1e300;
+      bx[3 + a] = -1e300;
+    }
     for (int k = 0; k < 3; k++) {
       const double* v = &m->verts[3 * (size_t)m->walls[3 * w + k]];
       for (int a = 0; a < 3; a++) {
-        lo[a] = std::min(lo[a], v[a]);
-        hi[a] = std::max(hi[a], v[a]);
+        bx[a] = std::min(bx[a], v[a] - R);
+        bx[3 + a] = std::max(bx[3 + a], v[a] + R);
       }
     }
-    ext += std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
   }
-  if (nw) ext /= (double)nw;
+  const uint32_t n_max = (uint32_t)std::max(1.0, std::min(300.0, std::floor(L / (4.0 * R))));
+  std::vector<uint32_t> cand;
+  for (int k = -16; k <= 12; k++) {
+    const uint32_t n = (uint32_t)std::lround(n_user * std::pow(2.0, k / 4.0));
+    if (n >= 1 && n <= n_max && std::find(cand.begin(), cand.end(), n) == cand.end()) cand.push_back(n);
+  }
+  if (std::find(cand.begin(), cand.end(), n_user) == cand.end()) cand.push_back(n_user);
   uint32_t best_n = n_user;
   bool best_oct = true;
   double best = 1e300;
-  for (uint32_t n = n_user; n >= 1; n--) {
+  for (uint32_t n : cand) {
     const double e = L / n;
-    if (e < 4.0 * m->cfg.rxn_radius && n != n_user) continue;
+    auto idx = [&](double x, int a) {
+      long i = (long)std::floor((x - O[a]) / e);
+      return (uint32_t)std::min<long>(std::max<long>(i, 0), (long)n - 1);
+    };
+    // sampled molecules per occupied subpartition
+    std::unordered_map<uint64_t, std::pair<double, double>> occ;  // subpartition -> (molecules, walls)
+    for (const double* p : smp) {
+      const uint64_t s = idx(p[0], 0) + (uint64_t)n * (idx(p[1], 1) + (uint64_t)n * idx(p[2], 2));
+      occ[s].first += 1.0;
+    }
+    for (size_t w = 0; w < nw; w++) {
+      const double* bx = &box[6 * w];
+      const uint32_t x0 = idx(bx[0], 0), y0 = idx(bx[1], 1), z0 = idx(bx[2], 2);
+      const uint32_t x1 = idx(bx[3], 0), y1 = idx(bx[4], 1), z1 = idx(bx[5], 2);
+      if ((uint64_t)(x1 - x0 + 1) * (y1 - y0 + 1) * (z1 - z0 + 1) > 4096) continue;  // huge walls: any n sees them
+      for (uint32_t z = z0; z <= z1; z++)
+        for (uint32_t y = y0; y <= y1; y++)
+          for (uint32_t x = x0; x <= x1; x++) {
+            auto it = occ.find(x + (uint64_t)n * (y + (uint64_t)n * z));
+            if (it != occ.end()) it->second.second += 1.0;
+          }
+    }
+    double mates = 0, walls = 0;
+    for (const auto& kv : occ) {
+      mates += kv.second.first * kv.second.first;
+      walls += kv.second.first * kv.second.second;
+    }
+    mates *= (double)N / (S * S);  // molecule-weighted molecules per subpartition
+    walls /= S;                    // molecule-weighted walls per subpartition
+    const double rho_p = 0.5 * mates / (e * e * e);  // local density of partners
+    const double a_oct = d + 2.0 * R, a_col = d + 2.0 * R * 1.41421356;
+    const double collected = std::pow(1.0 + a_col / e, 3.0);
     const double n3 = (double)n * n * n;
-    const double inc = (double)nw * (1.0 + ext / e) * (1.0 + ext / e);
     for (int oct = 1; oct >= 0; oct--) {
       const double keys = nsp * n3 * (oct ? 8.0 : 1.0);
       if (oct && keys > (double)(1u << 26)) continue;
-      const double cost = 0.5 * rho * e * e * e * (oct ? 0.35 : 1.0) * 1.3 + 3.0 * (inc / n3) * 0.35 + 0.07 * keys / N;
+      const double scanned = oct ? std::pow(0.5 * e + a_oct, 3.0) : std::pow(e + a_col, 3.0);
+      const double cost = rho_p * scanned + 3.6 * collected + 2.0 * walls + 0.07 * keys / (double)N;
       if (cost < best) {
         best = cost;
         best_n = n;
