@@ -26,6 +26,11 @@
 
 #include "mcg_math.cuh"
 
+// inlining of the fp32 side guard (run at the end of most segments)
+#ifndef MCG_GUARD_INLINE
+#define MCG_GUARD_INLINE __forceinline__
+#endif
+
 // occupants whose positions one thread loads together in the partner scan
 #ifndef MCG_OCC_BATCH
 #define MCG_OCC_BATCH 1
@@ -555,6 +560,48 @@ __device__ __forceinline__ int tri_test(S b, S c, S uv1u, S uv2u, S uv2v, S eps)
   return TRI_OUT;
 }
 
+// fp32 tie-break of the plane test, in fp64 with the fp64 plane (the float
+// position and move are exact in fp64): near the plane the fp32 side test can
+// have the wrong sign (its error grows with the coordinates), letting a molecule
+// moving outwards pass a reflective wall. Out of line: rarely taken.
+template <typename T>
+__device__ __noinline__ int plane_test_fp64(const double* w64, V3<T> pos, V3<T> move, T& a, T& dv) {
+  const double ddd = (w64[0] * (double)pos.x + w64[1] * (double)pos.y + w64[2] * (double)pos.z) - w64[3];
+  const double dvd = w64[0] * (double)move.x + w64[1] * (double)move.y + w64[2] * (double)move.z;
+  double ad = 0;
+  const int pt = plane_test<double>(ddd, dvd, (double)Eps<T>::pos, ad);
+  a = (T)ad;
+  dv = (T)dvd;
+  return pt;
+}
+
+// fp32 tie-break near an edge or vertex: the float in-triangle test is within its
+// own rounding there, and the float constants of two triangles sharing an edge do
+// not meet exactly (a ray can pass between them, or re-try at a face diagonal
+// until the watchdog). The crossing and the in-triangle test are redone in fp64
+// with the fp64 wall constants and band; only a crossing within that band of the
+// edge is re-tried. Returns a TRI_* code (crossing time and point updated), or
+// -1 when the fp64 plane test misses. Out of line: rarely taken.
+template <typename T>
+__device__ __noinline__ int edge_test_fp64(const double* w64, V3<T> pos, V3<T> move, int tr, T& ct, V3<T>& cpos,
+                                           T& dv) {
+  const double px = pos.x, py = pos.y, pz = pos.z, mx = move.x, my = move.y, mz = move.z;
+  const double ddd = (w64[0] * px + w64[1] * py + w64[2] * pz) - w64[3];
+  const double dvd = w64[0] * mx + w64[1] * my + w64[2] * mz;
+  double ad = 0;
+  const int ptd = plane_test<double>(ddd, dvd, Eps<double>::pos, ad);
+  if (ptd == PT_MISS) return -1;
+  if (ptd != PT_HIT) return tr;
+  const double cx = px + mx * ad, cy = py + my * ad, cz = pz + mz * ad;
+  const double lx = cx - w64[10], ly = cy - w64[11], lz = cz - w64[12];
+  const double bd = lx * w64[4] + ly * w64[5] + lz * w64[6];
+  const double cd = lx * w64[7] + ly * w64[8] + lz * w64[9];
+  ct = (T)ad;
+  cpos = v3<T>((T)cx, (T)cy, (T)cz);
+  dv = (T)dvd;
+  return tri_test<double>(bd, cd, w64[13], w64[14], w64[15], Eps<double>::pos);
+}
+
 // collide_wall (collision_utils.inl:629-812)
 template <typename T, class D>
 __device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V3<T>& move, T& ct, V3<T>& cpos) {
@@ -565,21 +612,10 @@ __device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V
   T dd = dp - rj.w;
   T a;
   int pt;
-  const double* w64 = (sizeof(T) == 4) ? g.w64 + 16 * (size_t)wi : nullptr;
-  if (sizeof(T) == 4 && tabs(dd) < (T)1e-2) {
-    // fp32 tie-break: near the plane the fp32 side test can have the wrong sign (its
-    // error grows with the coordinates), letting a molecule moving outwards pass a
-    // reflective wall. The side test is redone in fp64 with the fp64 plane (the float
-    // position is exact in fp64).
-    const double ddd = (w64[0] * (double)pos.x + w64[1] * (double)pos.y + w64[2] * (double)pos.z) - w64[3];
-    const double dvd = w64[0] * (double)move.x + w64[1] * (double)move.y + w64[2] * (double)move.z;
-    double ad = 0;
-    pt = plane_test<double>(ddd, dvd, (double)Eps<T>::pos, ad);
-    a = (T)ad;
-    dv = (T)dvd;
-  } else {
+  if (sizeof(T) == 4 && tabs(dd) < (T)1e-2)
+    pt = plane_test_fp64<T>(g.w64 + 16 * (size_t)wi, pos, move, a, dv);
+  else
     pt = plane_test<T>(dd, dv, Eps<T>::pos, a);
-  }
   if (pt == PT_MISS) return CT_MISS;
   if (pt == PT_PARALLEL) {
     a = (abs_max_2vec(pos, move) + (T)1.0) * Eps<T>::pos;
@@ -593,28 +629,8 @@ __device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V
   V3<T> local = cpos - w.v0;
   int tr = tri_test<T>(dot(local, w.u), dot(local, w.v), w.uv1u, w.uv2u, w.uv2v, Eps<T>::pos);
   if (sizeof(T) == 4 && tr >= TRI_E12) {
-    // fp32 tie-break near an edge or vertex: the float test is within its own
-    // rounding there, and the float constants of two triangles sharing an edge do
-    // not meet exactly (a ray can pass between them, or re-try at a face diagonal
-    // until the watchdog). The crossing and the in-triangle test are redone in fp64
-    // with the fp64 wall constants and band; only a crossing within that band of
-    // the edge is re-tried.
-    const double px = pos.x, py = pos.y, pz = pos.z, mx = move.x, my = move.y, mz = move.z;
-    const double ddd = (w64[0] * px + w64[1] * py + w64[2] * pz) - w64[3];
-    const double dvd = w64[0] * mx + w64[1] * my + w64[2] * mz;
-    double ad = 0;
-    const int ptd = plane_test<double>(ddd, dvd, Eps<double>::pos, ad);
-    if (ptd == PT_MISS) return CT_MISS;
-    if (ptd == PT_HIT) {
-      const double cx = px + mx * ad, cy = py + my * ad, cz = pz + mz * ad;
-      const double lx = cx - w64[10], ly = cy - w64[11], lz = cz - w64[12];
-      const double bd = lx * w64[4] + ly * w64[5] + lz * w64[6];
-      const double cd = lx * w64[7] + ly * w64[8] + lz * w64[9];
-      tr = tri_test<double>(bd, cd, w64[13], w64[14], w64[15], Eps<double>::pos);
-      ct = (T)ad;
-      cpos = v3<T>((T)cx, (T)cy, (T)cz);
-      dv = (T)dvd;
-    }
+    tr = edge_test_fp64<T>(g.w64 + 16 * (size_t)wi, pos, move, tr, ct, cpos, dv);
+    if (tr < 0) return CT_MISS;
   }
   if (tr == TRI_IN) return dv > 0 ? CT_BACK : CT_FRONT;
   if (tr == TRI_OUT) return CT_MISS;
@@ -649,7 +665,7 @@ __device__ bool keep_side(const P4<T>& rj, double side, V3<T>& pos, bool near_on
 // reached a rounded position on a segment from `ref` that crossed none of these
 // walls (except `skip`).
 template <typename T>
-__device__ __noinline__ void guard_sides(const Geo<T>& g, uint32_t sp, V3<T>& pos, V3<T> ref, uint32_t skip) {
+__device__ MCG_GUARD_INLINE void guard_sides(const Geo<T>& g, uint32_t sp, V3<T>& pos, V3<T> ref, uint32_t skip) {
   V3<T> glo, ghi;
   seg_box(pos, v3<T>(0, 0, 0), (T)2e-2, glo, ghi);
   const uint32_t gm = octants_touched(g, sp, glo, ghi);
