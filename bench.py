@@ -314,6 +314,70 @@ def run_batching(args):
     }
 
 
+# ---------------------------------------------------------------- serving form
+
+def run_serving(args):
+    """Requests drawn from the batching distribution with iteration counts
+    log-uniform in 100-10,000 arrive as a Poisson stream (args.serve_rate per s for
+    args.serve_seconds) and are served by the continuous-batching loop
+    (mcg_serve_*; slots 256, device-memory budget 150 GB). Time-to-result is
+    measured per request from submission to result. The same requests are then run
+    one after another on the plain engine; their time-to-result under first-come,
+    first-served is computed from those measured run times and the same arrivals."""
+    import numpy as np
+
+    from mcell_gb300 import _native
+    from mcell_gb300 import workloads as W
+
+    rng = np.random.default_rng(11)
+    n_req = max(1, int(rng.poisson(args.serve_rate * args.serve_seconds)))
+    arrivals = np.sort(rng.uniform(0, args.serve_seconds, n_req))
+    iters = np.exp(rng.uniform(np.log(100), np.log(10_000), n_req)).astype(int)
+    models = W.replica_models(n_req, seed=11)
+    handles = [W.model_handle(m, "fp32", seed=2000 + k) for k, m in enumerate(models)]
+    srv = _native.Server("fp32", 3, max_slots=256, hbm_budget_bytes=150 << 30, autotune=True)
+    t0 = time.perf_counter()
+    tickets = []
+    for k in range(n_req):
+        delay = arrivals[k] - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        tickets.append(srv.submit(handles[k], int(iters[k])))
+    lat = []
+    for t in tickets:
+        assert srv.wait(t, 3600.0) == "done"
+        lat.append(srv.poll(t)[1])
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    # plain engine, one request after another (first come, first served)
+    service = []
+    for k, m in enumerate(models):
+        e = W.engine_for(m, "fp32", seed=2000 + k)
+        e.sync()
+        t1 = time.perf_counter()
+        e.step(int(iters[k]))
+        e.sync()
+        service.append(time.perf_counter() - t1)
+        e.close()
+    for h in handles:
+        h.close()
+    done, plain_lat = 0.0, []
+    for a, sv in zip(arrivals, service):
+        done = max(done, a) + sv
+        plain_lat.append(done - a)
+    mol_steps = float(st["mol_steps"])
+    return {
+        "workload": f"{n_req} requests, Poisson {args.serve_rate}/s over {args.serve_seconds} s, models of the batching "
+                    f"distribution, iterations log-uniform 100-10000 ({int(iters.sum())} in total), fp32",
+        "served": {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                   "makespan_s": wall, "molecule_steps_per_s": mol_steps / wall,
+                   "busy_molecule_steps_per_s": mol_steps / max(st["busy_seconds"], 1e-9)},
+        "plain_sequential": {"p50_s": float(np.percentile(plain_lat, 50)), "p99_s": float(np.percentile(plain_lat, 99)),
+                             "makespan_s": float(done), "molecule_steps_per_s": mol_steps / max(sum(service), 1e-9)},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -327,6 +391,9 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batching measurement")
     ap.add_argument("--batch-replicas", type=int, default=256)
     ap.add_argument("--batch-iters", type=int, default=1000)
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--serve-seconds", type=float, default=3.0)
     args = ap.parse_args()
     rank, world, _ = _rank_env()
     procs = args.cpu_procs or os.cpu_count() or 1
@@ -369,6 +436,8 @@ def main():
     line = run_gpu(args, rank, world)
     if rank == 0 and not args.no_batch:
         line["batching"] = run_batching(args)
+    if rank == 0 and not args.no_serve:
+        line["serving"] = run_serving(args)
     if rank == 0:
         if cpu:
             line["cpu_baseline"] = cpu
