@@ -843,14 +843,17 @@ class DeviceEngineT : public DeviceEngine {
     MCG_CUDA(cudaMalloc(&d_st_, cap));
     MCG_CUDA(cudaMalloc(&d_claim_, sizeof(uint64_t) * cap));
     MCG_CUDA(cudaMemset(d_claim_, 0xFF, sizeof(uint64_t) * cap));
-    uint64_t pc = std::max<uint64_t>(4096, cap / 8);
+    // every molecule can propose once per iteration (dense models at high rates
+    // propose with a large share of their molecules)
+    uint64_t pc = std::max<uint64_t>(4096, cap);
     MCG_CUDA(cudaMalloc(&d_props_, sizeof(Proposal) * pc));
     MCG_CUDA(cudaMalloc(&d_losers_, sizeof(uint32_t) * 2 * pc));
     MCG_CUDA(cudaMalloc(&d_redo_, sizeof(Proposal) * pc));
     base_.prop_cap = (uint32_t)pc;
     cap_ = cap;
     base_.cap = (uint32_t)cap;
-    if (ensure_prod(std::max<uint64_t>(4096, cap / 4), err)) return -2;
+    // products: at most one per reactant of a bimolecular reaction with two products
+    if (ensure_prod(std::max<uint64_t>(4096, cap), err)) return -2;
     invalidate_graphs();
     return 0;
   }

@@ -68,7 +68,7 @@ uint64_t estimate_bytes(const mcg_engine& m, int precision) {
   const uint64_t n = m.cfg.subparts_per_edge;
   const uint64_t keys = (uint64_t)m.cfg.n_species * n * n * n * 8;
   const uint64_t per_wall = precision == MCG_PRECISION_FP64 ? 232 : 120;
-  const uint64_t per_mol = precision == MCG_PRECISION_FP64 ? 190 : 110;
+  const uint64_t per_mol = precision == MCG_PRECISION_FP64 ? 330 : 240;
   const uint64_t mol = (uint64_t)(m.pend_species.size() * 3 / 2 + 1024);
   return nw * (per_wall + 8 + m.cfg.n_species) + keys * 16 + mol * per_mol + (1u << 20);
 }

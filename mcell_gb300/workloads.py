@@ -10,6 +10,8 @@ and parameters of the configurations (no public dataset is involved):
 - replica_models: the batching / serving distribution of independent models
   (cubes of 0.5-3 um, optional icospheres of level 2-5, 1k-200k molecules,
   k from 1e6 to 1e9 M^-1 s^-1).
+- bumpy_tube: the precision stress model (10M molecules in a 200k-triangle
+  bumpy tube, 5% within 1 nm of mesh edges and vertices, dt = 0.1 us).
 - sphere_in_cube: an icosphere of radius 1 um (20,480 triangles at 5 subdivision
   levels) transparent to A and reflective to B and C, centred in a reflective
   2.5 um cube; A and B 1:1 uniformly in the cube; A + B -> C at 1e8 M^-1 s^-1,
@@ -91,6 +93,60 @@ def sphere_in_cube(n_mol=1_000_000, seed=1, levels=5, radius_um=1.0, cube_um=2.5
     pos = rng.uniform(-half, half, size=(n_mol, 3))
     sp = (np.arange(n_mol) % 2).astype(np.uint32)
     return Model("sphere_in_cube", lay.origin, lay.edge, lay.nsub, R_um / lu, v / lu, w, wc, steps, bimol, unimol,
+                 pos, sp, dt)
+
+
+def bumpy_tube(n_mol=10_000_000, seed=1, length_um=10.0, radius_um=0.2, bump_um=0.05, n_theta=200, n_z=500,
+               near_edge_frac=0.05, near_nm=1.0, dt=1e-7, subparts_per_edge=300) -> Model:
+    """Precision stress: the bumpy tube of geometry.create_bumpy_tube (reflective,
+    200,400 triangles at the defaults) holding n_mol molecules, A:B 1:1; a fraction
+    near_edge_frac of them sits within near_nm nm of a mesh edge or vertex (moved
+    inwards from a random point of a random side edge, or from a random side
+    vertex), the rest uniform inside (at least 2 nm from the analytic surface, so
+    inside the triangulated one). A + B -> C at 1e8 M^-1 s^-1, D = 1e-6 cm^2/s
+    (C: 5e-7), dt = 1e-7 s. The partition is the cube around the tube with
+    subparts_per_edge subpartitions per edge."""
+    lu = conversion.length_unit_um()
+    R_um = conversion.default_rxn_radius_um()
+    waves = 2.0 * length_um  # 20 axial waves over the 10 um tube
+    v, w = geometry.create_bumpy_tube(radius_um, length_um, bump_um, n_theta, n_z, axial_waves=waves)
+    edge = length_um + 0.2
+    lay = conversion.partition_layout(v.min(0), v.max(0), partition_dimension_um=edge,
+                                      subpartition_dimension_um=edge / subparts_per_edge)
+    steps, bimol, unimol = _chemistry(dt, lu, R_um)
+    rng = np.random.default_rng(seed)
+    n_near = int(round(n_mol * near_edge_frac))
+    n_uni = n_mol - n_near
+    # uniform inside: z, theta uniform, r^2 uniform below the surface radius - 2 nm
+    z = rng.uniform(-length_um / 2 + 0.002, length_um / 2 - 0.002, n_uni)
+    th = rng.uniform(0, 2 * np.pi, n_uni)
+    rs = radius_um + bump_um * np.sin(2 * np.pi * waves * (z + length_um / 2) / length_um) * np.sin(4 * th) - 0.002
+    r = rs * np.sqrt(rng.uniform(0, 1, n_uni))
+    uni = np.stack([r * np.cos(th), r * np.sin(th), z], axis=1)
+    # near edges / vertices of the side: a point of a side edge (or a side vertex)
+    # moved towards the axis by up to near_nm, plus a jitter of the same size along it
+    n_side = n_theta * (n_z + 1)
+    half = n_near // 2
+    sw = rng.integers(0, 2 * n_theta * n_z, half)  # side triangles come first
+    k = rng.integers(0, 3, half)
+    a = v[w[sw, k]]
+    b = v[w[sw, (k + 1) % 3]]
+    p_edge = a + (b - a) * rng.uniform(0, 1, (half, 1))
+    p_vert = v[rng.integers(n_theta, n_side - n_theta, n_near - half)]  # not the end rings
+    near = np.concatenate([p_edge, p_vert])
+    inward = -near.copy()
+    inward[:, 2] = 0
+    inward /= np.linalg.norm(inward, axis=1, keepdims=True)
+    dist = rng.uniform(1e-3, near_nm, len(near)) * 1e-3  # um
+    jitter = rng.normal(size=near.shape)
+    jitter -= (jitter * inward).sum(1, keepdims=True) * inward
+    jitter *= (rng.uniform(0, 0.5, (len(near), 1)) * dist[:, None]) / np.linalg.norm(jitter, axis=1, keepdims=True)
+    near = near + inward * dist[:, None] + jitter
+    near[:, 2] = np.clip(near[:, 2], -length_um / 2 + 0.002, length_um / 2 - 0.002)
+    pos = np.concatenate([uni, near]) / lu
+    sp = (np.arange(n_mol) % 2).astype(np.uint32)
+    wc = np.zeros((len(w), 3), np.uint8)
+    return Model("bumpy_tube", lay.origin, lay.edge, lay.nsub, R_um / lu, v / lu, w, wc, steps, bimol, unimol,
                  pos, sp, dt)
 
 
