@@ -95,8 +95,9 @@ class DeviceEngineT : public DeviceEngine {
     }
     uint64_t n_new = 0;
     for (uint32_t k = 0; k < n; k++) n_new += specs[k].n_mol;
-    std::vector<Product<T>> stage;
-    stage.reserve(n_new);
+    Product<T>* stage = nullptr;
+    if (pinned_reserve(n_new, &stage, err)) return -2;
+    uint64_t staged = 0;
     for (uint32_t k = 0; k < n; k++) {
       const ReplicaSpec& sp = specs[k];
       const uint32_t r = slots[k];
@@ -105,7 +106,8 @@ class DeviceEngineT : public DeviceEngine {
         for (uint32_t j = 0; j <= k; j++) free_replica(slots[j]);
         return rc;
       }
-      rc = stage_molecules(r, sp.n_mol, sp.pos, sp.species, 0, stage, err);
+      rc = stage_molecules(r, sp.n_mol, sp.pos, sp.species, 0, stage + staged, err);
+      staged += sp.n_mol;
       if (rc) {
         for (uint32_t j = 0; j <= k; j++) free_replica(slots[j]);
         return rc;
@@ -115,7 +117,7 @@ class DeviceEngineT : public DeviceEngine {
     }
     int rc = layout_keys(err);
     if (rc) return rc;
-    return rebin(stage, err);
+    return rebin(stage, n_new, err);
   }
 
   int remove_replicas(const uint32_t* reps, uint32_t n, std::string& err) override {
@@ -133,8 +135,7 @@ class DeviceEngineT : public DeviceEngine {
     }
     rc = layout_keys(err);
     if (rc) return rc;
-    std::vector<Product<T>> none;
-    rc = rebin(none, err);
+    rc = rebin(nullptr, 0, err);
     if (rc) return rc;
     for (uint32_t k = 0; k < n; k++) free_replica(reps[k]);
     return 0;
@@ -147,13 +148,13 @@ class DeviceEngineT : public DeviceEngine {
       err = "no such replica";
       return -1;
     }
-    std::vector<Product<T>> stage;
-    stage.reserve(n);
+    Product<T>* stage = nullptr;
+    if (pinned_reserve(n, &stage, err)) return -2;
     int rc = stage_molecules(rep, n, pos, species, uid0, stage, err);
     if (rc) return rc;
     reps_[rep].next_uid = std::max<uint64_t>(reps_[rep].next_uid, uid0 + n);
     if (read_counters(err)) return -2;
-    return rebin(stage, err);
+    return rebin(stage, n, err);
   }
 
   int step(uint32_t n, std::string& err) override {
@@ -509,14 +510,18 @@ class DeviceEngineT : public DeviceEngine {
     const size_t sp = (size_t)ix[0] + (size_t)ix[1] * R.nsub + (size_t)ix[2] * R.nsub * R.nsub;
     const double mag = std::max(std::fabs(p[0]), std::max(std::fabs(p[1]), std::fabs(p[2])));
     const double margin = std::max(1e-4, 8.0 * mag * 1.1920928955078125e-07);
-    for (int pass = 0; pass < 2; pass++)
+    for (int pass = 0; pass < 2; pass++) {  // a second pass only after a move (edges, corners)
+      bool moved = false;
       for (uint32_t k = R.h_wsp_off[sp]; k < R.h_wsp_off[sp + 1]; k++) {
         const double* pl = &R.planes[4 * (size_t)R.h_wsp_list[k]];
         const double dd = pl[0] * p[0] + pl[1] * p[1] + pl[2] * p[2] - pl[3];
         if (std::fabs(dd) >= margin) continue;
         const double shift = (dd >= 0 ? margin : -margin) - dd;
         for (int a = 0; a < 3; a++) p[a] += shift * pl[a];
+        moved = true;
       }
+      if (!moved) break;
+    }
   }
 
   static uint32_t host_meta(const P4<T>& p) {
@@ -680,7 +685,7 @@ class DeviceEngineT : public DeviceEngine {
 
   // molecules of replica r into the staging list (checked against its partition)
   int stage_molecules(uint32_t r, uint64_t n, const double* pos, const uint32_t* species, uint64_t uid0,
-                      std::vector<Product<T>>& stage, std::string& err) {
+                      Product<T>* stage, std::string& err) {
     const Geo<T>& g = geos_h_[r];
     const double o[3] = {(double)g.origin.x, (double)g.origin.y, (double)g.origin.z};
     const double q[3] = {(double)g.opposite.x, (double)g.opposite.y, (double)g.opposite.z};
@@ -703,8 +708,24 @@ class DeviceEngineT : public DeviceEngine {
       m.birth = 0;
       m.uid = uid0 + i;
       m.tuni = TIME_FOREVER;
-      stage.push_back(m);
+      stage[i] = m;
     }
+    return 0;
+  }
+
+  // pinned host staging for n uploads (kept for later uploads: pageable copies run
+  // at a fraction of the link's rate)
+  int pinned_reserve(uint64_t n, Product<T>** out, std::string& err) {
+    const size_t bytes = sizeof(Product<T>) * std::max<uint64_t>(n, 1);
+    if (bytes > pinned_bytes_) {
+      MCG_CUDA(cudaStreamSynchronize(stream_));  // an earlier upload may still read it
+      if (pinned_) cudaFreeHost(pinned_);
+      pinned_ = nullptr;
+      pinned_bytes_ = 0;
+      MCG_CUDA(cudaHostAlloc(&pinned_, bytes, cudaHostAllocDefault));
+      pinned_bytes_ = bytes;
+    }
+    *out = static_cast<Product<T>*>(pinned_);
     return 0;
   }
 
@@ -751,8 +772,7 @@ class DeviceEngineT : public DeviceEngine {
 
   // re-sorts the live molecules plus the staged ones into the other sorted arrays
   // (molecules of dropped replicas are left out); counters must be fresh
-  int rebin(const std::vector<Product<T>>& stage, std::string& err) {
-    const uint64_t n = stage.size();
+  int rebin(const Product<T>* stage, uint64_t n, std::string& err) {
     const uint64_t live = cnt_.n_live;
     if (live + n > 0xFFFFFFF0ull) {
       err = "too many molecules for 32-bit indices";
@@ -768,7 +788,7 @@ class DeviceEngineT : public DeviceEngine {
       cnt_ = c;
       return 0;
     }
-    if (n) MCG_CUDA(cudaMemcpyAsync(base_.prod, stage.data(), sizeof(Product<T>) * n, cudaMemcpyHostToDevice, stream_));
+    if (n) MCG_CUDA(cudaMemcpyAsync(base_.prod, stage, sizeof(Product<T>) * n, cudaMemcpyHostToDevice, stream_));
     // staged molecules sit in the product list, already "diffused"
     Counters c = cnt_;
     c.n_prod = (uint32_t)n;
@@ -974,6 +994,7 @@ class DeviceEngineT : public DeviceEngine {
     cudaFree(d_cnt_);
     cudaFree(d_debug_);
     cudaFree(d_geos_);
+    if (pinned_) cudaFreeHost(pinned_);
     if (stream_) cudaStreamDestroy(stream_);
   }
 
@@ -1009,6 +1030,8 @@ class DeviceEngineT : public DeviceEngine {
   unsigned long long* d_traj_ = nullptr;
   Counters* d_cnt_ = nullptr;
   double* d_debug_ = nullptr;
+  void* pinned_ = nullptr;  // host staging for uploads
+  size_t pinned_bytes_ = 0;
 };
 
 }  // namespace mcg
