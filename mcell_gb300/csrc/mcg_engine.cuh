@@ -470,7 +470,7 @@ class DeviceEngineT : public DeviceEngine {
     if (launches) *launches = launches_;
   }
 
-  static constexpr int kernels_per_iteration_ = 15;
+  static constexpr int kernels_per_iteration_ = 15 + 3 * GRID_REDO_ROUNDS;
 
  private:
   // host view of one replica slot
@@ -932,6 +932,11 @@ class DeviceEngineT : public DeviceEngine {
     k_resolve<T><<<gs, TPB, 0, stream_>>>(s);
     k_collect_losers<T><<<gs, TPB, 0, stream_>>>(s);
     k_reset_claims<T><<<gs, TPB, 0, stream_>>>(s);
+    for (int r = 0; r < GRID_REDO_ROUNDS; r++) {
+      k_redo_trace<T><<<diffuse_grid_, TPB, 0, stream_>>>(s, r);
+      k_redo_commit<T><<<gs, TPB, 0, stream_>>>(s, r);
+      k_redo_next<T><<<gs, TPB, 0, stream_>>>(s, r);
+    }
     k_redo<T><<<1, TPB, 0, stream_>>>(s);
     mark(2, prof);
     k_prod_window<T><<<1, 1, 0, stream_>>>(s);

@@ -8,8 +8,9 @@
 //   k_resolve      a proposal wins if it holds the minimum claim key on both
 //                  molecules; winners kill both reactants and emit products
 //   k_collect_losers / k_reset_claims
-//   k_redo         one CTA re-traces the (rare) losers with used-up partners
-//                  excluded, in rounds, until every proposal is decided
+//   k_redo_*       losers re-trace with used-up partners excluded, in rounds
+//                  over the whole GPU, then the rest in one CTA (k_redo),
+//                  until every proposal is decided
 //   k_products     newborn products diffuse for the rest of the step (twice)
 //   k_scan_*       histogram -> start offsets of the sorted ranges
 //   k_scatter      survivors move into the next iteration's sorted arrays
@@ -32,14 +33,16 @@ constexpr int TPB = 256;
 #define MCG_DIFFUSE_MIN_BLOCKS 6
 #endif
 constexpr int SCAN_TILE = 2048;
-constexpr int REDO_ROUNDS = 64;
+constexpr int REDO_ROUNDS = 64;      // loser rounds in the one-CTA pass
+constexpr int GRID_REDO_ROUNDS = 3;  // loser rounds over the whole GPU before it
 constexpr uint64_t CLAIM_FREE = ~0ull;
 
 struct Counters {
   uint32_t n_live;       // molecules in the current sorted arrays
   uint32_t n_live_next;  // survivors after this iteration
   uint32_t n_props;      // proposals made in k_diffuse
-  uint32_t n_losers;
+  uint32_t redo_n[GRID_REDO_ROUNDS + 1];  // losers entering loser round r (redo_n[0] from the first resolution)
+  uint32_t redo_np[GRID_REDO_ROUNDS];     // proposals made in grid loser round r
   uint32_t n_prod;       // products created this iteration
   uint32_t n_prod_done;  // products already diffused
   uint32_t prod_hi;      // end of the products pass window
@@ -428,8 +431,8 @@ __global__ void k_collect_losers(State<T> s) {
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const Proposal p = s.props[k];
     if (s.st[p.i] == 1) {
-      uint32_t m = atomicAdd(&s.cnt->n_losers, 1u);
-      s.losers[m] = p.i;  // n_losers <= n_props <= prop_cap
+      uint32_t m = atomicAdd(&s.cnt->redo_n[0], 1u);
+      s.losers[m] = p.i;  // losers <= n_props <= prop_cap
     }
   }
 }
@@ -444,43 +447,84 @@ __global__ void k_reset_claims(State<T> s) {
   }
 }
 
-// One CTA re-traces the losers in rounds: a loser's partner was taken by an
-// earlier-keyed reaction, so it replays its own draws (counter-based RNG) with
-// every used-up molecule excluded, and proposes again or finishes.
+// Losers (their partner was taken by an earlier-keyed reaction) re-trace their
+// step in rounds: each replays its own draws (counter-based RNG) with every
+// used-up molecule excluded, and proposes again or finishes; the proposals of a
+// round are resolved like the first ones. The first GRID_REDO_ROUNDS rounds run
+// over the whole GPU (three launches each, empty when nothing is left: dense
+// models at high rates lose a large share of their proposals), the rest in one
+// CTA. Round r reads its losers from half (r & 1) of the loser buffer and
+// their count from redo_n[r], and appends the next round's to the other half.
+
+// one loser re-traced: a new proposal (counted in *n_props) or a final state
+template <typename T>
+__device__ __forceinline__ void redo_one(const State<T>& s, uint32_t i, uint32_t* n_props, uint32_t& err) {
+  Proposal p;
+  int kind = run_molecule(s, i, s.st, &p, err);
+  if (kind == 1) {
+    s.st[i] = 1;
+    uint32_t k = atomicAdd(n_props, 1u);
+    s.redo_props[k] = p;  // k < number of losers <= prop_cap
+    atomicMin((unsigned long long*)&s.claim[i], (unsigned long long)p.key);
+    atomicMin((unsigned long long*)&s.claim[p.partner], (unsigned long long)p.key);
+  } else if (kind == 0 || kind == 3) {
+    s.st[i] = 0;
+    atomicAdd(&s.counts[key_of_rec(s, s.b_pos[i])], 1u);
+  } else {
+    s.st[i] = (uint8_t)kind;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_redo_trace(State<T> s, int round) {
+  const uint32_t n = min(s.cnt->redo_n[round], s.prop_cap);
+  const uint32_t* cur = s.losers + (size_t)(round & 1) * s.prop_cap;
+  uint32_t err = 0;
+  for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < n; l += gridDim.x * blockDim.x)
+    redo_one(s, cur[l], &s.cnt->redo_np[round], err);
+  if (err) atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
+}
+
+template <typename T>
+__global__ void k_redo_commit(State<T> s, int round) {
+  const uint32_t n = s.cnt->redo_np[round];
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const Proposal p = s.redo_props[k];
+    if (s.claim[p.i] == p.key && s.claim[p.partner] == p.key) commit(s, p);
+  }
+}
+
+// proposals that lost again become the next round's losers; claims are released
+template <typename T>
+__global__ void k_redo_next(State<T> s, int round) {
+  const uint32_t n = s.cnt->redo_np[round];
+  uint32_t* next = s.losers + (size_t)((round + 1) & 1) * s.prop_cap;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const Proposal p = s.redo_props[k];
+    if (s.st[p.i] == 1) next[atomicAdd(&s.cnt->redo_n[round + 1], 1u)] = p.i;
+    s.claim[p.i] = CLAIM_FREE;
+    s.claim[p.partner] = CLAIM_FREE;
+  }
+}
+
+// the remaining rounds in one CTA
 template <typename T>
 __global__ void __launch_bounds__(TPB) k_redo(State<T> s) {
   __shared__ uint32_t n_cur, n_next, n_rp;
   uint32_t err = 0;
-  if (threadIdx.x == 0) {
-    n_cur = min(s.cnt->n_losers, s.prop_cap);
-  }
+  if (threadIdx.x == 0) n_cur = min(s.cnt->redo_n[GRID_REDO_ROUNDS], s.prop_cap);
   __syncthreads();
-  uint32_t* cur = s.losers;
+  int half = GRID_REDO_ROUNDS & 1;
   for (int round = 0; round < REDO_ROUNDS; round++) {
     if (n_cur == 0) break;
+    const uint32_t* cur = s.losers + (size_t)half * s.prop_cap;
+    uint32_t* next = s.losers + (size_t)(half ^ 1) * s.prop_cap;
     if (threadIdx.x == 0) {
       n_next = 0;
       n_rp = 0;
     }
     __syncthreads();
-    for (uint32_t l = threadIdx.x; l < n_cur; l += blockDim.x) {
-      const uint32_t i = cur[l];
-      Proposal p;
-      int kind = run_molecule(s, i, s.st, &p, err);
-      if (kind == 1) {
-        s.st[i] = 1;
-        uint32_t k = atomicAdd(&n_rp, 1u);
-        s.redo_props[k] = p;
-        atomicMin((unsigned long long*)&s.claim[i], (unsigned long long)p.key);
-        atomicMin((unsigned long long*)&s.claim[p.partner], (unsigned long long)p.key);
-      } else {
-        s.st[i] = (uint8_t)kind;
-        if (kind == 0 || kind == 3) {
-          s.st[i] = 0;
-          atomicAdd(&s.counts[key_of_rec(s, s.b_pos[i])], 1u);
-        }
-      }
-    }
+    for (uint32_t l = threadIdx.x; l < n_cur; l += blockDim.x) redo_one(s, cur[l], &n_rp, err);
     __syncthreads();
     for (uint32_t k = threadIdx.x; k < n_rp; k += blockDim.x) {
       const Proposal p = s.redo_props[k];
@@ -489,10 +533,7 @@ __global__ void __launch_bounds__(TPB) k_redo(State<T> s) {
     __syncthreads();
     for (uint32_t k = threadIdx.x; k < n_rp; k += blockDim.x) {
       const Proposal p = s.redo_props[k];
-      if (s.st[p.i] == 1) {
-        uint32_t m = atomicAdd(&n_next, 1u);
-        s.losers[s.prop_cap + m] = p.i;  // second half of the loser buffer
-      }
+      if (s.st[p.i] == 1) next[atomicAdd(&n_next, 1u)] = p.i;
     }
     __syncthreads();
     for (uint32_t k = threadIdx.x; k < n_rp; k += blockDim.x) {
@@ -500,14 +541,15 @@ __global__ void __launch_bounds__(TPB) k_redo(State<T> s) {
       s.claim[p.i] = CLAIM_FREE;
       s.claim[p.partner] = CLAIM_FREE;
     }
-    for (uint32_t m = threadIdx.x; m < n_next; m += blockDim.x) s.losers[m] = s.losers[s.prop_cap + m];
     __syncthreads();
     if (threadIdx.x == 0) n_cur = n_next;
+    half ^= 1;
     __syncthreads();
   }
   if (n_cur != 0) {
     // undecided after the round limit: report and drop them as dead rather than loop on
     if (threadIdx.x == 0) atomicOr(&s.cnt->status, ST_WATCHDOG);
+    const uint32_t* cur = s.losers + (size_t)half * s.prop_cap;
     for (uint32_t l = threadIdx.x; l < n_cur; l += blockDim.x) s.st[cur[l]] = 2;
   }
   if (err) atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
@@ -781,7 +823,8 @@ __global__ void k_end(State<T> s) {
   if (c->n_prod > c->n_prod_done) atomicOr(&c->status, ST_WATCHDOG);  // product chain deeper than the passes
   c->n_live = min(c->n_live_next, s.cap);
   c->n_props = 0;
-  c->n_losers = 0;
+  for (int r = 0; r <= GRID_REDO_ROUNDS; r++) c->redo_n[r] = 0;
+  for (int r = 0; r < GRID_REDO_ROUNDS; r++) c->redo_np[r] = 0;
   c->n_prod = 0;
   c->n_prod_done = 0;
   c->prod_hi = 0;
