@@ -171,7 +171,8 @@ def run_gpu(args, rank, world):
     prof = np.zeros(6)
     with ClockSampler(dev) as clk:
         for _ in range(args.steps):
-            flush.zero_()  # L2 flush between timed steps (legacy stream, ordered before the engine stream)
+            flush.zero_()  # L2 flush between timed steps (on torch's stream, finished before the step)
+            torch.cuda.synchronize()
             e.step(1)
             e.sync()
             prof += e.profile()

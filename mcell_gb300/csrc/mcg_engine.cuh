@@ -41,8 +41,10 @@ class DeviceEngineT : public DeviceEngine {
       err = "invalid species count or replica slots";
       return -1;
     }
-    // a blocking stream: setup copies on the legacy default stream are ordered before its kernels
-    MCG_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamDefault));
+    // a non-blocking stream, and every copy and memset of the engine is ordered on it:
+    // nothing synchronises with the legacy default stream, so engines driven from
+    // other threads (a serving loop) do not disturb a graph capture on this one
+    MCG_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     int dev = 0;
     MCG_CUDA(cudaGetDevice(&dev));
     MCG_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
@@ -63,14 +65,14 @@ class DeviceEngineT : public DeviceEngine {
       geos_h_[r].rep = r;
     }
     MCG_CUDA(cudaMalloc(&d_geos_, sizeof(Geo<T>) * max_rep));
-    MCG_CUDA(cudaMemcpy(d_geos_, geos_h_.data(), sizeof(Geo<T>) * max_rep, cudaMemcpyHostToDevice));
+    MCG_CUDA(cudaMemcpyAsync(d_geos_, geos_h_.data(), sizeof(Geo<T>) * max_rep, cudaMemcpyHostToDevice, stream_));
     // count trajectory ring: [row][replica][species], at most 64 MB
     const uint64_t row_bytes = sizeof(unsigned long long) * (uint64_t)max_rep * nsp;
     traj_cap_ = (uint32_t)std::max<uint64_t>(64, std::min<uint64_t>(65536, (64ull << 20) / row_bytes));
     MCG_CUDA(cudaMalloc(&d_traj_, row_bytes * traj_cap_));
-    MCG_CUDA(cudaMemset(d_traj_, 0, row_bytes * traj_cap_));
+    MCG_CUDA(cudaMemsetAsync(d_traj_, 0, row_bytes * traj_cap_, stream_));
     MCG_CUDA(cudaMalloc(&d_cnt_, sizeof(Counters)));
-    MCG_CUDA(cudaMemset(d_cnt_, 0, sizeof(Counters)));
+    MCG_CUDA(cudaMemsetAsync(d_cnt_, 0, sizeof(Counters), stream_));
     base_.geos = d_geos_;
     base_.n_rep = max_rep;
     base_.nsp = (int)nsp;
@@ -201,8 +203,7 @@ class DeviceEngineT : public DeviceEngine {
       // species counts of the last finished iteration (k_end)
       const uint64_t row = (cnt_.iteration - 1) % traj_cap_;
       std::vector<unsigned long long> h(nsp_);
-      MCG_CUDA(cudaMemcpy(h.data(), d_traj_ + (row * max_rep_ + rep) * nsp_, sizeof(unsigned long long) * nsp_,
-                          cudaMemcpyDeviceToHost));
+      MCG_CUDA(d2h(h.data(), d_traj_ + (row * max_rep_ + rep) * nsp_, sizeof(unsigned long long) * nsp_));
       for (uint32_t a = 0; a < nsp_; a++) out[a] = h[a];
       return 0;
     }
@@ -211,8 +212,8 @@ class DeviceEngineT : public DeviceEngine {
     const uint32_t* st = state(parity_).start;
     for (uint32_t a = 0; a < nsp_; a++) {
       uint32_t lo = 0, hi = 0;
-      MCG_CUDA(cudaMemcpy(&lo, st + g.kbase + a * span, sizeof(uint32_t), cudaMemcpyDeviceToHost));
-      MCG_CUDA(cudaMemcpy(&hi, st + g.kbase + (a + 1) * span, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+      MCG_CUDA(d2h(&lo, st + g.kbase + a * span, sizeof(uint32_t)));
+      MCG_CUDA(d2h(&hi, st + g.kbase + (a + 1) * span, sizeof(uint32_t)));
       out[a] = hi - lo;
     }
     return 0;
@@ -236,9 +237,10 @@ class DeviceEngineT : public DeviceEngine {
     while (k < n) {
       const uint64_t row = (last - n + k) % traj_cap_;
       const uint32_t rows = (uint32_t)std::min<uint64_t>(n - k, traj_cap_ - row);
-      MCG_CUDA(cudaMemcpy2D(h.data() + (size_t)k * nsp_, sizeof(unsigned long long) * nsp_,
-                            d_traj_ + (row * max_rep_ + rep) * nsp_, sizeof(unsigned long long) * nsp_ * max_rep_,
-                            sizeof(unsigned long long) * nsp_, rows, cudaMemcpyDeviceToHost));
+      MCG_CUDA(cudaMemcpy2DAsync(h.data() + (size_t)k * nsp_, sizeof(unsigned long long) * nsp_,
+                                 d_traj_ + (row * max_rep_ + rep) * nsp_, sizeof(unsigned long long) * nsp_ * max_rep_,
+                                 sizeof(unsigned long long) * nsp_, rows, cudaMemcpyDeviceToHost, stream_));
+      MCG_CUDA(cudaStreamSynchronize(stream_));
       k += rows;
     }
     for (size_t q = 0; q < h.size(); q++) out[q] = h[q];
@@ -256,16 +258,15 @@ class DeviceEngineT : public DeviceEngine {
     const Geo<T>& g = geos_h_[rep];
     State<T> s = state(parity_);
     uint32_t lo = 0, hi = 0;
-    MCG_CUDA(cudaMemcpy(&lo, s.start + g.kbase, sizeof(uint32_t), cudaMemcpyDeviceToHost));
-    MCG_CUDA(cudaMemcpy(&hi, s.start + g.kbase + nsp_ * (g.n3 << g.oct_shift), sizeof(uint32_t),
-                        cudaMemcpyDeviceToHost));
+    MCG_CUDA(d2h(&lo, s.start + g.kbase, sizeof(uint32_t)));
+    MCG_CUDA(d2h(&hi, s.start + g.kbase + nsp_ * (g.n3 << g.oct_shift), sizeof(uint32_t)));
     const uint32_t n = hi - lo;
     *n_out = n;
     if (n == 0) return 0;
     std::vector<P4<T>> p(n);
     std::vector<uint64_t> u(n);
-    MCG_CUDA(cudaMemcpy(p.data(), s.a_pos + lo, sizeof(P4<T>) * n, cudaMemcpyDeviceToHost));
-    MCG_CUDA(cudaMemcpy(u.data(), s.a_uid + lo, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
+    MCG_CUDA(d2h(p.data(), s.a_pos + lo, sizeof(P4<T>) * n));
+    MCG_CUDA(d2h(u.data(), s.a_uid + lo, sizeof(uint64_t) * n));
     for (uint64_t i = 0; i < std::min<uint64_t>(n, capn); i++) {
       if (pos) {
         pos[3 * i] = (double)p[i].x;
@@ -311,7 +312,7 @@ class DeviceEngineT : public DeviceEngine {
     const uint32_t n = cnt_.n_live;
     State<T> s = state(parity_);
     std::vector<uint64_t> u(n);
-    MCG_CUDA(cudaMemcpy(u.data(), s.a_uid, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
+    MCG_CUDA(d2h(u.data(), s.a_uid, sizeof(uint64_t) * n));
     std::unordered_map<uint64_t, uint32_t> where;
     for (uint32_t i = 0; i < n; i++) where[u[i]] = i;
     std::vector<uint32_t> idx(nc);
@@ -332,16 +333,16 @@ class DeviceEngineT : public DeviceEngine {
     MCG_CUDA(cudaMalloc(&d_tst, sizeof(double) * nc));
     MCG_CUDA(cudaMalloc(&d_out, sizeof(double) * 265 * nc));
     MCG_CUDA(cudaMalloc(&d_draws, sizeof(uint32_t) * std::max<uint64_t>((uint64_t)ndraws * nc, 1)));
-    MCG_CUDA(cudaMemcpy(d_idx, idx.data(), sizeof(uint32_t) * nc, cudaMemcpyHostToDevice));
-    MCG_CUDA(cudaMemcpy(d_disp, disp, sizeof(double) * 3 * nc, cudaMemcpyHostToDevice));
-    MCG_CUDA(cudaMemcpy(d_rrf, rrf, sizeof(double) * nc, cudaMemcpyHostToDevice));
-    MCG_CUDA(cudaMemcpy(d_tst, tst, sizeof(double) * nc, cudaMemcpyHostToDevice));
-    if (ndraws) MCG_CUDA(cudaMemcpy(d_draws, draws, sizeof(uint32_t) * ndraws * nc, cudaMemcpyHostToDevice));
+    MCG_CUDA(cudaMemcpyAsync(d_idx, idx.data(), sizeof(uint32_t) * nc, cudaMemcpyHostToDevice, stream_));
+    MCG_CUDA(cudaMemcpyAsync(d_disp, disp, sizeof(double) * 3 * nc, cudaMemcpyHostToDevice, stream_));
+    MCG_CUDA(cudaMemcpyAsync(d_rrf, rrf, sizeof(double) * nc, cudaMemcpyHostToDevice, stream_));
+    MCG_CUDA(cudaMemcpyAsync(d_tst, tst, sizeof(double) * nc, cudaMemcpyHostToDevice, stream_));
+    if (ndraws) MCG_CUDA(cudaMemcpyAsync(d_draws, draws, sizeof(uint32_t) * ndraws * nc, cudaMemcpyHostToDevice, stream_));
     k_trace_cases<T><<<(nc + 127) / 128, 128, 0, stream_>>>(s, nc, d_idx, d_disp, d_draws, ndraws, d_rrf, d_tst, d_out);
     launches_ += 1;
     MCG_CUDA(cudaGetLastError());
     MCG_CUDA(cudaStreamSynchronize(stream_));
-    MCG_CUDA(cudaMemcpy(out, d_out, sizeof(double) * 265 * nc, cudaMemcpyDeviceToHost));
+    MCG_CUDA(d2h(out, d_out, sizeof(double) * 265 * nc));
     cudaFree(d_idx);
     cudaFree(d_disp);
     cudaFree(d_rrf);
@@ -436,7 +437,7 @@ class DeviceEngineT : public DeviceEngine {
     if (!d_debug_) {
       MCG_CUDA(cudaMalloc(&d_debug_, sizeof(double) * 64 * 271));
     }
-    MCG_CUDA(cudaMemset(d_debug_, 0, sizeof(double) * 64 * 271));
+    MCG_CUDA(cudaMemsetAsync(d_debug_, 0, sizeof(double) * 64 * 271, stream_));
     base_.debug_uid = uid;
     base_.debug_log = d_debug_;
     invalidate_graphs();
@@ -449,7 +450,7 @@ class DeviceEngineT : public DeviceEngine {
       err = "no molecule is being logged";
       return -1;
     }
-    MCG_CUDA(cudaMemcpy(out, d_debug_, sizeof(double) * 64 * 271, cudaMemcpyDeviceToHost));
+    MCG_CUDA(d2h(out, d_debug_, sizeof(double) * 64 * 271));
     return 0;
   }
 
@@ -524,6 +525,12 @@ class DeviceEngineT : public DeviceEngine {
     }
   }
 
+  // device -> host copy ordered on the engine stream; returns when the data is there
+  cudaError_t d2h(void* h, const void* d, size_t n) {
+    cudaError_t e = cudaMemcpyAsync(h, d, n, cudaMemcpyDeviceToHost, stream_);
+    return e != cudaSuccess ? e : cudaStreamSynchronize(stream_);
+  }
+
   static uint32_t host_meta(const P4<T>& p) {
     if (sizeof(T) == 8) {
       uint64_t m64;
@@ -549,7 +556,7 @@ class DeviceEngineT : public DeviceEngine {
     const size_t sz = sizeof(V) * std::max<size_t>(h.size(), 1);
     MCG_CUDA(cudaMalloc((void**)d, sz));
     bytes += sz;
-    if (!h.empty()) MCG_CUDA(cudaMemcpy(*d, h.data(), sizeof(V) * h.size(), cudaMemcpyHostToDevice));
+    if (!h.empty()) MCG_CUDA(cudaMemcpyAsync(*d, h.data(), sizeof(V) * h.size(), cudaMemcpyHostToDevice, stream_));
     return 0;
   }
 
@@ -754,18 +761,18 @@ class DeviceEngineT : public DeviceEngine {
       key_alloc_ = 0;
       for (int p = 0; p < 2; p++) {
         MCG_CUDA(cudaMalloc(&d_start_[p], sizeof(uint32_t) * (na + 1)));
-        MCG_CUDA(cudaMemset(d_start_[p], 0, sizeof(uint32_t) * (na + 1)));
+        MCG_CUDA(cudaMemsetAsync(d_start_[p], 0, sizeof(uint32_t) * (na + 1), stream_));
       }
       MCG_CUDA(cudaMalloc(&d_counts_, sizeof(uint32_t) * na));
-      MCG_CUDA(cudaMemset(d_counts_, 0, sizeof(uint32_t) * na));
+      MCG_CUDA(cudaMemsetAsync(d_counts_, 0, sizeof(uint32_t) * na, stream_));
       MCG_CUDA(cudaMalloc(&d_cursor_, sizeof(uint32_t) * na));
-      MCG_CUDA(cudaMemset(d_cursor_, 0, sizeof(uint32_t) * na));
+      MCG_CUDA(cudaMemsetAsync(d_cursor_, 0, sizeof(uint32_t) * na, stream_));
       MCG_CUDA(cudaMalloc(&d_tile_, sizeof(uint32_t) * ((na + SCAN_TILE - 1) / SCAN_TILE + 1)));
       key_alloc_ = (uint32_t)na;
     }
     base_.nkeys = nkeys_;
     ntiles_ = (nkeys_ + SCAN_TILE - 1) / SCAN_TILE;
-    MCG_CUDA(cudaMemcpy(d_geos_, geos_h_.data(), sizeof(Geo<T>) * max_rep_, cudaMemcpyHostToDevice));
+    MCG_CUDA(cudaMemcpyAsync(d_geos_, geos_h_.data(), sizeof(Geo<T>) * max_rep_, cudaMemcpyHostToDevice, stream_));
     invalidate_graphs();
     return 0;
   }
@@ -784,7 +791,7 @@ class DeviceEngineT : public DeviceEngine {
       // no replica left: nothing to sort
       Counters c = cnt_;
       c.n_live = 0;
-      MCG_CUDA(cudaMemcpy(d_cnt_, &c, sizeof(Counters), cudaMemcpyHostToDevice));
+      MCG_CUDA(cudaMemcpyAsync(d_cnt_, &c, sizeof(Counters), cudaMemcpyHostToDevice, stream_));
       cnt_ = c;
       return 0;
     }
@@ -808,7 +815,7 @@ class DeviceEngineT : public DeviceEngine {
     Counters c2 = cnt_;
     c2.n_live = std::min<uint32_t>(c2.n_live_next, (uint32_t)cap_);
     c2.n_prod = c2.n_prod_done = c2.prod_hi = 0;
-    MCG_CUDA(cudaMemcpy(d_cnt_, &c2, sizeof(Counters), cudaMemcpyHostToDevice));
+    MCG_CUDA(cudaMemcpyAsync(d_cnt_, &c2, sizeof(Counters), cudaMemcpyHostToDevice, stream_));
     parity_ ^= 1;  // the re-binned arrays became the current ones
     cnt_ = c2;
     invalidate_graphs();
@@ -822,7 +829,7 @@ class DeviceEngineT : public DeviceEngine {
   }
 
   int read_counters(std::string& err) {
-    MCG_CUDA(cudaMemcpy(&cnt_, d_cnt_, sizeof(Counters), cudaMemcpyDeviceToHost));
+    MCG_CUDA(d2h(&cnt_, d_cnt_, sizeof(Counters)));
     return 0;
   }
 
@@ -842,9 +849,9 @@ class DeviceEngineT : public DeviceEngine {
       MCG_CUDA(cudaMalloc(&nu[k], sizeof(uint64_t) * cap));
       MCG_CUDA(cudaMalloc(&nt[k], sizeof(T) * cap));
       if (cap_) {
-        MCG_CUDA(cudaMemcpy(np[k], pos_[k], sizeof(P4<T>) * cap_, cudaMemcpyDeviceToDevice));
-        MCG_CUDA(cudaMemcpy(nu[k], uid_[k], sizeof(uint64_t) * cap_, cudaMemcpyDeviceToDevice));
-        MCG_CUDA(cudaMemcpy(nt[k], tuni_[k], sizeof(T) * cap_, cudaMemcpyDeviceToDevice));
+        MCG_CUDA(cudaMemcpyAsync(np[k], pos_[k], sizeof(P4<T>) * cap_, cudaMemcpyDeviceToDevice, stream_));
+        MCG_CUDA(cudaMemcpyAsync(nu[k], uid_[k], sizeof(uint64_t) * cap_, cudaMemcpyDeviceToDevice, stream_));
+        MCG_CUDA(cudaMemcpyAsync(nt[k], tuni_[k], sizeof(T) * cap_, cudaMemcpyDeviceToDevice, stream_));
         cudaFree(pos_[k]);
         cudaFree(uid_[k]);
         cudaFree(tuni_[k]);
@@ -862,7 +869,7 @@ class DeviceEngineT : public DeviceEngine {
     MCG_CUDA(cudaMalloc(&d_b_pos_, sizeof(P4<T>) * cap));
     MCG_CUDA(cudaMalloc(&d_st_, cap));
     MCG_CUDA(cudaMalloc(&d_claim_, sizeof(uint64_t) * cap));
-    MCG_CUDA(cudaMemset(d_claim_, 0xFF, sizeof(uint64_t) * cap));
+    MCG_CUDA(cudaMemsetAsync(d_claim_, 0xFF, sizeof(uint64_t) * cap, stream_));
     // every molecule can propose once per iteration (dense models at high rates
     // propose with a large share of their molecules)
     uint64_t pc = std::max<uint64_t>(4096, cap);
