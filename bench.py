@@ -312,7 +312,93 @@ def run_batching(args):
                              "molecule_steps_per_s": steps_p / job_p},
         "speedup_replicas_per_hour": job_p / job_b,
         "final_counts_replica0": [int(x) for x in finals_b[0]],
+        "note": f"both arms run {iters} iterations of each replica; replicas_per_hour is for jobs of that length",
     }
+
+
+# ---------------------------------------------------------------- closed cube (CPU-runnable case)
+
+def _cube_cpu_worker(args):
+    seed, iters = args
+    from mcell_gb300 import workloads
+    from oracle.oracle_py import oracle_engine_for_model
+
+    m = workloads.closed_cube(seed=seed)
+    e = oracle_engine_for_model(m, seed=seed)
+    t0 = time.perf_counter()
+    e.run(iters)
+    dt = time.perf_counter() - t0
+    return e.lib.orc_engine_mol_steps(e.h), dt
+
+
+def run_closed_cube(args, cpu_pool=None):
+    """The reference's CPU-runnable configuration: a reflective 1 um cube, A and B
+    5,000 each, A+B->C, fp64, 1,000 iterations, seeds 1..8 — each seed run alone on
+    the plain engine, all eight as one batch, and (when a pool of host processes is
+    given) the oracle's serial engine for 100 iterations per seed, one process per
+    seed."""
+    from mcell_gb300 import _native
+    from mcell_gb300 import workloads as W
+
+    seeds = list(range(1, 9))
+    iters = 1000
+    models = [W.closed_cube(seed=sd) for sd in seeds]
+    alone_s, steps_alone = 0.0, 0
+    for sd, m in zip(seeds, models):
+        e = W.engine_for(m, "fp64", seed=sd)
+        e.sync()
+        t0 = time.perf_counter()
+        e.step(iters)
+        e.sync()
+        alone_s += time.perf_counter() - t0
+        steps_alone += e.stats()[1]
+        e.close()
+    b = _native.Batch("fp64", 3, len(models))
+    hs = [W.model_handle(m, "fp64", seed=sd) for sd, m in zip(seeds, models)]
+    b.add(hs)
+    for h in hs:
+        h.close()
+    b.sync()
+    t0 = time.perf_counter()
+    b.step(iters)
+    b.sync()
+    batch_s = time.perf_counter() - t0
+    steps_batch = b.stats()[1]
+    b.close()
+    out = {"workload": "closed 1 um cube, 12 reflective walls, A 5,000 + B 5,000, A+B->C 1e8/M/s, dt 1 us, "
+                       "fp64, 1,000 iterations, seeds 1..8",
+           "plain_gpu_one_seed_after_another": {"job_s": alone_s, "molecule_steps_per_s": steps_alone / alone_s},
+           "batched_gpu_8_seeds": {"job_s": batch_s, "molecule_steps_per_s": steps_batch / batch_s}}
+    if cpu_pool is not None:
+        res = cpu_pool.map(_cube_cpu_worker, [(sd, 100) for sd in seeds])
+        out["cpu_oracle_8_processes"] = {"molecule_steps_per_s": sum(st / dt for st, dt in res), "cores": len(seeds),
+                                         "sample": "100 of the 1,000 iterations per seed"}
+    return out
+
+
+# ---------------------------------------------------------------- precision form
+
+def run_precision(args):
+    """fp32 engine (fp64 tie-breaks) against the fp64 engine on the bumpy tube:
+    wall-hit identity on 100,000 traced cases of the full model (10M molecules,
+    200,400 triangles; half of the cases start within 1 nm of an edge or vertex),
+    and the count trajectories of a 1M-molecule tube over 50 iterations (the full
+    model runs ~3 s per fp64 iteration)."""
+    import numpy as np
+
+    from mcell_gb300 import precision
+    from mcell_gb300 import workloads as W
+
+    m = W.bumpy_tube(n_mol=10_000_000)
+    n = len(m.species)
+    near = np.arange(n - int(round(0.05 * n)), n)
+    mism = precision.wall_hit_mismatch(m, n_cases=100_000, near_ids=near)
+    del m
+    small = W.bumpy_tube(n_mol=1_000_000, seed=2)
+    cnt = precision.count_error(small, n_iter=50)
+    return {"workload": "bumpy tube r = 0.2 um (+-0.05 um), 10 um, 200,400 reflective triangles, 5% of the molecules "
+                        "within 1 nm of edges/vertices, A+B->C, dt 0.1 us",
+            "wall_hit_mismatch_10M": mism, "count_error_1M_50_iterations": cnt}
 
 
 # ---------------------------------------------------------------- serving form
@@ -391,10 +477,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batching measurement")
     ap.add_argument("--batch-replicas", type=int, default=256)
-    ap.add_argument("--batch-iters", type=int, default=1000)
+    ap.add_argument("--batch-iters", type=int, default=200)
+    ap.add_argument("--no-cube", action="store_true", help="skip the closed-cube measurement")
+    ap.add_argument("--no-precision", action="store_true", help="skip the precision measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--serve-rate", type=float, default=50.0)
-    ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--serve-seconds", type=float, default=2.0)
     args = ap.parse_args()
     rank, world, _ = _rank_env()
     procs = args.cpu_procs or os.cpu_count() or 1
@@ -425,12 +513,15 @@ def main():
 
     # our arm: CPU baseline first (spawned processes, before any GPU call)
     cpu = None
+    cube_pool = None
     if rank == 0 and not args.no_cpu_baseline:
         _ensure_oracle_built()
         rate, res = cpu_measure(procs, args.n_mol, args.cpu_iters)
         cpu = {"value": rate, "unit": UNIT, "cores": procs, "kind": "port",
                "sample": f"{procs} independent seeded processes x {args.cpu_iters} iterations of the "
                          f"1M-molecule model (oracle serial engine, fp64)"}
+        if not args.no_cube:
+            cube_pool = mp.get_context("spawn").Pool(8)  # started before the first GPU call
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
@@ -439,6 +530,12 @@ def main():
         line["batching"] = run_batching(args)
     if rank == 0 and not args.no_serve:
         line["serving"] = run_serving(args)
+    if rank == 0 and not args.no_cube:
+        line["closed_cube"] = run_closed_cube(args, cube_pool)
+    if cube_pool is not None:
+        cube_pool.close()
+    if rank == 0 and not args.no_precision:
+        line["precision"] = run_precision(args)
     if rank == 0:
         if cpu:
             line["cpu_baseline"] = cpu
