@@ -14,6 +14,7 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <unordered_map>
 
 #include "mcg_engine.h"
@@ -97,8 +98,7 @@ class DeviceEngineT : public DeviceEngine {
     }
     uint64_t n_new = 0;
     for (uint32_t k = 0; k < n; k++) n_new += specs[k].n_mol;
-    Product<T>* stage = nullptr;
-    if (pinned_reserve(n_new, &stage, err)) return -2;
+    std::vector<Product<T>> stage(n_new);
     uint64_t staged = 0;
     for (uint32_t k = 0; k < n; k++) {
       const ReplicaSpec& sp = specs[k];
@@ -108,7 +108,7 @@ class DeviceEngineT : public DeviceEngine {
         for (uint32_t j = 0; j <= k; j++) free_replica(slots[j]);
         return rc;
       }
-      rc = stage_molecules(r, sp.n_mol, sp.pos, sp.species, 0, stage + staged, err);
+      rc = stage_molecules(r, sp.n_mol, sp.pos, sp.species, 0, stage.data() + staged, err);
       staged += sp.n_mol;
       if (rc) {
         for (uint32_t j = 0; j <= k; j++) free_replica(slots[j]);
@@ -119,7 +119,7 @@ class DeviceEngineT : public DeviceEngine {
     }
     int rc = layout_keys(err);
     if (rc) return rc;
-    return rebin(stage, n_new, err);
+    return rebin(stage.data(), n_new, err);
   }
 
   int remove_replicas(const uint32_t* reps, uint32_t n, std::string& err) override {
@@ -150,13 +150,12 @@ class DeviceEngineT : public DeviceEngine {
       err = "no such replica";
       return -1;
     }
-    Product<T>* stage = nullptr;
-    if (pinned_reserve(n, &stage, err)) return -2;
-    int rc = stage_molecules(rep, n, pos, species, uid0, stage, err);
+    std::vector<Product<T>> stage(n);
+    int rc = stage_molecules(rep, n, pos, species, uid0, stage.data(), err);
     if (rc) return rc;
     reps_[rep].next_uid = std::max<uint64_t>(reps_[rep].next_uid, uid0 + n);
     if (read_counters(err)) return -2;
-    return rebin(stage, n, err);
+    return rebin(stage.data(), n, err);
   }
 
   int step(uint32_t n, std::string& err) override {
@@ -696,43 +695,36 @@ class DeviceEngineT : public DeviceEngine {
     const Geo<T>& g = geos_h_[r];
     const double o[3] = {(double)g.origin.x, (double)g.origin.y, (double)g.origin.z};
     const double q[3] = {(double)g.opposite.x, (double)g.opposite.y, (double)g.opposite.z};
-    for (uint64_t i = 0; i < n; i++) {
-      if (species[i] >= nsp_) {
-        err = "species index out of range";
-        return -1;
+    // large uploads are staged by several host threads (independent ranges)
+    auto work = [&](uint64_t a, uint64_t b) -> int {
+      for (uint64_t i = a; i < b; i++) {
+        if (species[i] >= nsp_) return -1;
+        double p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+        if (!(p[0] >= o[0] && p[1] >= o[1] && p[2] >= o[2] && p[0] < q[0] && p[1] < q[1] && p[2] < q[2])) return -4;
+        place_fp32(reps_[r], p);
+        Product<T> m;
+        m.pos.x = (T)p[0];
+        m.pos.y = (T)p[1];
+        m.pos.z = (T)p[2];
+        put_meta(m.pos, make_meta(species[i], r, META_SCHEDULE_UNIMOL));
+        m.birth = 0;
+        m.uid = uid0 + i;
+        m.tuni = TIME_FOREVER;
+        stage[i] = m;
       }
-      double p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
-      if (!(p[0] >= o[0] && p[1] >= o[1] && p[2] >= o[2] && p[0] < q[0] && p[1] < q[1] && p[2] < q[2])) {
-        err = "molecule outside the partition";
-        return -4;
-      }
-      place_fp32(reps_[r], p);
-      Product<T> m;
-      m.pos.x = (T)p[0];
-      m.pos.y = (T)p[1];
-      m.pos.z = (T)p[2];
-      put_meta(m.pos, make_meta(species[i], r, META_SCHEDULE_UNIMOL));
-      m.birth = 0;
-      m.uid = uid0 + i;
-      m.tuni = TIME_FOREVER;
-      stage[i] = m;
+      return 0;
+    };
+    const unsigned nt = n < 200000 ? 1u : std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+    std::vector<int> rcs(nt, 0);
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < nt; t++) th.emplace_back([&, t] { rcs[t] = work(n * t / nt, n * (t + 1) / nt); });
+    rcs[0] = work(0, n / nt);
+    for (auto& x : th) x.join();
+    for (int rc : rcs) {
+      if (rc == -1) err = "species index out of range";
+      if (rc == -4) err = "molecule outside the partition";
+      if (rc) return rc;
     }
-    return 0;
-  }
-
-  // pinned host staging for n uploads (kept for later uploads: pageable copies run
-  // at a fraction of the link's rate)
-  int pinned_reserve(uint64_t n, Product<T>** out, std::string& err) {
-    const size_t bytes = sizeof(Product<T>) * std::max<uint64_t>(n, 1);
-    if (bytes > pinned_bytes_) {
-      MCG_CUDA(cudaStreamSynchronize(stream_));  // an earlier upload may still read it
-      if (pinned_) cudaFreeHost(pinned_);
-      pinned_ = nullptr;
-      pinned_bytes_ = 0;
-      MCG_CUDA(cudaHostAlloc(&pinned_, bytes, cudaHostAllocDefault));
-      pinned_bytes_ = bytes;
-    }
-    *out = static_cast<Product<T>*>(pinned_);
     return 0;
   }
 
@@ -1006,7 +998,6 @@ class DeviceEngineT : public DeviceEngine {
     cudaFree(d_cnt_);
     cudaFree(d_debug_);
     cudaFree(d_geos_);
-    if (pinned_) cudaFreeHost(pinned_);
     if (stream_) cudaStreamDestroy(stream_);
   }
 
@@ -1042,8 +1033,6 @@ class DeviceEngineT : public DeviceEngine {
   unsigned long long* d_traj_ = nullptr;
   Counters* d_cnt_ = nullptr;
   double* d_debug_ = nullptr;
-  void* pinned_ = nullptr;  // host staging for uploads
-  size_t pinned_bytes_ = 0;
 };
 
 }  // namespace mcg
