@@ -422,11 +422,37 @@ struct SubSet {
     else
       overflow = true;
   }
+  template <typename T>
+  __device__ __forceinline__ void insert3(const Geo<T>& g, int x, int y, int z) {
+    insert(sub_of3(g, x, y, z));
+  }
+};
+
+// The same set as a bit mask over a 4x4x4 window of subpartitions (registers, no
+// dynamic indexing). Bit dx | dy << 2 | dz << 4 stands for subpartition
+// (x0 + dx, y0 + dy, z0 + dz); an index outside the grid is skipped exactly as
+// SubSet skips it, and an insertion outside the window marks the mask unusable
+// (the caller then builds the list instead).
+struct SubMask {
+  uint64_t bits;
+  int x0, y0, z0;
+  uint32_t n3;
+  bool bad;
+  template <typename T>
+  __device__ __forceinline__ void insert3(const Geo<T>& g, int x, int y, int z) {
+    if (sub_of3(g, x, y, z) >= n3) return;
+    const unsigned dx = (unsigned)(x - x0), dy = (unsigned)(y - y0), dz = (unsigned)(z - z0);
+    if ((dx | dy | dz) > 3u) {
+      bad = true;
+      return;
+    }
+    bits |= 1ull << (dx | (dy << 2) | (dz << 4));
+  }
 };
 
 // collect_neighboring_subparts (collision_utils_subparts.inl:38-122)
-template <typename T>
-__device__ void collect_neighbors(const Geo<T>& g, V3<T> pos, int ix, int iy, int iz, T r, SubSet& st) {
+template <typename T, class Set>
+__device__ void collect_neighbors(const Geo<T>& g, V3<T> pos, int ix, int iy, int iz, T r, Set& st) {
   T part_len = g.part_edge;
   V3<T> rel = pos - g.origin;
   V3<T> plus = rel + v3<T>(r, r, r);
@@ -434,46 +460,44 @@ __device__ void collect_neighbors(const Geo<T>& g, V3<T> pos, int ix, int iy, in
   V3<T> b = cmul(v3<T>((T)ix, (T)iy, (T)iz), v3<T>(g.sp_edge, g.sp_edge, g.sp_edge));
   int xd = 0, yd = 0, zd = 0;
   if (minus.x < b.x && minus.x > (T)0.0) {
-    st.insert(sub_of3(g, ix - 1, iy, iz));
+    st.insert3(g, ix - 1, iy, iz);
     xd = -1;
   } else if (plus.x > b.x + g.sp_edge && plus.x < part_len) {
-    st.insert(sub_of3(g, ix + 1, iy, iz));
+    st.insert3(g, ix + 1, iy, iz);
     xd = 1;
   }
   if (minus.y < b.y && minus.y > (T)0.0) {
-    st.insert(sub_of3(g, ix, iy - 1, iz));
+    st.insert3(g, ix, iy - 1, iz);
     yd = -1;
   } else if (plus.y > b.y + g.sp_edge && plus.y < part_len) {
-    st.insert(sub_of3(g, ix, iy + 1, iz));
+    st.insert3(g, ix, iy + 1, iz);
     yd = 1;
   }
   if (minus.z < b.z && minus.z > (T)0.0) {
-    st.insert(sub_of3(g, ix, iy, iz - 1));
+    st.insert3(g, ix, iy, iz - 1);
     zd = -1;
   } else if (plus.z > b.z + g.sp_edge && plus.z < part_len) {
-    st.insert(sub_of3(g, ix, iy, iz + 1));
+    st.insert3(g, ix, iy, iz + 1);
     zd = 1;
   }
-  if (xd && yd) st.insert(sub_of3(g, ix + xd, iy + yd, iz));
-  if (xd && zd) st.insert(sub_of3(g, ix + xd, iy, iz + zd));
-  if (yd && zd) st.insert(sub_of3(g, ix, iy + yd, iz + zd));
-  if (xd && yd && zd) st.insert(sub_of3(g, ix + xd, iy + yd, iz + zd));
+  if (xd && yd) st.insert3(g, ix + xd, iy + yd, iz);
+  if (xd && zd) st.insert3(g, ix + xd, iy, iz + zd);
+  if (yd && zd) st.insert3(g, ix, iy + yd, iz + zd);
+  if (xd && yd && zd) st.insert3(g, ix + xd, iy + yd, iz + zd);
 }
 
 // subpartitions whose occupants can collide with the segment: crossed ones and
 // their neighbours within R*sqrt(2) (the molecule half of collect_crossed_subparts)
-template <typename T>
-__device__ void collect_for_molecules(const Geo<T>& g, V3<T> pos, uint32_t sp, V3<T> disp, SubSet& st) {
-  st.n = 0;
-  st.n3 = (uint32_t)g.nsub2 * (uint32_t)g.nsub;
+template <typename T, class Set>
+__device__ void collect_for_molecules(const Geo<T>& g, V3<T> pos, uint32_t sp, V3<T> disp, Set& st) {
   const T rn = g.R * (T)1.41421356238;  // POS_SQRT2
-  st.insert(sp);
   int sx = (int)(sp % g.nsub), sy = (int)((sp / g.nsub) % g.nsub), sz = (int)((sp / g.nsub2) % g.nsub);
+  st.insert3(g, sx, sy, sz);
   collect_neighbors(g, pos, sx, sy, sz, rn, st);
   Walk<T> w;
   w.start(g, pos, sp, disp);
   while (w.next(g)) {
-    st.insert(w.cur);
+    st.insert3(g, w.cx, w.cy, w.cz);
     collect_neighbors(g, w.cp, w.cx, w.cy, w.cz, rn, st);
   }
   V3<T> dest = pos + disp;
@@ -806,6 +830,54 @@ __device__ __forceinline__ uint32_t octant_of(const Geo<T>& g, V3<T> p, int ix, 
 
 // collide_mol (collision_utils.inl:464-515) against every reacting occupant of the
 // collected subpartitions
+// occupants of one subpartition (the partner species' octant ranges the segment box touches)
+template <typename T>
+__device__ __forceinline__ void occupants_of(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos,
+                                             V3<T> disp, uint32_t pmask, T movelen2, T sigma2, V3<T> lo, V3<T> hi,
+                                             uint32_t sp, Colls<T>& out) {
+  const uint32_t om = g.oct_shift ? octants_touched(g, sp, lo, hi) : 1u;
+  uint32_t m = pmask;
+  while (m) {
+    const int b = __ffs(m) - 1;
+    m &= m - 1;
+    // the octants of (subpartition, species) are consecutive keys: load their starts
+    // together (independent loads, one or two cache lines), then scan the wanted ones
+    const uint32_t base = g.kbase + (((uint32_t)b * g.n3 + sp) << g.oct_shift);
+    uint32_t s9[9];
+    const uint32_t noct = 1u << g.oct_shift;
+#pragma unroll
+    for (int o = 0; o < 9; o++) s9[o] = (o <= (int)noct) ? __ldg(cells.start + base + o) : 0u;
+    for (uint32_t oo = om; oo; oo &= oo - 1) {
+      const uint32_t o = (uint32_t)(__ffs(oo) - 1);
+      const uint32_t j0 = s9[o], j1 = s9[o + 1];
+      // MCG_OCC_BATCH occupants per round: their loads are issued together (latency overlap)
+      for (uint32_t j4 = j0; j4 < j1; j4 += MCG_OCC_BATCH) {
+        P4<T> q4[MCG_OCC_BATCH];
+#pragma unroll
+        for (int u = 0; u < MCG_OCC_BATCH; u++)
+          if (j4 + u < j1) q4[u] = cells.pos[j4 + u];
+#pragma unroll
+        for (int u = 0; u < MCG_OCC_BATCH; u++) {
+          const uint32_t j = j4 + u;
+          if (j >= j1) break;
+          const V3<T> dir = v3<T>(q4[u].x, q4[u].y, q4[u].z) - pos;
+          const T d = dot(dir, disp);
+          if (d < 0) continue;
+          if (d > movelen2) continue;
+          const T dirlen2 = dot(dir, dir);
+          if (movelen2 * dirlen2 - d * d > movelen2 * sigma2) continue;
+          if (j == self) continue;
+          if (cells.dead && cells.dead[j] == 2) continue;
+          VV<T> c;
+          c.t = d / movelen2;
+          c.idx = j;
+          out.insert(c, cells.uid);
+        }
+      }
+    }
+  }
+}
+
 template <typename T>
 __device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos, int species,
                                        V3<T> disp, const SubSet& st, Colls<T>& out) {
@@ -818,50 +890,43 @@ __device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, u
   const T mg = g.R * (T)1.01 + g.sp_edge * (T)1e-3;
   const V3<T> lo = v3<T>(min(pos.x, e.x) - mg, min(pos.y, e.y) - mg, min(pos.z, e.z) - mg);
   const V3<T> hi = v3<T>(max(pos.x, e.x) + mg, max(pos.y, e.y) + mg, max(pos.z, e.z) + mg);
-  for (int i = 0; i < st.n; i++) {
-    const uint32_t sp = st.s[i];
-    const uint32_t om = g.oct_shift ? octants_touched(g, sp, lo, hi) : 1u;
-    uint32_t m = pmask;
-    while (m) {
-      const int b = __ffs(m) - 1;
-      m &= m - 1;
-      // the octants of (subpartition, species) are consecutive keys: load their starts
-      // together (independent loads, one or two cache lines), then scan the wanted ones
-      const uint32_t base = g.kbase + (((uint32_t)b * g.n3 + sp) << g.oct_shift);
-      uint32_t s9[9];
-      const uint32_t noct = 1u << g.oct_shift;
-#pragma unroll
-      for (int o = 0; o < 9; o++) s9[o] = (o <= (int)noct) ? __ldg(cells.start + base + o) : 0u;
-      for (uint32_t oo = om; oo; oo &= oo - 1) {
-        const uint32_t o = (uint32_t)(__ffs(oo) - 1);
-        const uint32_t j0 = s9[o], j1 = s9[o + 1];
-        // MCG_OCC_BATCH occupants per round: their loads are issued together (latency overlap)
-        for (uint32_t j4 = j0; j4 < j1; j4 += MCG_OCC_BATCH) {
-          P4<T> q4[MCG_OCC_BATCH];
-#pragma unroll
-          for (int u = 0; u < MCG_OCC_BATCH; u++)
-            if (j4 + u < j1) q4[u] = cells.pos[j4 + u];
-#pragma unroll
-          for (int u = 0; u < MCG_OCC_BATCH; u++) {
-            const uint32_t j = j4 + u;
-            if (j >= j1) break;
-            const V3<T> dir = v3<T>(q4[u].x, q4[u].y, q4[u].z) - pos;
-            const T d = dot(dir, disp);
-            if (d < 0) continue;
-            if (d > movelen2) continue;
-            const T dirlen2 = dot(dir, dir);
-            if (movelen2 * dirlen2 - d * d > movelen2 * sigma2) continue;
-            if (j == self) continue;
-            if (cells.dead && cells.dead[j] == 2) continue;
-            VV<T> c;
-            c.t = d / movelen2;
-            c.idx = j;
-            out.insert(c, cells.uid);
-          }
-        }
-      }
-    }
+  for (int i = 0; i < st.n; i++) occupants_of(g, cells, self, pos, disp, pmask, movelen2, sigma2, lo, hi, st.s[i], out);
+}
+
+// the same over a mask (set bits in index order; the candidate list keeps the
+// earliest collisions by time and id, so the visiting order does not matter)
+template <typename T>
+__device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos, int species,
+                                       V3<T> disp, const SubMask& sm, Colls<T>& out) {
+  const Chem& ch = *g.chem;
+  const uint32_t pmask = ch.partners[species];
+  const T movelen2 = dot(disp, disp);
+  const T sigma2 = g.R * g.R;
+  // segment box grown by R plus a margin that covers rounding in the octant test
+  const V3<T> e = pos + disp;
+  const T mg = g.R * (T)1.01 + g.sp_edge * (T)1e-3;
+  const V3<T> lo = v3<T>(min(pos.x, e.x) - mg, min(pos.y, e.y) - mg, min(pos.z, e.z) - mg);
+  const V3<T> hi = v3<T>(max(pos.x, e.x) + mg, max(pos.y, e.y) + mg, max(pos.z, e.z) + mg);
+  for (uint64_t mb = sm.bits; mb; mb &= mb - 1) {
+    const int bit = __ffsll((long long)mb) - 1;
+    const uint32_t sp = sub_of3(g, sm.x0 + (bit & 3), sm.y0 + ((bit >> 2) & 3), sm.z0 + (bit >> 4));
+    occupants_of(g, cells, self, pos, disp, pmask, movelen2, sigma2, lo, hi, sp, out);
   }
+}
+
+// the partner scan over a list of subpartitions, for segments whose set does not fit
+// the 4x4x4 mask (long moves, fine grids); out of line: rarely taken
+template <typename T>
+__device__ __noinline__ void partners_by_list(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos,
+                                              uint32_t sp, V3<T> mdisp, int species, V3<T> remaining,
+                                              Colls<T>& colls, uint32_t& err) {
+  SubSet st;
+  st.n = 0;
+  st.n3 = (uint32_t)g.nsub2 * (uint32_t)g.nsub;
+  st.overflow = false;
+  collect_for_molecules(g, pos, sp, mdisp, st);
+  if (st.overflow) err |= ST_SET_OVERFLOW;
+  collide_with_occupants(g, cells, self, pos, species, remaining, st, colls);
 }
 
 // ------------------------------------------------------------------ exact disk
@@ -1270,15 +1335,33 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
     colls.n = 0;
     colls.overflow = false;
     if (can_vol_react) {
-      SubSet st;
-      st.overflow = false;
       // ray_trace_vol keeps the set of the first collection unless a wall was hit
       // before the last crossed subpartition, then re-collects up to the hit
       V3<T> mdisp = pdisp;
       if (hit_wall && !hit_in_last) mdisp = used_tentative ? up_to_init : hit.pos - pos;
-      collect_for_molecules(g, pos, sp, mdisp, st);
-      if (st.overflow) res.err |= ST_SET_OVERFLOW;
-      collide_with_occupants(g, cells, self, pos, species, remaining, st, colls);
+      // the set lies within the segment's box grown by R*sqrt(2): a 4x4x4 mask when
+      // that box spans at most 4 subpartitions per axis, else (or if an insertion
+      // falls outside) the list
+      const T rn = g.R * (T)1.41421356238 * (T)1.01;
+      const V3<T> me = pos + mdisp;
+      SubMask sm;
+      sm.bits = 0;
+      sm.n3 = (uint32_t)g.nsub2 * (uint32_t)g.nsub;
+      sm.bad = false;
+      sm.x0 = (int)floor((min(pos.x, me.x) - rn - g.origin.x) * g.sp_rcp);
+      sm.y0 = (int)floor((min(pos.y, me.y) - rn - g.origin.y) * g.sp_rcp);
+      sm.z0 = (int)floor((min(pos.z, me.z) - rn - g.origin.z) * g.sp_rcp);
+      if ((int)floor((max(pos.x, me.x) + rn - g.origin.x) * g.sp_rcp) - sm.x0 > 3 ||
+          (int)floor((max(pos.y, me.y) + rn - g.origin.y) * g.sp_rcp) - sm.y0 > 3 ||
+          (int)floor((max(pos.z, me.z) + rn - g.origin.z) * g.sp_rcp) - sm.z0 > 3)
+        sm.bad = true;
+      else
+        collect_for_molecules(g, pos, sp, mdisp, sm);
+      if (!sm.bad) {
+        collide_with_occupants(g, cells, self, pos, species, remaining, sm, colls);
+      } else {
+        partners_by_list(g, cells, self, pos, sp, mdisp, species, remaining, colls, res.err);
+      }
       if (colls.overflow) res.err |= ST_COLL_OVERFLOW;
     }
     const V3<T> pos_at_start = pos;  // collision points are measured from here
