@@ -706,6 +706,12 @@ __device__ MCG_GUARD_INLINE void guard_sides(const Geo<T>& g, uint32_t sp, V3<T>
   }
 }
 
+// the same, out of line, for the rare sites (reflection and crossing points)
+template <typename T>
+__device__ __noinline__ void guard_sides_rare(const Geo<T>& g, uint32_t sp, V3<T>& pos, V3<T> ref, uint32_t skip) {
+  guard_sides(g, sp, pos, ref, skip);
+}
+
 template <typename T>
 struct WallHit {
   int type;
@@ -1406,7 +1412,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
           // triangle of the crossed edge is hit again at t ~ 0 and re-tried without end
           if (sizeof(T) == 4) {
             keep_side(g.wrej[hit.wall], hit.type == CT_FRONT ? -1.0 : 1.0, pos);
-            guard_sides(g, sp, pos, pos_at_start, hit.wall);  // every other plane: the side it came from
+            guard_sides_rare(g, sp, pos, pos_at_start, hit.wall);  // every other plane: the side it came from
             sp = subpart_of(g, pos);
           }
           ev.put(2, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
@@ -1436,7 +1442,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
           // edge of two faces rounds onto both planes)
           if (sizeof(T) == 4) {
             keep_side(rj, hit.type == CT_FRONT ? 1.0 : -1.0, pos);
-            guard_sides(g, sp, pos, pos_at_start, hit.wall);
+            guard_sides_rare(g, sp, pos, pos_at_start, hit.wall);
             sp = subpart_of(g, pos);
           }
           ev.put(1, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);

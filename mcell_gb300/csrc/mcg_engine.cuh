@@ -52,7 +52,7 @@ class DeviceEngineT : public DeviceEngine {
     {
       // k_diffuse runs persistent warps: as many blocks as can be resident
       int bps = 1;
-      MCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_diffuse<T>, TPB, 0));
+      MCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_diffuse<T, false>, TPB, 0));
       bps_max_ = std::max(1, bps);
       diffuse_grid_ = bps_max_ * sms_;
     }
@@ -926,7 +926,10 @@ class DeviceEngineT : public DeviceEngine {
     const unsigned g = grid(cap_);
     const unsigned gs = (unsigned)std::max(1, sms_);
     mark(0, prof);
-    k_diffuse<T><<<diffuse_grid_, TPB, 0, stream_>>>(s);
+    if (s.debug_log)
+      k_diffuse<T, true><<<diffuse_grid_, TPB, 0, stream_>>>(s);
+    else
+      k_diffuse<T, false><<<diffuse_grid_, TPB, 0, stream_>>>(s);
     mark(1, prof);
     k_resolve<T><<<gs, TPB, 0, stream_>>>(s);
     k_collect_losers<T><<<gs, TPB, 0, stream_>>>(s);

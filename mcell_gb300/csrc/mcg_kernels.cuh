@@ -212,8 +212,9 @@ struct StepDecision {
   int kind;  // 0 survivor, 1 proposal, 2 dead
 };
 
-// returns 0 survivor, 1 proposal, 2 dead, 3 survivor of a frozen replica (not stepped)
-template <typename T>
+// returns 0 survivor, 1 proposal, 2 dead, 3 survivor of a frozen replica (not stepped).
+// LOG: the build that can log one molecule's events (mcg_debug_molecule)
+template <typename T, bool LOG = true>
 __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, Proposal* prop_out, uint32_t& err) {
   P4<T> rec = s.a_pos[i];
   uint32_t meta = meta_of(rec);
@@ -272,27 +273,32 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
     cells.uid = s.a_uid;
     cells.start = s.start;
     cells.dead = dead;
-    MaybeEvents ev;
-    ev.out = nullptr;
-    if (uid == s.debug_uid && s.debug_log) {
-      // per-iteration record of one chosen molecule: 9 + 32*8 result doubles, start xyz, displacement xyz
-      ev.out = s.debug_log + (size_t)(it % 64) * 271;
-      for (int q = 0; q < 271; q++) ev.out[q] = 0;
-      ev.out[265] = (double)pos.x;
-      ev.out[266] = (double)pos.y;
-      ev.out[267] = (double)pos.z;
-      ev.out[268] = (double)disp.x;
-      ev.out[269] = (double)disp.y;
-      ev.out[270] = (double)disp.z;
-    }
-    r = trace_molecule<T>(g, cells, i, pos, species, disp, r_rate_factor, t_steps, 0.0, draws, ev);
-    if (ev.out) {
-      ev.out[0] = r.status;
-      ev.out[1] = (double)r.pos.x;
-      ev.out[2] = (double)r.pos.y;
-      ev.out[3] = (double)r.pos.z;
-      ev.out[4] = r.subpart;
-      ev.out[5] = it;
+    if (LOG) {
+      MaybeEvents ev;
+      ev.out = nullptr;
+      if (uid == s.debug_uid && s.debug_log) {
+        // per-iteration record of one chosen molecule: 9 + 32*8 result doubles, start xyz, displacement xyz
+        ev.out = s.debug_log + (size_t)(it % 64) * 271;
+        for (int q = 0; q < 271; q++) ev.out[q] = 0;
+        ev.out[265] = (double)pos.x;
+        ev.out[266] = (double)pos.y;
+        ev.out[267] = (double)pos.z;
+        ev.out[268] = (double)disp.x;
+        ev.out[269] = (double)disp.y;
+        ev.out[270] = (double)disp.z;
+      }
+      r = trace_molecule<T>(g, cells, i, pos, species, disp, r_rate_factor, t_steps, 0.0, draws, ev);
+      if (ev.out) {
+        ev.out[0] = r.status;
+        ev.out[1] = (double)r.pos.x;
+        ev.out[2] = (double)r.pos.y;
+        ev.out[3] = (double)r.pos.z;
+        ev.out[4] = r.subpart;
+        ev.out[5] = it;
+      }
+    } else {
+      NoEvents ev;  // production kernel: no event code in the hot path
+      r = trace_molecule<T>(g, cells, i, pos, species, disp, r_rate_factor, t_steps, 0.0, draws, ev);
     }
     err |= r.err;
   } else {
@@ -345,7 +351,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   return 0;
 }
 
-template <typename T>
+template <typename T, bool LOG>
 __global__ void __launch_bounds__(TPB, MCG_DIFFUSE_MIN_BLOCKS) k_diffuse(State<T> s) {
   const uint32_t n = s.cnt->n_live;
   uint32_t err = 0;
@@ -363,7 +369,7 @@ __global__ void __launch_bounds__(TPB, MCG_DIFFUSE_MIN_BLOCKS) k_diffuse(State<T
     uint32_t key = 0;
     if (active) {
       Proposal p;
-      kind = run_molecule(s, i, nullptr, &p, err);
+      kind = run_molecule<T, LOG>(s, i, nullptr, &p, err);
       if (kind == 3)
         kind = 0;  // frozen replica: kept, not stepped
       else
