@@ -319,7 +319,7 @@ __device__ __forceinline__ T abs_max_2vec(V3<T> a, V3<T> b) {
 
 // get_displacement_up_to_partition_boundary (collision_utils.inl:48-114)
 template <typename T>
-__device__ V3<T> disp_up_to_partition_boundary(const Geo<T>& g, V3<T> pos, V3<T> disp) {
+__device__ __noinline__ V3<T> disp_up_to_partition_boundary(const Geo<T>& g, V3<T> pos, V3<T> disp) {
   V3<T> nz = guard_zero(disp);
   V3<T> dir = v3<T>(nz.x > 0 ? 1 : 0, nz.y > 0 ? 1 : 0, nz.z > 0 ? 1 : 0);
   V3<T> edges = g.origin + scale(dir, g.part_edge);
@@ -512,7 +512,7 @@ enum : int { CT_MISS = 0, CT_REDO = 1, CT_FRONT = 2, CT_BACK = 3 };
 
 // jump_away_line (collision_utils.inl:568-603)
 template <typename T, class D>
-__device__ void jump_away_line(V3<T> p, T k, V3<T> A, V3<T> B, V3<T> n, D& draws, V3<T>& v) {
+__device__ __noinline__ void jump_away_line(V3<T> p, T k, V3<T> A, V3<T> B, V3<T> n, D& draws, V3<T>& v) {
   V3<T> e = B - A;
   T elen2 = dot(e, e);
   T le_1 = (T)1.0 / sqrt(elen2);

@@ -30,7 +30,7 @@ namespace mcg {
 constexpr int TPB = 256;
 // resident blocks of k_diffuse the register allocation must allow (occupancy vs spills)
 #ifndef MCG_DIFFUSE_MIN_BLOCKS
-#define MCG_DIFFUSE_MIN_BLOCKS 6
+#define MCG_DIFFUSE_MIN_BLOCKS 8
 #endif
 constexpr int SCAN_TILE = 2048;
 constexpr int REDO_ROUNDS = 64;      // loser rounds in the one-CTA pass
@@ -197,8 +197,8 @@ __device__ void add_product(const State<T>& s, int species, uint32_t rep, V3<T> 
 // unimolecular outcome: the molecule is destroyed, products appear at its position
 // (outcome_unimolecular, diffuse_react_event.cpp:2939). it: the replica's own iteration.
 template <typename T>
-__device__ void unimol_products(const State<T>& s, const Geo<T>& g, int species, V3<T> pos, double t, uint64_t uid,
-                                uint32_t it) {
+__device__ __noinline__ void unimol_products(const State<T>& s, const Geo<T>& g, int species, V3<T> pos, double t,
+                                             uint64_t uid, uint32_t it) {
   const Chem& ch = *g.chem;
   for (int k = 0; k < 2; k++) {
     int ps = ch.uni_prod[species][k];
