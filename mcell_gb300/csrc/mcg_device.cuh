@@ -138,7 +138,8 @@ struct Geo {
   const P4<T>* wrej;          // normal xyz, distance to origin
   const WallFace<T>* wface;
   const uint32_t* wsp_off;    // CSR: walls per subpartition (ascending wall index)
-  const uint32_t* wsp_list;   // entries: wall index << 8 | mask of the subpartition octants it reaches
+  const uint32_t* wsp_list;   // wall indices
+  const uint64_t* wsp_cells;  // per entry: cells of the subpartition's 4x4x4 grid the wall reaches
   const uint8_t* wall_class;  // [wall * nsp + species]: 0 reflect, 1 transparent, 2 absorptive
   const Chem* chem;
   // fp32 engines: the wall constants in fp64 for the tie-breaks, 16 per wall (normal
@@ -286,6 +287,27 @@ __device__ __forceinline__ uint32_t octants_touched(const Geo<T>& g, uint32_t sp
   return mx & my & mz;
 }
 // box around the segment p -> p + d, grown by m in each direction
+// cells of subpartition sp's 4x4x4 grid (bit x + 4y + 16z) that the box [lo, hi]
+// touches; the outer faces are not tested (the box may reach past the subpartition)
+template <typename T>
+__device__ __forceinline__ uint64_t cells_touched(const Geo<T>& g, uint32_t sp, V3<T> lo, V3<T> hi) {
+  const int ix = (int)(sp % g.nsub), iy = (int)((sp / g.nsub) % g.nsub), iz = (int)(sp / g.nsub2);
+  const T q = g.sp_edge * (T)0.25;
+  const V3<T> o = g.origin + cmul(v3<T>((T)ix, (T)iy, (T)iz), v3<T>(g.sp_edge, g.sp_edge, g.sp_edge));
+  auto axis = [q](T l, T h, T base) -> uint32_t {
+    const T q1 = base + q, q2 = base + (T)2 * q, q3 = base + (T)3 * q;
+    return (l < q1 ? 1u : 0u) | (l < q2 && h >= q1 ? 2u : 0u) | (l < q3 && h >= q2 ? 4u : 0u) | (h >= q3 ? 8u : 0u);
+  };
+  const uint32_t ax = axis(lo.x, hi.x, o.x), ay = axis(lo.y, hi.y, o.y), az = axis(lo.z, hi.z, o.z);
+  // x: the same nibble in all 16 (y, z) positions; y: 4-bit groups per z; z: 16-bit groups
+  const uint64_t mx = (uint64_t)ax * 0x1111111111111111ull;
+  const uint64_t gy = (ay & 1 ? 0x000Full : 0) | (ay & 2 ? 0x00F0ull : 0) | (ay & 4 ? 0x0F00ull : 0) | (ay & 8 ? 0xF000ull : 0);
+  const uint64_t my = gy * 0x0001000100010001ull;
+  const uint64_t mz = (az & 1 ? 0xFFFFull : 0) | (az & 2 ? 0xFFFF0000ull : 0) | (az & 4 ? 0xFFFF00000000ull : 0) |
+                      (az & 8 ? 0xFFFF000000000000ull : 0);
+  return mx & my & mz;
+}
+
 template <typename T>
 __device__ __forceinline__ void seg_box(V3<T> p, V3<T> d, T m, V3<T>& lo, V3<T>& hi) {
   const V3<T> e = p + d;
@@ -692,11 +714,12 @@ template <typename T>
 __device__ MCG_GUARD_INLINE void guard_sides(const Geo<T>& g, uint32_t sp, V3<T>& pos, V3<T> ref, uint32_t skip) {
   V3<T> glo, ghi;
   seg_box(pos, v3<T>(0, 0, 0), (T)2e-2, glo, ghi);
-  const uint32_t gm = octants_touched(g, sp, glo, ghi);
+  const uint64_t gm = cells_touched(g, sp, glo, ghi);
   for (uint32_t k = g.wsp_off[sp]; k < g.wsp_off[sp + 1]; k++) {
-    const uint32_t ent = g.wsp_list[k];
-    if (!(ent & gm) || (ent >> 8) == skip) continue;
-    const P4<T> rj = g.wrej[ent >> 8];
+    if (!(g.wsp_cells[k] & gm)) continue;
+    const uint32_t wi = g.wsp_list[k];
+    if (wi == skip) continue;
+    const P4<T> rj = g.wrej[wi];
     // cheap fp32 screen first; the fp64 side test only for points near the plane
     const T d1 = dot(v3<T>(rj.x, rj.y, rj.z), pos) - rj.w;
     if (tabs(d1) > (T)1e-2) continue;
@@ -739,13 +762,12 @@ restart:
   // t = 1, or an axis-aligned injected move) is not filtered, so that re-try stays.
   V3<T> lo, hi;
   seg_box(pos, disp, g.sp_edge * (T)1e-3, lo, hi);
-  const uint32_t om =
-      (disp.x == 0 || disp.y == 0 || disp.z == 0) ? 0xFFu : octants_touched(g, sp, lo, hi);
+  const uint64_t om =
+      (disp.x == 0 || disp.y == 0 || disp.z == 0) ? ~0ull : cells_touched(g, sp, lo, hi);
   const uint32_t b = g.wsp_off[sp], e = g.wsp_off[sp + 1];
   for (uint32_t k = b; k < e; k++) {
-    const uint32_t ent = g.wsp_list[k];
-    if (!(ent & om)) continue;
-    const uint32_t wi = ent >> 8;
+    if (!(g.wsp_cells[k] & om)) continue;
+    const uint32_t wi = g.wsp_list[k];
     if (wi == last_hit) continue;
     T t;
     V3<T> cp;
@@ -1097,14 +1119,13 @@ __device__ __noinline__ T exact_disk(const Geo<T>& g, V3<T> loc, V3<T> mv, int m
   int n_edges = 0;
   const uint32_t sp = subpart_of(g, loc);
   const Chem& ch = *g.chem;
-  // only walls reaching the octants within R of the collision point can occlude the disk
+  // only walls reaching the cells within R of the collision point can occlude the disk
   V3<T> blo, bhi;
   seg_box(loc, v3<T>(0, 0, 0), R * (T)1.01 + g.sp_edge * (T)1e-3, blo, bhi);
-  const uint32_t om = octants_touched(g, sp, blo, bhi);
+  const uint64_t om = cells_touched(g, sp, blo, bhi);
   for (uint32_t k = g.wsp_off[sp]; k < g.wsp_off[sp + 1]; k++) {
-    const uint32_t ent = g.wsp_list[k];
-    if (!(ent & om)) continue;
-    const uint32_t wi = ent >> 8;
+    if (!(g.wsp_cells[k] & om)) continue;
+    const uint32_t wi = g.wsp_list[k];
     const P4<T> rj = g.wrej[wi];
     V3<T> wn = v3<T>(rj.x, rj.y, rj.z);
     T l_n = dot(loc, wn);

@@ -483,6 +483,7 @@ class DeviceEngineT : public DeviceEngine {
     WallFace<T>* wface = nullptr;
     uint32_t* wsp_off = nullptr;
     uint32_t* wsp_list = nullptr;
+    uint64_t* wsp_cells = nullptr;
     uint8_t* wclass = nullptr;
     Chem* chem = nullptr;
     double* w64 = nullptr;  // fp32 engines: fp64 wall constants for the tie-breaks
@@ -607,9 +608,13 @@ class DeviceEngineT : public DeviceEngine {
       face[w].v1 = v3<T>((T)o[16], (T)o[17], (T)o[18]);
       face[w].v2 = v3<T>((T)o[19], (T)o[20], (T)o[21]);
     }
-    // wall list entries on the device: wall index << 8 | octant mask
+    // wall lists on the device: wall indices and the 4x4x4 cell mask of each entry
     std::vector<uint32_t> ent(std::max<size_t>(hs.wsp_list.size(), 1), 0);
-    for (size_t k = 0; k < hs.wsp_list.size(); k++) ent[k] = (hs.wsp_list[k] << 8) | hs.wsp_mask[k];
+    std::vector<uint64_t> cells(std::max<size_t>(hs.wsp_list.size(), 1), ~0ull);
+    for (size_t k = 0; k < hs.wsp_list.size(); k++) {
+      ent[k] = hs.wsp_list[k];
+      cells[k] = hs.wsp_cells[k];
+    }
     Chem c;
     std::memset(&c, 0, sizeof(c));
     c.nsp = (int)ch.nsp;
@@ -631,6 +636,7 @@ class DeviceEngineT : public DeviceEngine {
     R.used = true;  // from here on free_replica() releases what was allocated
     if (alloc_copy(&R.wrej, rej, R.bytes, err) || alloc_copy(&R.wface, face, R.bytes, err) ||
         alloc_copy(&R.wsp_off, hs.wsp_off, R.bytes, err) || alloc_copy(&R.wsp_list, ent, R.bytes, err) ||
+        alloc_copy(&R.wsp_cells, cells, R.bytes, err) ||
         alloc_copy(&R.wclass, wall_class.empty() ? std::vector<uint8_t>(1, 0) : wall_class, R.bytes, err) ||
         alloc_copy(&R.chem, std::vector<Chem>(1, c), R.bytes, err))
       return -2;
@@ -638,6 +644,7 @@ class DeviceEngineT : public DeviceEngine {
     g.wface = R.wface;
     g.wsp_off = R.wsp_off;
     g.wsp_list = R.wsp_list;
+    g.wsp_cells = R.wsp_cells;
     g.wall_class = R.wclass;
     g.chem = R.chem;
     g.w64 = nullptr;
@@ -678,6 +685,7 @@ class DeviceEngineT : public DeviceEngine {
     cudaFree(R.wface);
     cudaFree(R.wsp_off);
     cudaFree(R.wsp_list);
+    cudaFree(R.wsp_cells);
     cudaFree(R.wclass);
     cudaFree(R.chem);
     cudaFree(R.w64);

@@ -12,6 +12,7 @@
 // ones the reference would build.
 #include "mcg_setup.h"
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -168,8 +169,10 @@ int compute_setup(const double* origin, double partition_edge, uint32_t nsub, do
     }
   }
   Grid g{d3(origin[0], origin[1], origin[2]), hs.sp_edge, hs.sp_rcp, hs.part_edge, rxn_radius, (int)nsub};
-  std::vector<std::vector<uint32_t>> lists((size_t)nsub * nsub * nsub);
-  std::vector<std::vector<uint8_t>> masks((size_t)nsub * nsub * nsub);
+  // incidences (subpartition, wall, cell mask) in wall order; bucketed by subpartition
+  // below (a stable counting sort keeps each list in ascending wall order)
+  std::vector<uint32_t> inc_sp, inc_w;
+  std::vector<uint64_t> inc_mask;
   for (uint32_t w = 0; w < nw; w++) {
     D3 v0 = V[tris[3 * w]], v1 = V[tris[3 * w + 1]], v2 = V[tris[3 * w + 2]];
     double* o = &hs.wall[(size_t)w * 24];
@@ -231,27 +234,44 @@ int compute_setup(const double* origin, double partition_edge, uint32_t nsub, do
           D3 su = sl + e3;
           if (wall_in_box(vert, n, dist, sl - l3, su + l3)) {
             const size_t s = (size_t)x + (size_t)y * nsub + (size_t)z * nsub * nsub;
-            lists[s].push_back(w);
-            // octants of this subpartition the wall reaches (same leeway)
-            const double h = 0.5 * hs.sp_edge;
-            uint8_t mask = 0;
-            for (int o = 0; o < 8; o++) {
-              D3 ol = sl + d3((o & 1) ? h : 0.0, (o & 2) ? h : 0.0, (o & 4) ? h : 0.0);
-              D3 ou = ol + d3(h, h, h);
-              if (wall_in_box(vert, n, dist, ol - l3, ou + l3)) mask |= (uint8_t)(1u << o);
+            inc_sp.push_back((uint32_t)s);
+            inc_w.push_back(w);
+            // cells of the subpartition's 4x4x4 grid the wall reaches (same leeway); only
+            // the cells the wall's grown box overlaps are tested
+            const double q = 0.25 * hs.sp_edge;
+            int c0[3], c1[3];
+            const double lo_[3] = {llf.x, llf.y, llf.z}, hi_[3] = {urb.x, urb.y, urb.z};
+            const double sl_[3] = {sl.x, sl.y, sl.z};
+            for (int a = 0; a < 3; a++) {
+              c0[a] = std::max(0, std::min(3, (int)std::floor((lo_[a] - sl_[a]) / q)));  // llf, urb are grown
+              c1[a] = std::max(0, std::min(3, (int)std::floor((hi_[a] - sl_[a]) / q)));
             }
-            masks[s].push_back(mask ? mask : (uint8_t)0xFF);
+            // a box of at most 8 cells is taken whole (a superset; small walls), larger
+            // ones cell by cell
+            const bool exact = (c1[0] - c0[0] + 1) * (c1[1] - c0[1] + 1) * (c1[2] - c0[2] + 1) > 8;
+            uint64_t mask = 0;
+            for (int cz = c0[2]; cz <= c1[2]; cz++)
+              for (int cy = c0[1]; cy <= c1[1]; cy++)
+                for (int cx = c0[0]; cx <= c1[0]; cx++) {
+                  D3 ol = sl + d3(cx * q, cy * q, cz * q);
+                  D3 ou = ol + d3(q, q, q);
+                  if (!exact || wall_in_box(vert, n, dist, ol - l3, ou + l3)) mask |= 1ull << (cx + 4 * cy + 16 * cz);
+                }
+            inc_mask.push_back(mask ? mask : ~0ull);
           }
         }
   }
   const size_t n3 = (size_t)nsub * nsub * nsub;
   hs.wsp_off.assign(n3 + 1, 0);
-  for (size_t s = 0; s < n3; s++) hs.wsp_off[s + 1] = hs.wsp_off[s] + (uint32_t)lists[s].size();
-  hs.wsp_list.resize(hs.wsp_off[n3]);
-  hs.wsp_mask.resize(hs.wsp_off[n3]);
-  for (size_t s = 0; s < n3; s++) {
-    std::copy(lists[s].begin(), lists[s].end(), hs.wsp_list.begin() + hs.wsp_off[s]);
-    std::copy(masks[s].begin(), masks[s].end(), hs.wsp_mask.begin() + hs.wsp_off[s]);
+  for (uint32_t sp : inc_sp) hs.wsp_off[sp + 1]++;
+  for (size_t s = 0; s < n3; s++) hs.wsp_off[s + 1] += hs.wsp_off[s];
+  hs.wsp_list.resize(inc_sp.size());
+  hs.wsp_cells.resize(inc_sp.size());
+  std::vector<uint32_t> fill(hs.wsp_off.begin(), hs.wsp_off.end() - 1);
+  for (size_t k = 0; k < inc_sp.size(); k++) {
+    const uint32_t at = fill[inc_sp[k]]++;
+    hs.wsp_list[at] = inc_w[k];
+    hs.wsp_cells[at] = inc_mask[k];
   }
   if (nw >= (1u << 24)) {
     err = "more than 16,777,215 walls";

@@ -15,9 +15,9 @@ struct HostSetup {
   // v0 xyz, v1 xyz, v2 xyz, 2 spare
   std::vector<double> wall;
   std::vector<uint32_t> wsp_off, wsp_list;  // walls per subpartition, ascending
-  // per list entry: octants of the subpartition (bit o = x + 2y + 4z halves) whose box,
-  // grown by the same leeway as the subpartition's, the wall intersects
-  std::vector<uint8_t> wsp_mask;
+  // per list entry: cells of the subpartition's 4x4x4 grid (bit x + 4y + 16z quarters)
+  // whose box, grown by the same leeway as the subpartition's, the wall intersects
+  std::vector<uint64_t> wsp_cells;
 };
 
 int compute_setup(const double* origin, double partition_edge, uint32_t nsub, double rxn_radius, uint32_t nv,
