@@ -128,6 +128,7 @@ struct Geo {
   T part_edge, sp_edge, sp_rcp, R;
   int nsub, nsub2, nsp;
   uint32_t n3;                // subpartitions (nsub^3)
+  float rcp_n, rcp_n2;        // 1 / nsub, 1 / nsub^2 (index decoding without integer division)
   uint32_t oct_shift;         // 3: occupants binned per subpartition octant, 0: per subpartition
   uint32_t kbase;             // first sort key of the replica; keys are (species, subpartition, octant)
   uint32_t rep;               // replica index
@@ -263,6 +264,35 @@ template <typename T>
 __device__ __forceinline__ uint32_t sub_of3(const Geo<T>& g, int x, int y, int z) {
   return (uint32_t)(x + y * g.nsub + z * g.nsub2);
 }
+// subpartition index -> grid coordinates without integer division: float reciprocals
+// and a +-1 correction (indices are below 300^3 < 2^25, so the estimate is off by at
+// most one)
+template <typename T>
+__device__ __forceinline__ void decode_sp(const Geo<T>& g, uint32_t sp, int& x, int& y, int& z) {
+  const int n = g.nsub, n2 = g.nsub2;
+  int zz = (int)((float)sp * g.rcp_n2);
+  int r = (int)sp - zz * n2;
+  if (r < 0) {
+    zz--;
+    r += n2;
+  } else if (r >= n2) {
+    zz++;
+    r -= n2;
+  }
+  int yy = (int)((float)r * g.rcp_n);
+  int xx = r - yy * n;
+  if (xx < 0) {
+    yy--;
+    xx += n;
+  } else if (xx >= n) {
+    yy++;
+    xx -= n;
+  }
+  x = xx;
+  y = yy;
+  z = zz;
+}
+
 template <typename T>
 __device__ __forceinline__ uint32_t subpart_of(const Geo<T>& g, V3<T> p) {
   int x, y, z;
@@ -273,7 +303,8 @@ __device__ __forceinline__ uint32_t subpart_of(const Geo<T>& g, V3<T> p) {
 // [lo, hi] overlaps
 template <typename T>
 __device__ __forceinline__ uint32_t octants_touched(const Geo<T>& g, uint32_t sp, V3<T> lo, V3<T> hi) {
-  const int ix = (int)(sp % g.nsub), iy = (int)((sp / g.nsub) % g.nsub), iz = (int)(sp / g.nsub2);
+  int ix, iy, iz;
+  decode_sp(g, sp, ix, iy, iz);
   const T h = g.sp_edge * (T)0.5;
   const V3<T> mid = g.origin + cmul(v3<T>((T)ix, (T)iy, (T)iz), v3<T>(g.sp_edge, g.sp_edge, g.sp_edge)) +
                     v3<T>(h, h, h);
@@ -291,7 +322,8 @@ __device__ __forceinline__ uint32_t octants_touched(const Geo<T>& g, uint32_t sp
 // touches; the outer faces are not tested (the box may reach past the subpartition)
 template <typename T>
 __device__ __forceinline__ uint64_t cells_touched(const Geo<T>& g, uint32_t sp, V3<T> lo, V3<T> hi) {
-  const int ix = (int)(sp % g.nsub), iy = (int)((sp / g.nsub) % g.nsub), iz = (int)(sp / g.nsub2);
+  int ix, iy, iz;
+  decode_sp(g, sp, ix, iy, iz);
   const T q = g.sp_edge * (T)0.25;
   const V3<T> o = g.origin + cmul(v3<T>((T)ix, (T)iy, (T)iz), v3<T>(g.sp_edge, g.sp_edge, g.sp_edge));
   auto axis = [q](T l, T h, T base) -> uint32_t {
@@ -380,9 +412,7 @@ struct Walk {
     dx = nz.x > 0;
     dy = nz.y > 0;
     dz = nz.z > 0;
-    cx = (int)(start_sp % g.nsub);
-    cy = (int)((start_sp / g.nsub) % g.nsub);
-    cz = (int)((start_sp / g.nsub2) % g.nsub);
+    decode_sp(g, start_sp, cx, cy, cz);
     int ex, ey, ez;
     sub3(g, dest_p, ex, ey, ez);
     dest = sub_of3(g, ex, ey, ez);
@@ -513,7 +543,8 @@ __device__ void collect_neighbors(const Geo<T>& g, V3<T> pos, int ix, int iy, in
 template <typename T, class Set>
 __device__ void collect_for_molecules(const Geo<T>& g, V3<T> pos, uint32_t sp, V3<T> disp, Set& st) {
   const T rn = g.R * (T)1.41421356238;  // POS_SQRT2
-  int sx = (int)(sp % g.nsub), sy = (int)((sp / g.nsub) % g.nsub), sz = (int)((sp / g.nsub2) % g.nsub);
+  int sx, sy, sz;
+  decode_sp(g, sp, sx, sy, sz);
   st.insert3(g, sx, sy, sz);
   collect_neighbors(g, pos, sx, sy, sz, rn, st);
   Walk<T> w;

@@ -578,6 +578,8 @@ class DeviceEngineT : public DeviceEngine {
     g.nsub2 = (int)(hs.nsub * hs.nsub);
     g.nsp = (int)nsp_;
     g.n3 = hs.nsub * hs.nsub * hs.nsub;
+    g.rcp_n = 1.0f / (float)hs.nsub;
+    g.rcp_n2 = 1.0f / (float)(hs.nsub * hs.nsub);
     const uint64_t base_keys = (uint64_t)g.n3 * nsp_;
     // occupants are binned per subpartition octant while the key space stays small
     g.oct_shift = (sp.octants && base_keys * 8 <= (1ull << 26)) ? 3 : 0;
