@@ -266,6 +266,35 @@ int mcg_serve_cancel(mcg_server* s, uint64_t ticket);
 int mcg_serve_release(mcg_server* s, uint64_t ticket);
 int mcg_serve_get_stats(mcg_server* s, mcg_serve_stats* out);
 
+/* ---- Checkpoints (the device side of ChkptVolMol, libmcell/api/model.cpp:591-650).
+   A checkpoint is the live molecules — position, species, id, unimolecular time
+   relative to the next iteration (1e20 = none), flags (bit 0: the unimolecular time
+   is not drawn yet) — and the iteration counter. With the same model definition and
+   seed, a run continued from it repeats the uninterrupted run (the random streams
+   are counter based: seed, molecule id, iteration). mcg_export_state: call with
+   cap = 0 for the count, then with arrays of that size. mcg_import_state: on a
+   handle that has no molecules and has not run an iteration; it prepares the
+   engine. */
+int mcg_export_state(mcg_engine* e, uint64_t cap, double* pos, uint32_t* species, uint64_t* ids,
+                     double* unimol_time, uint8_t* flags, uint64_t* n_out, uint64_t* iteration);
+int mcg_import_state(mcg_engine* e, uint64_t n, const double* pos, const uint32_t* species, const uint64_t* ids,
+                     const double* unimol_time, const uint8_t* flags, uint64_t iteration);
+
+/* ---- Visualisation output from device state (VizOutputEvent,
+   src4/viz_output_event.cpp:48-279): writes
+   "<prefix>.ascii.<iteration>.dat" (lines "name id x y z nx ny nz") or
+   "<prefix>.cellbin.<iteration>.dat" (CellBlender binary, version 1 or 2), with
+   positions in um (internal units x length_unit_um) and the iteration zero-padded
+   to the digits of total_iterations. species_names: n_species strings. */
+#define MCG_VIZ_ASCII 0
+#define MCG_VIZ_CELLBLENDER_V1 1
+#define MCG_VIZ_CELLBLENDER_V2 2
+int mcg_write_viz(mcg_engine* e, const char* prefix, int mode, const char* const* species_names, uint64_t iteration,
+                  uint64_t total_iterations, double length_unit_um);
+int mcg_batch_write_viz(mcg_batch* b, uint32_t replica, const char* prefix, int mode,
+                        const char* const* species_names, uint64_t iteration, uint64_t total_iterations,
+                        double length_unit_um);
+
 /* Setup queries for parity tests: wall constants (14 doubles per wall, same
    layout as the oracle) and the wall lists per subpartition. */
 int mcg_wall_consts(mcg_engine* e, double* out);

@@ -33,6 +33,7 @@ EXPORTS = [
     "mcg_autotune_subparts", "mcg_batch_get_escapes",
     "mcg_serve_create", "mcg_serve_destroy", "mcg_serve_last_error", "mcg_serve_submit", "mcg_serve_poll",
     "mcg_serve_wait", "mcg_serve_result", "mcg_serve_cancel", "mcg_serve_release", "mcg_serve_get_stats",
+    "mcg_export_state", "mcg_import_state", "mcg_write_viz", "mcg_batch_write_viz",
 ]
 
 
@@ -259,6 +260,36 @@ class Engine:
                                         ctypes.c_uint32(draws.shape[1]), _p(rrf), _p(tst), _p(out)))
         return out
 
+    def export_state(self):
+        """Checkpoint: dict of pos, species, ids, unimol_time, flags and the iteration."""
+        n = ctypes.c_uint64()
+        it = ctypes.c_uint64()
+        self._chk(lib().mcg_export_state(self.h, ctypes.c_uint64(0), None, None, None, None, None, ctypes.byref(n),
+                                         ctypes.byref(it)))
+        m = n.value
+        st = {"pos": np.zeros((m, 3)), "species": np.zeros(m, np.uint32), "ids": np.zeros(m, np.uint64),
+              "unimol_time": np.zeros(m), "flags": np.zeros(m, np.uint8)}
+        self._chk(lib().mcg_export_state(self.h, ctypes.c_uint64(m), _p(st["pos"]), _p(st["species"]), _p(st["ids"]),
+                                         _p(st["unimol_time"]), _p(st["flags"]), ctypes.byref(n), ctypes.byref(it)))
+        st["iteration"] = it.value
+        return st
+
+    def import_state(self, st):
+        pos = np.ascontiguousarray(st["pos"], np.float64)
+        sp = np.ascontiguousarray(st["species"], np.uint32)
+        ids = np.ascontiguousarray(st["ids"], np.uint64)
+        tu = np.ascontiguousarray(st["unimol_time"], np.float64)
+        fl = np.ascontiguousarray(st["flags"], np.uint8)
+        self._chk(lib().mcg_import_state(self.h, ctypes.c_uint64(len(sp)), _p(pos), _p(sp), _p(ids), _p(tu), _p(fl),
+                                         ctypes.c_uint64(int(st["iteration"]))))
+
+    def write_viz(self, prefix, species_names, iteration, total_iterations, mode="ascii", length_unit_um=0.01):
+        modes = {"ascii": 0, "cellblender_v1": 1, "cellblender_v2": 2}
+        names = (ctypes.c_char_p * len(species_names))(*[n.encode() for n in species_names])
+        self._chk(lib().mcg_write_viz(self.h, str(prefix).encode(), ctypes.c_int(modes[mode]), names,
+                                      ctypes.c_uint64(iteration), ctypes.c_uint64(total_iterations),
+                                      ctypes.c_double(length_unit_um)))
+
     def autotune_subparts(self):
         """The batch autotuner's (subpartitions per edge, octant bins) for this model."""
         n = ctypes.c_uint32()
@@ -394,6 +425,13 @@ class Batch:
         b = ctypes.c_uint64()
         self._chk(lib().mcg_batch_get_memory(self.h, ctypes.byref(b)))
         return b.value
+
+    def write_viz(self, rep, prefix, species_names, iteration, total_iterations, mode="ascii", length_unit_um=0.01):
+        modes = {"ascii": 0, "cellblender_v1": 1, "cellblender_v2": 2}
+        names = (ctypes.c_char_p * len(species_names))(*[n.encode() for n in species_names])
+        self._chk(lib().mcg_batch_write_viz(self.h, ctypes.c_uint32(rep), str(prefix).encode(),
+                                            ctypes.c_int(modes[mode]), names, ctypes.c_uint64(iteration),
+                                            ctypes.c_uint64(total_iterations), ctypes.c_double(length_unit_um)))
 
     def escapes(self):
         """Molecules that left their partition: rows of uid, species + 1000 * kind, iteration, start xyz,

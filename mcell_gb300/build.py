@@ -7,6 +7,7 @@ Translation units are compiled in parallel:
   mcg_api.cpp   C ABI (single models)
   mcg_batch.cpp C ABI of batches (replicas) and the batch autotuner
   mcg_serve.cpp C ABI of the serving loop (continuous batching on a worker thread)
+  mcg_viz.cpp   visualisation files (ASCII / CellBlender) from device state
   mcg_trace_static.cu  fixed device scratch of mcg_trace_cases_static
 Usage: python -m mcell_gb300.build [--force] [-v]
 """
@@ -46,6 +47,7 @@ def _units():
         ("mcg_api.cpp", ["-x", "c++"] + host),
         ("mcg_batch.cpp", ["-x", "c++"] + host),
         ("mcg_serve.cpp", ["-x", "c++"] + host),
+        ("mcg_viz.cpp", ["-x", "c++"] + host),
     ]
 
 

@@ -294,6 +294,31 @@ int mcg_trace_cases_static(mcg_engine* e, uint32_t n, const uint64_t* ids, const
   return rc ? fail(e, rc, err) : MCG_OK;
 }
 
+int mcg_export_state(mcg_engine* e, uint64_t cap, double* pos, uint32_t* species, uint64_t* ids, double* tuni,
+                     uint8_t* flags, uint64_t* n_out, uint64_t* iteration) {
+  if (!e || !n_out || !iteration || (cap && (!pos || !species || !ids || !tuni || !flags))) return MCG_ERR_ARG;
+  int rc = prepare(e);
+  if (rc) return rc;
+  std::string err;
+  rc = e->dev->export_state(0, cap, pos, species, ids, tuni, flags, n_out, iteration, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
+int mcg_import_state(mcg_engine* e, uint64_t n, const double* pos, const uint32_t* species, const uint64_t* ids,
+                     const double* tuni, const uint8_t* flags, uint64_t iteration) {
+  if (!e || (n && (!pos || !species || !ids || !tuni || !flags))) return MCG_ERR_ARG;
+  if (!e->pend_species.empty()) return fail(e, MCG_ERR_ARG, "mcg_import_state: the handle already has molecules");
+  for (uint64_t i = 0; i < n; i++)
+    if (species[i] >= e->cfg.n_species) return fail(e, MCG_ERR_ARG, "species index out of range");
+  int rc = prepare(e);
+  if (rc) return rc;
+  std::string err;
+  rc = e->dev->import_state(0, n, pos, species, ids, tuni, flags, iteration, err);
+  if (rc) return fail(e, rc, err);
+  for (uint64_t i = 0; i < n; i++) e->next_uid = std::max<uint64_t>(e->next_uid, ids[i] + 1);
+  return MCG_OK;
+}
+
 int mcg_wall_consts(mcg_engine* e, double* out) {
   if (!e || !out) return MCG_ERR_ARG;
   mcg::HostSetup hs;

@@ -198,7 +198,7 @@ class DeviceEngineT : public DeviceEngine {
       return -1;
     }
     const Geo<T>& g = geos_h_[rep];
-    if (cnt_.iteration > g.it0) {
+    if (cnt_.iteration > g.it0 && cnt_.iteration > rebin_it_) {
       // species counts of the last finished iteration (k_end)
       const uint64_t row = (cnt_.iteration - 1) % traj_cap_;
       std::vector<unsigned long long> h(nsp_);
@@ -276,6 +276,61 @@ class DeviceEngineT : public DeviceEngine {
       if (ids) ids[i] = u[i];
     }
     return 0;
+  }
+
+  int export_state(uint32_t rep, uint64_t capn, double* pos, uint32_t* species, uint64_t* ids, double* tuni,
+                   uint8_t* flags, uint64_t* n_out, uint64_t* iteration, std::string& err) override {
+    int rc = download(rep, capn, pos, species, ids, n_out, err);
+    if (rc) return rc;
+    *iteration = cnt_.iteration - geos_h_[rep].it0;
+    const uint64_t n = std::min<uint64_t>(*n_out, capn);
+    if (n == 0 || (!tuni && !flags)) return 0;
+    const Geo<T>& g = geos_h_[rep];
+    State<T> s = state(parity_);
+    uint32_t lo = 0;
+    MCG_CUDA(d2h(&lo, s.start + g.kbase, sizeof(uint32_t)));
+    std::vector<P4<T>> p(n);
+    std::vector<T> t(n);
+    MCG_CUDA(d2h(p.data(), s.a_pos + lo, sizeof(P4<T>) * n));
+    MCG_CUDA(d2h(t.data(), s.a_tuni + lo, sizeof(T) * n));
+    for (uint64_t i = 0; i < n; i++) {
+      if (tuni) tuni[i] = (double)t[i];
+      if (flags) flags[i] = (host_meta(p[i]) & META_SCHEDULE_UNIMOL) ? 1 : 0;
+    }
+    return 0;
+  }
+
+  int import_state(uint32_t rep, uint64_t n, const double* pos, const uint32_t* species, const uint64_t* ids,
+                   const double* tuni, const uint8_t* flags, uint64_t iteration, std::string& err) override {
+    if (rep >= max_rep_ || !reps_[rep].used) {
+      err = "no such replica";
+      return -1;
+    }
+    if (read_counters(err)) return -2;
+    if (iterations_ != 0 || cnt_.n_live != 0 || iteration > 0xFFFFFFF0ull) {
+      err = "a checkpoint is loaded into a prepared engine before any molecule or iteration";
+      return -1;
+    }
+    std::vector<Product<T>> stage(n);
+    int rc = stage_molecules(rep, n, pos, species, 0, stage.data(), err);
+    if (rc) return rc;
+    for (uint64_t i = 0; i < n; i++) {
+      stage[i].uid = ids[i];
+      stage[i].tuni = tuni[i];
+      put_meta(stage[i].pos, make_meta(species[i], rep, (flags[i] & 1) ? META_SCHEDULE_UNIMOL : 0));
+      reps_[rep].next_uid = std::max<uint64_t>(reps_[rep].next_uid, ids[i] + 1);
+    }
+    // the engine continues at the checkpoint's iteration: the replica's random streams
+    // (seed, molecule id, iteration) pick up where they stopped
+    Counters c = cnt_;
+    c.iteration = (uint32_t)iteration;
+    MCG_CUDA(cudaMemcpyAsync(d_cnt_, &c, sizeof(Counters), cudaMemcpyHostToDevice, stream_));
+    cnt_ = c;
+    geos_h_[rep].it0 = 0;
+    MCG_CUDA(cudaMemcpyAsync(d_geos_, geos_h_.data(), sizeof(Geo<T>) * max_rep_, cudaMemcpyHostToDevice, stream_));
+    rc = rebin(stage.data(), n, err);
+    rebin_it_ = cnt_.iteration;
+    return rc;
   }
 
   int replica_iterations(uint32_t rep, uint64_t* done, std::string& err) override {
@@ -820,6 +875,7 @@ class DeviceEngineT : public DeviceEngine {
     MCG_CUDA(cudaMemcpyAsync(d_cnt_, &c2, sizeof(Counters), cudaMemcpyHostToDevice, stream_));
     parity_ ^= 1;  // the re-binned arrays became the current ones
     cnt_ = c2;
+    rebin_it_ = cnt_.iteration;
     invalidate_graphs();
     return status_to_error(c2.status, err);
   }
@@ -1026,6 +1082,7 @@ class DeviceEngineT : public DeviceEngine {
   cudaGraphExec_t graph_[2] = {nullptr, nullptr};
   uint32_t nsp_ = 0, max_rep_ = 0, nkeys_ = 0, key_alloc_ = 0, ntiles_ = 0, traj_cap_ = 65536;
   uint64_t cap_ = 0, iterations_ = 0, launches_ = 0;
+  uint64_t rebin_it_ = 0;  // engine iteration of the last re-sort (counts then come from the starts)
   Counters cnt_{};
   std::vector<Rep> reps_;
   std::vector<Geo<T>> geos_h_;

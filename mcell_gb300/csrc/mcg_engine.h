@@ -63,6 +63,12 @@ class DeviceEngine {
   virtual int trajectory(uint32_t rep, uint32_t n, uint64_t* out, std::string& err) = 0;
   virtual int download(uint32_t rep, uint64_t cap, double* pos, uint32_t* species, uint64_t* ids, uint64_t* n_out,
                        std::string& err) = 0;
+  // checkpoints: molecules with ids, unimolecular times (relative to the next
+  // iteration) and flags (bit 0: time not drawn yet), and the replica's iteration
+  virtual int export_state(uint32_t rep, uint64_t cap, double* pos, uint32_t* species, uint64_t* ids, double* tuni,
+                           uint8_t* flags, uint64_t* n_out, uint64_t* iteration, std::string& err) = 0;
+  virtual int import_state(uint32_t rep, uint64_t n, const double* pos, const uint32_t* species, const uint64_t* ids,
+                           const double* tuni, const uint8_t* flags, uint64_t iteration, std::string& err) = 0;
   // iterations the replica has run (it freezes after its n_iterations)
   virtual int replica_iterations(uint32_t rep, uint64_t* done, std::string& err) = 0;
   // device bytes held for the replica (mesh, grid, its share of the molecule arrays)

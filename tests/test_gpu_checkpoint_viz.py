@@ -1,0 +1,80 @@
+"""Checkpoints and visualisation files from device state.
+
+A run restored from a checkpoint must repeat the uninterrupted run: the same count
+trajectory and, at the end, the same molecules (ids, species, positions bit for bit),
+since the random streams are counter based (seed, molecule id, iteration). Viz files
+must hold exactly the downloaded molecules in the reference's formats."""
+import struct
+
+import numpy as np
+import pytest
+
+from mcell_gb300 import checkpoint
+from mcell_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+NAMES = ["A", "B", "C"]
+
+
+def _by_id(pos, sp, ids):
+    o = np.argsort(ids)
+    return pos[o], sp[o], ids[o]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_checkpoint_continues_the_run(tmp_path, precision):
+    m = W.replica_models(1, seed=41, n_range=(6_000, 6_001), edge_range_um=(0.8, 0.8), k_range=(1e8, 1e8),
+                         sphere_fraction=1.0, levels=(3, 3))[0]
+    full = W.engine_for(m, precision, seed=9)
+    full.step(40)
+    want = full.trajectory(40)
+    wp, ws, wi = _by_id(*full.molecules())
+    first = W.engine_for(m, precision, seed=9)
+    first.step(20)
+    st = checkpoint.save(first, tmp_path / "ck.npz")
+    assert st["iteration"] == 20 and (st["flags"] <= 1).all()
+    assert (st["unimol_time"] < 1e19).any() or want[-1, 2] == 0  # products carry drawn unimolecular times
+    second = W.model_handle(m, precision, seed=9, with_molecules=False)
+    checkpoint.load(second, tmp_path / "ck.npz")
+    assert np.array_equal(second.counts(), want[19])
+    second.step(20)
+    assert np.array_equal(second.trajectory(20), want[20:])
+    gp, gs, gi = _by_id(*second.molecules())
+    assert np.array_equal(gi, wi) and np.array_equal(gs, ws) and np.array_equal(gp, wp)
+
+
+def test_viz_files_hold_the_molecules(tmp_path):
+    m = W.closed_cube(n_per_species=1000, seed=3)
+    e = W.engine_for(m, "fp32", seed=2)
+    e.step(5)
+    pos, sp, ids = e.molecules()
+    prefix = tmp_path / "viz_data" / "seed_00001" / "Scene"
+    e.write_viz(prefix, NAMES, 5, 1000, mode="ascii")
+    rows = (tmp_path / "viz_data" / "seed_00001" / "Scene.ascii.0005.dat").read_text().split("\n")[:-1]
+    assert len(rows) == len(ids)
+    got = {int(r.split()[1]): (r.split()[0], np.array([float(x) for x in r.split()[2:5]])) for r in rows}
+    for k in range(0, len(ids), 97):
+        name, xyz = got[int(ids[k])]
+        assert name == NAMES[sp[k]] and np.allclose(xyz, pos[k] * 0.01, rtol=1e-8, atol=0)
+    e.write_viz(prefix, NAMES, 5, 1000, mode="cellblender_v2")
+    b = (tmp_path / "viz_data" / "seed_00001" / "Scene.cellbin.0005.dat").read_bytes()
+    assert struct.unpack_from("<I", b, 0)[0] == 2
+    off, seen = 4, 0
+    while off < len(b):
+        (ln,) = struct.unpack_from("<I", b, off)
+        name = b[off + 4:off + 4 + ln].decode()
+        off += 4 + ln
+        assert b[off] == 0
+        (cnt,) = struct.unpack_from("<I", b, off + 1)
+        off += 5
+        fid = np.frombuffer(b, np.uint32, cnt, off)
+        off += 4 * cnt
+        xyz = np.frombuffer(b, np.float32, 3 * cnt, off).reshape(cnt, 3)
+        off += 12 * cnt
+        a = NAMES.index(name)
+        sel = sp == a
+        assert sorted(fid.tolist()) == sorted(ids[sel].astype(np.uint32).tolist())
+        assert np.allclose(np.sort(xyz[:, 0]), np.sort((pos[sel, 0] * 0.01).astype(np.float32)))
+        seen += cnt
+    assert seen == len(ids)
