@@ -266,6 +266,26 @@ int mcg_serve_cancel(mcg_server* s, uint64_t ticket);
 int mcg_serve_release(mcg_server* s, uint64_t ticket);
 int mcg_serve_get_stats(mcg_server* s, mcg_serve_stats* out);
 
+/* ---- Volume releases generated on the device (ReleaseEvent::
+   release_ellipsoid_or_rectcuboid and release_inside_regions,
+   src4/release_event.cpp:904-1006): n molecules of a species, uniform in an
+   ellipsoid, a cuboid or on an ellipsoid shell (center and diameter, internal
+   units), or inside a closed geometry object (rejection in the object's bounding
+   box with the reference's ray-parity inside test). The random numbers come from
+   the counter-based generator keyed by release_seed, so positions are not the
+   reference's; their distribution is. Molecule ids continue the model's. The
+   region must lie inside the partition. Walls are assigned to objects with
+   mcg_set_wall_objects (before the first step). */
+#define MCG_RELEASE_SPHERE 0
+#define MCG_RELEASE_CUBOID 1
+#define MCG_RELEASE_SHELL 2
+#define MCG_RELEASE_INSIDE_OBJECT 3
+int mcg_set_wall_objects(mcg_engine* e, uint32_t n_walls, const uint16_t* object_of_wall);
+int mcg_release(mcg_engine* e, uint32_t species, uint64_t n, int shape, const double* center, const double* diameter,
+                uint32_t object, uint64_t release_seed);
+int mcg_batch_release(mcg_batch* b, uint32_t replica, uint32_t species, uint64_t n, int shape, const double* center,
+                      const double* diameter, uint32_t object, uint64_t release_seed);
+
 /* ---- Checkpoints (the device side of ChkptVolMol, libmcell/api/model.cpp:591-650).
    A checkpoint is the live molecules — position, species, id, unimolecular time
    relative to the next iteration (1e20 = none), flags (bit 0: the unimolecular time

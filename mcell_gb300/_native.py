@@ -34,6 +34,7 @@ EXPORTS = [
     "mcg_serve_create", "mcg_serve_destroy", "mcg_serve_last_error", "mcg_serve_submit", "mcg_serve_poll",
     "mcg_serve_wait", "mcg_serve_result", "mcg_serve_cancel", "mcg_serve_release", "mcg_serve_get_stats",
     "mcg_export_state", "mcg_import_state", "mcg_write_viz", "mcg_batch_write_viz",
+    "mcg_set_wall_objects", "mcg_release", "mcg_batch_release",
 ]
 
 
@@ -259,6 +260,17 @@ class Engine:
         self._chk(lib().mcg_trace_cases(self.h, ctypes.c_uint32(n), _p(ids), _p(disp), _p(draws),
                                         ctypes.c_uint32(draws.shape[1]), _p(rrf), _p(tst), _p(out)))
         return out
+
+    def set_wall_objects(self, object_of_wall):
+        o = np.ascontiguousarray(object_of_wall, np.uint16)
+        self._chk(lib().mcg_set_wall_objects(self.h, ctypes.c_uint32(len(o)), _p(o)))
+
+    def release(self, species, n, shape="sphere", center=(0, 0, 0), diameter=(1, 1, 1), obj=0, seed=1):
+        shapes = {"sphere": 0, "cuboid": 1, "shell": 2, "inside": 3}
+        c = np.ascontiguousarray(center, np.float64)
+        d = np.ascontiguousarray(diameter, np.float64)
+        self._chk(lib().mcg_release(self.h, ctypes.c_uint32(species), ctypes.c_uint64(n), ctypes.c_int(shapes[shape]),
+                                    _p(c), _p(d), ctypes.c_uint32(obj), ctypes.c_uint64(seed)))
 
     def export_state(self):
         """Checkpoint: dict of pos, species, ids, unimol_time, flags and the iteration."""

@@ -54,6 +54,7 @@ static int prepare(mcg_engine* e) {
   sp.hs = &hs;
   sp.chem = &e->chem;
   sp.wall_class = &e->wclass;
+  sp.wall_obj = e->wall_obj.empty() ? nullptr : &e->wall_obj;
   sp.seed = e->cfg.seed;
   sp.n_mol = e->pend_species.size();
   sp.pos = e->pend_pos.data();
@@ -292,6 +293,28 @@ int mcg_trace_cases_static(mcg_engine* e, uint32_t n, const uint64_t* ids, const
   std::string err;
   int rc = e->dev->trace_static(n, ids, disp, draws, draws_per_case, rrf, tst, out, err);
   return rc ? fail(e, rc, err) : MCG_OK;
+}
+
+int mcg_set_wall_objects(mcg_engine* e, uint32_t n_walls, const uint16_t* object_of_wall) {
+  if (!e || (n_walls && !object_of_wall)) return MCG_ERR_ARG;
+  if (e->dev) return fail(e, MCG_ERR_ARG, "wall objects must be set before the first step");
+  if (n_walls != e->walls.size() / 3) return fail(e, MCG_ERR_ARG, "wall count differs from the uploaded mesh");
+  e->wall_obj.assign(object_of_wall, object_of_wall + n_walls);
+  return MCG_OK;
+}
+
+int mcg_release(mcg_engine* e, uint32_t species, uint64_t n, int shape, const double* center,
+                const double* diameter, uint32_t object, uint64_t release_seed) {
+  if (!e || (shape != MCG_RELEASE_INSIDE_OBJECT && (!center || !diameter))) return MCG_ERR_ARG;
+  if (!e->pend_species.empty() || !e->dev) {
+    int rc = prepare(e);  // pending host molecules are uploaded first
+    if (rc) return rc;
+  }
+  std::string err;
+  int rc = e->dev->release(0, species, n, shape, center, diameter, object, release_seed, err);
+  if (rc) return fail(e, rc, err);
+  e->next_uid += n;
+  return MCG_OK;
 }
 
 int mcg_export_state(mcg_engine* e, uint64_t cap, double* pos, uint32_t* species, uint64_t* ids, double* tuni,

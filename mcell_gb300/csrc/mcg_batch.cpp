@@ -222,6 +222,7 @@ int mcg_batch_add(mcg_batch* b, uint32_t n, mcg_engine* const* models, const uin
     sp.hs = &hs[k];
     sp.chem = &m->chem;
     sp.wall_class = &m->wclass;
+    sp.wall_obj = m->wall_obj.empty() ? nullptr : &m->wall_obj;
     sp.seed = m->cfg.seed;
     sp.n_mol = m->pend_species.size();
     sp.pos = m->pend_pos.data();
@@ -332,6 +333,15 @@ int mcg_batch_get_memory(mcg_batch* b, uint64_t* bytes) {
   if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
   *bytes = b->dev->device_bytes();
   return MCG_OK;
+}
+
+int mcg_batch_release(mcg_batch* b, uint32_t replica, uint32_t species, uint64_t n, int shape, const double* center,
+                      const double* diameter, uint32_t object, uint64_t release_seed) {
+  if (!b || (shape != MCG_RELEASE_INSIDE_OBJECT && (!center || !diameter))) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  std::string err;
+  int rc = b->dev->release(replica, species, n, shape, center, diameter, object, release_seed, err);
+  return rc ? bfail(b, rc, err) : MCG_OK;
 }
 
 int mcg_batch_get_escapes(mcg_batch* b, uint32_t cap, double* out, uint32_t* n) {

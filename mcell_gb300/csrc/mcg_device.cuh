@@ -146,6 +146,7 @@ struct Geo {
   // fp32 engines: the wall constants in fp64 for the tie-breaks, 16 per wall (normal
   // xyz, d, unit_u xyz, unit_v xyz, v0 xyz, uv_vert1_u, uv_vert2 u v); null in fp64
   const double* w64;
+  const uint16_t* wall_obj;   // geometry object of each wall (releases inside objects), or null
 };
 
 // molecules at the start of the iteration, sorted by key (replica, species, subpartition, octant)
@@ -830,6 +831,85 @@ restart:
     }
   }
   return found;
+}
+
+// ------------------------------------------------------------------ inside a closed object
+
+// wall constants in fp64 (the fp64 engine's own, the fp32 engine's tie-break copy)
+template <typename T>
+__device__ __forceinline__ void wall_fp64(const Geo<T>& g, uint32_t wi, double* c) {
+  if (sizeof(T) == 4) {
+    for (int k = 0; k < 16; k++) c[k] = g.w64[16 * (size_t)wi + k];
+  } else {
+    const P4<T> r = g.wrej[wi];
+    const WallFace<T> f = g.wface[wi];
+    const double q[16] = {(double)r.x,    (double)r.y,    (double)r.z,    (double)r.w,    (double)f.u.x, (double)f.u.y,
+                          (double)f.u.z,  (double)f.v.x,  (double)f.v.y,  (double)f.v.z,  (double)f.v0.x, (double)f.v0.y,
+                          (double)f.v0.z, (double)f.uv1u, (double)f.uv2u, (double)f.uv2v};
+    for (int k = 0; k < 16; k++) c[k] = q[k];
+  }
+}
+
+// Is p inside closed object `obj`? The reference's test
+// (compute_counted_volume_for_pos, collision_utils.inl:1515-1545): a ray from p to
+// the partition's origin corner moved by (edge/11, edge/21, 0) subpartition edges,
+// an odd number of crossed walls of the object means inside. The ray walks the
+// subpartition grid; a wall listed in several subpartitions counts once, in the
+// subpartition that holds its crossing point. fp64 throughout.
+template <typename T>
+__device__ bool inside_object(const Geo<T>& g, V3<double> p, uint32_t obj) {
+  const double e = (double)g.sp_edge;
+  const V3<double> o = v3<double>((double)g.origin.x, (double)g.origin.y, (double)g.origin.z);
+  const V3<double> dst = v3<double>(o.x + e / 11.0, o.y + e / 21.0, o.z);
+  const V3<double> d = dst - p;
+  const double rcp = (double)g.sp_rcp;
+  auto cell = [&](double v, double ov) {
+    int c = (int)floor((v - ov) * rcp);
+    return c < 0 ? 0 : (c >= g.nsub ? g.nsub - 1 : c);
+  };
+  int cx = cell(p.x, o.x), cy = cell(p.y, o.y), cz = cell(p.z, o.z);
+  const int ex = cell(dst.x, o.x), ey = cell(dst.y, o.y), ez = cell(dst.z, o.z);
+  uint32_t crossed = 0;
+  for (int guard = 0; guard < 3 * g.nsub + 3; guard++) {
+    const uint32_t sp = (uint32_t)cx + (uint32_t)cy * g.nsub + (uint32_t)cz * g.nsub2;
+    for (uint32_t k = g.wsp_off[sp]; k < g.wsp_off[sp + 1]; k++) {
+      const uint32_t wi = g.wsp_list[k];
+      if (g.wall_obj[wi] != obj) continue;
+      double c[16];
+      wall_fp64(g, wi, c);
+      const double a = c[0] * p.x + c[1] * p.y + c[2] * p.z - c[3];
+      const double b = c[0] * dst.x + c[1] * dst.y + c[2] * dst.z - c[3];
+      if ((a > 0 && b > 0) || (a < 0 && b < 0) || a == b) continue;
+      const double t = a / (a - b);
+      const V3<double> x = p + scale(d, t);
+      if (cell(x.x, o.x) != cx || cell(x.y, o.y) != cy || cell(x.z, o.z) != cz) continue;
+      const double lx = x.x - c[10], ly = x.y - c[11], lz = x.z - c[12];
+      const int tr = tri_test<double>(lx * c[4] + ly * c[5] + lz * c[6], lx * c[7] + ly * c[8] + lz * c[9], c[13], c[14],
+                                      c[15], Eps<double>::pos);
+      if (tr != TRI_OUT) crossed++;
+    }
+    if (cx == ex && cy == ey && cz == ez) break;
+    // next cell along the ray: the axis whose cell boundary comes first
+    double tb[3];
+    const double pv[3] = {p.x, p.y, p.z}, dv[3] = {d.x, d.y, d.z}, ov[3] = {o.x, o.y, o.z};
+    const int cv[3] = {cx, cy, cz};
+    for (int k = 0; k < 3; k++) {
+      if (dv[k] == 0) {
+        tb[k] = 1e300;
+        continue;
+      }
+      const double bnd = ov[k] + e * (double)(cv[k] + (dv[k] > 0 ? 1 : 0));
+      tb[k] = (bnd - pv[k]) / dv[k];
+    }
+    if (tb[0] <= tb[1] && tb[0] <= tb[2])
+      cx += d.x > 0 ? 1 : -1;
+    else if (tb[1] <= tb[2])
+      cy += d.y > 0 ? 1 : -1;
+    else
+      cz += d.z > 0 ? 1 : -1;
+    if (cx < 0 || cy < 0 || cz < 0 || cx >= g.nsub || cy >= g.nsub || cz >= g.nsub) break;
+  }
+  return (crossed & 1) != 0;
 }
 
 // ------------------------------------------------------------------ collisions with molecules

@@ -300,6 +300,62 @@ class DeviceEngineT : public DeviceEngine {
     return 0;
   }
 
+  int release(uint32_t rep, uint32_t species, uint64_t n, int shape, const double* center, const double* diameter,
+              uint32_t object, uint64_t seed, std::string& err) override {
+    if (rep >= max_rep_ || !reps_[rep].used) {
+      err = "no such replica";
+      return -1;
+    }
+    if (species >= nsp_ || shape < REL_SPHERE || shape > REL_INSIDE || n == 0 || n > 0xFFFFFFF0ull) {
+      err = "invalid release";
+      return -1;
+    }
+    const Rep& R = reps_[rep];
+    const Geo<T>& g = geos_h_[rep];
+    ReleaseDesc d{};
+    d.rep = rep;
+    d.species = species;
+    d.n = (uint32_t)n;
+    d.object = object;
+    d.shape = shape;
+    d.seed = seed;
+    d.uid0 = R.next_uid;
+    double lo[3], hi[3];
+    if (shape == REL_INSIDE) {
+      if (!R.has_obj || object >= R.obj_llf.size() / 3 || R.obj_llf[3 * object] > R.obj_urb[3 * object]) {
+        err = "release inside an object: no walls of that object (mcg_set_wall_objects)";
+        return -1;
+      }
+      for (int a = 0; a < 3; a++) {
+        d.llf[a] = lo[a] = R.obj_llf[3 * object + a];
+        d.urb[a] = hi[a] = R.obj_urb[3 * object + a];
+      }
+    } else {
+      for (int a = 0; a < 3; a++) {
+        d.center[a] = center[a];
+        d.diameter[a] = diameter[a];
+        lo[a] = center[a] - 0.5 * std::fabs(diameter[a]);
+        hi[a] = center[a] + 0.5 * std::fabs(diameter[a]);
+      }
+    }
+    const double o[3] = {(double)g.origin.x, (double)g.origin.y, (double)g.origin.z};
+    const double q[3] = {(double)g.opposite.x, (double)g.opposite.y, (double)g.opposite.z};
+    for (int a = 0; a < 3; a++)
+      if (!(lo[a] >= o[a] && hi[a] < q[a])) {
+        err = "release region outside the partition";
+        return -4;
+      }
+    if (read_counters(err)) return -2;
+    const uint64_t live = cnt_.n_live;
+    if (live + n > cap_ && ensure_capacity(std::max<uint64_t>((live + n) * 3 / 2, 1024), err)) return -2;
+    if (n > base_.prod_cap && ensure_prod(n, err)) return -2;
+    k_release<T><<<grid(n), TPB, 0, stream_>>>(state(parity_), d);
+    launches_ += 1;
+    MCG_CUDA(cudaGetLastError());
+    reps_[rep].next_uid += n;
+    return rebin(nullptr, n, err);
+  }
+
   int import_state(uint32_t rep, uint64_t n, const double* pos, const uint32_t* species, const uint64_t* ids,
                    const double* tuni, const uint8_t* flags, uint64_t iteration, std::string& err) override {
     if (rep >= max_rep_ || !reps_[rep].used) {
@@ -542,6 +598,9 @@ class DeviceEngineT : public DeviceEngine {
     uint8_t* wclass = nullptr;
     Chem* chem = nullptr;
     double* w64 = nullptr;  // fp32 engines: fp64 wall constants for the tie-breaks
+    uint16_t* wall_obj = nullptr;  // geometry object of each wall
+    bool has_obj = false;
+    std::vector<double> obj_llf, obj_urb;  // bounding box of each object's walls
     // host copies for placing fp32 molecules: wall planes (n xyz, d), walls per
     // subpartition, and the grid
     std::vector<double> planes;
@@ -721,6 +780,25 @@ class DeviceEngineT : public DeviceEngine {
       if (alloc_copy(&R.w64, w64, R.bytes, err)) return -2;
       g.w64 = R.w64;
     }
+    g.wall_obj = nullptr;
+    if (sp.wall_obj && sp.wall_obj->size() == nw && nw) {
+      if (alloc_copy(&R.wall_obj, *sp.wall_obj, R.bytes, err)) return -2;
+      g.wall_obj = R.wall_obj;
+      R.has_obj = true;
+      uint32_t nobj = 0;
+      for (uint16_t o : *sp.wall_obj) nobj = std::max<uint32_t>(nobj, (uint32_t)o + 1);
+      R.obj_llf.assign(3 * (size_t)nobj, 1e300);
+      R.obj_urb.assign(3 * (size_t)nobj, -1e300);
+      for (uint32_t w = 0; w < nw; w++) {
+        const uint32_t ob = (*sp.wall_obj)[w];
+        for (int v = 0; v < 3; v++)
+          for (int a = 0; a < 3; a++) {
+            const double x = hs.wall[(size_t)w * 24 + 13 + 3 * v + a];
+            R.obj_llf[3 * ob + a] = std::min(R.obj_llf[3 * ob + a], x);
+            R.obj_urb[3 * ob + a] = std::max(R.obj_urb[3 * ob + a], x);
+          }
+      }
+    }
     R.span = (uint32_t)(base_keys << g.oct_shift);
     if (sizeof(T) == 4) {
       R.planes.resize(4 * (size_t)nw);
@@ -746,6 +824,7 @@ class DeviceEngineT : public DeviceEngine {
     cudaFree(R.wclass);
     cudaFree(R.chem);
     cudaFree(R.w64);
+    cudaFree(R.wall_obj);
     R = Rep();
     Geo<T> g{};
     g.mode = REP_DROP;
@@ -852,7 +931,8 @@ class DeviceEngineT : public DeviceEngine {
       cnt_ = c;
       return 0;
     }
-    if (n) MCG_CUDA(cudaMemcpyAsync(base_.prod, stage, sizeof(Product<T>) * n, cudaMemcpyHostToDevice, stream_));
+    // staged molecules come from the host, or (stage == nullptr) are already in the list
+    if (n && stage) MCG_CUDA(cudaMemcpyAsync(base_.prod, stage, sizeof(Product<T>) * n, cudaMemcpyHostToDevice, stream_));
     // staged molecules sit in the product list, already "diffused"
     Counters c = cnt_;
     c.n_prod = (uint32_t)n;

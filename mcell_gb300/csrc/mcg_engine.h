@@ -42,6 +42,7 @@ struct ReplicaSpec {
   uint64_t n_mol = 0;
   const double* pos = nullptr;       // [n_mol][3]
   const uint32_t* species = nullptr;  // [n_mol]
+  const std::vector<uint16_t>* wall_obj = nullptr;  // geometry object of each wall (optional)
   uint32_t n_iterations = 0;         // iterations to run, then the replica freezes; 0 = unlimited
   bool octants = true;               // bin occupants per subpartition octant when the key space allows
 };
@@ -69,6 +70,10 @@ class DeviceEngine {
                            uint8_t* flags, uint64_t* n_out, uint64_t* iteration, std::string& err) = 0;
   virtual int import_state(uint32_t rep, uint64_t n, const double* pos, const uint32_t* species, const uint64_t* ids,
                            const double* tuni, const uint8_t* flags, uint64_t iteration, std::string& err) = 0;
+  // volume release on the device (shape: 0 ellipsoid, 1 cuboid, 2 ellipsoid shell, 3
+  // inside geometry object `object`); ids continue the replica's
+  virtual int release(uint32_t rep, uint32_t species, uint64_t n, int shape, const double* center,
+                      const double* diameter, uint32_t object, uint64_t seed, std::string& err) = 0;
   // iterations the replica has run (it freezes after its n_iterations)
   virtual int replica_iterations(uint32_t rep, uint64_t* done, std::string& err) = 0;
   // device bytes held for the replica (mesh, grid, its share of the molecule arrays)

@@ -873,6 +873,61 @@ __global__ void k_rebin_count(State<T> s, uint32_t n_staged) {
   }
 }
 
+// ---- volume releases on the device (ReleaseEvent::release_ellipsoid_or_rectcuboid,
+// release_inside_regions; release_event.cpp:904-1006): new molecules written into
+// the staging (product) list, then binned like an upload
+
+constexpr int REL_SPHERE = 0, REL_CUBOID = 1, REL_SHELL = 2, REL_INSIDE = 3;
+
+struct ReleaseDesc {
+  uint32_t rep, species, n, object;
+  int shape;
+  double center[3], diameter[3];  // ellipsoid / cuboid / shell
+  double llf[3], urb[3];          // sampling box of a release inside an object
+  uint64_t seed, uid0;
+};
+
+template <typename T>
+__global__ void k_release(State<T> s, ReleaseDesc r) {
+  const Geo<T>& g = s.geos[r.rep];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < r.n; i += gridDim.x * blockDim.x) {
+    PhiloxDraws d;
+    d.ph.init(r.seed, i, 0, 7);
+    auto uni = [&d]() { return ((double)d.u32() + 0.5) * (1.0 / 4294967296.0); };
+    V3<double> p = v3<double>(0, 0, 0);
+    bool ok = false;
+    for (int attempt = 0; attempt < 1024 && !ok; attempt++) {
+      if (r.shape == REL_INSIDE) {
+        p = v3<double>(r.llf[0] + (r.urb[0] - r.llf[0]) * uni(), r.llf[1] + (r.urb[1] - r.llf[1]) * uni(),
+                       r.llf[2] + (r.urb[2] - r.llf[2]) * uni());
+        ok = inside_object(g, p, r.object);
+      } else {
+        // unit cube around 0, spheroidal shapes keep only the unit ball (radius 0.5)
+        V3<double> q = v3<double>(uni() - 0.5, uni() - 0.5, uni() - 0.5);
+        const double r2 = dot(q, q);
+        if ((r.shape == REL_SPHERE || r.shape == REL_SHELL) && r2 >= 0.25) continue;
+        if (r.shape == REL_SHELL) {
+          const double rr = sqrt(r2) * 2;
+          q = rr == 0 ? v3<double>(0, 0, 0.5) : scale(q, 1.0 / rr);
+        }
+        p = v3<double>(q.x * r.diameter[0] + r.center[0], q.y * r.diameter[1] + r.center[1],
+                       q.z * r.diameter[2] + r.center[2]);
+        ok = true;
+      }
+    }
+    if (!ok) atomicOr(&s.cnt->status, ST_WATCHDOG);
+    Product<T> m;
+    m.pos.x = (T)p.x;
+    m.pos.y = (T)p.y;
+    m.pos.z = (T)p.z;
+    set_meta(m.pos, make_meta(r.species, r.rep, META_SCHEDULE_UNIMOL));
+    m.birth = 0;
+    m.uid = r.uid0 + i;
+    m.tuni = TIME_FOREVER;
+    s.prod[i] = m;
+  }
+}
+
 // ---- per-routine parity harness: injected displacement and draws
 
 template <typename T>
