@@ -286,10 +286,23 @@ int mcg_release(mcg_engine* e, uint32_t species, uint64_t n, int shape, const do
 int mcg_batch_release(mcg_batch* b, uint32_t replica, uint32_t species, uint64_t n, int shape, const double* center,
                       const double* diameter, uint32_t object, uint64_t release_seed);
 
+/* ---- Counted volumes: molecules inside closed geometry objects, per species, for
+   MolOrRxnCountEvent (src4/mol_or_rxn_count_event.cpp:707). As MCell4's counted-
+   volume index, each molecule carries its membership (up to 7 counted objects per
+   model), set at upload or release by the reference's ray-parity test
+   (compute_counted_volume_for_pos, src4/collision_utils.inl:1515-1545) and flipped
+   whenever it crosses a (transparent) wall of a counted object; products inherit
+   their reactant's. Objects are named by the ids of mcg_set_wall_objects; set
+   before the first step. Counts: [n_species][n_counted] after the last iteration
+   or upload; trajectory: [n][n_species][n_counted] for the last n iterations. */
+int mcg_set_counted_objects(mcg_engine* e, uint32_t n, const uint16_t* objects);
+int mcg_get_counted_volume_counts(mcg_engine* e, uint64_t* counts);
+int mcg_get_counted_volume_trajectory(mcg_engine* e, uint32_t n_iterations, uint64_t* counts);
+
 /* ---- Checkpoints (the device side of ChkptVolMol, libmcell/api/model.cpp:591-650).
    A checkpoint is the live molecules — position, species, id, unimolecular time
    relative to the next iteration (1e20 = none), flags (bit 0: the unimolecular time
-   is not drawn yet) — and the iteration counter. With the same model definition and
+   is not drawn yet; bits 1-7: inside counted object k) — and the iteration counter. With the same model definition and
    seed, a run continued from it repeats the uninterrupted run (the random streams
    are counter based: seed, molecule id, iteration). mcg_export_state: call with
    cap = 0 for the count, then with arrays of that size. mcg_import_state: on a

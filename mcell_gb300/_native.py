@@ -34,7 +34,8 @@ EXPORTS = [
     "mcg_serve_create", "mcg_serve_destroy", "mcg_serve_last_error", "mcg_serve_submit", "mcg_serve_poll",
     "mcg_serve_wait", "mcg_serve_result", "mcg_serve_cancel", "mcg_serve_release", "mcg_serve_get_stats",
     "mcg_export_state", "mcg_import_state", "mcg_write_viz", "mcg_batch_write_viz",
-    "mcg_set_wall_objects", "mcg_release", "mcg_batch_release",
+    "mcg_set_wall_objects", "mcg_release", "mcg_batch_release", "mcg_set_counted_objects",
+    "mcg_get_counted_volume_counts", "mcg_get_counted_volume_trajectory",
 ]
 
 
@@ -264,6 +265,21 @@ class Engine:
     def set_wall_objects(self, object_of_wall):
         o = np.ascontiguousarray(object_of_wall, np.uint16)
         self._chk(lib().mcg_set_wall_objects(self.h, ctypes.c_uint32(len(o)), _p(o)))
+
+    def set_counted_objects(self, objects):
+        o = np.ascontiguousarray(objects, np.uint16)
+        self.n_counted = len(o)
+        self._chk(lib().mcg_set_counted_objects(self.h, ctypes.c_uint32(len(o)), _p(o)))
+
+    def counted_counts(self):
+        out = np.zeros((self.n_species, self.n_counted), np.uint64)
+        self._chk(lib().mcg_get_counted_volume_counts(self.h, _p(out)))
+        return out
+
+    def counted_trajectory(self, n):
+        out = np.zeros((n, self.n_species, self.n_counted), np.uint64)
+        self._chk(lib().mcg_get_counted_volume_trajectory(self.h, ctypes.c_uint32(n), _p(out)))
+        return out
 
     def release(self, species, n, shape="sphere", center=(0, 0, 0), diameter=(1, 1, 1), obj=0, seed=1):
         shapes = {"sphere": 0, "cuboid": 1, "shell": 2, "inside": 3}

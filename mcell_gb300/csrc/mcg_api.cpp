@@ -55,6 +55,7 @@ static int prepare(mcg_engine* e) {
   sp.chem = &e->chem;
   sp.wall_class = &e->wclass;
   sp.wall_obj = e->wall_obj.empty() ? nullptr : &e->wall_obj;
+  sp.counted = e->counted;
   sp.seed = e->cfg.seed;
   sp.n_mol = e->pend_species.size();
   sp.pos = e->pend_pos.data();
@@ -301,6 +302,33 @@ int mcg_set_wall_objects(mcg_engine* e, uint32_t n_walls, const uint16_t* object
   if (n_walls != e->walls.size() / 3) return fail(e, MCG_ERR_ARG, "wall count differs from the uploaded mesh");
   e->wall_obj.assign(object_of_wall, object_of_wall + n_walls);
   return MCG_OK;
+}
+
+int mcg_set_counted_objects(mcg_engine* e, uint32_t n, const uint16_t* objects) {
+  if (!e || (n && !objects)) return MCG_ERR_ARG;
+  if (e->dev) return fail(e, MCG_ERR_ARG, "counted objects must be set before the first step");
+  if (n > 7) return fail(e, MCG_ERR_UNSUPPORTED, "at most 7 counted objects per model on the GPU path");
+  if (n && e->wall_obj.empty()) return fail(e, MCG_ERR_ARG, "counted objects need mcg_set_wall_objects first");
+  e->counted.assign(objects, objects + n);
+  return MCG_OK;
+}
+
+int mcg_get_counted_volume_counts(mcg_engine* e, uint64_t* counts) {
+  if (!e || !counts) return MCG_ERR_ARG;
+  int rc = prepare(e);
+  if (rc) return rc;
+  std::string err;
+  rc = e->dev->counted_counts(0, counts, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
+int mcg_get_counted_volume_trajectory(mcg_engine* e, uint32_t n, uint64_t* counts) {
+  if (!e || (n && !counts)) return MCG_ERR_ARG;
+  int rc = prepare(e);
+  if (rc) return rc;
+  std::string err;
+  rc = e->dev->counted_trajectory(0, n, counts, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
 }
 
 int mcg_release(mcg_engine* e, uint32_t species, uint64_t n, int shape, const double* center,

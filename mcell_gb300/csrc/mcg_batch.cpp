@@ -223,6 +223,7 @@ int mcg_batch_add(mcg_batch* b, uint32_t n, mcg_engine* const* models, const uin
     sp.chem = &m->chem;
     sp.wall_class = &m->wclass;
     sp.wall_obj = m->wall_obj.empty() ? nullptr : &m->wall_obj;
+    sp.counted = m->counted;
     sp.seed = m->cfg.seed;
     sp.n_mol = m->pend_species.size();
     sp.pos = m->pend_pos.data();

@@ -53,15 +53,19 @@ constexpr uint32_t ST_COLL_OVERFLOW = 1u << 3;   // more than MAXC candidates (e
 constexpr uint32_t ST_SET_OVERFLOW = 1u << 4;    // more than MAXSET subpartitions
 
 // molecule meta word (w lane of the position record): species in bits 0-7, the
-// schedule flag in bit 8, the replica (model) the molecule belongs to in bits 16-31
+// schedule flag in bit 8, counted-volume membership in bits 9-15, the replica
+// (model) the molecule belongs to in bits 16-31
 constexpr uint32_t META_SPECIES_MASK = 0xFFu;
 constexpr uint32_t META_SCHEDULE_UNIMOL = 1u << 8;  // MOLECULE_FLAG_SCHEDULE_UNIMOL_RXN
+constexpr uint32_t META_CV_SHIFT = 9;   // bits 9-15: inside counted object k (membership, updated at crossings)
+constexpr uint32_t MAX_COUNTED = 7;
 constexpr uint32_t META_REP_SHIFT = 16;
 constexpr uint32_t MAX_REPLICAS = 1u << 16;
 __host__ __device__ __forceinline__ uint32_t make_meta(uint32_t species, uint32_t rep, uint32_t flags = 0) {
   return species | flags | (rep << META_REP_SHIFT);
 }
 __host__ __device__ __forceinline__ uint32_t meta_rep(uint32_t m) { return m >> META_REP_SHIFT; }
+__host__ __device__ __forceinline__ uint32_t meta_cv(uint32_t m) { return (m >> META_CV_SHIFT) & 0x7Fu; }
 
 // replica modes: advancing, frozen (finished, kept until collected), dropped at the next sort
 constexpr uint32_t REP_RUN = 0, REP_FROZEN = 1, REP_DROP = 2;
@@ -147,7 +151,20 @@ struct Geo {
   // xyz, d, unit_u xyz, unit_v xyz, v0 xyz, uv_vert1_u, uv_vert2 u v); null in fp64
   const double* w64;
   const uint16_t* wall_obj;   // geometry object of each wall (releases inside objects), or null
+  uint32_t n_cv;              // counted objects (volumes whose contents are counted)
+  uint16_t cv_obj[MAX_COUNTED];
 };
+
+// membership bits a crossing of wall wi flips (walls of counted objects only)
+template <typename T>
+__device__ __forceinline__ uint32_t cv_flip_of_wall(const Geo<T>& g, uint32_t wi) {
+  if (!g.n_cv) return 0;
+  const uint16_t o = g.wall_obj[wi];
+  uint32_t f = 0;
+  for (uint32_t k = 0; k < g.n_cv; k++)
+    if (g.cv_obj[k] == o) f |= 1u << k;
+  return f;
+}
 
 // molecules at the start of the iteration, sorted by key (replica, species, subpartition, octant)
 template <typename T>
@@ -168,6 +185,7 @@ struct TraceOut {
   V3<T> rxn_pos;
   double elapsed, t_steps;
   uint32_t err;
+  uint32_t flip;     // counted-volume bits flipped by transparent crossings (up to the reaction)
 };
 
 // ------------------------------------------------------------------ draws
@@ -1423,6 +1441,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
   TraceOut<T> res;
   res.status = 0;
   res.err = 0;
+  res.flip = 0;
   res.partner = NONE;
   res.t_abs = 0;
   res.rxn_pos = pos;
@@ -1531,6 +1550,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
         const int kind = ch.can_volwall[species] ? g.wall_class[(size_t)hit.wall * g.nsp + species] : 0;
         const double t_abs = elapsed + t_steps * (double)hit.t;
         if (kind == 1) {
+          res.flip ^= cv_flip_of_wall(g, hit.wall);
           pos = hit.pos;
           sp = subpart_of(g, pos);
           double t_smash = (double)hit.t;

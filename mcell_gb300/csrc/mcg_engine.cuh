@@ -117,9 +117,25 @@ class DeviceEngineT : public DeviceEngine {
       reps_[r].next_uid = sp.n_mol;
       out_reps[k] = r;
     }
+    bool any_cv = false;
+    for (uint32_t k = 0; k < n; k++) any_cv = any_cv || !specs[k].counted.empty();
+    if (any_cv && !d_cv_count_) {
+      const size_t nq = (size_t)max_rep_ * nsp_ * MAX_COUNTED;
+      cv_traj_cap_ = std::min<uint32_t>(traj_cap_, 4096);
+      MCG_CUDA(cudaMalloc(&d_cv_count_, sizeof(uint32_t) * nq));
+      MCG_CUDA(cudaMalloc(&d_cv_now_, sizeof(uint32_t) * nq));
+      MCG_CUDA(cudaMalloc(&d_cv_traj_, sizeof(uint32_t) * nq * cv_traj_cap_));
+      MCG_CUDA(cudaMemsetAsync(d_cv_count_, 0, sizeof(uint32_t) * nq, stream_));
+      MCG_CUDA(cudaMemsetAsync(d_cv_now_, 0, sizeof(uint32_t) * nq, stream_));
+      MCG_CUDA(cudaMemsetAsync(d_cv_traj_, 0, sizeof(uint32_t) * nq * cv_traj_cap_, stream_));
+      base_.cv_count = d_cv_count_;
+      base_.cv_now = d_cv_now_;
+      base_.cv_traj = d_cv_traj_;
+      base_.cv_traj_cap = cv_traj_cap_;
+    }
     int rc = layout_keys(err);
     if (rc) return rc;
-    return rebin(stage.data(), n_new, err);
+    return rebin(stage.data(), n_new, err, true);
   }
 
   int remove_replicas(const uint32_t* reps, uint32_t n, std::string& err) override {
@@ -155,7 +171,7 @@ class DeviceEngineT : public DeviceEngine {
     if (rc) return rc;
     reps_[rep].next_uid = std::max<uint64_t>(reps_[rep].next_uid, uid0 + n);
     if (read_counters(err)) return -2;
-    return rebin(stage.data(), n, err);
+    return rebin(stage.data(), n, err, true);
   }
 
   int step(uint32_t n, std::string& err) override {
@@ -295,7 +311,7 @@ class DeviceEngineT : public DeviceEngine {
     MCG_CUDA(d2h(t.data(), s.a_tuni + lo, sizeof(T) * n));
     for (uint64_t i = 0; i < n; i++) {
       if (tuni) tuni[i] = (double)t[i];
-      if (flags) flags[i] = (host_meta(p[i]) & META_SCHEDULE_UNIMOL) ? 1 : 0;
+      if (flags) flags[i] = (uint8_t)(((host_meta(p[i]) & META_SCHEDULE_UNIMOL) ? 1 : 0) | (meta_cv(host_meta(p[i])) << 1));
     }
     return 0;
   }
@@ -373,7 +389,8 @@ class DeviceEngineT : public DeviceEngine {
     for (uint64_t i = 0; i < n; i++) {
       stage[i].uid = ids[i];
       stage[i].tuni = tuni[i];
-      put_meta(stage[i].pos, make_meta(species[i], rep, (flags[i] & 1) ? META_SCHEDULE_UNIMOL : 0));
+      put_meta(stage[i].pos, make_meta(species[i], rep,
+                                       ((flags[i] & 1) ? META_SCHEDULE_UNIMOL : 0) | ((uint32_t)(flags[i] >> 1) << META_CV_SHIFT)));
       reps_[rep].next_uid = std::max<uint64_t>(reps_[rep].next_uid, ids[i] + 1);
     }
     // the engine continues at the checkpoint's iteration: the replica's random streams
@@ -387,6 +404,44 @@ class DeviceEngineT : public DeviceEngine {
     rc = rebin(stage.data(), n, err);
     rebin_it_ = cnt_.iteration;
     return rc;
+  }
+
+  int counted_counts(uint32_t rep, uint64_t* out, std::string& err) override {
+    int rc = sync(err);
+    if (rc) return rc;
+    if (rep >= max_rep_ || !reps_[rep].used || !reps_[rep].n_cv || !d_cv_now_) {
+      err = "no counted objects in this model";
+      return -1;
+    }
+    const uint32_t nc = reps_[rep].n_cv;
+    std::vector<uint32_t> h((size_t)nsp_ * MAX_COUNTED);
+    MCG_CUDA(d2h(h.data(), d_cv_now_ + (size_t)rep * nsp_ * MAX_COUNTED, sizeof(uint32_t) * h.size()));
+    for (uint32_t a = 0; a < nsp_; a++)
+      for (uint32_t k = 0; k < nc; k++) out[a * nc + k] = h[a * MAX_COUNTED + k];
+    return 0;
+  }
+
+  int counted_trajectory(uint32_t rep, uint32_t n, uint64_t* out, std::string& err) override {
+    int rc = sync(err);
+    if (rc) return rc;
+    if (rep >= max_rep_ || !reps_[rep].used || !reps_[rep].n_cv || !d_cv_traj_) {
+      err = "no counted objects in this model";
+      return -1;
+    }
+    if (n > cnt_.iteration - geos_h_[rep].it0 || n > cv_traj_cap_ - 1) {
+      err = "trajectory longer than the iterations run or the ring";
+      return -1;
+    }
+    const uint32_t nc = reps_[rep].n_cv;
+    const size_t nq = (size_t)max_rep_ * nsp_ * MAX_COUNTED;
+    std::vector<uint32_t> h((size_t)nsp_ * MAX_COUNTED);
+    for (uint32_t k = 0; k < n; k++) {
+      const uint64_t row = (cnt_.iteration - n + k) % cv_traj_cap_;
+      MCG_CUDA(d2h(h.data(), d_cv_traj_ + row * nq + (size_t)rep * nsp_ * MAX_COUNTED, sizeof(uint32_t) * h.size()));
+      for (uint32_t a = 0; a < nsp_; a++)
+        for (uint32_t o = 0; o < nc; o++) out[((size_t)k * nsp_ + a) * nc + o] = h[a * MAX_COUNTED + o];
+    }
+    return 0;
   }
 
   int replica_iterations(uint32_t rep, uint64_t* done, std::string& err) override {
@@ -600,6 +655,7 @@ class DeviceEngineT : public DeviceEngine {
     double* w64 = nullptr;  // fp32 engines: fp64 wall constants for the tie-breaks
     uint16_t* wall_obj = nullptr;  // geometry object of each wall
     bool has_obj = false;
+    uint32_t n_cv = 0;     // counted objects
     std::vector<double> obj_llf, obj_urb;  // bounding box of each object's walls
     // host copies for placing fp32 molecules: wall planes (n xyz, d), walls per
     // subpartition, and the grid
@@ -799,6 +855,16 @@ class DeviceEngineT : public DeviceEngine {
           }
       }
     }
+    g.n_cv = 0;
+    if (!sp.counted.empty()) {
+      if (!g.wall_obj || sp.counted.size() > MAX_COUNTED) {
+        err = "counted objects need wall objects (mcg_set_wall_objects), at most 7";
+        return -1;
+      }
+      g.n_cv = (uint32_t)sp.counted.size();
+      for (uint32_t k = 0; k < g.n_cv; k++) g.cv_obj[k] = sp.counted[k];
+      R.n_cv = g.n_cv;
+    }
     R.span = (uint32_t)(base_keys << g.oct_shift);
     if (sizeof(T) == 4) {
       R.planes.resize(4 * (size_t)nw);
@@ -915,7 +981,7 @@ class DeviceEngineT : public DeviceEngine {
 
   // re-sorts the live molecules plus the staged ones into the other sorted arrays
   // (molecules of dropped replicas are left out); counters must be fresh
-  int rebin(const Product<T>* stage, uint64_t n, std::string& err) {
+  int rebin(const Product<T>* stage, uint64_t n, std::string& err, bool init_cv = false) {
     const uint64_t live = cnt_.n_live;
     if (live + n > 0xFFFFFFF0ull) {
       err = "too many molecules for 32-bit indices";
@@ -940,12 +1006,20 @@ class DeviceEngineT : public DeviceEngine {
     c.prod_hi = (uint32_t)n;
     MCG_CUDA(cudaMemcpyAsync(d_cnt_, &c, sizeof(Counters), cudaMemcpyHostToDevice, stream_));
     State<T> s = state(parity_);
+    if (init_cv && n && d_cv_count_) {
+      k_cv_init<T><<<grid(n), TPB, 0, stream_>>>(s, (uint32_t)n);
+      launches_ += 1;
+    }
     k_rebin_count<T><<<grid(live + n), TPB, 0, stream_>>>(s, (uint32_t)n);
     k_scan_tiles<T><<<ntiles_, TPB, 0, stream_>>>(s);
     k_scan_top<T><<<1, TPB, 0, stream_>>>(s, ntiles_);
     k_scan_apply<T><<<ntiles_, TPB, 0, stream_>>>(s);
     k_scatter<T><<<grid(live + n), TPB, 0, stream_>>>(s, 0);
     launches_ += 5;
+    if (d_cv_count_) {
+      k_publish_cv<T><<<1, TPB, 0, stream_>>>(s);
+      launches_ += 1;
+    }
     MCG_CUDA(cudaGetLastError());
     MCG_CUDA(cudaStreamSynchronize(stream_));
     if (read_counters(err)) return -2;
@@ -1147,6 +1221,9 @@ class DeviceEngineT : public DeviceEngine {
     cudaFree(d_cnt_);
     cudaFree(d_debug_);
     cudaFree(d_geos_);
+    cudaFree(d_cv_count_);
+    cudaFree(d_cv_now_);
+    cudaFree(d_cv_traj_);
     if (stream_) cudaStreamDestroy(stream_);
   }
 
@@ -1183,6 +1260,8 @@ class DeviceEngineT : public DeviceEngine {
   unsigned long long* d_traj_ = nullptr;
   Counters* d_cnt_ = nullptr;
   double* d_debug_ = nullptr;
+  uint32_t *d_cv_count_ = nullptr, *d_cv_now_ = nullptr, *d_cv_traj_ = nullptr;
+  uint32_t cv_traj_cap_ = 0;
 };
 
 }  // namespace mcg

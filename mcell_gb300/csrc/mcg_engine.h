@@ -43,6 +43,7 @@ struct ReplicaSpec {
   const double* pos = nullptr;       // [n_mol][3]
   const uint32_t* species = nullptr;  // [n_mol]
   const std::vector<uint16_t>* wall_obj = nullptr;  // geometry object of each wall (optional)
+  std::vector<uint16_t> counted;     // objects whose contents are counted (at most 7)
   uint32_t n_iterations = 0;         // iterations to run, then the replica freezes; 0 = unlimited
   bool octants = true;               // bin occupants per subpartition octant when the key space allows
 };
@@ -74,6 +75,10 @@ class DeviceEngine {
   // inside geometry object `object`); ids continue the replica's
   virtual int release(uint32_t rep, uint32_t species, uint64_t n, int shape, const double* center,
                       const double* diameter, uint32_t object, uint64_t seed, std::string& err) = 0;
+  // counted volumes: molecules of each species inside each counted object after the
+  // last iteration or upload ([nsp][n_counted]), and their trajectory
+  virtual int counted_counts(uint32_t rep, uint64_t* out, std::string& err) = 0;
+  virtual int counted_trajectory(uint32_t rep, uint32_t n, uint64_t* out, std::string& err) = 0;
   // iterations the replica has run (it freezes after its n_iterations)
   virtual int replica_iterations(uint32_t rep, uint64_t* done, std::string& err) = 0;
   // device bytes held for the replica (mesh, grid, its share of the molecule arrays)

@@ -59,6 +59,7 @@ struct Counters {
 
 struct Proposal {
   uint32_t i, partner;
+  uint32_t cv;  // counted-volume bits of the reactant at the collision (the products')
   uint64_t key;
   double t_abs;
   double x, y, z;
@@ -103,6 +104,12 @@ struct State {
   Product<T>* prod;
   uint8_t* pst;      // product status
   unsigned long long* traj;  // [traj_cap][n_rep][nsp] species counts after each iteration
+  // counted volumes (null when no replica counts any): molecules inside counted
+  // object k per (replica, species): accumulated by k_scatter, published by k_end
+  uint32_t* cv_count;  // [n_rep][nsp][MAX_COUNTED] of the iteration being sorted
+  uint32_t* cv_now;    // [n_rep][nsp][MAX_COUNTED] after the last iteration or upload
+  uint32_t* cv_traj;   // [cv_traj_cap][n_rep][nsp][MAX_COUNTED]
+  uint32_t cv_traj_cap;
   Counters* cnt;
 };
 
@@ -176,7 +183,8 @@ __device__ __forceinline__ uint32_t key_of_rec(const State<T>& s, const P4<T>& b
 }
 
 template <typename T>
-__device__ void add_product(const State<T>& s, int species, uint32_t rep, V3<T> pos, double birth, uint64_t uid) {
+__device__ void add_product(const State<T>& s, int species, uint32_t rep, uint32_t cv, V3<T> pos, double birth,
+                            uint64_t uid) {
   if (species < 0) return;
   uint32_t k = atomicAdd(&s.cnt->n_prod, 1u);
   if (k >= s.prod_cap) {
@@ -187,7 +195,7 @@ __device__ void add_product(const State<T>& s, int species, uint32_t rep, V3<T> 
   p.pos.x = pos.x;
   p.pos.y = pos.y;
   p.pos.z = pos.z;
-  set_meta(p.pos, make_meta((uint32_t)species, rep, META_SCHEDULE_UNIMOL));
+  set_meta(p.pos, make_meta((uint32_t)species, rep, META_SCHEDULE_UNIMOL | (cv << META_CV_SHIFT)));
   p.birth = birth;
   p.uid = uid;
   p.tuni = TIME_FOREVER;
@@ -197,13 +205,13 @@ __device__ void add_product(const State<T>& s, int species, uint32_t rep, V3<T> 
 // unimolecular outcome: the molecule is destroyed, products appear at its position
 // (outcome_unimolecular, diffuse_react_event.cpp:2939). it: the replica's own iteration.
 template <typename T>
-__device__ __noinline__ void unimol_products(const State<T>& s, const Geo<T>& g, int species, V3<T> pos, double t,
-                                             uint64_t uid, uint32_t it) {
+__device__ __noinline__ void unimol_products(const State<T>& s, const Geo<T>& g, int species, uint32_t cv, V3<T> pos,
+                                             double t, uint64_t uid, uint32_t it) {
   const Chem& ch = *g.chem;
   for (int k = 0; k < 2; k++) {
     int ps = ch.uni_prod[species][k];
     if (ps >= 0)
-      add_product(s, ps, g.rep, pos, t, mix64(uid ^ ((uint64_t)(it + 1) << 40) ^ (0xA5ull << 32) ^ (uint64_t)k));
+      add_product(s, ps, g.rep, cv, pos, t, mix64(uid ^ ((uint64_t)(it + 1) << 40) ^ (0xA5ull << 32) ^ (uint64_t)k));
   }
 }
 
@@ -239,7 +247,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   }
   if (tuni <= 0.0) {
     // scheduled at or before the start of the step: react first (diffuse_single_molecule :214-223)
-    unimol_products(s, g, species, pos, 0.0, uid, it);
+    unimol_products(s, g, species, meta_cv(meta), pos, 0.0, uid, it);
     return 2;
   }
   // get_max_time (:164-198) with the barrier at the end of the iteration
@@ -304,6 +312,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   } else {
     r.status = 0;
     r.pos = pos;
+    r.flip = 0;
   }
   if (r.status == 1) {
     Proposal p;
@@ -313,6 +322,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
     // earliest reaction wins; the molecule index makes keys unique within the iteration
     p.key = ((uint64_t)__float_as_uint(tf < 0.f ? 0.f : tf) << 32) | i;
     p.t_abs = r.t_abs;
+    p.cv = meta_cv(meta) ^ r.flip;
     p.x = (double)r.rxn_pos.x;
     p.y = (double)r.rxn_pos.y;
     p.z = (double)r.rxn_pos.z;
@@ -322,7 +332,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   if (r.status == 2) return 2;
   if (max_time < 1.0) {
     // the unimolecular reaction happens where the molecule stopped
-    unimol_products(s, g, species, r.pos, tuni, uid, it);
+    unimol_products(s, g, species, meta_cv(meta) ^ r.flip, r.pos, tuni, uid, it);
     return 2;
   }
   const bool escaped = !in_partition(g, r.pos);
@@ -345,7 +355,8 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   out.x = r.pos.x;
   out.y = r.pos.y;
   out.z = r.pos.z;
-  set_meta(out, make_meta((uint32_t)species, g.rep));  // schedule flag consumed
+  // schedule flag consumed; counted-volume bits as left by the crossings
+  set_meta(out, make_meta((uint32_t)species, g.rep, (meta_cv(meta) ^ r.flip) << META_CV_SHIFT));
   s.b_pos[i] = out;
   if (meta & META_SCHEDULE_UNIMOL) s.a_tuni[i] = (T)tuni;  // keep the drawn time for the scatter
   return 0;
@@ -416,7 +427,7 @@ __device__ void commit(const State<T>& s, const Proposal& p) {
   for (int k = 0; k < 2; k++) {
     int ps = ch.bimol_prod[sa][sb][k];
     if (ps >= 0) {
-      add_product(s, ps, g.rep, v3<T>((T)p.x, (T)p.y, (T)p.z), p.t_abs,
+      add_product(s, ps, g.rep, p.cv, v3<T>((T)p.x, (T)p.y, (T)p.z), p.t_abs,
                   mix64(uid ^ ((uint64_t)(it + 1) << 40) ^ (0x5Aull << 32) ^ (uint64_t)k));
     }
   }
@@ -589,9 +600,10 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
       double max_time = 1.0 - p.birth;
       if (unimol_time < p.birth + max_time) max_time = unimol_time - p.birth;
       V3<T> pos = v3<T>(p.pos.x, p.pos.y, p.pos.z);
+      uint32_t cv = meta_cv(meta);
       bool dead = false;
       if (max_time <= 0.0) {
-        unimol_products(s, g, species, pos, unimol_time, p.uid, it);
+        unimol_products(s, g, species, meta_cv(meta), pos, unimol_time, p.uid, it);
         dead = true;
       } else {
         double steps = 1.0, t_steps = 1.0;
@@ -623,6 +635,7 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
           TraceOut<T> r = trace_molecule<T>(g, cells, NONE, pos, species, disp, r_rate_factor, t_steps, p.birth,
                                             draws, ev, false);
           err |= r.err;
+          cv ^= r.flip;
           if (r.status == 2) {
             dead = true;
           } else {
@@ -630,7 +643,7 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
           }
         }
         if (!dead && unimol_time < 1.0) {
-          unimol_products(s, g, species, pos, unimol_time, p.uid, it);
+          unimol_products(s, g, species, cv, pos, unimol_time, p.uid, it);
           dead = true;
         }
       }
@@ -642,7 +655,7 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
         p.pos.x = pos.x;
         p.pos.y = pos.y;
         p.pos.z = pos.z;
-        set_meta(p.pos, make_meta((uint32_t)species, g.rep));
+        set_meta(p.pos, make_meta((uint32_t)species, g.rep, cv << META_CV_SHIFT));
         p.tuni = unimol_time - 1.0;
         s.prod[k] = p;
         key = key_of(g, pos, (uint32_t)species);
@@ -751,7 +764,8 @@ __global__ void k_scan_apply(State<T> s) {
 // ---- scatter into the next sorted arrays
 
 template <typename T>
-__device__ __forceinline__ void scatter_one(const State<T>& s, bool active, const P4<T>& pos, uint64_t uid, T tuni) {
+__device__ __forceinline__ void scatter_one(const State<T>& s, bool active, const P4<T>& pos, uint64_t uid, T tuni,
+                                            bool count_cv) {
   uint32_t key = 0;
   if (active) key = key_of_rec(s, pos);
   unsigned mask = __ballot_sync(0xffffffffu, active);
@@ -768,11 +782,25 @@ __device__ __forceinline__ void scatter_one(const State<T>& s, bool active, cons
     s.n_uid[slot] = uid;
     s.n_tuni[slot] = tuni;
   }
+  if (count_cv) {
+    // molecules inside counted objects, one atomic per (replica, species, object) of the peers
+    const uint32_t m = meta_of(pos);
+    const uint32_t cv = meta_cv(m);
+    const uint32_t cell = (meta_rep(m) * (uint32_t)s.nsp + (m & META_SPECIES_MASK)) * MAX_COUNTED;
+    for (uint32_t k = 0; k < MAX_COUNTED; k++) {
+      const bool in = (cv >> k) & 1u;
+      const unsigned im = __ballot_sync(peers, in);
+      if (!in) continue;
+      const unsigned same = __match_any_sync(im, cell + k);
+      if ((int)lane_id() == __ffs(same) - 1) atomicAdd(&s.cv_count[cell + k], (uint32_t)__popc(same));
+    }
+  }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(TPB) k_scatter(State<T> s, int tuni_shift) {
   const uint32_t n = s.cnt->n_live;
+  const bool count_cv = s.cv_count != nullptr;
   for (uint32_t base = blockIdx.x * TPB; base < n; base += gridDim.x * TPB) {
     uint32_t i = base + threadIdx.x;
     bool active = i < n && s.st[i] == 0;
@@ -784,7 +812,7 @@ __global__ void __launch_bounds__(TPB) k_scatter(State<T> s, int tuni_shift) {
       uid = s.a_uid[i];
       tuni = s.a_tuni[i] - (T)tuni_shift;
     }
-    scatter_one(s, active, p, uid, tuni);
+    scatter_one(s, active, p, uid, tuni, count_cv);
   }
   const uint32_t np = min(s.cnt->n_prod, s.prod_cap);
   for (uint32_t base = blockIdx.x * TPB; base < np; base += gridDim.x * TPB) {
@@ -799,7 +827,7 @@ __global__ void __launch_bounds__(TPB) k_scatter(State<T> s, int tuni_shift) {
       uid = q.uid;
       tuni = (T)q.tuni;
     }
-    scatter_one(s, active, p, uid, tuni);
+    scatter_one(s, active, p, uid, tuni, count_cv);
   }
 }
 
@@ -818,12 +846,52 @@ __device__ void count_species(const State<T>& s, uint32_t row) {
   }
 }
 
+// counted-volume counts of the sort just done: to the latest counts (and, after an
+// iteration, to the trajectory ring); the accumulator is cleared
+template <typename T>
+__device__ void publish_cv(const State<T>& s, uint32_t it, bool to_ring) {
+  if (!s.cv_count) return;
+  const uint32_t nq = s.n_rep * (uint32_t)s.nsp * MAX_COUNTED;
+  uint32_t* row = s.cv_traj + (size_t)(it % s.cv_traj_cap) * nq;
+  for (uint32_t q = threadIdx.x; q < nq; q += blockDim.x) {
+    const uint32_t v = s.cv_count[q];
+    s.cv_now[q] = v;
+    if (to_ring) row[q] = v;
+    s.cv_count[q] = 0;
+  }
+}
+
+// after an upload's sort: the latest counted-volume counts (no ring row)
+template <typename T>
+__global__ void k_publish_cv(State<T> s) {
+  publish_cv(s, 0, false);
+}
+
+// initial counted-volume membership of staged molecules (uploads): the reference's
+// ray-parity test against each counted object
+template <typename T>
+__global__ void k_cv_init(State<T> s, uint32_t n_staged) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_staged; k += gridDim.x * blockDim.x) {
+    Product<T> p = s.prod[k];
+    const uint32_t m = meta_of(p.pos);
+    const Geo<T>& g = geo_of(s, m);
+    if (!g.n_cv) continue;
+    uint32_t cv = 0;
+    const V3<double> x = v3<double>((double)p.pos.x, (double)p.pos.y, (double)p.pos.z);
+    for (uint32_t o = 0; o < g.n_cv; o++)
+      if (inside_object(g, x, g.cv_obj[o])) cv |= 1u << o;
+    set_meta(p.pos, (m & ~(0x7Fu << META_CV_SHIFT)) | (cv << META_CV_SHIFT));
+    s.prod[k].pos = p.pos;
+  }
+}
+
 // bookkeeping at the end of an iteration (one block)
 template <typename T>
 __global__ void k_end(State<T> s) {
   Counters* c = s.cnt;
   const uint32_t it = c->iteration;
   count_species(s, it % s.traj_cap);
+  publish_cv(s, it, true);
   __syncthreads();
   if (threadIdx.x != 0) return;
   if (c->n_prod > c->n_prod_done) atomicOr(&c->status, ST_WATCHDOG);  // product chain deeper than the passes
@@ -920,7 +988,10 @@ __global__ void k_release(State<T> s, ReleaseDesc r) {
     m.pos.x = (T)p.x;
     m.pos.y = (T)p.y;
     m.pos.z = (T)p.z;
-    set_meta(m.pos, make_meta(r.species, r.rep, META_SCHEDULE_UNIMOL));
+    uint32_t cv = 0;
+    for (uint32_t o = 0; o < g.n_cv; o++)
+      if (inside_object(g, p, g.cv_obj[o])) cv |= 1u << o;
+    set_meta(m.pos, make_meta(r.species, r.rep, META_SCHEDULE_UNIMOL | (cv << META_CV_SHIFT)));
     m.birth = 0;
     m.uid = r.uid0 + i;
     m.tuni = TIME_FOREVER;

@@ -17,6 +17,7 @@ struct mcg_engine {
   std::vector<uint32_t> walls;
   std::vector<uint8_t> wclass;
   std::vector<uint16_t> wall_obj;     // geometry object of each wall (optional)
+  std::vector<uint16_t> counted;      // counted objects (at most 7)
   std::vector<double> pend_pos;       // molecules added before the device engine exists
   std::vector<uint32_t> pend_species;
   uint64_t next_uid = 0;
