@@ -656,6 +656,7 @@ class DeviceEngineT : public DeviceEngine {
     uint16_t* wall_obj = nullptr;  // geometry object of each wall
     bool has_obj = false;
     uint32_t n_cv = 0;     // counted objects
+    double wall_density = 0;  // wall-list entries per subpartition (orders the key space)
     std::vector<double> obj_llf, obj_urb;  // bounding box of each object's walls
     // host copies for placing fp32 molecules: wall planes (n xyz, d), walls per
     // subpartition, and the grid
@@ -866,6 +867,7 @@ class DeviceEngineT : public DeviceEngine {
       R.n_cv = g.n_cv;
     }
     R.span = (uint32_t)(base_keys << g.oct_shift);
+    R.wall_density = (double)hs.wsp_list.size() / (double)g.n3;
     if (sizeof(T) == 4) {
       R.planes.resize(4 * (size_t)nw);
       for (uint32_t w = 0; w < nw; w++)
@@ -939,9 +941,17 @@ class DeviceEngineT : public DeviceEngine {
   }
 
   // key ranges of the used replicas in slot order; grows the key arrays when needed
+  // Replicas whose molecules cost most per step (most walls per subpartition) come
+  // first in the key space: the persistent diffuse warps take molecules in key
+  // order, so the slow ones start early instead of forming the kernel's tail.
   int layout_keys(std::string& err) {
+    std::vector<uint32_t> order;
+    for (uint32_t r = 0; r < max_rep_; r++) order.push_back(r);
+    std::stable_sort(order.begin(), order.end(), [this](uint32_t a, uint32_t b) {
+      return reps_[a].wall_density > reps_[b].wall_density;
+    });
     uint64_t k = 0;
-    for (uint32_t r = 0; r < max_rep_; r++) {
+    for (uint32_t r : order) {
       geos_h_[r].kbase = (uint32_t)k;
       if (reps_[r].used) k += reps_[r].span;
     }
