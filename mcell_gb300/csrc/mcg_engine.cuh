@@ -1172,9 +1172,9 @@ class DeviceEngineT : public DeviceEngine {
     k_redo<T><<<1, TPB, 0, stream_>>>(s);
     mark(2, prof);
     k_prod_window<T><<<1, 1, 0, stream_>>>(s);
-    k_products<T><<<gs, TPB, 0, stream_>>>(s);
+    k_products<T><<<2 * gs, TPB, 0, stream_>>>(s);
     k_prod_window<T><<<1, 1, 0, stream_>>>(s);
-    k_products<T><<<gs, TPB, 0, stream_>>>(s);
+    k_products<T><<<2 * gs, TPB, 0, stream_>>>(s);
     k_prod_window<T><<<1, 1, 0, stream_>>>(s);
     mark(3, prof);
     k_scan_tiles<T><<<ntiles_, TPB, 0, stream_>>>(s);

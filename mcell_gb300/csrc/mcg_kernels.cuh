@@ -473,6 +473,16 @@ __global__ void k_reset_claims(State<T> s) {
 // CTA. Round r reads its losers from half (r & 1) of the loser buffer and
 // their count from redo_n[r], and appends the next round's to the other half.
 
+// Items a warp takes at a time when a pass has n scattered items (products, losers)
+// for nwarps warps: the fewest lanes (a power of two) that still cover all items in
+// one round. Scattered items diverge, so a full warp of them costs nearly 32 traces
+// in a row; spread thin, the pass costs about one.
+__device__ __forceinline__ uint32_t lanes_per_warp(uint32_t n, uint32_t nwarps) {
+  uint32_t per = 32;
+  while (per > 1 && (uint64_t)nwarps * (per / 2) >= n) per >>= 1;
+  return per;
+}
+
 // one loser re-traced: a new proposal (counted in *n_props) or a final state
 template <typename T>
 __device__ __forceinline__ void redo_one(const State<T>& s, uint32_t i, uint32_t* n_props, uint32_t& err) {
@@ -497,8 +507,14 @@ __global__ void __launch_bounds__(TPB) k_redo_trace(State<T> s, int round) {
   const uint32_t n = min(s.cnt->redo_n[round], s.prop_cap);
   const uint32_t* cur = s.losers + (size_t)(round & 1) * s.prop_cap;
   uint32_t err = 0;
-  for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < n; l += gridDim.x * blockDim.x)
-    redo_one(s, cur[l], &s.cnt->redo_np[round], err);
+  // losers are few and scattered: as few per warp as covers them in one round (as in
+  // k_products), so the round takes about one trace
+  const uint32_t nwarps = gridDim.x * (TPB / 32);
+  const uint32_t per = lanes_per_warp(n, nwarps);
+  const uint32_t lane = lane_id();
+  if (lane < per)
+    for (uint32_t l = (blockIdx.x * (TPB / 32) + threadIdx.x / 32) * per + lane; l < n; l += nwarps * per)
+      redo_one(s, cur[l], &s.cnt->redo_np[round], err);
   if (err) atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
 }
 
@@ -581,9 +597,14 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
   const uint32_t b1 = s.cnt->prod_hi;
   const uint32_t it_engine = s.cnt->iteration;
   uint32_t err = 0;
-  for (uint32_t base = b0 + blockIdx.x * TPB; base < b1; base += gridDim.x * TPB) {
-    uint32_t k = base + threadIdx.x;
-    bool active = k < b1;
+  // products are scattered over the model: spread thin over the warps (2,000 products
+  // on 2,432 warps: one each); large windows still fill whole warps
+  const uint32_t nwarps = gridDim.x * (TPB / 32);
+  const uint32_t per = lanes_per_warp(b1 > b0 ? b1 - b0 : 0u, nwarps);
+  const uint32_t lane = lane_id();
+  for (uint32_t base = b0 + (blockIdx.x * (TPB / 32) + threadIdx.x / 32) * per; base < b1; base += nwarps * per) {
+    uint32_t k = base + lane;
+    bool active = lane < per && k < b1;
     uint32_t key = 0;
     bool survive = false;
     if (active) {
