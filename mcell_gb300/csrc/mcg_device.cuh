@@ -762,6 +762,7 @@ __device__ bool keep_side(const P4<T>& rj, double side, V3<T>& pos, bool near_on
 // walls (except `skip`).
 template <typename T>
 __device__ MCG_GUARD_INLINE void guard_sides(const Geo<T>& g, uint32_t sp, V3<T>& pos, V3<T> ref, uint32_t skip) {
+  if (g.wsp_off[sp] == g.wsp_off[sp + 1]) return;  // no wall listed here
   V3<T> glo, ghi;
   seg_box(pos, v3<T>(0, 0, 0), (T)2e-2, glo, ghi);
   const uint64_t gm = cells_touched(g, sp, glo, ghi);
@@ -799,6 +800,7 @@ template <typename T, class D>
 __device__ bool closest_wall_collision(const Geo<T>& g, V3<T> pos, uint32_t sp, uint32_t last_hit, D& draws,
                                        V3<T>& disp, WallHit<T>& closest, WallHit<T>& tentative,
                                        uint32_t& err) {
+  if (g.wsp_off[sp] == g.wsp_off[sp + 1]) return false;  // no wall listed here
   int redo = 0;
 restart:
   bool found = false;
@@ -1609,7 +1611,12 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
       const P4<T> q = cells.pos[c.idx];
       const uint64_t cuid = cells.uid[c.idx];
       const V3<T> cpos = pos_at_start + scale(remaining, c.t);  // collide_mol's rel_collision_pos
-      const T factor = exact_disk(g, cpos, remaining, species, v3<T>(q.x, q.y, q.z));
+      // exact_disk returns exactly 1 when the collision point's subpartition lists no
+      // wall (its wall loop finds no edge); the call is skipped then
+      const uint32_t csp = subpart_of(g, cpos);
+      const T factor = g.wsp_off[csp] == g.wsp_off[csp + 1]
+                           ? (T)1
+                           : exact_disk(g, cpos, remaining, species, v3<T>(q.x, q.y, q.z));
       if (factor < 0) {
         ev.put(6, cuid, 0, (double)c.t, t_abs, (double)cpos.x, (double)cpos.y, (double)cpos.z);
         continue;
