@@ -8,8 +8,8 @@ by properties that hold at any size:
   - determinism (same seed -> identical molecules, ids and counts),
   - closed forms: mean squared displacement 6 D t, unimolecular decay exp(-k t),
   - transparency (A crosses the sphere, B never does) and absorption,
-and by ensemble statistics against the oracle's serial engine (north-star
-check (b)): mean counts within 3 standard errors.
+and by ensemble statistics against the oracle's serial engine: mean counts
+within 3 standard errors.
 """
 import numpy as np
 import pytest

@@ -1,4 +1,4 @@
-"""GPU parity of the per-molecule step (spec check (a)).
+"""GPU parity of the per-molecule step: the per-routine harness with injected draws.
 
 The CUDA device functions that the production kernel runs are driven through
 the C ABI (mcg_trace_cases) with injected displacements and injected 32-bit
