@@ -50,7 +50,18 @@ class DeviceEngineT : public DeviceEngine {
     MCG_CUDA(cudaGetDevice(&dev));
     MCG_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
     {
-      // k_diffuse runs persistent warps: as many blocks as can be resident
+      // k_diffuse runs persistent warps: as many blocks as can be resident. It uses no
+      // shared memory; its spills and per-thread arrays live in local memory, cached in
+      // L1, so the whole L1/shared carveout goes to L1.
+#ifndef MCG_DIFFUSE_CARVEOUT
+#define MCG_DIFFUSE_CARVEOUT 0
+#endif
+      if (MCG_DIFFUSE_CARVEOUT >= 0) {
+        MCG_CUDA(cudaFuncSetAttribute(k_diffuse<T, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      MCG_DIFFUSE_CARVEOUT));
+        MCG_CUDA(cudaFuncSetAttribute(k_diffuse<T, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      MCG_DIFFUSE_CARVEOUT));
+      }
       int bps = 1;
       MCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_diffuse<T, false>, TPB, 0));
       bps_max_ = std::max(1, bps);
