@@ -382,8 +382,10 @@ def run_precision(args):
     """fp32 engine (fp64 tie-breaks) against the fp64 engine on the bumpy tube:
     wall-hit identity on 100,000 traced cases of the full model (10M molecules,
     200,400 triangles; half of the cases start within 1 nm of an edge or vertex),
-    and the count trajectories of a 1M-molecule tube over 50 iterations (the full
-    model runs ~3 s per fp64 iteration)."""
+    once with each engine at its own stored positions and once with the fp64 engine
+    at the fp32 engine's (trace arithmetic alone), and the count trajectories of a
+    1M-molecule tube over 50 iterations (the full model runs ~3 s per fp64
+    iteration)."""
     import numpy as np
 
     from mcell_gb300 import precision
@@ -393,12 +395,14 @@ def run_precision(args):
     n = len(m.species)
     near = np.arange(n - int(round(0.05 * n)), n)
     mism = precision.wall_hit_mismatch(m, n_cases=100_000, near_ids=near)
+    mism_same = precision.wall_hit_mismatch(m, n_cases=100_000, near_ids=near, same_start=True)
     del m
     small = W.bumpy_tube(n_mol=1_000_000, seed=2)
     cnt = precision.count_error(small, n_iter=50)
     return {"workload": "bumpy tube r = 0.2 um (+-0.05 um), 10 um, 200,400 reflective triangles, 5% of the molecules "
                         "within 1 nm of edges/vertices, A+B->C, dt 0.1 us",
-            "wall_hit_mismatch_10M": mism, "count_error_1M_50_iterations": cnt}
+            "wall_hit_mismatch_10M": mism, "wall_hit_mismatch_10M_same_start": mism_same,
+            "count_error_1M_50_iterations": cnt}
 
 
 # ---------------------------------------------------------------- serving form

@@ -741,7 +741,16 @@ __device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V
   cpos = pos + scale(move, a);
   const WallFace<T>& w = g.wface[wi];
   V3<T> local = cpos - w.v0;
-  int tr = tri_test<T>(dot(local, w.u), dot(local, w.v), w.uv1u, w.uv2u, w.uv2v, Eps<T>::pos);
+  // fp32: a crossing within the rounding of this computation of an edge (16 ulp of
+  // the coordinates: cpos and v0 each carry about one) is decided in fp64 by
+  // edge_test_fp64. POS_EPS alone is far narrower than fp32's rounding away from the
+  // origin, where the fp32 test would otherwise pick the neighbour across the edge.
+  T teps = Eps<T>::pos;
+  if (sizeof(T) == 4) {
+    const T mag = tmax(tmax(tabs(cpos.x), tabs(cpos.y)), tmax(tabs(cpos.z), (T)1));
+    teps = tmax(teps, mag * (T)(16.0 * 1.1920928955078125e-07));
+  }
+  int tr = tri_test<T>(dot(local, w.u), dot(local, w.v), w.uv1u, w.uv2u, w.uv2v, teps);
   if (sizeof(T) == 4 && tr >= TRI_E12) {
     tr = edge_test_fp64<T>(g.w64 + 16 * (size_t)wi, pos, move, tr, ct, cpos, dv);
     if (tr < 0) return CT_MISS;

@@ -5,7 +5,11 @@ follows the reference routines bit for bit.
 wall_hit_mismatch  the same diffusion cases (start molecule, injected
                    displacement and random draws) traced by both engines
                    through mcg_trace_cases; a case mismatches when the sequence
-                   of wall events (kind and wall) differs
+                   of wall events (kind and wall) differs. Two readings: each
+                   engine starts from its own stored position (fp32 storage
+                   rounds it, by up to half an ulp of the coordinate), or
+                   (same_start) the fp64 engine holds the fp32 engine's stored
+                   positions, so only the trace arithmetic differs
 count_error        both engines run the model for n iterations with the same
                    seed; the species-count trajectories are compared, next to
                    two fp64 runs with different seeds (the stochastic scale)
@@ -28,11 +32,27 @@ def _wall_events(rows):
     return out
 
 
-def wall_hit_mismatch(model: W.Model, n_cases=100_000, near_ids=None, seed=5, chunk=20_000, e32=None, e64=None):
+def fp32_stored(model: W.Model, e32=None) -> W.Model:
+    """The model with each molecule at the position the fp32 engine stores for it
+    (rounded to fp32 and, within a few ulp of a wall plane, moved off it on upload)."""
+    from dataclasses import replace
+    own = e32 is None
+    e32 = e32 or W.engine_for(model, "fp32", seed=1)
+    pos, sp, ids = e32.molecules()
+    if own:
+        e32.close()
+    out = np.empty_like(model.pos)
+    out[ids.astype(np.int64)] = pos
+    return replace(model, pos=out)
+
+
+def wall_hit_mismatch(model: W.Model, n_cases=100_000, near_ids=None, seed=5, chunk=20_000, e32=None, e64=None,
+                      same_start=False):
     """Fraction of cases whose wall events differ between fp32 and fp64, and the
     largest final-position difference among the cases that agree (internal units).
     Half of the cases start from near_ids (e.g. molecules released next to edges)
-    when given. Displacements are Gaussian with the species' space step."""
+    when given. Displacements are Gaussian with the species' space step.
+    same_start: the fp64 engine starts from the fp32 engine's stored positions."""
     rng = np.random.default_rng(seed)
     n_mol = len(model.species)
     if near_ids is not None and len(near_ids):
@@ -44,7 +64,7 @@ def wall_hit_mismatch(model: W.Model, n_cases=100_000, near_ids=None, seed=5, ch
     draws = rng.integers(0, 2 ** 32, size=(n_cases, 64), dtype=np.uint64).astype(np.uint32)
     own32, own64 = e32 is None, e64 is None
     e32 = e32 or W.engine_for(model, "fp32", seed=1)
-    e64 = e64 or W.engine_for(model, "fp64", seed=1)
+    e64 = e64 or W.engine_for(fp32_stored(model, e32) if same_start else model, "fp64", seed=1)
     mism, err, hits = 0, 0.0, 0
     for a in range(0, n_cases, chunk):
         b = min(n_cases, a + chunk)
@@ -61,7 +81,7 @@ def wall_hit_mismatch(model: W.Model, n_cases=100_000, near_ids=None, seed=5, ch
     if own64:
         e64.close()
     return {"cases": n_cases, "cases_with_wall_events": hits, "mismatches": mism, "rate": mism / n_cases,
-            "max_position_error": err}
+            "max_position_error": err, "same_start": bool(same_start)}
 
 
 def count_error(model: W.Model, n_iter=50, seed=3):

@@ -3,7 +3,8 @@ molecules, 5% within 1 nm of mesh edges and vertices, dt = 0.1 us): the fp32
 engine against the fp64 engine (which follows the reference routines bit for bit).
 
 Bars: wall-hit identity mismatch rate below 1e-3 (half of the cases start next
-to edges), no molecule leaves the tube in either precision, and the product
+to edges) and below 2e-4 when both engines start from the fp32 engine's stored
+positions, no molecule leaves the tube in either precision, and the product
 count after 40 iterations within 3x the difference two fp64 seeds give."""
 import numpy as np
 import pytest
@@ -27,6 +28,17 @@ def test_fp32_wall_hits_match_fp64_near_edges(tube):
     assert r["cases_with_wall_events"] > 1000
     assert r["rate"] < 1e-3
     assert r["max_position_error"] < 0.1
+
+
+def test_fp32_trace_arithmetic_matches_fp64_from_the_same_start(tube):
+    # the fp64 engine holds the fp32 engine's stored positions: what remains is the
+    # fp32 ray arithmetic with its fp64 tie-breaks
+    n = len(tube.species)
+    near = np.arange(n - int(round(0.05 * n)), n)
+    r = precision.wall_hit_mismatch(tube, n_cases=40_000, near_ids=near, same_start=True)
+    print("tube fp32 vs fp64, same start:", r)
+    assert r["cases_with_wall_events"] > 1000
+    assert r["rate"] < 2e-4
 
 
 def test_fp32_counts_follow_fp64(tube):
