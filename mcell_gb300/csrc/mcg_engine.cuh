@@ -14,6 +14,7 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <thread>
 #include <unordered_map>
 
@@ -109,7 +110,7 @@ class DeviceEngineT : public DeviceEngine {
     }
     uint64_t n_new = 0;
     for (uint32_t k = 0; k < n; k++) n_new += specs[k].n_mol;
-    std::vector<Product<T>> stage(n_new);
+    std::unique_ptr<Product<T>[]> stage(new Product<T>[n_new]);  // filled below (no zeroing of 40 B/molecule)
     uint64_t staged = 0;
     for (uint32_t k = 0; k < n; k++) {
       const ReplicaSpec& sp = specs[k];
@@ -119,7 +120,7 @@ class DeviceEngineT : public DeviceEngine {
         for (uint32_t j = 0; j <= k; j++) free_replica(slots[j]);
         return rc;
       }
-      rc = stage_molecules(r, sp.n_mol, sp.pos, sp.species, 0, stage.data() + staged, err);
+      rc = stage_molecules(r, sp.n_mol, sp.pos, sp.species, 0, stage.get() + staged, err);
       staged += sp.n_mol;
       if (rc) {
         for (uint32_t j = 0; j <= k; j++) free_replica(slots[j]);
@@ -146,7 +147,7 @@ class DeviceEngineT : public DeviceEngine {
     }
     int rc = layout_keys(err);
     if (rc) return rc;
-    return rebin(stage.data(), n_new, err, true);
+    return rebin(stage.get(), n_new, err, true);
   }
 
   int remove_replicas(const uint32_t* reps, uint32_t n, std::string& err) override {
@@ -177,12 +178,12 @@ class DeviceEngineT : public DeviceEngine {
       err = "no such replica";
       return -1;
     }
-    std::vector<Product<T>> stage(n);
-    int rc = stage_molecules(rep, n, pos, species, uid0, stage.data(), err);
+    std::unique_ptr<Product<T>[]> stage(new Product<T>[n]);  // filled by stage_molecules
+    int rc = stage_molecules(rep, n, pos, species, uid0, stage.get(), err);
     if (rc) return rc;
     reps_[rep].next_uid = std::max<uint64_t>(reps_[rep].next_uid, uid0 + n);
     if (read_counters(err)) return -2;
-    return rebin(stage.data(), n, err, true);
+    return rebin(stage.get(), n, err, true);
   }
 
   int step(uint32_t n, std::string& err) override {
@@ -394,8 +395,8 @@ class DeviceEngineT : public DeviceEngine {
       err = "a checkpoint is loaded into a prepared engine before any molecule or iteration";
       return -1;
     }
-    std::vector<Product<T>> stage(n);
-    int rc = stage_molecules(rep, n, pos, species, 0, stage.data(), err);
+    std::unique_ptr<Product<T>[]> stage(new Product<T>[n]);  // filled by stage_molecules
+    int rc = stage_molecules(rep, n, pos, species, 0, stage.get(), err);
     if (rc) return rc;
     for (uint64_t i = 0; i < n; i++) {
       stage[i].uid = ids[i];
@@ -412,7 +413,7 @@ class DeviceEngineT : public DeviceEngine {
     cnt_ = c;
     geos_h_[rep].it0 = 0;
     MCG_CUDA(cudaMemcpyAsync(d_geos_, geos_h_.data(), sizeof(Geo<T>) * max_rep_, cudaMemcpyHostToDevice, stream_));
-    rc = rebin(stage.data(), n, err);
+    rc = rebin(stage.get(), n, err);
     rebin_it_ = cnt_.iteration;
     return rc;
   }
@@ -918,7 +919,8 @@ class DeviceEngineT : public DeviceEngine {
     const Geo<T>& g = geos_h_[r];
     const double o[3] = {(double)g.origin.x, (double)g.origin.y, (double)g.origin.z};
     const double q[3] = {(double)g.opposite.x, (double)g.opposite.y, (double)g.opposite.z};
-    // large uploads are staged by several host threads (independent ranges)
+    // large uploads are staged by all host threads (independent ranges; the wall-plane
+    // checks of place_fp32 dominate: ~4 ns per molecule on 8 Arm cores)
     auto work = [&](uint64_t a, uint64_t b) -> int {
       for (uint64_t i = a; i < b; i++) {
         if (species[i] >= nsp_) return -1;
@@ -937,7 +939,7 @@ class DeviceEngineT : public DeviceEngine {
       }
       return 0;
     };
-    const unsigned nt = n < 200000 ? 1u : std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+    const unsigned nt = n < 200000 ? 1u : std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
     std::vector<int> rcs(nt, 0);
     std::vector<std::thread> th;
     for (unsigned t = 1; t < nt; t++) th.emplace_back([&, t] { rcs[t] = work(n * t / nt, n * (t + 1) / nt); });
