@@ -187,10 +187,13 @@ class DeviceEngineT : public DeviceEngine {
   }
 
   int step(uint32_t n, std::string& err) override {
-    if (nkeys_ == 0 || cap_ == 0) {
-      err = "no molecules";
+    if (nkeys_ == 0) {
+      err = "no replica to step";
       return -1;
     }
+    // a model without molecules yet (a release may add them later) steps on empty arrays,
+    // as the reference's event does with an empty molecule list
+    if (cap_ == 0 && ensure_capacity(1024, err)) return -2;
     uint32_t done = 0;
     while (done < n) {
       if (n - done >= 2 && use_graphs_ && !profile_) {

@@ -57,3 +57,29 @@ def test_releases(precision):
     h.step(5)
     h.sync()
     h.close()
+
+
+def test_model_without_molecules_steps_then_takes_a_release():
+    # no molecules and no capacity reserved: the iterations run on empty arrays (counts
+    # zero), as the reference's event does with an empty list; a release then fills it
+    from mcell_gb300._native import Engine
+    m, obj = _model()
+    h = Engine("fp32", m.origin, m.partition_edge, m.nsub, m.rxn_radius, m.n_species, seed=5, capacity=0)
+    h.set_species(m.space_steps)
+    h.upload_mesh(m.verts, m.walls, m.wall_class)
+    for a, b, p, pr in m.bimol:
+        h.add_bimol_rxn(a, b, p, pr)
+    for a, k, pr in m.unimol:
+        h.add_unimol_rxn(a, k, pr)
+    h.set_wall_objects(obj)
+    h.prepare()
+    h.step(3)
+    assert (h.counts() == 0).all()
+    assert (h.trajectory(3) == 0).all()
+    h.release(0, 5000, "inside", obj=0, seed=21)
+    h.step(4)
+    c = h.counts()
+    assert c[0] + c[2] == 5000 and c[1] == 0
+    it, steps, _ = h.stats()
+    assert it == 7 and steps >= 4 * 4000
+    h.close()
