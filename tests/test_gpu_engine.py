@@ -8,6 +8,8 @@ by properties that hold at any size:
   - determinism (same seed -> identical molecules, ids and counts),
   - closed forms: mean squared displacement 6 D t, unimolecular decay exp(-k t),
   - transparency (A crosses the sphere, B never does) and absorption,
+  - the well-mixed A + B -> C rate against the second-order law, and a uniform
+    density after a long run in a reflective box,
 and by ensemble statistics against the oracle's serial engine: mean counts
 within 3 standard errors.
 """
@@ -208,3 +210,52 @@ def test_fp32_molecules_released_on_walls_stay_inside():
     e.sync()  # raises MCG_ERR_ESCAPE on a leak
     p, _, _ = e.molecules()
     assert len(p) == n and (np.abs(p) <= float(np.float32(h))).all()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_well_mixed_rate_follows_mass_action(precision):
+    """A + B -> C at k = 1e8 /M/s, 5,000 + 5,000 molecules in a 1 um cube: C(t) against
+    the second-order law N0 - N0 / (1 + k' N0 t), k' = k / (N_A V). The reference's
+    algorithm sits a few percent below it here (walls occlude part of the reaction disk
+    near the faces; the oracle's serial engine gives 0.96 at 100 iterations), so the
+    band is 0.90-1.02 of the law, over four seeds."""
+    from mcell_gb300 import conversion as C
+    lu, R, dt, k, n0, n_iter = C.length_unit_um(), C.default_rxn_radius_um(), 1e-6, 1e8, 5000, 100
+    ss = C.space_step(1e-6, dt, lu)
+    p = C.bimol_probability(k, ss, ss, R, dt, lu)
+    km = k / (C.N_AV * 1e-15)
+    got = []
+    for seed in range(4):
+        rng = np.random.default_rng(50 + seed)
+        sc = H.cube_scene(rng, n_mol=2 * n0)
+        sc.mol_species = np.repeat(np.array([0, 1], np.uint32), n0)
+        e = H.make_gpu_engine(sc, precision, bimol=[(0, 1, p, (2, -1))], seed=seed + 1)
+        e.step(n_iter)
+        got.append(float(e.counts()[2]))
+        e.close()
+    law = n0 - n0 / (1 + km * n0 * n_iter * dt)
+    ratio = np.mean(got) / law
+    print(f"C after {n_iter} it: {np.mean(got):.1f} (law {law:.1f}, ratio {ratio:.3f})")
+    assert 0.90 < ratio < 1.02
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_density_becomes_uniform_in_a_reflective_box(precision):
+    """20,000 molecules released in one corner octant of a closed 1 um cube spread over
+    it: after 10,000 iterations (10 ms; the slowest box mode has decayed to
+    exp(-pi^2 D t / L^2) = 5e-5) the counts in 8 x 8 x 8 cells pass a chi-square test
+    of uniformity (511 degrees of freedom, 5 standard deviations), and none is lost."""
+    rng = np.random.default_rng(8)
+    sc = H.cube_scene(rng, n_mol=20000)
+    half = 50.0
+    sc.mol_pos = rng.uniform(-half, 0.0, size=(20000, 3))
+    e = H.make_gpu_engine(sc, precision, seed=3)
+    e.step(10000)
+    pos, sp, ids = e.molecules()
+    assert len(ids) == 20000
+    h, _ = np.histogramdd(pos, bins=8, range=[(-half, half)] * 3)
+    expected = 20000 / 512
+    chi2 = ((h - expected) ** 2 / expected).sum()
+    print(f"chi2 {chi2:.1f} (511 dof)")
+    assert chi2 < 511 + 5 * np.sqrt(2 * 511)
+    e.close()
