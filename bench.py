@@ -146,6 +146,20 @@ def _traffic_per_mol_step():
     return None
 
 
+def combine_ranks(seconds, units, world, device):
+    """Whole-job figures of a replicas-only run: the slowest rank's time (max) and the
+    units every rank processed (sum). One rank: the inputs. `device` is where the
+    reduction tensors live ("cuda" under NCCL, "cpu" under gloo)."""
+    if world <= 1:
+        return float(seconds), float(units)
+    import torch
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    n = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.all_reduce(n, op=torch.distributed.ReduceOp.SUM)
+    return t.item(), n.item()
+
+
 def run_gpu(args, rank, world):
     import numpy as np
     import torch
@@ -181,12 +195,8 @@ def run_gpu(args, rank, world):
     clocks = clk.summary()
     mol_steps = ms1 - ms0
     iter_ms = prof[0]
-    t = torch.tensor([iter_ms], dtype=torch.float64, device="cuda")
-    steps_t = torch.tensor([float(mol_steps)], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(steps_t, op=torch.distributed.ReduceOp.SUM)
-    value = steps_t.item() / (t.item() / 1e3)
+    t_ms, all_steps = combine_ranks(iter_ms, mol_steps, world, "cuda")
+    value = all_steps / (t_ms / 1e3)
     diffuse_ms_per_launch = prof[1] / args.steps
     mols_per_launch = mol_steps / args.steps
     achieved = ALG_BYTES_PER_MOL_STEP * mols_per_launch / (diffuse_ms_per_launch / 1e3) / 1e9
@@ -219,15 +229,11 @@ def run_gpu(args, rank, world):
     e2_s = time.perf_counter() - t0
     _, e2_steps, _ = e2.stats()
     e2.close()
-    e2e_t = torch.tensor([e2_s], dtype=torch.float64, device="cuda")
-    e2e_n = torch.tensor([float(e2_steps)], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(e2e_n, op=torch.distributed.ReduceOp.SUM)
+    e2e_s_all, e2e_steps_all = combine_ranks(e2_s, e2_steps, world, "cuda")
     h2d = pos.nbytes + sp.nbytes
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": t.item() / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded uniform release; icosphere + cube mesh generated)",
         "config": {"workload": "sphere_in_cube: icosphere r=1um 20480 tris transparent to A in a 2.5um "
@@ -239,7 +245,7 @@ def run_gpu(args, rank, world):
                      "peak_kind": peak_kind, "kernel": "k_diffuse",
                      "algorithmic_bytes_per_mol_step": ALG_BYTES_PER_MOL_STEP,
                      "traffic": (tpm * mols_per_launch) if tpm else None},
-        "e2e": {"value": e2e_n.item() / e2e_t.item(), "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
+        "e2e": {"value": e2e_steps_all / e2e_s_all, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
                 "d2h_bytes_per_step": 8 * model.n_species},
         "gpu_launches": int(l1 - l0),
         "clocks": clocks,
