@@ -107,6 +107,12 @@ int mcg_get_stats(mcg_engine* e, uint64_t* iterations, uint64_t* mol_steps, uint
    default on) and profile (record CUDA events around the kernel groups of each
    iteration; implies no graphs). */
 int mcg_set_options(mcg_engine* e, int use_graphs, int profile);
+/* Test hook (no counterpart in the reference): the device allocation that follows
+   `after` more successful ones, in any engine of the process, fails as if the device
+   were out of memory (once; the call returns MCG_ERR_CUDA); a negative value turns it
+   off. Lets tests run the out-of-memory paths (no leak, the engine left as it was)
+   without exhausting HBM. */
+int mcg_inject_device_alloc_failure(int64_t after);
 /* Profile since the last call: out[0] iteration ms, [1] diffuse kernel ms, [2] reaction
    resolution ms, [3] products ms, [4] sort (scan + scatter) ms, [5] iterations profiled. */
 int mcg_get_profile(mcg_engine* e, double* out);

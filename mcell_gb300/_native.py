@@ -24,7 +24,7 @@ EXPORTS = [
     "mcg_create", "mcg_destroy", "mcg_last_error", "mcg_set_species", "mcg_upload_mesh", "mcg_add_bimol_rxn",
     "mcg_add_unimol_rxn", "mcg_add_molecules", "mcg_step", "mcg_sync", "mcg_get_counts",
     "mcg_get_count_trajectory", "mcg_download_molecules", "mcg_get_stats", "mcg_prepare", "mcg_trace_cases",
-    "mcg_wall_consts", "mcg_walls_in_subparts", "mcg_set_options", "mcg_get_profile",
+    "mcg_wall_consts", "mcg_walls_in_subparts", "mcg_set_options", "mcg_inject_device_alloc_failure", "mcg_get_profile",
     "mcg_get_escapes", "mcg_debug_molecule", "mcg_get_debug_log", "mcg_trace_cases_static",
     "mcg_batch_create", "mcg_batch_destroy", "mcg_batch_last_error", "mcg_batch_add", "mcg_batch_remove",
     "mcg_batch_step", "mcg_batch_sync", "mcg_batch_replica_info", "mcg_batch_get_counts",
@@ -127,6 +127,12 @@ def lib():
 
 def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def inject_device_alloc_failure(after):
+    """Test hook: the device allocation after `after` more successful ones fails as if
+    out of memory (once); None or a negative value turns it off."""
+    lib().mcg_inject_device_alloc_failure(ctypes.c_int64(-1 if after is None else int(after)))
 
 
 class Engine:

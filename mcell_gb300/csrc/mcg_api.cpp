@@ -232,6 +232,11 @@ int mcg_set_options(mcg_engine* e, int use_graphs, int profile) {
   return MCG_OK;
 }
 
+int mcg_inject_device_alloc_failure(int64_t after) {
+  mcg::set_alloc_failure((long long)after);
+  return MCG_OK;
+}
+
 int mcg_get_profile(mcg_engine* e, double* out) {
   if (!e || !out || !e->dev) return MCG_ERR_ARG;
   std::string err;

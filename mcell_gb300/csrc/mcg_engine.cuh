@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <array>
 #include <climits>
 #include <cmath>
@@ -23,6 +24,41 @@
 #include "mcg_trace_static.h"
 
 namespace mcg {
+
+// Device allocations go through dev_malloc. A test hook (mcg_inject_device_alloc_failure)
+// can make one of them fail as if the device were out of memory, so that the error
+// paths (status codes, no leak, the engine left as it was) run without exhausting HBM.
+inline std::atomic<long long>& alloc_failure_countdown() {
+  static std::atomic<long long> c{-1};
+  return c;
+}
+template <typename P>
+inline cudaError_t dev_malloc(P** p, size_t bytes) {
+  *p = nullptr;
+  if (alloc_failure_countdown().load() >= 0 && alloc_failure_countdown().fetch_sub(1) == 0)
+    return cudaErrorMemoryAllocation;
+  return cudaMalloc((void**)p, bytes);
+}
+
+// The allocations of one resize: freed together unless the resize commits them, so a
+// failed resize leaks nothing and leaves the engine's buffers as they were.
+struct AllocSet {
+  std::vector<void*> ptrs;
+  bool keep = false;
+  AllocSet() = default;
+  AllocSet(const AllocSet&) = delete;
+  AllocSet& operator=(const AllocSet&) = delete;
+  ~AllocSet() {
+    if (!keep)
+      for (void* p : ptrs) cudaFree(p);
+  }
+  template <typename P>
+  cudaError_t get(P** p, size_t bytes) {
+    cudaError_t e = dev_malloc(p, bytes);
+    if (e == cudaSuccess) ptrs.push_back((void*)*p);
+    return e;
+  }
+};
 
 #define MCG_CUDA(call)                                                             \
   do {                                                                             \
@@ -77,14 +113,14 @@ class DeviceEngineT : public DeviceEngine {
       geos_h_[r].nsp = (int)nsp;
       geos_h_[r].rep = r;
     }
-    MCG_CUDA(cudaMalloc(&d_geos_, sizeof(Geo<T>) * max_rep));
+    MCG_CUDA(dev_malloc(&d_geos_, sizeof(Geo<T>) * max_rep));
     MCG_CUDA(cudaMemcpyAsync(d_geos_, geos_h_.data(), sizeof(Geo<T>) * max_rep, cudaMemcpyHostToDevice, stream_));
     // count trajectory ring: [row][replica][species], at most 64 MB
     const uint64_t row_bytes = sizeof(unsigned long long) * (uint64_t)max_rep * nsp;
     traj_cap_ = (uint32_t)std::max<uint64_t>(64, std::min<uint64_t>(65536, (64ull << 20) / row_bytes));
-    MCG_CUDA(cudaMalloc(&d_traj_, row_bytes * traj_cap_));
+    MCG_CUDA(dev_malloc(&d_traj_, row_bytes * traj_cap_));
     MCG_CUDA(cudaMemsetAsync(d_traj_, 0, row_bytes * traj_cap_, stream_));
-    MCG_CUDA(cudaMalloc(&d_cnt_, sizeof(Counters)));
+    MCG_CUDA(dev_malloc(&d_cnt_, sizeof(Counters)));
     MCG_CUDA(cudaMemsetAsync(d_cnt_, 0, sizeof(Counters), stream_));
     base_.geos = d_geos_;
     base_.n_rep = max_rep;
@@ -134,12 +170,18 @@ class DeviceEngineT : public DeviceEngine {
     if (any_cv && !d_cv_count_) {
       const size_t nq = (size_t)max_rep_ * nsp_ * MAX_COUNTED;
       cv_traj_cap_ = std::min<uint32_t>(traj_cap_, 4096);
-      MCG_CUDA(cudaMalloc(&d_cv_count_, sizeof(uint32_t) * nq));
-      MCG_CUDA(cudaMalloc(&d_cv_now_, sizeof(uint32_t) * nq));
-      MCG_CUDA(cudaMalloc(&d_cv_traj_, sizeof(uint32_t) * nq * cv_traj_cap_));
-      MCG_CUDA(cudaMemsetAsync(d_cv_count_, 0, sizeof(uint32_t) * nq, stream_));
-      MCG_CUDA(cudaMemsetAsync(d_cv_now_, 0, sizeof(uint32_t) * nq, stream_));
-      MCG_CUDA(cudaMemsetAsync(d_cv_traj_, 0, sizeof(uint32_t) * nq * cv_traj_cap_, stream_));
+      AllocSet a;
+      uint32_t *cc, *cn, *ct;
+      MCG_CUDA(a.get(&cc, sizeof(uint32_t) * nq));
+      MCG_CUDA(a.get(&cn, sizeof(uint32_t) * nq));
+      MCG_CUDA(a.get(&ct, sizeof(uint32_t) * nq * cv_traj_cap_));
+      MCG_CUDA(cudaMemsetAsync(cc, 0, sizeof(uint32_t) * nq, stream_));
+      MCG_CUDA(cudaMemsetAsync(cn, 0, sizeof(uint32_t) * nq, stream_));
+      MCG_CUDA(cudaMemsetAsync(ct, 0, sizeof(uint32_t) * nq * cv_traj_cap_, stream_));
+      a.keep = true;
+      d_cv_count_ = cc;
+      d_cv_now_ = cn;
+      d_cv_traj_ = ct;
       base_.cv_count = d_cv_count_;
       base_.cv_now = d_cv_now_;
       base_.cv_traj = d_cv_traj_;
@@ -507,12 +549,13 @@ class DeviceEngineT : public DeviceEngine {
     uint32_t* d_idx;
     double *d_disp, *d_rrf, *d_tst, *d_out;
     uint32_t* d_draws;
-    MCG_CUDA(cudaMalloc(&d_idx, sizeof(uint32_t) * nc));
-    MCG_CUDA(cudaMalloc(&d_disp, sizeof(double) * 3 * nc));
-    MCG_CUDA(cudaMalloc(&d_rrf, sizeof(double) * nc));
-    MCG_CUDA(cudaMalloc(&d_tst, sizeof(double) * nc));
-    MCG_CUDA(cudaMalloc(&d_out, sizeof(double) * 265 * nc));
-    MCG_CUDA(cudaMalloc(&d_draws, sizeof(uint32_t) * std::max<uint64_t>((uint64_t)ndraws * nc, 1)));
+    AllocSet tmp;  // freed on every return
+    MCG_CUDA(tmp.get(&d_idx, sizeof(uint32_t) * nc));
+    MCG_CUDA(tmp.get(&d_disp, sizeof(double) * 3 * nc));
+    MCG_CUDA(tmp.get(&d_rrf, sizeof(double) * nc));
+    MCG_CUDA(tmp.get(&d_tst, sizeof(double) * nc));
+    MCG_CUDA(tmp.get(&d_out, sizeof(double) * 265 * nc));
+    MCG_CUDA(tmp.get(&d_draws, sizeof(uint32_t) * std::max<uint64_t>((uint64_t)ndraws * nc, 1)));
     MCG_CUDA(cudaMemcpyAsync(d_idx, idx.data(), sizeof(uint32_t) * nc, cudaMemcpyHostToDevice, stream_));
     MCG_CUDA(cudaMemcpyAsync(d_disp, disp, sizeof(double) * 3 * nc, cudaMemcpyHostToDevice, stream_));
     MCG_CUDA(cudaMemcpyAsync(d_rrf, rrf, sizeof(double) * nc, cudaMemcpyHostToDevice, stream_));
@@ -523,12 +566,6 @@ class DeviceEngineT : public DeviceEngine {
     MCG_CUDA(cudaGetLastError());
     MCG_CUDA(cudaStreamSynchronize(stream_));
     MCG_CUDA(d2h(out, d_out, sizeof(double) * 265 * nc));
-    cudaFree(d_idx);
-    cudaFree(d_disp);
-    cudaFree(d_rrf);
-    cudaFree(d_tst);
-    cudaFree(d_out);
-    cudaFree(d_draws);
     return 0;
   }
 
@@ -615,7 +652,7 @@ class DeviceEngineT : public DeviceEngine {
 
   int debug_molecule(uint64_t uid, std::string& err) override {
     if (!d_debug_) {
-      MCG_CUDA(cudaMalloc(&d_debug_, sizeof(double) * 64 * 271));
+      MCG_CUDA(dev_malloc(&d_debug_, sizeof(double) * 64 * 271));
     }
     MCG_CUDA(cudaMemsetAsync(d_debug_, 0, sizeof(double) * 64 * 271, stream_));
     base_.debug_uid = uid;
@@ -740,7 +777,7 @@ class DeviceEngineT : public DeviceEngine {
   template <typename V>
   int alloc_copy(V** d, const std::vector<V>& h, uint64_t& bytes, std::string& err) {
     const size_t sz = sizeof(V) * std::max<size_t>(h.size(), 1);
-    MCG_CUDA(cudaMalloc((void**)d, sz));
+    MCG_CUDA(dev_malloc((void**)d, sz));
     bytes += sz;
     if (!h.empty()) MCG_CUDA(cudaMemcpyAsync(*d, h.data(), sizeof(V) * h.size(), cudaMemcpyHostToDevice, stream_));
     return 0;
@@ -978,24 +1015,26 @@ class DeviceEngineT : public DeviceEngine {
     nkeys_ = (uint32_t)k;
     if (nkeys_ > key_alloc_) {
       const uint64_t na = std::max<uint64_t>(nkeys_, (uint64_t)key_alloc_ * 5 / 4);
+      AllocSet a;
+      uint32_t *st[2], *cn, *cu, *ti;
+      for (int p = 0; p < 2; p++) MCG_CUDA(a.get(&st[p], sizeof(uint32_t) * (na + 1)));
+      MCG_CUDA(a.get(&cn, sizeof(uint32_t) * na));
+      MCG_CUDA(a.get(&cu, sizeof(uint32_t) * na));
+      MCG_CUDA(a.get(&ti, sizeof(uint32_t) * ((na + SCAN_TILE - 1) / SCAN_TILE + 1)));
+      for (int p = 0; p < 2; p++) MCG_CUDA(cudaMemsetAsync(st[p], 0, sizeof(uint32_t) * (na + 1), stream_));
+      MCG_CUDA(cudaMemsetAsync(cn, 0, sizeof(uint32_t) * na, stream_));
+      MCG_CUDA(cudaMemsetAsync(cu, 0, sizeof(uint32_t) * na, stream_));
+      a.keep = true;
       for (int p = 0; p < 2; p++) {
         cudaFree(d_start_[p]);
-        d_start_[p] = nullptr;
+        d_start_[p] = st[p];
       }
       cudaFree(d_counts_);
       cudaFree(d_cursor_);
       cudaFree(d_tile_);
-      d_counts_ = d_cursor_ = d_tile_ = nullptr;
-      key_alloc_ = 0;
-      for (int p = 0; p < 2; p++) {
-        MCG_CUDA(cudaMalloc(&d_start_[p], sizeof(uint32_t) * (na + 1)));
-        MCG_CUDA(cudaMemsetAsync(d_start_[p], 0, sizeof(uint32_t) * (na + 1), stream_));
-      }
-      MCG_CUDA(cudaMalloc(&d_counts_, sizeof(uint32_t) * na));
-      MCG_CUDA(cudaMemsetAsync(d_counts_, 0, sizeof(uint32_t) * na, stream_));
-      MCG_CUDA(cudaMalloc(&d_cursor_, sizeof(uint32_t) * na));
-      MCG_CUDA(cudaMemsetAsync(d_cursor_, 0, sizeof(uint32_t) * na, stream_));
-      MCG_CUDA(cudaMalloc(&d_tile_, sizeof(uint32_t) * ((na + SCAN_TILE - 1) / SCAN_TILE + 1)));
+      d_counts_ = cn;
+      d_cursor_ = cu;
+      d_tile_ = ti;
       key_alloc_ = (uint32_t)na;
     }
     base_.nkeys = nkeys_;
@@ -1079,21 +1118,49 @@ class DeviceEngineT : public DeviceEngine {
       std::string e2;
       if (sync(e2) < -1) return -2;
     }
+    // every new buffer first; the old ones are replaced only when all exist
+    AllocSet a;
     P4<T>* np[2];
     uint64_t* nu[2];
     T* nt[2];
     for (int k = 0; k < 2; k++) {
-      MCG_CUDA(cudaMalloc(&np[k], sizeof(P4<T>) * cap));
-      MCG_CUDA(cudaMalloc(&nu[k], sizeof(uint64_t) * cap));
-      MCG_CUDA(cudaMalloc(&nt[k], sizeof(T) * cap));
-      if (cap_) {
-        MCG_CUDA(cudaMemcpyAsync(np[k], pos_[k], sizeof(P4<T>) * cap_, cudaMemcpyDeviceToDevice, stream_));
-        MCG_CUDA(cudaMemcpyAsync(nu[k], uid_[k], sizeof(uint64_t) * cap_, cudaMemcpyDeviceToDevice, stream_));
-        MCG_CUDA(cudaMemcpyAsync(nt[k], tuni_[k], sizeof(T) * cap_, cudaMemcpyDeviceToDevice, stream_));
-        cudaFree(pos_[k]);
-        cudaFree(uid_[k]);
-        cudaFree(tuni_[k]);
-      }
+      MCG_CUDA(a.get(&np[k], sizeof(P4<T>) * cap));
+      MCG_CUDA(a.get(&nu[k], sizeof(uint64_t) * cap));
+      MCG_CUDA(a.get(&nt[k], sizeof(T) * cap));
+    }
+    // every molecule can propose once per iteration (dense models at high rates
+    // propose with a large share of their molecules)
+    const uint64_t pc = std::max<uint64_t>(4096, cap);
+    P4<T>* nb;
+    uint8_t* nst;
+    uint64_t* ncl;
+    Proposal *npr, *nre;
+    uint32_t* nlo;
+    MCG_CUDA(a.get(&nb, sizeof(P4<T>) * cap));
+    MCG_CUDA(a.get(&nst, cap));
+    MCG_CUDA(a.get(&ncl, sizeof(uint64_t) * cap));
+    MCG_CUDA(a.get(&npr, sizeof(Proposal) * pc));
+    MCG_CUDA(a.get(&nlo, sizeof(uint32_t) * 2 * pc));
+    MCG_CUDA(a.get(&nre, sizeof(Proposal) * pc));
+    // products: at most one per reactant of a bimolecular reaction with two products
+    Product<T>* nprod = nullptr;
+    uint8_t* npst = nullptr;
+    if (pc > base_.prod_cap) {
+      MCG_CUDA(a.get(&nprod, sizeof(Product<T>) * pc));
+      MCG_CUDA(a.get(&npst, pc));
+    }
+    for (int k = 0; k < 2 && cap_; k++) {
+      MCG_CUDA(cudaMemcpyAsync(np[k], pos_[k], sizeof(P4<T>) * cap_, cudaMemcpyDeviceToDevice, stream_));
+      MCG_CUDA(cudaMemcpyAsync(nu[k], uid_[k], sizeof(uint64_t) * cap_, cudaMemcpyDeviceToDevice, stream_));
+      MCG_CUDA(cudaMemcpyAsync(nt[k], tuni_[k], sizeof(T) * cap_, cudaMemcpyDeviceToDevice, stream_));
+    }
+    MCG_CUDA(cudaMemsetAsync(ncl, 0xFF, sizeof(uint64_t) * cap, stream_));
+    MCG_CUDA(cudaStreamSynchronize(stream_));
+    a.keep = true;
+    for (int k = 0; k < 2; k++) {
+      cudaFree(pos_[k]);
+      cudaFree(uid_[k]);
+      cudaFree(tuni_[k]);
       pos_[k] = np[k];
       uid_[k] = nu[k];
       tuni_[k] = nt[k];
@@ -1104,36 +1171,41 @@ class DeviceEngineT : public DeviceEngine {
     cudaFree(d_props_);
     cudaFree(d_losers_);
     cudaFree(d_redo_);
-    MCG_CUDA(cudaMalloc(&d_b_pos_, sizeof(P4<T>) * cap));
-    MCG_CUDA(cudaMalloc(&d_st_, cap));
-    MCG_CUDA(cudaMalloc(&d_claim_, sizeof(uint64_t) * cap));
-    MCG_CUDA(cudaMemsetAsync(d_claim_, 0xFF, sizeof(uint64_t) * cap, stream_));
-    // every molecule can propose once per iteration (dense models at high rates
-    // propose with a large share of their molecules)
-    uint64_t pc = std::max<uint64_t>(4096, cap);
-    MCG_CUDA(cudaMalloc(&d_props_, sizeof(Proposal) * pc));
-    MCG_CUDA(cudaMalloc(&d_losers_, sizeof(uint32_t) * 2 * pc));
-    MCG_CUDA(cudaMalloc(&d_redo_, sizeof(Proposal) * pc));
+    d_b_pos_ = nb;
+    d_st_ = nst;
+    d_claim_ = ncl;
+    d_props_ = npr;
+    d_losers_ = nlo;
+    d_redo_ = nre;
     base_.prop_cap = (uint32_t)pc;
     cap_ = cap;
     base_.cap = (uint32_t)cap;
-    // products: at most one per reactant of a bimolecular reaction with two products
-    if (ensure_prod(std::max<uint64_t>(4096, cap), err)) return -2;
+    if (nprod) adopt_prod(nprod, npst, pc);
     invalidate_graphs();
     return 0;
   }
 
   int ensure_prod(uint64_t pc, std::string& err) {
     if (pc <= base_.prod_cap) return 0;
+    AllocSet a;
+    Product<T>* nprod;
+    uint8_t* npst;
+    MCG_CUDA(a.get(&nprod, sizeof(Product<T>) * pc));
+    MCG_CUDA(a.get(&npst, pc));
+    a.keep = true;
+    adopt_prod(nprod, npst, pc);
+    invalidate_graphs();
+    return 0;
+  }
+
+  void adopt_prod(Product<T>* prod, uint8_t* pst, uint64_t pc) {
     cudaFree(d_prod_);
     cudaFree(d_pst_);
-    MCG_CUDA(cudaMalloc(&d_prod_, sizeof(Product<T>) * pc));
-    MCG_CUDA(cudaMalloc(&d_pst_, pc));
+    d_prod_ = prod;
+    d_pst_ = pst;
     base_.prod_cap = (uint32_t)pc;
     base_.prod = d_prod_;
     base_.pst = d_pst_;
-    invalidate_graphs();
-    return 0;
   }
 
   State<T> state(int parity) const {

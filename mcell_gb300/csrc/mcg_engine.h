@@ -100,6 +100,10 @@ class DeviceEngine {
   virtual int escapes(double* out, uint32_t cap, uint32_t* n, std::string& err) = 0;
 };
 
+// test hook: the device allocation after `after` more successful ones fails as if the
+// device were out of memory (once); negative: off (mcg_inject_device_alloc_failure)
+void set_alloc_failure(long long after);
+
 DeviceEngine* make_engine_f64();
 DeviceEngine* make_engine_f32();
 
