@@ -148,26 +148,48 @@ class DeviceEngineT : public DeviceEngine {
     for (uint32_t k = 0; k < n; k++) n_new += specs[k].n_mol;
     std::unique_ptr<Product<T>[]> stage(new Product<T>[n_new]);  // filled below (no zeroing of 40 B/molecule)
     uint64_t staged = 0;
+    // any failure before the re-sort leaves the engine as it was: the new slots are
+    // freed and the key space laid out again without them (it needs no new memory then)
+    auto undo = [&](int rc) {
+      for (uint32_t k = 0; k < n; k++) free_replica(slots[k]);
+      std::string e2;
+      layout_keys(e2);
+      return rc;
+    };
     for (uint32_t k = 0; k < n; k++) {
       const ReplicaSpec& sp = specs[k];
       const uint32_t r = slots[k];
       int rc = upload_replica(sp, r, err);
-      if (rc) {
-        for (uint32_t j = 0; j <= k; j++) free_replica(slots[j]);
-        return rc;
-      }
+      if (rc) return undo(rc);
       rc = stage_molecules(r, sp.n_mol, sp.pos, sp.species, 0, stage.get() + staged, err);
       staged += sp.n_mol;
-      if (rc) {
-        for (uint32_t j = 0; j <= k; j++) free_replica(slots[j]);
-        return rc;
-      }
+      if (rc) return undo(rc);
       reps_[r].next_uid = sp.n_mol;
       out_reps[k] = r;
     }
     bool any_cv = false;
     for (uint32_t k = 0; k < n; k++) any_cv = any_cv || !specs[k].counted.empty();
     if (any_cv && !d_cv_count_) {
+      int rc = alloc_counted(err);
+      if (rc) return undo(rc);
+    }
+    // room for the new molecules before the key space changes
+    if (cnt_.n_live + n_new > cap_) {
+      int rc = ensure_capacity(std::max<uint64_t>((cnt_.n_live + n_new) * 3 / 2, 1024), err);
+      if (rc) return undo(rc);
+    }
+    if (n_new > base_.prod_cap) {
+      int rc = ensure_prod(n_new, err);
+      if (rc) return undo(rc);
+    }
+    int rc = layout_keys(err);
+    if (rc) return undo(rc);
+    return rebin(stage.get(), n_new, err, true);
+  }
+
+  // counted-volume count arrays (allocated when the first replica counts a volume)
+  int alloc_counted(std::string& err) {
+    {
       const size_t nq = (size_t)max_rep_ * nsp_ * MAX_COUNTED;
       cv_traj_cap_ = std::min<uint32_t>(traj_cap_, 4096);
       AllocSet a;
@@ -187,9 +209,7 @@ class DeviceEngineT : public DeviceEngine {
       base_.cv_traj = d_cv_traj_;
       base_.cv_traj_cap = cv_traj_cap_;
     }
-    int rc = layout_keys(err);
-    if (rc) return rc;
-    return rebin(stage.get(), n_new, err, true);
+    return 0;
   }
 
   int remove_replicas(const uint32_t* reps, uint32_t n, std::string& err) override {

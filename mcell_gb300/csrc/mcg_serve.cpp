@@ -30,6 +30,7 @@ struct Request {
   uint64_t est_bytes = 0;       // device bytes reserved against the budget
   Clock::time_point t_submit, t_done;
   std::vector<uint64_t> traj;   // [iterations][n_species], harvested block by block
+  std::string err;              // why the request failed
 };
 
 }  // namespace
@@ -96,6 +97,20 @@ int serve_once(mcg_server* s, std::unique_lock<std::mutex>& lk) {
   lk.unlock();
   std::vector<uint32_t> ids(admit.size());
   int rc = admit.empty() ? MCG_OK : mcg_batch_add(s->batch, (uint32_t)admit.size(), models.data(), iters.data(), ids.data());
+  if (rc && mcg_batch_sync(s->batch) == MCG_OK) {
+    // the admission failed (device memory, a model the batch rejects) but left the
+    // batch as it was: those requests fail, the running ones go on
+    lk.lock();
+    const std::string why = std::string("admission: ") + s->batch->err;
+    for (uint64_t t : admit) {
+      Request& r = s->reqs[t];
+      r.state = MCG_REQ_FAILED;
+      r.err = why;
+      r.t_done = Clock::now();
+    }
+    s->cv_done.notify_all();
+    return MCG_OK;
+  }
   lk.lock();
   if (rc) return sfail(s, rc, std::string("admission: ") + s->batch->err);
   for (size_t k = 0; k < admit.size(); k++) {
@@ -295,6 +310,7 @@ int mcg_serve_result(mcg_server* s, uint64_t ticket, uint64_t* final_counts, uin
   auto it = s->reqs.find(ticket);
   if (it == s->reqs.end()) return sfail(s, MCG_ERR_ARG, "unknown ticket");
   const Request& r = it->second;
+  if (r.state == MCG_REQ_FAILED && !r.err.empty()) return sfail(s, MCG_ERR_CUDA, "request failed: " + r.err);
   if (r.state != MCG_REQ_DONE) return sfail(s, MCG_ERR_ARG, "request has no result (not done)");
   const uint32_t nsp = s->cfg.n_species;
   const uint32_t rows = (uint32_t)(r.traj.size() / nsp);

@@ -63,3 +63,36 @@ def test_failed_growth_keeps_the_engine_as_it_was():
     h.add_molecules(more, np.zeros(len(more), np.uint32))
     assert int(h.counts().sum()) == int(want[-1].sum()) + len(more)
     h.close()
+
+
+def test_server_fails_only_the_request_whose_admission_failed():
+    ms = W.replica_models(3, seed=41, n_range=(1_000, 4_000), edge_range_um=(0.5, 1.0), levels=(2, 3))
+    srv = _native.Server("fp32", 3, max_slots=4, autotune=False)
+    try:
+        h = W.model_handle(ms[0], "fp32", seed=700)
+        t0 = srv.submit(h, 30)
+        h.close()
+        assert srv.wait(t0, 120) == "done"
+        h = W.model_handle(ms[1], "fp32", seed=701)
+        _native.inject_device_alloc_failure(0)  # the admission's first device allocation
+        try:
+            t1 = srv.submit(h, 30)
+            assert srv.wait(t1, 120) == "failed"
+        finally:
+            _native.inject_device_alloc_failure(None)
+            h.close()
+        with pytest.raises(_native.EngineError) as ei:
+            srv.result(t1)
+        assert "memory" in str(ei.value).lower()
+        # the server goes on: the next request runs and equals the model run alone
+        h = W.model_handle(ms[2], "fp32", seed=702)
+        t2 = srv.submit(h, 30)
+        h.close()
+        assert srv.wait(t2, 120) == "done"
+        e = W.engine_for(ms[2], "fp32", seed=702)
+        e.step(30)
+        assert np.array_equal(srv.result(t2)[1], e.trajectory(30))
+        e.close()
+        assert srv.stats()["failed"] == 0  # the server itself never failed
+    finally:
+        srv.close()
