@@ -334,6 +334,21 @@ int mcg_batch_write_viz(mcg_batch* b, uint32_t replica, const char* prefix, int 
                         const char* const* species_names, uint64_t iteration, uint64_t total_iterations,
                         double length_unit_um);
 
+/* ---- Count output from device counts (MolOrRxnCountEvent::compute_counts and
+   CountBuffer, src4/mol_or_rxn_count_event.cpp:607-700, src4/count_buffer.cpp:30-128):
+   for the last n_iterations iterations, those whose number of iterations run is a
+   multiple of `every`, the counts at time (iterations run) x time_step_s, as DAT files
+   ("<prefix>.<name>.dat", lines "time value", C++ stream defaults) or one GDAT file
+   ("<prefix>.gdat": a '#' header of right-aligned names, then per row the time and the
+   values in scientific notation, 8 decimals, two-digit exponents). Column k counts
+   species[k] in the whole world (objects[k] = -1) or inside counted object objects[k]
+   (an index into the list given to mcg_set_counted_objects), named names[k]. */
+#define MCG_COUNTS_DAT 0
+#define MCG_COUNTS_GDAT 1
+int mcg_write_counts(mcg_engine* e, const char* prefix, int format, uint32_t n_iterations, uint32_t every,
+                     double time_step_s, uint32_t n_columns, const uint32_t* species, const int32_t* objects,
+                     const char* const* names);
+
 /* Setup queries for parity tests: wall constants (14 doubles per wall, same
    layout as the oracle) and the wall lists per subpartition. */
 int mcg_wall_consts(mcg_engine* e, double* out);

@@ -10,9 +10,13 @@
 // uint; version 2: molecules), version 2 only: the uint ids, then float x y z per
 // molecule (um). Molecules are written in the engine's sorted order (the
 // reference writes them in its own array order).
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <filesystem>
+#include <fstream>
+#include <iomanip>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -100,9 +104,132 @@ int write_viz(mcg::DeviceEngine* dev, uint32_t rep, const char* prefix, int mode
   return MCG_OK;
 }
 
+// CountBuffer's GDAT number (count_buffer.cpp:35-61): scientific with 8 decimals and
+// a signed two-digit exponent
+std::string gdat_number(double d) {
+  std::stringstream ss;
+  ss << std::scientific << std::setprecision(8) << d;
+  const std::string s = ss.str();
+  const size_t pos = s.find('e');
+  int exponent = std::stoi(s.substr(pos + 1));
+  std::ostringstream out;
+  out << s.substr(0, pos) << "e" << (exponent >= 0 ? "+" : "-") << std::setfill('0') << std::setw(2)
+      << (exponent >= 0 ? exponent : -exponent);
+  return out.str();
+}
+
+int write_counts(mcg::DeviceEngine* dev, uint32_t rep, uint32_t nsp, uint32_t n_cv, const char* prefix, int format,
+                 uint32_t n_it, uint32_t every, double dt, uint32_t ncol, const uint32_t* species,
+                 const int32_t* objects, const char* const* names, std::string& err) {
+  if (format != MCG_COUNTS_DAT && format != MCG_COUNTS_GDAT) {
+    err = "unknown count format";
+    return MCG_ERR_ARG;
+  }
+  if (every == 0 || ncol == 0 || !species || !objects || !names || !(dt > 0)) {
+    err = "mcg_write_counts: every, columns, species, objects, names and time step are required";
+    return MCG_ERR_ARG;
+  }
+  bool any_cv = false;
+  for (uint32_t c = 0; c < ncol; c++) {
+    if (species[c] >= nsp || !names[c] || objects[c] < -1 || (objects[c] >= 0 && (uint32_t)objects[c] >= n_cv)) {
+      err = "count column " + std::to_string(c) + ": species or counted object out of range";
+      return MCG_ERR_ARG;
+    }
+    any_cv = any_cv || objects[c] >= 0;
+  }
+  uint64_t ran = 0;
+  int rc = dev->replica_iterations(rep, &ran, err);
+  if (rc) return rc;
+  std::vector<uint64_t> world((size_t)n_it * nsp), inside;
+  if (n_it) {
+    rc = dev->trajectory(rep, n_it, world.data(), err);
+    if (rc) return rc;
+    if (any_cv) {
+      inside.resize((size_t)n_it * nsp * n_cv);
+      rc = dev->counted_trajectory(rep, n_it, inside.data(), err);
+      if (rc) return rc;
+    }
+  }
+  auto value = [&](uint32_t k, uint32_t c) -> double {
+    if (objects[c] < 0) return (double)world[(size_t)k * nsp + species[c]];
+    return (double)inside[((size_t)k * nsp + species[c]) * n_cv + (uint32_t)objects[c]];
+  };
+  std::vector<uint32_t> rows;
+  std::vector<double> times;
+  for (uint32_t k = 0; k < n_it; k++) {
+    const uint64_t it = ran - n_it + k + 1;  // iterations run after row k
+    if (it % every) continue;
+    rows.push_back(k);
+    times.push_back((double)it * dt);
+  }
+  auto open = [&](const std::string& path, std::ofstream& f) -> bool {
+    std::error_code ec;
+    const std::filesystem::path parent = std::filesystem::path(path).parent_path();
+    if (!parent.empty()) std::filesystem::create_directories(parent, ec);
+    f.open(path);
+    if (!f) err = "cannot open " + path;
+    return (bool)f;
+  };
+  if (format == MCG_COUNTS_DAT) {
+    for (uint32_t c = 0; c < ncol; c++) {
+      std::ofstream f;
+      const std::string path = std::string(prefix) + "." + names[c] + ".dat";
+      if (!open(path, f)) return MCG_ERR_ARG;
+      for (size_t r = 0; r < rows.size(); r++) f << times[r] << " " << value(rows[r], c) << "\n";
+      if (!f) {
+        err = "writing " + path + " failed";
+        return MCG_ERR_ARG;
+      }
+    }
+    return MCG_OK;
+  }
+  std::ofstream f;
+  const std::string path = std::string(prefix) + ".gdat";
+  if (!open(path, f)) return MCG_ERR_ARG;
+  // header (CountBuffer::write_gdat_header): '#', "time" and the names right-aligned
+  std::string t = "time";
+  t.insert(t.begin(), 14 - t.size(), ' ');
+  f << "#" << t;
+  for (uint32_t c = 0; c < ncol; c++) {
+    std::string col = names[c];
+    if (14 > col.size())
+      col.insert(col.begin(), 14 - col.size() + 2, ' ');
+    else
+      col = " " + col;
+    f << col;
+  }
+  f << "\n";
+  for (size_t r = 0; r < rows.size(); r++) {
+    f << " " << gdat_number(times[r]);
+    for (uint32_t c = 0; c < ncol; c++) f << "  " << gdat_number(value(rows[r], c));
+    f << "\n";
+  }
+  if (!f) {
+    err = "writing " + path + " failed";
+    return MCG_ERR_ARG;
+  }
+  return MCG_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int mcg_write_counts(mcg_engine* e, const char* prefix, int format, uint32_t n_iterations, uint32_t every,
+                     double time_step_s, uint32_t n_columns, const uint32_t* species, const int32_t* objects,
+                     const char* const* names) {
+  if (!e || !prefix) return MCG_ERR_ARG;
+  if (!e->dev) {
+    e->err = "mcg_write_counts needs a prepared engine";
+    return MCG_ERR_ARG;
+  }
+  std::string err;
+  int rc = write_counts(e->dev, 0, e->cfg.n_species, (uint32_t)e->counted.size(), prefix, format, n_iterations, every,
+                        time_step_s, n_columns, species, objects, names, err);
+  if (rc) e->err = err;
+  return rc;
+}
+
 
 int mcg_write_viz(mcg_engine* e, const char* prefix, int mode, const char* const* species_names, uint64_t iteration,
                   uint64_t total_iterations, double length_unit_um) {

@@ -78,3 +78,39 @@ def test_viz_files_hold_the_molecules(tmp_path):
         assert np.allclose(np.sort(xyz[:, 0]), np.sort((pos[sel, 0] * 0.01).astype(np.float32)))
         seen += cnt
     assert seen == len(ids)
+
+
+def test_count_files_in_the_reference_formats(tmp_path):
+    """DAT ("time value" per line, C++ stream defaults) and GDAT (a '#' header of
+    right-aligned names, then scientific numbers with two-digit exponents) written from
+    the device counts: the same numbers as the count trajectory, in the world and
+    inside a counted object."""
+    from tests.test_gpu_counted import _model as counted_model
+
+    m, obj, _, _ = counted_model()
+    h = W.model_handle(m, "fp32", seed=4)
+    h.set_wall_objects(obj)
+    h.set_counted_objects([0])
+    h.prepare()
+    h.step(12)
+    world = h.trajectory(12)
+    inside = h.counted_trajectory(12)
+    cols = [(0, -1, "A_world"), (2, -1, "C_world"), (0, 0, "A_in_sphere")]
+    h.write_counts(tmp_path / "run", cols, n_iterations=12, every=3, time_step_s=1e-6, fmt="dat")
+    h.write_counts(tmp_path / "run", cols, n_iterations=12, every=3, time_step_s=1e-6, fmt="gdat")
+    h.close()
+    rows = [2, 5, 8, 11]  # iterations 3, 6, 9, 12
+    times = [3e-6, 6e-6, 9e-6, 1.2e-5]
+    want = {"A_world": world[rows, 0], "C_world": world[rows, 2], "A_in_sphere": inside[rows, 0, 0]}
+    for name, vals in want.items():
+        lines = (tmp_path / f"run.{name}.dat").read_text().splitlines()
+        assert lines[0].split()[0] == "3e-06" and lines[3].split()[0] == "1.2e-05"
+        got = np.array([[float(x) for x in ln.split()] for ln in lines])
+        assert np.allclose(got[:, 0], times) and np.array_equal(got[:, 1], vals.astype(float))
+    text = (tmp_path / "run.gdat").read_text().splitlines()
+    assert text[0] == "#" + "time".rjust(14) + "".join(n.rjust(16) for n in ("A_world", "C_world", "A_in_sphere"))
+    first = text[1].split()
+    assert text[1].startswith(" 3.00000000e-06  ") and len(first) == 4
+    g = np.array([[float(x) for x in ln.split()] for ln in text[1:]])
+    for k, name in enumerate(("A_world", "C_world", "A_in_sphere")):
+        assert np.array_equal(g[:, k + 1], want[name].astype(float))
