@@ -92,13 +92,29 @@ class ClockSampler:
         self.idx = gpu_index
         self.p = None
 
+    def _lines(self):
+        self.f.flush()
+        try:
+            with open(self.f.name) as fh:
+                return sum(1 for _ in fh)
+        except OSError:
+            return 0
+
     def __enter__(self):
+        # sampling every 20 ms; the timed region starts once nvidia-smi has written its
+        # first row (it takes ~0.1 s to start), and rows from before it are dropped
+        self.skip = 0
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                       "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.f,
                                       stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
+        if self.p:
+            t0 = time.time()
+            while self._lines() == 0 and time.time() - t0 < 5 and self.p.poll() is None:
+                time.sleep(0.01)
+            self.skip = self._lines()
         return self
 
     def __exit__(self, *a):
@@ -118,6 +134,8 @@ class ClockSampler:
                 if len(parts) >= 9:
                     rows.append(parts)
         os.unlink(self.f.name)
+        if len(rows) > self.skip:
+            rows = rows[self.skip:]  # the timed region's rows
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
