@@ -348,6 +348,11 @@ int mcg_batch_write_viz(mcg_batch* b, uint32_t replica, const char* prefix, int 
 int mcg_write_counts(mcg_engine* e, const char* prefix, int format, uint32_t n_iterations, uint32_t every,
                      double time_step_s, uint32_t n_columns, const uint32_t* species, const int32_t* objects,
                      const char* const* names);
+/* The same for one replica of a batch; a replica frozen after its iteration budget
+   keeps its last counts in the later rows (times count from its admission). */
+int mcg_batch_write_counts(mcg_batch* b, uint32_t replica, const char* prefix, int format, uint32_t n_iterations,
+                           uint32_t every, double time_step_s, uint32_t n_columns, const uint32_t* species,
+                           const int32_t* objects, const char* const* names);
 
 /* Setup queries for parity tests: wall constants (14 doubles per wall, same
    layout as the oracle) and the wall lists per subpartition. */

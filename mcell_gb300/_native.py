@@ -33,7 +33,7 @@ EXPORTS = [
     "mcg_autotune_subparts", "mcg_batch_get_escapes",
     "mcg_serve_create", "mcg_serve_destroy", "mcg_serve_last_error", "mcg_serve_submit", "mcg_serve_poll",
     "mcg_serve_wait", "mcg_serve_result", "mcg_serve_cancel", "mcg_serve_release", "mcg_serve_get_stats",
-    "mcg_export_state", "mcg_import_state", "mcg_write_viz", "mcg_batch_write_viz", "mcg_write_counts",
+    "mcg_export_state", "mcg_import_state", "mcg_write_viz", "mcg_batch_write_viz", "mcg_write_counts", "mcg_batch_write_counts",
     "mcg_set_wall_objects", "mcg_release", "mcg_batch_release", "mcg_set_counted_objects",
     "mcg_get_counted_volume_counts", "mcg_get_counted_volume_trajectory",
 ]
@@ -470,6 +470,16 @@ class Batch:
         b = ctypes.c_uint64()
         self._chk(lib().mcg_batch_get_memory(self.h, ctypes.byref(b)))
         return b.value
+
+    def write_counts(self, rep, prefix, columns, n_iterations, every=1, time_step_s=1e-6, fmt="dat"):
+        """Count files of one replica (as Engine.write_counts)."""
+        sp = np.ascontiguousarray([c[0] for c in columns], np.uint32)
+        ob = np.ascontiguousarray([c[1] for c in columns], np.int32)
+        names = (ctypes.c_char_p * len(columns))(*[c[2].encode() for c in columns])
+        self._chk(lib().mcg_batch_write_counts(self.h, ctypes.c_uint32(rep), str(prefix).encode(),
+                                               ctypes.c_int({"dat": 0, "gdat": 1}[fmt]), ctypes.c_uint32(n_iterations),
+                                               ctypes.c_uint32(every), ctypes.c_double(time_step_s),
+                                               ctypes.c_uint32(len(columns)), _p(sp), _p(ob), names))
 
     def write_viz(self, rep, prefix, species_names, iteration, total_iterations, mode="ascii", length_unit_um=0.01):
         modes = {"ascii": 0, "cellblender_v1": 1, "cellblender_v2": 2}

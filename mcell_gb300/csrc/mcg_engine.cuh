@@ -521,6 +521,18 @@ class DeviceEngineT : public DeviceEngine {
     return 0;
   }
 
+  int replica_rows(uint32_t rep, uint32_t* n_counted, uint64_t* since_added, std::string& err) override {
+    int rc = sync(err);
+    if (rc) return rc;
+    if (rep >= max_rep_ || !reps_[rep].used) {
+      err = "no such replica";
+      return -1;
+    }
+    *n_counted = reps_[rep].n_cv;
+    *since_added = cnt_.iteration - geos_h_[rep].it0;
+    return 0;
+  }
+
   int replica_iterations(uint32_t rep, uint64_t* done, std::string& err) override {
     int rc = sync(err);
     if (rc) return rc;

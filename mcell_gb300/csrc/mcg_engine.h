@@ -81,6 +81,9 @@ class DeviceEngine {
   virtual int counted_trajectory(uint32_t rep, uint32_t n, uint64_t* out, std::string& err) = 0;
   // iterations the replica has run (it freezes after its n_iterations)
   virtual int replica_iterations(uint32_t rep, uint64_t* done, std::string& err) = 0;
+  // the replica's counted objects and the engine iterations since it was added (the
+  // rows of its count trajectories, frozen ones included)
+  virtual int replica_rows(uint32_t rep, uint32_t* n_counted, uint64_t* since_added, std::string& err) = 0;
   // device bytes held for the replica (mesh, grid, its share of the molecule arrays)
   virtual uint64_t replica_bytes(uint32_t rep) = 0;
   virtual uint64_t device_bytes() = 0;

@@ -118,7 +118,7 @@ std::string gdat_number(double d) {
   return out.str();
 }
 
-int write_counts(mcg::DeviceEngine* dev, uint32_t rep, uint32_t nsp, uint32_t n_cv, const char* prefix, int format,
+int write_counts(mcg::DeviceEngine* dev, uint32_t rep, uint32_t nsp, const char* prefix, int format,
                  uint32_t n_it, uint32_t every, double dt, uint32_t ncol, const uint32_t* species,
                  const int32_t* objects, const char* const* names, std::string& err) {
   if (format != MCG_COUNTS_DAT && format != MCG_COUNTS_GDAT) {
@@ -129,6 +129,10 @@ int write_counts(mcg::DeviceEngine* dev, uint32_t rep, uint32_t nsp, uint32_t n_
     err = "mcg_write_counts: every, columns, species, objects, names and time step are required";
     return MCG_ERR_ARG;
   }
+  uint32_t n_cv = 0;
+  uint64_t ran = 0;  // rows of the replica's trajectories so far
+  int rc = dev->replica_rows(rep, &n_cv, &ran, err);
+  if (rc) return rc;
   bool any_cv = false;
   for (uint32_t c = 0; c < ncol; c++) {
     if (species[c] >= nsp || !names[c] || objects[c] < -1 || (objects[c] >= 0 && (uint32_t)objects[c] >= n_cv)) {
@@ -137,9 +141,10 @@ int write_counts(mcg::DeviceEngine* dev, uint32_t rep, uint32_t nsp, uint32_t n_
     }
     any_cv = any_cv || objects[c] >= 0;
   }
-  uint64_t ran = 0;
-  int rc = dev->replica_iterations(rep, &ran, err);
-  if (rc) return rc;
+  if (n_it > ran) {
+    err = "mcg_write_counts: more rows asked for than iterations run";
+    return MCG_ERR_ARG;
+  }
   std::vector<uint64_t> world((size_t)n_it * nsp), inside;
   if (n_it) {
     rc = dev->trajectory(rep, n_it, world.data(), err);
@@ -224,8 +229,8 @@ int mcg_write_counts(mcg_engine* e, const char* prefix, int format, uint32_t n_i
     return MCG_ERR_ARG;
   }
   std::string err;
-  int rc = write_counts(e->dev, 0, e->cfg.n_species, (uint32_t)e->counted.size(), prefix, format, n_iterations, every,
-                        time_step_s, n_columns, species, objects, names, err);
+  int rc = write_counts(e->dev, 0, e->cfg.n_species, prefix, format, n_iterations, every, time_step_s, n_columns,
+                        species, objects, names, err);
   if (rc) e->err = err;
   return rc;
 }
@@ -242,6 +247,21 @@ int mcg_write_viz(mcg_engine* e, const char* prefix, int mode, const char* const
   int rc = write_viz(e->dev, 0, prefix, mode, e->cfg.n_species, species_names, iteration, total_iterations,
                      length_unit_um, err);
   if (rc) e->err = err;
+  return rc;
+}
+
+int mcg_batch_write_counts(mcg_batch* b, uint32_t replica, const char* prefix, int format, uint32_t n_iterations,
+                           uint32_t every, double time_step_s, uint32_t n_columns, const uint32_t* species,
+                           const int32_t* objects, const char* const* names) {
+  if (!b || !prefix) return MCG_ERR_ARG;
+  if (!b->dev) {
+    b->err = "batch has no device engine";
+    return MCG_ERR_CUDA;
+  }
+  std::string err;
+  int rc = write_counts(b->dev, replica, b->cfg.n_species, prefix, format, n_iterations, every, time_step_s, n_columns,
+                        species, objects, names, err);
+  if (rc) b->err = err;
   return rc;
 }
 

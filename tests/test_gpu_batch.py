@@ -115,3 +115,19 @@ def test_batch_molecules_stay_in_their_replica():
         assert (pos >= lo).all() and (pos < hi).all()
         assert len(np.unique(uid)) == len(uid)
     b.close()
+
+
+def test_batch_count_files_follow_the_replica(tmp_path):
+    ms = _models(2, seed=25)
+    b = _native.Batch("fp32", NSP, 2)
+    ids = b.add([W.model_handle(m, "fp32", seed=800 + k) for k, m in enumerate(ms)], n_iterations=[6, 0])
+    b.step(10)
+    r = ids[0]  # frozen after 6 iterations: its last rows repeat
+    b.write_counts(r, tmp_path / "rep", [(2, -1, "C")], n_iterations=10, every=2, fmt="gdat")
+    t = b.trajectory(r, 10)
+    lines = (tmp_path / "rep.gdat").read_text().splitlines()
+    g = np.array([[float(x) for x in ln.split()] for ln in lines[1:]])
+    assert np.allclose(g[:, 0], [2e-6, 4e-6, 6e-6, 8e-6, 1e-5])
+    assert np.array_equal(g[:, 1], t[[1, 3, 5, 7, 9], 2].astype(float))
+    assert g[3, 1] == g[2, 1] == g[4, 1]  # frozen from iteration 6 on
+    b.close()
