@@ -105,3 +105,16 @@ def test_server_needs_the_device():
     with pytest.raises(_native.EngineError) as ei:
         _native.Server("fp32", 3, max_slots=4)
     assert ei.value.code == -2
+
+
+def test_output_and_test_hook_entry_points_check_their_arguments():
+    import ctypes
+    L = _native.lib()
+    null = ctypes.c_void_p(None)
+    # count and viz writers refuse a missing handle or prefix without touching a device
+    assert L.mcg_write_counts(null, b"x", 0, 1, 1, ctypes.c_double(1e-6), 1, null, null, null) == -1
+    assert L.mcg_batch_write_counts(null, 0, b"x", 0, 1, 1, ctypes.c_double(1e-6), 1, null, null, null) == -1
+    assert L.mcg_write_viz(null, b"x", 0, null, ctypes.c_uint64(0), ctypes.c_uint64(1), ctypes.c_double(0.01)) == -1
+    # the out-of-memory hook arms and disarms without a device
+    assert L.mcg_inject_device_alloc_failure(ctypes.c_int64(5)) == 0
+    assert L.mcg_inject_device_alloc_failure(ctypes.c_int64(-1)) == 0
