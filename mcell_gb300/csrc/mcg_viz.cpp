@@ -1,5 +1,9 @@
-// Visualisation output and checkpoints from device state (declared in
+// Visualisation and count output from device state (declared in
 // include/mcell_gb300.h).
+//
+// Count files follow CountBuffer (src4/count_buffer.cpp:30-128): DAT lines
+// "time value" with C++ stream defaults, GDAT a '#' header of right-aligned names
+// and rows of scientific numbers with two-digit exponents.
 //
 // Viz files follow VizOutputEvent (src4/viz_output_event.cpp:48-279): the name
 // "<prefix>.<ascii|cellbin>.<iteration, zero-padded to the digits of the total>.dat";
