@@ -139,7 +139,7 @@ class ClockSampler:
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
-        mx = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        mx = max((float(r[2]) for r in rows if r[2].replace(".", "").isdigit()), default=None)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
@@ -178,6 +178,10 @@ def combine_ranks(seconds, units, world, device):
     return t.item(), n.item()
 
 
+GPU_WORKLOAD = ("sphere_in_cube: icosphere r=1um 20480 tris transparent to A in a 2.5um reflective cube, 1M molecules "
+                "A:B 1:1, A+B->C 1e8/M/s, C->0 1e3/s, dt=1us")
+
+
 def run_gpu(args, rank, world):
     import numpy as np
     import torch
@@ -210,6 +214,7 @@ def run_gpu(args, rank, world):
             prof += e.profile()
     torch.cuda.synchronize()
     _, ms1, l1 = e.stats()
+    fallbacks = e.fallbacks()
     clocks = clk.summary()
     mol_steps = ms1 - ms0
     iter_ms = prof[0]
@@ -254,8 +259,7 @@ def run_gpu(args, rank, world):
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded uniform release; icosphere + cube mesh generated)",
-        "config": {"workload": "sphere_in_cube: icosphere r=1um 20480 tris transparent to A in a 2.5um "
-                               "reflective cube, 1M molecules A:B 1:1, A+B->C 1e8/M/s, C->0 1e3/s, dt=1us",
+        "config": {"workload": GPU_WORKLOAD,
                    "molecules": args.n_mol, "walls": int(len(model.walls)), "subparts_per_edge": int(model.nsub),
                    "precision": "fp32 positions", "parallelism": f"replicas x{world}",
                    "l2": "flushed (512 MB write) before every timed step"},
@@ -271,6 +275,9 @@ def run_gpu(args, rank, world):
                                "products": prof[3] / args.steps, "sort": prof[4] / args.steps},
         "graph_replay_value": graph_rate,
         "final_counts": [int(x) for x in counts] if counts is not None else None,
+        "fallbacks": {"page_refills": fallbacks[0], "walk_scans": fallbacks[1],
+                      "note": "ray traces since upload that took the exact fallbacks of the fixed-size candidate "
+                              "page (16) and partner list (48); results do not depend on them"},
     }
     return line
 
@@ -306,6 +313,7 @@ def run_batching(args):
     b.sync()
     job_b = time.perf_counter() - t0
     _, steps_b, launches_b = b.stats()
+    fallbacks_b = b.fallbacks()
     finals_b = [b.counts(r) for r in ids]
     blocks = b.diffuse_blocks_per_sm()
     mem_b = b.device_bytes()
@@ -336,6 +344,7 @@ def run_batching(args):
                              "molecule_steps_per_s": steps_p / job_p},
         "speedup_replicas_per_hour": job_p / job_b,
         "final_counts_replica0": [int(x) for x in finals_b[0]],
+        "fallbacks_batched": {"page_refills": fallbacks_b[0], "walk_scans": fallbacks_b[1]},
         "note": f"both arms run {iters} iterations of each replica; replicas_per_hour is for jobs of that length",
     }
 
@@ -408,7 +417,7 @@ def run_precision(args):
     200,400 triangles; half of the cases start within 1 nm of an edge or vertex),
     once with each engine at its own stored positions and once with the fp64 engine
     at the fp32 engine's (trace arithmetic alone), and the count trajectories of a
-    1M-molecule tube over 50 iterations (the full model runs ~3 s per fp64
+    1M-molecule tube over args.precision_iters iterations (the full model runs ~3 s per fp64
     iteration)."""
     import numpy as np
 
@@ -422,33 +431,38 @@ def run_precision(args):
     mism_same = precision.wall_hit_mismatch(m, n_cases=100_000, near_ids=near, same_start=True)
     del m
     small = W.bumpy_tube(n_mol=1_000_000, seed=2)
-    cnt = precision.count_error(small, n_iter=50)
+    cnt = precision.count_error(small, n_iter=args.precision_iters)
     return {"workload": "bumpy tube r = 0.2 um (+-0.05 um), 10 um, 200,400 reflective triangles, 5% of the molecules "
                         "within 1 nm of edges/vertices, A+B->C, dt 0.1 us",
             "wall_hit_mismatch_10M": mism, "wall_hit_mismatch_10M_same_start": mism_same,
-            "count_error_1M_50_iterations": cnt}
+            f"count_error_1M_{args.precision_iters}_iterations": cnt,
+            "reduction": f"count error on a 1M-molecule tube over {args.precision_iters} iterations, not 10M x 500: "
+                         "the fp64 engine takes ~3 s per iteration of the full model (about 25 minutes for 500)"}
 
 
 # ---------------------------------------------------------------- serving form
 
-def run_serving(args):
+def run_serving(rate, seconds, plain=True, seed=11):
     """Requests drawn from the batching distribution with iteration counts
-    log-uniform in 100-10,000 arrive as a Poisson stream (args.serve_rate per s for
-    args.serve_seconds) and are served by the continuous-batching loop
-    (mcg_serve_*; slots 256, device-memory budget 150 GB). Time-to-result is
-    measured per request from submission to result. The same requests are then run
-    one after another on the plain engine; their time-to-result under first-come,
-    first-served is computed from those measured run times and the same arrivals."""
+    log-uniform in 100-10,000 arrive as a Poisson stream (rate per s for `seconds`)
+    and are served by the continuous-batching loop (mcg_serve_*; slots 256,
+    device-memory budget 150 GB). Time-to-result is measured per request from
+    submission to result. With `plain`, the same requests are then run one after
+    another on the plain engine; their time-to-result under first-come,
+    first-served is computed from those measured run times and the same arrivals.
+    Without it, the offered load is set against the plain engine's capacity (the
+    molecule-steps/s it sustains on this distribution, `plain_capacity`)."""
     import numpy as np
 
     from mcell_gb300 import _native
     from mcell_gb300 import workloads as W
 
-    rng = np.random.default_rng(11)
-    n_req = max(1, int(rng.poisson(args.serve_rate * args.serve_seconds)))
-    arrivals = np.sort(rng.uniform(0, args.serve_seconds, n_req))
+    rng = np.random.default_rng(seed)
+    n_req = max(1, int(rng.poisson(rate * seconds)))
+    arrivals = np.sort(rng.uniform(0, seconds, n_req))
     iters = np.exp(rng.uniform(np.log(100), np.log(10_000), n_req)).astype(int)
-    models = W.replica_models(n_req, seed=11)
+    models = W.replica_models(n_req, seed=seed)
+    offered = float(sum(len(m.species) * int(k) for m, k in zip(models, iters))) / seconds
     handles = [W.model_handle(m, "fp32", seed=2000 + k) for k, m in enumerate(models)]
     srv = _native.Server("fp32", 3, max_slots=256, hbm_budget_bytes=150 << 30, autotune=True)
     t0 = time.perf_counter()
@@ -465,32 +479,36 @@ def run_serving(args):
     wall = time.perf_counter() - t0
     st = srv.stats()
     srv.close()
-    # plain engine, one request after another (first come, first served)
-    service = []
-    for k, m in enumerate(models):
-        e = W.engine_for(m, "fp32", seed=2000 + k)
-        e.sync()
-        t1 = time.perf_counter()
-        e.step(int(iters[k]))
-        e.sync()
-        service.append(time.perf_counter() - t1)
-        e.close()
-    for h in handles:
-        h.close()
-    done, plain_lat = 0.0, []
-    for a, sv in zip(arrivals, service):
-        done = max(done, a) + sv
-        plain_lat.append(done - a)
     mol_steps = float(st["mol_steps"])
-    return {
-        "workload": f"{n_req} requests, Poisson {args.serve_rate}/s over {args.serve_seconds} s, models of the batching "
-                    f"distribution, iterations log-uniform 100-10000 ({int(iters.sum())} in total), fp32",
+    out = {
+        "workload": f"{n_req} requests, Poisson {rate}/s over {seconds} s, models of the batching distribution, "
+                    f"iterations log-uniform 100-10000 ({int(iters.sum())} in total), fp32",
+        "offered_molecule_steps_per_s": offered,
         "served": {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                    "makespan_s": wall, "molecule_steps_per_s": mol_steps / wall,
                    "busy_molecule_steps_per_s": mol_steps / max(st["busy_seconds"], 1e-9)},
-        "plain_sequential": {"p50_s": float(np.percentile(plain_lat, 50)), "p99_s": float(np.percentile(plain_lat, 99)),
-                             "makespan_s": float(done), "molecule_steps_per_s": mol_steps / max(sum(service), 1e-9)},
     }
+    if plain:
+        # plain engine, one request after another (first come, first served)
+        service = []
+        for k, m in enumerate(models):
+            e = W.engine_for(m, "fp32", seed=2000 + k)
+            e.sync()
+            t1 = time.perf_counter()
+            e.step(int(iters[k]))
+            e.sync()
+            service.append(time.perf_counter() - t1)
+            e.close()
+        done, plain_lat = 0.0, []
+        for a, sv in zip(arrivals, service):
+            done = max(done, a) + sv
+            plain_lat.append(done - a)
+        out["plain_sequential"] = {"p50_s": float(np.percentile(plain_lat, 50)),
+                                   "p99_s": float(np.percentile(plain_lat, 99)), "makespan_s": float(done),
+                                   "molecule_steps_per_s": mol_steps / max(sum(service), 1e-9)}
+    for h in handles:
+        h.close()
+    return out
 
 
 def main():
@@ -505,12 +523,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batching measurement")
     ap.add_argument("--batch-replicas", type=int, default=256)
-    ap.add_argument("--batch-iters", type=int, default=200)
+    ap.add_argument("--batch-iters", type=int, default=1000)
     ap.add_argument("--no-cube", action="store_true", help="skip the closed-cube measurement")
     ap.add_argument("--no-precision", action="store_true", help="skip the precision measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
-    ap.add_argument("--serve-rate", type=float, default=50.0)
-    ap.add_argument("--serve-seconds", type=float, default=2.0)
+    ap.add_argument("--serve-rate", type=float, default=50.0, help="the overload burst's arrival rate")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="the overload burst's duration")
+    ap.add_argument("--sustained-rate", type=float, default=10.0)
+    ap.add_argument("--sustained-seconds", type=float, default=60.0, help="0 skips the sustained serving run")
+    ap.add_argument("--precision-iters", type=int, default=100)
     args = ap.parse_args()
     rank, world, _ = _rank_env()
     procs = args.cpu_procs or os.cpu_count() or 1
@@ -531,7 +552,10 @@ def main():
         line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": "sphere_in_cube, 1M molecules (see the GPU arm)", "molecules": args.n_mol},
+                "config": {"workload": GPU_WORKLOAD, "molecules": args.n_mol,
+                           "precision": "fp64 positions (the oracle's serial engine restates the reference's fp64 "
+                                        "build; the GPU arm computes positions in fp32)",
+                           "parallelism": f"{procs} independent seeded processes (MCell4 is single-threaded)"},
                 "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
                                  "sample": f"{procs} processes x {args.cpu_iters} iterations of the 1M-molecule model "
                                            f"per step, up to 3 steps"},
@@ -557,7 +581,19 @@ def main():
     if rank == 0 and not args.no_batch:
         line["batching"] = run_batching(args)
     if rank == 0 and not args.no_serve:
-        line["serving"] = run_serving(args)
+        burst = run_serving(args.serve_rate, args.serve_seconds)
+        burst["note"] = ("overload: the configured 50 requests/s offer several times what one GB300 serves, so "
+                         "the burst measures a queue draining after arrivals stop")
+        line["serving"] = {"overload_burst": burst}
+        if args.sustained_seconds > 0:
+            sus = run_serving(args.sustained_rate, args.sustained_seconds, plain=False, seed=12)
+            cap = burst["plain_sequential"]["molecule_steps_per_s"]
+            sus["plain_capacity_molecule_steps_per_s"] = cap
+            sus["plain_offered_load_ratio"] = sus["offered_molecule_steps_per_s"] / cap
+            sus["note"] = ("sustained arrivals; the plain engine's capacity is measured on the burst's requests run "
+                           "one after another: an offered load ratio above 1 means its first-come-first-served "
+                           "queue grows without bound at this rate")
+            line["serving"]["sustained"] = sus
     if rank == 0 and not args.no_cube:
         line["closed_cube"] = run_closed_cube(args, cube_pool)
     if cube_pool is not None:

@@ -73,12 +73,20 @@ int mcg_set_species(mcg_engine* e, uint32_t n, const double* space_step);
 int mcg_upload_mesh(mcg_engine* e, uint32_t n_vertices, const double* vertices, uint32_t n_walls,
                     const uint32_t* walls, const uint8_t* wall_class);
 
-/* Bimolecular vol+vol reaction a+b -> products (-1 = none): max_fixed_p
-   (RxnClass::get_max_fixed_p as used by test_bimolecular, src4/rxn_utils.inl:336). */
-int mcg_add_bimol_rxn(mcg_engine* e, uint32_t a, uint32_t b, double max_fixed_p, int32_t product0,
-                      int32_t product1);
-/* Unimolecular reaction a -> products: k_tot = rate * time_step
-   (time_of_unimol, src4/rxn_utils.inl:721). */
+/* Bimolecular vol+vol reaction a+b -> products (-1 = none) with probability p
+   (k * pb_factor). The reactions of one reactant pair form its reaction class
+   (BNG::RxnClass): each call adds a pathway, in call order, up to MCG_MAX_PATHWAYS;
+   the class's cumulative probabilities are what test_bimolecular
+   (src4/rxn_utils.inl:336-414) compares with and selects the pathway from
+   (max_fixed_p = their sum). A product species that is also a bimolecular
+   reactant makes the model unsupported (MCG_ERR_UNSUPPORTED at mcg_prepare,
+   mcg_batch_add or mcg_serve_submit): its same-step reactions are not on the path. */
+#define MCG_MAX_PATHWAYS 4
+int mcg_add_bimol_rxn(mcg_engine* e, uint32_t a, uint32_t b, double p, int32_t product0, int32_t product1);
+/* Unimolecular reaction a -> products with k = rate * time_step. Each call adds a
+   pathway of a's unimolecular class (up to MCG_MAX_PATHWAYS): the lifetime is drawn
+   from their sum (time_of_unimol, src4/rxn_utils.inl:721) and the pathway by
+   which_unimolecular (src4/rxn_utils.inl:774-783). */
 int mcg_add_unimol_rxn(mcg_engine* e, uint32_t a, double k_tot, int32_t product0, int32_t product1);
 
 /* Volume molecules released before the first iteration (ReleaseEvent::step,
@@ -113,6 +121,18 @@ int mcg_set_options(mcg_engine* e, int use_graphs, int profile);
    off. Lets tests run the out-of-memory paths (no leak, the engine left as it was)
    without exhausting HBM. */
 int mcg_inject_device_alloc_failure(int64_t after);
+/* Exact fallbacks taken since the engine was prepared (the step's results do not
+   depend on them; they cost time): out[0] ray traces with more vol-vol collision
+   candidates than one fixed-size page holds (16; the reference's list grows), whose
+   later candidates were collected again in time order, page by page; out[1] traces
+   whose partner subpartitions overflowed the fixed-size list (48), whose partners
+   were then scanned along the walk with repeated candidates dropped. Both restate the
+   growable lists of ray_trace_vol / collect_crossed_subparts
+   (src4/diffuse_react_event.cpp:627-780, src4/collision_utils_subparts.inl:127-300). */
+int mcg_get_fallbacks(mcg_engine* e, uint64_t* out /* [2] */);
+/* Test hook (no counterpart in the reference): smaller page and list capacities
+   (1..16 candidates, 1..48 subpartitions) so that tests can drive the fallbacks. */
+int mcg_set_trace_limits(mcg_engine* e, uint32_t max_candidates, uint32_t max_subparts);
 /* Profile since the last call: out[0] iteration ms, [1] diffuse kernel ms, [2] reaction
    resolution ms, [3] products ms, [4] sort (scan + scatter) ms, [5] iterations profiled. */
 int mcg_get_profile(mcg_engine* e, double* out);
@@ -139,6 +159,16 @@ int mcg_trace_cases(mcg_engine* e, uint32_t n_cases, const uint64_t* mol_ids, co
                     const uint32_t* draws, uint32_t draws_per_case, const double* r_rate_factor,
                     const double* t_steps, double* out);
 
+/* Parity harness of the reaction decisions (no engine; test infrastructure): for
+   case c, the device's test_bimolecular (kind 0: a class of n_pathways[c]
+   pathways with cumulative probabilities cum_probs[c * MCG_MAX_PATHWAYS ...],
+   scaling[c], one injected 32-bit draw; src4/rxn_utils.inl:336-414) or
+   which_unimolecular (kind 1: cumulative rates, the draw used only for several
+   pathways; src4/rxn_utils.inl:774-783). pathway[c] = the pathway index, or -1
+   for no reaction. */
+int mcg_reaction_decisions(int kind, uint32_t n, const double* cum_probs, const uint32_t* n_pathways,
+                           const double* scaling, const uint32_t* draws, int32_t* pathway);
+
 /* mcg_trace_cases without device allocation. It has no counterpart in the
    reference: it exists for callers that must not allocate device memory while
    they check a model, for example a loop that keeps other engines running on
@@ -149,12 +179,15 @@ int mcg_trace_cases(mcg_engine* e, uint32_t n_cases, const uint64_t* mol_ids, co
    Limits: n_cases <= MCG_TRACE_STATIC_MAX_CASES and
    n_cases * draws_per_case <= MCG_TRACE_STATIC_MAX_DRAWS; larger requests
    return MCG_ERR_ARG without running anything. The engine must be prepared
-   (mcg_prepare) with no molecules pending, else MCG_ERR_ARG. The first call on
-   each device looks up the scratch's device address; make that first call
-   before any CUDA stream capture begins. All handles of a process on one
-   device share the one scratch: calls that overlap in time (from several
-   threads) race on it and must be serialised by the caller. Same arguments,
-   results and errors as mcg_trace_cases. */
+   (mcg_prepare) with no molecules pending, else MCG_ERR_ARG. The scratch's
+   device memory is taken, and its address looked up, when the engine is
+   prepared (mcg_prepare or the first mcg_step), not by this call; call it from
+   a thread whose current device is the one the engine was prepared on (else
+   MCG_ERR_ARG). After a cudaDeviceReset in the process, engines prepared before
+   it are invalid, this call included. All handles of a process on one device
+   share the one scratch: calls that overlap in time (from several threads)
+   race on it and must be serialised by the caller. Same arguments, results and
+   errors as mcg_trace_cases. */
 #define MCG_TRACE_STATIC_MAX_CASES 256
 #define MCG_TRACE_STATIC_MAX_DRAWS 16384
 int mcg_trace_cases_static(mcg_engine* e, uint32_t n_cases, const uint64_t* mol_ids, const double* disp,
@@ -206,6 +239,8 @@ int mcg_batch_download_molecules(mcg_batch* b, uint32_t replica, uint64_t cap, d
                                  uint64_t* ids, uint64_t* n_out);
 int mcg_batch_get_stats(mcg_batch* b, uint64_t* iterations, uint64_t* mol_steps, uint64_t* launches);
 int mcg_batch_set_options(mcg_batch* b, int use_graphs, int profile);
+/* As mcg_get_fallbacks, over all replicas. */
+int mcg_batch_get_fallbacks(mcg_batch* b, uint64_t* out /* [2] */);
 int mcg_batch_get_profile(mcg_batch* b, double* out);
 /* Device bytes held by the batch, and the resident blocks per SM the diffuse
    kernel runs with (the autotuner's choice, or the maximum). */
@@ -342,7 +377,11 @@ int mcg_batch_write_viz(mcg_batch* b, uint32_t replica, const char* prefix, int 
    ("<prefix>.gdat": a '#' header of right-aligned names, then per row the time and the
    values in scientific notation, 8 decimals, two-digit exponents). Column k counts
    species[k] in the whole world (objects[k] = -1) or inside counted object objects[k]
-   (an index into the list given to mcg_set_counted_objects), named names[k]. */
+   (an index into the list given to mcg_set_counted_objects), named names[k]. A window
+   that reaches back to the model's first iteration (n_iterations = all iterations
+   run) starts with a row at time 0: the counts before the first iteration, after the
+   uploads and releases, as the reference's count event runs before the diffusion
+   event in iteration 0. */
 #define MCG_COUNTS_DAT 0
 #define MCG_COUNTS_GDAT 1
 int mcg_write_counts(mcg_engine* e, const char* prefix, int format, uint32_t n_iterations, uint32_t every,

@@ -36,7 +36,9 @@ EXPORTS = [
     "mcg_export_state", "mcg_import_state", "mcg_write_viz", "mcg_batch_write_viz", "mcg_write_counts", "mcg_batch_write_counts",
     "mcg_set_wall_objects", "mcg_release", "mcg_batch_release", "mcg_set_counted_objects",
     "mcg_get_counted_volume_counts", "mcg_get_counted_volume_trajectory",
+    "mcg_get_fallbacks", "mcg_set_trace_limits", "mcg_batch_get_fallbacks", "mcg_reaction_decisions",
 ]
+MAX_PATHWAYS = 4
 
 
 class McgConfig(ctypes.Structure):
@@ -133,6 +135,26 @@ def inject_device_alloc_failure(after):
     """Test hook: the device allocation after `after` more successful ones fails as if
     out of memory (once); None or a negative value turns it off."""
     lib().mcg_inject_device_alloc_failure(ctypes.c_int64(-1 if after is None else int(after)))
+
+
+def reaction_decisions(kind, cum, scaling, draws):
+    """Device reaction decisions on injected draws (mcg_reaction_decisions): kind
+    "bimol" (test_bimolecular) or "unimol" (which_unimolecular); cum: one list of
+    cumulative pathway values per case. Returns the pathway per case, -1 = none."""
+    n = len(cum)
+    c = np.zeros((n, MAX_PATHWAYS))
+    npw = np.zeros(n, np.uint32)
+    for i, row in enumerate(cum):
+        c[i, :len(row)] = row
+        npw[i] = len(row)
+    sc = np.ascontiguousarray(np.zeros(n) if scaling is None else scaling, np.float64)
+    dr = np.ascontiguousarray(draws, np.uint32)
+    out = np.zeros(n, np.int32)
+    rc = lib().mcg_reaction_decisions(ctypes.c_int({"bimol": 0, "unimol": 1}[kind]), ctypes.c_uint32(n), _p(c),
+                                      _p(npw), _p(sc), _p(dr), _p(out))
+    if rc:
+        raise EngineError(rc, "mcg_reaction_decisions failed")
+    return out
 
 
 class Engine:
@@ -234,6 +256,16 @@ class Engine:
 
     def set_options(self, use_graphs=True, profile=False):
         self._chk(lib().mcg_set_options(self.h, ctypes.c_int(int(use_graphs)), ctypes.c_int(int(profile))))
+
+    def fallbacks(self):
+        """(traces that refilled a full candidate page, traces that scanned partners along the walk)."""
+        out = np.zeros(2, np.uint64)
+        self._chk(lib().mcg_get_fallbacks(self.h, _p(out)))
+        return int(out[0]), int(out[1])
+
+    def set_trace_limits(self, max_candidates, max_subparts):
+        """Test hook: smaller candidate page / partner list capacities (drives the fallbacks)."""
+        self._chk(lib().mcg_set_trace_limits(self.h, ctypes.c_uint32(max_candidates), ctypes.c_uint32(max_subparts)))
 
     def profile(self):
         """ms since the last call: iteration, diffuse, reactions, products, sort; iterations profiled"""
@@ -460,6 +492,11 @@ class Batch:
 
     def set_options(self, use_graphs=True, profile=False):
         self._chk(lib().mcg_batch_set_options(self.h, int(use_graphs), int(profile)))
+
+    def fallbacks(self):
+        out = np.zeros(2, np.uint64)
+        self._chk(lib().mcg_batch_get_fallbacks(self.h, _p(out)))
+        return int(out[0]), int(out[1])
 
     def profile(self):
         out = np.zeros(6)

@@ -34,6 +34,10 @@ static int fail(mcg_engine* e, int code, const std::string& msg) {
 static int prepare(mcg_engine* e) {
   if (e->dev) return MCG_OK;
   if (!e->species_set) return fail(e, MCG_ERR_ARG, "mcg_set_species must be called first");
+  {
+    std::string why;
+    if (int rc = mcg::check_model_supported(*e, why)) return fail(e, rc, why);
+  }
   if (e->wclass.empty() && !e->walls.empty()) return fail(e, MCG_ERR_ARG, "mesh without wall classes");
   mcg::HostSetup hs;
   std::string err;
@@ -127,10 +131,9 @@ int mcg_add_bimol_rxn(mcg_engine* e, uint32_t a, uint32_t b, double p, int32_t p
   if (e->dev) return fail(e, MCG_ERR_ARG, "reactions must be added before the first step");
   if (a >= (uint32_t)ns || b >= (uint32_t)ns || p0 >= ns || p1 >= ns || p0 < -1 || p1 < -1 || !(p >= 0))
     return fail(e, MCG_ERR_ARG, "invalid bimolecular reaction");
-  if (e->chem.bimol_p[a][b] >= 0) return fail(e, MCG_ERR_UNSUPPORTED, "one reaction per reactant pair on the GPU path");
-  e->chem.bimol_p[a][b] = e->chem.bimol_p[b][a] = p;
-  e->chem.bimol_prod[a][b][0] = e->chem.bimol_prod[b][a][0] = p0;
-  e->chem.bimol_prod[a][b][1] = e->chem.bimol_prod[b][a][1] = p1;
+  // a further reaction of the same reactant pair is a further pathway of its class
+  if (!e->chem.add_bimol((int)a, (int)b, p, p0, p1))
+    return fail(e, MCG_ERR_UNSUPPORTED, "more than MCG_MAX_PATHWAYS reactions for one reactant pair");
   return MCG_OK;
 }
 
@@ -140,10 +143,8 @@ int mcg_add_unimol_rxn(mcg_engine* e, uint32_t a, double k, int32_t p0, int32_t 
   if (e->dev) return fail(e, MCG_ERR_ARG, "reactions must be added before the first step");
   if (a >= (uint32_t)ns || p0 >= ns || p1 >= ns || p0 < -1 || p1 < -1 || !(k >= 0))
     return fail(e, MCG_ERR_ARG, "invalid unimolecular reaction");
-  if (e->chem.unimol_k[a] >= 0) return fail(e, MCG_ERR_UNSUPPORTED, "one unimolecular reaction per species");
-  e->chem.unimol_k[a] = k;
-  e->chem.uni_prod[a][0] = p0;
-  e->chem.uni_prod[a][1] = p1;
+  if (!e->chem.add_unimol((int)a, k, p0, p1))
+    return fail(e, MCG_ERR_UNSUPPORTED, "more than MCG_MAX_PATHWAYS unimolecular reactions for one species");
   return MCG_OK;
 }
 
@@ -222,6 +223,39 @@ int mcg_get_stats(mcg_engine* e, uint64_t* iterations, uint64_t* mol_steps, uint
   }
   e->dev->stats(iterations, mol_steps, launches);
   return MCG_OK;
+}
+
+int mcg_reaction_decisions(int kind, uint32_t n, const double* cum, const uint32_t* npw, const double* scaling,
+                           const uint32_t* draws, int32_t* out) {
+  if ((kind != 0 && kind != 1) || (n && (!cum || !npw || !draws || !out || (kind == 0 && !scaling))))
+    return MCG_ERR_ARG;
+  for (uint32_t c = 0; c < n; c++)
+    if (npw[c] < 1 || npw[c] > MCG_MAX_PATHWAYS) return MCG_ERR_ARG;
+  std::vector<double> sc;
+  if (kind == 1) sc.assign(n, 0.0);
+  std::string err;
+  return mcg::rxn_decisions(kind, n, cum, npw, kind == 0 ? scaling : sc.data(), draws, out, err);
+}
+
+int mcg_get_fallbacks(mcg_engine* e, uint64_t* out) {
+  if (!e || !out) return MCG_ERR_ARG;
+  if (!e->dev) {
+    out[0] = out[1] = 0;
+    return MCG_OK;
+  }
+  std::string err;
+  int rc = e->dev->fallbacks(out, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
+int mcg_set_trace_limits(mcg_engine* e, uint32_t max_candidates, uint32_t max_subparts) {
+  if (!e) return MCG_ERR_ARG;
+  int rc = prepare(e);
+  if (rc) return rc;
+  std::string err;
+  rc = e->dev->set_trace_limits((int)std::min<uint32_t>(max_candidates, 1u << 30),
+                                (int)std::min<uint32_t>(max_subparts, 1u << 30), err);
+  return rc ? fail(e, rc, err) : MCG_OK;
 }
 
 int mcg_set_options(mcg_engine* e, int use_graphs, int profile) {

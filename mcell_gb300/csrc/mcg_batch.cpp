@@ -211,6 +211,10 @@ int mcg_batch_add(mcg_batch* b, uint32_t n, mcg_engine* const* models, const uin
     if (m->cfg.n_species != b->cfg.n_species) return bfail(b, MCG_ERR_ARG, "model species count differs from the batch");
     if (!m->species_set) return bfail(b, MCG_ERR_ARG, "model without mcg_set_species");
     if (m->wclass.empty() && !m->walls.empty()) return bfail(b, MCG_ERR_ARG, "mesh without wall classes");
+    {
+      std::string why;
+      if (int rc = mcg::check_model_supported(*m, why)) return bfail(b, rc, why);
+    }
     bool oct = true;
     nsub[k] = b->cfg.autotune ? choose_subparts(m, &oct) : m->cfg.subparts_per_edge;
     std::string err;
@@ -312,6 +316,14 @@ int mcg_batch_get_stats(mcg_batch* b, uint64_t* iterations, uint64_t* mol_steps,
   if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
   b->dev->stats(iterations, mol_steps, launches);
   return MCG_OK;
+}
+
+int mcg_batch_get_fallbacks(mcg_batch* b, uint64_t* out) {
+  if (!b || !out) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  std::string err;
+  int rc = b->dev->fallbacks(out, err);
+  return rc ? bfail(b, rc, err) : MCG_OK;
 }
 
 int mcg_batch_set_options(mcg_batch* b, int use_graphs, int profile) {

@@ -39,8 +39,8 @@
 namespace mcg {
 
 constexpr int MAXSP = 16;
-constexpr int MAXC = 16;        // vol-vol collision candidates kept per ray trace (earliest first)
-constexpr int MAXSET = 48;      // subpartitions collected per ray trace for partner tests
+constexpr int MAXC = 16;        // vol-vol collision candidates per page of a ray trace (earliest first)
+constexpr int MAXSET = 48;      // subpartitions a ray trace's partner list holds
 constexpr int MAX_REDO = 256;   // edge/vertex re-tries in one get_closest_wall_collision
 constexpr int MAX_BOUNCES = 4096;
 constexpr uint32_t NONE = 0xFFFFFFFFu;
@@ -49,8 +49,13 @@ constexpr uint32_t NONE = 0xFFFFFFFFu;
 constexpr uint32_t ST_CAPACITY = 1u << 0;
 constexpr uint32_t ST_ESCAPE = 1u << 1;
 constexpr uint32_t ST_WATCHDOG = 1u << 2;
-constexpr uint32_t ST_COLL_OVERFLOW = 1u << 3;   // more than MAXC candidates (earliest kept)
-constexpr uint32_t ST_SET_OVERFLOW = 1u << 4;    // more than MAXSET subpartitions
+// exact fallbacks taken (counted, results unchanged): more candidates than one page
+// holds (later pages refilled in time order), more partner subpartitions than the list
+// holds (partners scanned along the walk, candidates deduplicated)
+constexpr uint32_t ST_COLL_OVERFLOW = 1u << 3;
+constexpr uint32_t ST_SET_OVERFLOW = 1u << 4;
+// the bits that end a trace (the fallback bits only count)
+constexpr uint32_t ST_ERRORS = ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG;
 
 // molecule meta word (w lane of the position record): species in bits 0-7, the
 // schedule flag in bit 8, counted-volume membership in bits 9-15, the replica
@@ -103,17 +108,26 @@ __device__ __forceinline__ void set_meta(P4<double>& p, uint32_t m) {
   p.w = __longlong_as_double((long long)m);
 }
 
-// species and reaction tables (read-only on the device)
+constexpr int MAXPW = 4;  // pathways of one reaction class
+
+// species and reaction tables (read-only on the device). A reaction class (one per
+// reactant pair, one per unimolecular reactant) holds its pathways' cumulative
+// probabilities (bimolecular) or rates x time step (unimolecular) and their products
+// (-1 = none), as BNG::RxnClass's cum_probs.
 struct Chem {
   int nsp;
   int nuni;
   double space_step[MAXSP];
-  double unimol_k[MAXSP];       // k_tot per time step, < 0: no unimolecular reaction
-  int uni_prod[MAXSP][2];
-  double bimol_p[MAXSP][MAXSP];  // max_fixed_p, < 0: no reaction
-  int bimol_prod[MAXSP][MAXSP][2];
-  uint32_t partners[MAXSP];      // bit b: species b reacts with this species
-  uint32_t can_volwall[MAXSP];   // has a non-reflective wall class somewhere
+  double unimol_k[MAXSP];               // k_tot per time step (last cumulative rate), < 0: none
+  double uni_cum[MAXSP][MAXPW];
+  double bimol_p[MAXSP][MAXSP];         // max_fixed_p (last cumulative probability), < 0: none
+  double bimol_cum[MAXSP][MAXSP][MAXPW];
+  uint32_t partners[MAXSP];             // bit b: species b reacts with this species
+  uint32_t can_volwall[MAXSP];          // has a non-reflective wall class somewhere
+  int8_t uni_npw[MAXSP];
+  int8_t uni_prod[MAXSP][MAXPW][2];
+  int8_t bimol_npw[MAXSP][MAXSP];
+  int8_t bimol_prod[MAXSP][MAXSP][MAXPW][2];
 };
 
 template <typename T>
@@ -173,6 +187,7 @@ struct Cells {
   const uint64_t* uid;
   const uint32_t* start;  // [nkeys + 1]
   const uint8_t* dead;    // optional: partners already used up this iteration
+  int maxc, maxset;       // capacities of a candidate page and of the partner list (tests lower them)
 };
 
 template <typename T>
@@ -182,6 +197,7 @@ struct TraceOut {
   uint32_t subpart;
   uint32_t partner;  // index into Cells
   double t_abs;      // time of the reaction / absorption
+  int pathway;       // pathway of the reaction class that fired (status 1)
   V3<T> rxn_pos;
   double elapsed, t_steps;
   uint32_t err;
@@ -481,14 +497,14 @@ struct Walk {
 
 struct SubSet {
   uint32_t s[MAXSET];
-  int n;
+  int n, cap;
   uint32_t n3;  // number of subpartitions (indices are checked against it)
   bool overflow;
   __device__ __forceinline__ void insert(uint32_t v) {
     if (v >= n3) return;
     for (int i = 0; i < n; i++)
       if (s[i] == v) return;
-    if (n < MAXSET)
+    if (n < cap)
       s[n++] = v;
     else
       overflow = true;
@@ -981,12 +997,13 @@ struct Colls {
     if (a.t > b.t) return false;
     return uid[a.idx] > uid[b.idx];
   }
-  __device__ void insert(const VV<T>& x, const uint64_t* uid) {
+  // cap: the page's capacity (MAXC; tests lower it)
+  __device__ void insert(const VV<T>& x, const uint64_t* uid, int cap) {
     int i = n;
-    if (n == MAXC) {
+    if (n == cap) {
       overflow = true;
-      if (!before(x, c[MAXC - 1], uid)) return;
-      i = MAXC - 1;
+      if (!before(x, c[cap - 1], uid)) return;
+      i = cap - 1;
     } else {
       n++;
     }
@@ -996,6 +1013,38 @@ struct Colls {
     }
     c[i] = x;
   }
+};
+
+// The collector of the exact fallbacks (out of line, rare): a later page of
+// candidates takes only those after the last one of the previous page in
+// sort_collisions_by_time order (the cursor); a partner scan along the walk visits
+// subpartitions more than once and drops repeated candidates. A candidate evicted
+// from a full page is always later than the page's last one, so it is refused again
+// when it comes back: the pages together hold every candidate exactly once, in order.
+template <typename T>
+struct CollsX {
+  Colls<T>& c;
+  bool cursor, dedupe;
+  T ct;
+  uint64_t cuid;
+  __device__ void insert(const VV<T>& x, const uint64_t* uid, int cap) {
+    if (cursor && (x.t < ct || (x.t == ct && !(cuid > uid[x.idx])))) return;
+    if (dedupe)
+      for (int i = 0; i < c.n; i++)
+        if (c.c[i].idx == x.idx) return;
+    c.insert(x, uid, cap);
+  }
+};
+
+// What a refill of a full candidate page needs to collect the segment's candidates
+// again: kept in the stack frame (written only when a page overflows, through an
+// out-of-line call), so that the common path holds none of it in registers.
+template <typename T>
+struct RefillState {
+  SubMask sm;
+  V3<T> mdisp;
+  uint32_t sp;
+  int mode;
 };
 
 // Occupants of a subpartition are binned by octant (key = ((subpart * 8 + octant) *
@@ -1017,10 +1066,10 @@ __device__ __forceinline__ uint32_t octant_of(const Geo<T>& g, V3<T> p, int ix, 
 // collide_mol (collision_utils.inl:464-515) against every reacting occupant of the
 // collected subpartitions
 // occupants of one subpartition (the partner species' octant ranges the segment box touches)
-template <typename T>
+template <typename T, class C>
 __device__ __forceinline__ void occupants_of(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos,
                                              V3<T> disp, uint32_t pmask, T movelen2, T sigma2, V3<T> lo, V3<T> hi,
-                                             uint32_t sp, Colls<T>& out) {
+                                             uint32_t sp, C& out) {
   const uint32_t om = g.oct_shift ? octants_touched(g, sp, lo, hi) : 1u;
   uint32_t m = pmask;
   while (m) {
@@ -1057,16 +1106,16 @@ __device__ __forceinline__ void occupants_of(const Geo<T>& g, const Cells<T>& ce
           VV<T> c;
           c.t = d / movelen2;
           c.idx = j;
-          out.insert(c, cells.uid);
+          out.insert(c, cells.uid, cells.maxc);
         }
       }
     }
   }
 }
 
-template <typename T>
+template <typename T, class C>
 __device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos, int species,
-                                       V3<T> disp, const SubSet& st, Colls<T>& out) {
+                                       V3<T> disp, const SubSet& st, C& out) {
   const Chem& ch = *g.chem;
   const uint32_t pmask = ch.partners[species];
   const T movelen2 = dot(disp, disp);
@@ -1081,9 +1130,9 @@ __device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, u
 
 // the same over a mask (set bits in index order; the candidate list keeps the
 // earliest collisions by time and id, so the visiting order does not matter)
-template <typename T>
+template <typename T, class C>
 __device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos, int species,
-                                       V3<T> disp, const SubMask& sm, Colls<T>& out) {
+                                       V3<T> disp, const SubMask& sm, C& out) {
   const Chem& ch = *g.chem;
   const uint32_t pmask = ch.partners[species];
   const T movelen2 = dot(disp, disp);
@@ -1126,19 +1175,97 @@ __device__ __noinline__ void recollect_mask(const Geo<T>& g, V3<T> pos, uint32_t
   if (!sm.bad) collect_for_molecules(g, pos, sp, mdisp, sm);
 }
 
-// the partner scan over a list of subpartitions, for segments whose set does not fit
-// the 4x4x4 mask (long moves, fine grids); out of line: rarely taken
+// The partner set visited without storing it: every subpartition the collection
+// generates (crossed ones and their neighbours, with repeats) has its occupants
+// scanned at once; the collector drops repeated candidates.
 template <typename T>
-__device__ __noinline__ void partners_by_list(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos,
-                                              uint32_t sp, V3<T> mdisp, int species, V3<T> remaining,
-                                              Colls<T>& colls, uint32_t& err) {
-  SubSet st;
-  st.n = 0;
-  st.n3 = (uint32_t)g.nsub2 * (uint32_t)g.nsub;
-  st.overflow = false;
-  collect_for_molecules(g, pos, sp, mdisp, st);
-  if (st.overflow) err |= ST_SET_OVERFLOW;
-  collide_with_occupants(g, cells, self, pos, species, remaining, st, colls);
+struct StreamSet {
+  const Cells<T>* cells;
+  CollsX<T>* out;
+  uint32_t self, pmask, n3;
+  V3<T> pos, disp, lo, hi;
+  T movelen2, sigma2;
+  template <typename G>
+  __device__ void insert3(const G& g, int x, int y, int z) {
+    const uint32_t sp = sub_of3(g, x, y, z);
+    if (sp >= n3) return;
+    occupants_of(g, *cells, self, pos, disp, pmask, movelen2, sigma2, lo, hi, sp, *out);
+  }
+};
+
+// partner modes of a segment: how its candidates were collected (a refill repeats it)
+enum : int { PM_MASK = 0, PM_LIST = 1, PM_STREAM = 2 };
+
+// candidates of a segment over its partner list (PM_LIST), or, when the list
+// overflows its capacity, along the walk (PM_STREAM); out: cursor and dedupe as the
+// caller sets them
+template <typename T>
+__device__ int partners_listed(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos, uint32_t sp,
+                               V3<T> mdisp, int species, V3<T> remaining, int mode, CollsX<T>& out, uint32_t& err) {
+  if (mode == PM_LIST) {
+    SubSet st;
+    st.n = 0;
+    st.cap = cells.maxset;
+    st.n3 = (uint32_t)g.nsub2 * (uint32_t)g.nsub;
+    st.overflow = false;
+    collect_for_molecules(g, pos, sp, mdisp, st);
+    if (!st.overflow) {
+      collide_with_occupants(g, cells, self, pos, species, remaining, st, out);
+      return PM_LIST;
+    }
+    err |= ST_SET_OVERFLOW;
+  }
+  StreamSet<T> ss;
+  ss.cells = &cells;
+  ss.out = &out;
+  ss.self = self;
+  ss.pmask = g.chem->partners[species];
+  ss.n3 = (uint32_t)g.nsub2 * (uint32_t)g.nsub;
+  ss.pos = pos;
+  ss.disp = remaining;
+  ss.movelen2 = dot(remaining, remaining);
+  ss.sigma2 = g.R * g.R;
+  const V3<T> e = pos + remaining;
+  const T mg = g.R * (T)1.01 + g.sp_edge * (T)1e-3;
+  ss.lo = v3<T>(min(pos.x, e.x) - mg, min(pos.y, e.y) - mg, min(pos.z, e.z) - mg);
+  ss.hi = v3<T>(max(pos.x, e.x) + mg, max(pos.y, e.y) + mg, max(pos.z, e.z) + mg);
+  out.dedupe = true;
+  collect_for_molecules(g, pos, sp, mdisp, ss);
+  return PM_STREAM;
+}
+
+// the partner scan over a list of subpartitions, for segments whose set does not fit
+// the 4x4x4 mask (long moves, fine grids); out of line: rarely taken. Returns the
+// partner mode used (PM_LIST or PM_STREAM).
+template <typename T>
+__device__ __noinline__ int partners_by_list(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos,
+                                             uint32_t sp, V3<T> mdisp, int species, V3<T> remaining,
+                                             Colls<T>& colls, uint32_t& err) {
+  CollsX<T> x{colls, false, false, (T)0, 0};
+  return partners_listed(g, cells, self, pos, sp, mdisp, species, remaining, PM_LIST, x, err);
+}
+
+template <typename T>
+__device__ __noinline__ void save_refill(RefillState<T>* rs, const SubMask& sm, V3<T> mdisp, uint32_t sp, int mode) {
+  rs->sm = sm;
+  rs->mdisp = mdisp;
+  rs->sp = sp;
+  rs->mode = mode;
+}
+
+// The next page of candidates after a page that overflowed: those after its last
+// one in time order, collected the way the first page was. Out of line: rare.
+template <typename T>
+__device__ __noinline__ void refill_colls(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos, int species,
+                                          V3<T> remaining, const RefillState<T>* rs, Colls<T>& colls, uint32_t& err) {
+  const VV<T> last = colls.c[colls.n - 1];
+  CollsX<T> x{colls, true, false, last.t, cells.uid[last.idx]};
+  colls.n = 0;
+  colls.overflow = false;
+  if (rs->mode == PM_MASK)
+    collide_with_occupants(g, cells, self, pos, species, remaining, rs->sm, x);
+  else
+    partners_listed(g, cells, self, pos, rs->sp, rs->mdisp, species, remaining, rs->mode, x, err);
 }
 
 // ------------------------------------------------------------------ exact disk
@@ -1444,22 +1571,50 @@ __device__ __noinline__ T exact_disk(const Geo<T>& g, V3<T> loc, V3<T> mv, int m
 
 // ------------------------------------------------------------------ reaction tests
 
-// test_bimolecular (rxn_utils.inl:336-414), single pathway; true if it fires. Out of
+// binary_search_double (rxn_utils.inl:301-321) with mult = 1 over a class's cumulative
+// pathway probabilities: the pathway a probability below the class's maximum selects
+// (RxnClass::get_pathway_index_for_probability; MCell3 src/react_cond.c:80-104)
+__device__ __forceinline__ int pathway_for(const double* cum, int npw, double match) {
+  int lo = 0, hi = npw - 1;
+  while (hi - lo > 1) {
+    const int mid = (hi + lo) / 2;
+    if (match > cum[mid])
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return match > cum[lo] ? hi : lo;
+}
+
+// test_bimolecular (rxn_utils.inl:336-414): the pathway that fires, or -1. Out of
 // line (fp64 arithmetic, run for few candidates): a smaller diffuse kernel.
 template <class D>
-__device__ __noinline__ bool test_bimolecular(double max_fixed_p, double scaling, D& draws) {
+__device__ __noinline__ int test_bimolecular(const double* cum, int npw, double scaling, D& draws) {
+  const double max_fixed_p = cum[npw - 1];
   double prob;
   if (max_fixed_p < scaling) {
     prob = draw_dbl(draws) * scaling;
-    return !(prob >= max_fixed_p);
+    if (prob >= max_fixed_p) return -1;
+  } else {
+    const float max_p = (float)max_fixed_p;
+    if (max_p >= scaling) {
+      // cannot scale enough: keep the proportions of the pathways
+      prob = draw_dbl(draws) * max_p;
+    } else {
+      prob = draw_dbl(draws) * scaling;
+      if (prob >= max_p) return -1;
+    }
   }
-  float max_p = (float)max_fixed_p;
-  if (max_p >= scaling) {
-    (void)draw_dbl(draws);
-    return true;
-  }
-  prob = draw_dbl(draws) * scaling;
-  return !(prob >= max_p);
+  return npw == 1 ? 0 : pathway_for(cum, npw, prob);
+}
+
+// which_unimolecular (rxn_utils.inl:774-783): the pathway of a unimolecular reaction
+// that happens; a draw only when the class has several
+template <class D>
+__device__ __forceinline__ int which_unimolecular(const double* cum, int npw, D& draws) {
+  if (npw <= 1) return 0;
+  const double match = draw_dbl(draws) * cum[npw - 1];
+  return pathway_for(cum, npw, match);
 }
 
 // test_intersect (rxn_utils.inl:593-626) for an absorptive surface class (rate DBL_GIGANTIC)
@@ -1500,6 +1655,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
   res.flip = 0;
   res.partner = NONE;
   res.t_abs = 0;
+  res.pathway = 0;
   res.rxn_pos = pos;
   const Chem& ch = *g.chem;
   const bool can_vol_react = allow_vv && ch.partners[species] != 0;
@@ -1510,6 +1666,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
   int bounces = 0;
   bool was_defunct = false;
   bool hit_wall;
+  RefillState<T> rs;  // written only when a candidate page overflows
   do {
     // ---- ray_trace_vol (diffuse_react_event.cpp:627-780)
     hit_wall = false;
@@ -1539,7 +1696,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
           hit_in_last = (cur == w.dest);
           break;
         }
-        if (res.err) break;
+        if (res.err & ST_ERRORS) break;
         if (!w.next(g)) break;
         cur = w.cur;
         if (!sm.bad) collect_crossing(g, w, sm);
@@ -1550,7 +1707,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
         used_tentative = true;
       }
     }
-    if (res.err) {
+    if (res.err & ST_ERRORS) {
       res.status = 3;
       break;
     }
@@ -1570,12 +1727,14 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
       } else if (!sm.bad) {
         collect_end(g, pos, pdisp, sm);
       }
+      int pmode = PM_MASK;
       if (!sm.bad) {
         collide_with_occupants(g, cells, self, pos, species, remaining, sm, colls);
       } else {
-        partners_by_list(g, cells, self, pos, sp, mdisp, species, remaining, colls, res.err);
+        pmode = partners_by_list(g, cells, self, pos, sp, mdisp, species, remaining, colls, res.err);
       }
-      if (colls.overflow) res.err |= ST_COLL_OVERFLOW;
+      // a full page: how to collect the next one (rare)
+      if (colls.overflow) save_refill(&rs, sm, mdisp, sp, pmode);
     }
     const V3<T> pos_at_start = pos;  // collision points are measured from here
     if (!hit_wall) {
@@ -1594,6 +1753,13 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
     // ---- collisions in time order (diffuse_react_event.cpp:450-572)
     bool wall_done = false;
     for (int i = 0; i <= colls.n; i++) {
+      if (i == colls.n && colls.overflow) {
+        // the page held only the earliest candidates: the next ones, in time order
+        res.err |= ST_COLL_OVERFLOW;
+        refill_colls(g, cells, self, pos_at_start, species, remaining, &rs, colls, res.err);
+        i = -1;
+        continue;
+      }
       bool take_wall;
       if (i == colls.n) {
         take_wall = hit_wall;
@@ -1676,13 +1842,16 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
         continue;
       }
       double scaling = (double)factor * r_rate_factor;
-      if (!test_bimolecular(ch.bimol_p[species][meta_of(q) & META_SPECIES_MASK], scaling, draws)) {
+      const uint32_t ps = meta_of(q) & META_SPECIES_MASK;
+      const int pw = test_bimolecular(ch.bimol_cum[species][ps], ch.bimol_npw[species][ps], scaling, draws);
+      if (pw < 0) {
         ev.put(4, cuid, 0, (double)c.t, t_abs, (double)cpos.x, (double)cpos.y, (double)cpos.z);
         continue;
       }
-      ev.put(5, cuid, 0, (double)c.t, t_abs, (double)cpos.x, (double)cpos.y, (double)cpos.z);
+      ev.put(5, cuid, pw, (double)c.t, t_abs, (double)cpos.x, (double)cpos.y, (double)cpos.z);
       was_defunct = true;
       res.status = 1;
+      res.pathway = pw;
       res.partner = c.idx;
       res.t_abs = t_abs;
       res.rxn_pos = cpos;

@@ -85,7 +85,16 @@ class DeviceEngineT : public DeviceEngine {
     MCG_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     int dev = 0;
     MCG_CUDA(cudaGetDevice(&dev));
+    dev_ = dev;
     MCG_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
+    // the fixed scratch of the allocation-free trace (mcg_trace_cases_static): its
+    // module is loaded, and its device memory taken, here rather than on the first
+    // such call (which may come when device memory is fully committed, or while
+    // another thread captures a graph)
+    {
+      const int rc = trace_static_scratch(&static_scratch_, err);
+      if (rc) return rc;
+    }
     {
       // k_diffuse runs persistent warps: as many blocks as can be resident. It uses no
       // shared memory; its spills and per-thread arrays live in local memory, cached in
@@ -130,6 +139,8 @@ class DeviceEngineT : public DeviceEngine {
     base_.cnt = d_cnt_;
     base_.debug_uid = ~0ull;
     base_.debug_log = nullptr;
+    base_.maxc = MAXC;
+    base_.maxset = MAXSET;
     if (capacity && ensure_capacity(capacity, err)) return -2;
     return 0;
   }
@@ -603,11 +614,15 @@ class DeviceEngineT : public DeviceEngine {
 
   int trace_static(uint32_t nc, const uint64_t* ids, const double* disp, const uint32_t* draws, uint32_t ndraws,
                    const double* rrf, const double* tst, double* out, std::string& err) override {
+    int cur = -1;
+    MCG_CUDA(cudaGetDevice(&cur));
+    if (cur != dev_) {
+      err = "mcg_trace_cases_static: the calling thread's current device is not the engine's";
+      return -1;
+    }
     int rc = sync(err);
     if (rc) return rc;
-    unsigned char* sc = nullptr;
-    rc = trace_static_scratch(&sc, err);
-    if (rc) return rc;
+    unsigned char* sc = static_scratch_;
     if (nc == 0) return 0;
     using L = TraceStaticLayout;
     uint64_t* d_ids = reinterpret_cast<uint64_t*>(sc + L::ids);
@@ -640,6 +655,25 @@ class DeviceEngineT : public DeviceEngine {
     MCG_CUDA(cudaGetLastError());
     MCG_CUDA(cudaMemcpyAsync(out, d_out, sizeof(double) * MCG_TRACE_RESULT_SIZE * nc, cudaMemcpyDeviceToHost, stream_));
     MCG_CUDA(cudaStreamSynchronize(stream_));
+    return 0;
+  }
+
+  int set_trace_limits(int maxc, int maxset, std::string& err) override {
+    if (maxc < 1 || maxc > MAXC || maxset < 1 || maxset > MAXSET) {
+      err = "trace limits out of range (1..16 candidates, 1..48 subpartitions)";
+      return -1;
+    }
+    base_.maxc = maxc;
+    base_.maxset = maxset;
+    invalidate_graphs();
+    return 0;
+  }
+
+  int fallbacks(uint64_t* out, std::string& err) override {
+    int rc = sync(err);
+    if (rc) return rc;
+    out[0] = cnt_.warn_coll_overflow;
+    out[1] = cnt_.warn_set_overflow;
     return 0;
   }
 
@@ -741,6 +775,9 @@ class DeviceEngineT : public DeviceEngine {
     bool has_obj = false;
     uint32_t n_cv = 0;     // counted objects
     double wall_density = 0;  // wall-list entries per subpartition (orders the key space)
+    // counts before the replica's first iteration (the t = 0 row of its count files):
+    // per species in the world, and per species and counted object
+    std::vector<uint64_t> init_world, init_cv;
     std::vector<double> obj_llf, obj_urb;  // bounding box of each object's walls
     // host copies for placing fp32 molecules: wall planes (n xyz, d), walls per
     // subpartition, and the grid
@@ -874,17 +911,26 @@ class DeviceEngineT : public DeviceEngine {
     }
     Chem c;
     std::memset(&c, 0, sizeof(c));
+    static_assert(MAXPW == MAX_PATHWAYS, "pathway tables of host and device differ");
     c.nsp = (int)ch.nsp;
     for (int a = 0; a < MAXSP; a++) {
       c.space_step[a] = ch.space_step[a];
       c.unimol_k[a] = ch.unimol_k[a];
-      c.uni_prod[a][0] = ch.uni_prod[a][0];
-      c.uni_prod[a][1] = ch.uni_prod[a][1];
+      c.uni_npw[a] = (int8_t)ch.uni_npw[a];
+      for (int k = 0; k < MAXPW; k++) {
+        c.uni_cum[a][k] = ch.uni_cum[a][k];
+        c.uni_prod[a][k][0] = (int8_t)ch.uni_prod[a][k][0];
+        c.uni_prod[a][k][1] = (int8_t)ch.uni_prod[a][k][1];
+      }
       for (int b = 0; b < MAXSP; b++) {
         c.bimol_p[a][b] = ch.bimol_p[a][b];
-        c.bimol_prod[a][b][0] = ch.bimol_prod[a][b][0];
-        c.bimol_prod[a][b][1] = ch.bimol_prod[a][b][1];
-        if (ch.bimol_p[a][b] >= 0) c.partners[a] |= 1u << b;
+        c.bimol_npw[a][b] = (int8_t)ch.bimol_npw[a][b];
+        for (int k = 0; k < MAXPW; k++) {
+          c.bimol_cum[a][b][k] = ch.bimol_cum[a][b][k];
+          c.bimol_prod[a][b][k][0] = (int8_t)ch.bimol_prod[a][b][k][0];
+          c.bimol_prod[a][b][k][1] = (int8_t)ch.bimol_prod[a][b][k][1];
+        }
+        if (ch.bimol_npw[a][b] > 0) c.partners[a] |= 1u << b;
       }
     }
     for (uint32_t w = 0; w < nw; w++)
@@ -1128,8 +1174,52 @@ class DeviceEngineT : public DeviceEngine {
     cnt_ = c2;
     rebin_it_ = cnt_.iteration;
     invalidate_graphs();
+    if (int rc = capture_initial_counts(err)) return rc;
     return status_to_error(c2.status, err);
   }
+
+  // counts of every replica that has not run an iteration yet, from the start offsets
+  // of its key ranges (and its counted-volume counts as just published)
+  int capture_initial_counts(std::string& err) {
+    const uint32_t* st = state(parity_).start;
+    for (uint32_t r = 0; r < max_rep_; r++) {
+      if (!reps_[r].used || geos_h_[r].it0 < cnt_.iteration) continue;
+      const Geo<T>& g = geos_h_[r];
+      const size_t span = (size_t)g.n3 << g.oct_shift;
+      std::vector<uint32_t> b(nsp_ + 1);
+      MCG_CUDA(cudaMemcpy2DAsync(b.data(), sizeof(uint32_t), st + g.kbase, sizeof(uint32_t) * span, sizeof(uint32_t),
+                                 nsp_ + 1, cudaMemcpyDeviceToHost, stream_));
+      Rep& R = reps_[r];
+      if (R.n_cv && d_cv_now_) {
+        std::vector<uint32_t> h((size_t)nsp_ * MAX_COUNTED);
+        MCG_CUDA(cudaMemcpyAsync(h.data(), d_cv_now_ + (size_t)r * nsp_ * MAX_COUNTED, sizeof(uint32_t) * h.size(),
+                                 cudaMemcpyDeviceToHost, stream_));
+        MCG_CUDA(cudaStreamSynchronize(stream_));
+        R.init_cv.assign((size_t)nsp_ * R.n_cv, 0);
+        for (uint32_t a = 0; a < nsp_; a++)
+          for (uint32_t k = 0; k < R.n_cv; k++) R.init_cv[a * R.n_cv + k] = h[a * MAX_COUNTED + k];
+      }
+      MCG_CUDA(cudaStreamSynchronize(stream_));
+      R.init_world.assign(nsp_, 0);
+      for (uint32_t a = 0; a < nsp_; a++) R.init_world[a] = b[a + 1] - b[a];
+    }
+    return 0;
+  }
+
+ public:
+  int initial_counts(uint32_t rep, uint64_t* world, uint64_t* inside, std::string& err) override {
+    if (rep >= max_rep_ || !reps_[rep].used || reps_[rep].init_world.size() != nsp_) {
+      err = "no initial counts for this replica";
+      return -1;
+    }
+    const Rep& R = reps_[rep];
+    for (uint32_t a = 0; a < nsp_; a++) world[a] = R.init_world[a];
+    if (inside)
+      for (size_t k = 0; k < R.init_cv.size(); k++) inside[k] = R.init_cv[k];
+    return 0;
+  }
+
+ private:
 
   unsigned grid(uint64_t n) const {
     uint64_t b = (n + TPB - 1) / TPB;
@@ -1359,6 +1449,8 @@ class DeviceEngineT : public DeviceEngine {
 
   State<T> base_{};
   cudaStream_t stream_ = nullptr;
+  int dev_ = 0;                             // device the engine was created on
+  unsigned char* static_scratch_ = nullptr;  // that device's fixed trace scratch
   int sms_ = 1;
   int bps_max_ = 1;
   int diffuse_grid_ = 1;

@@ -14,22 +14,82 @@
 
 namespace mcg {
 
+// Reaction classes of a model (BNG::RxnClass as test_bimolecular and
+// which_unimolecular use it, src4/rxn_utils.inl:336-414, :774-783): per reactant pair
+// and per unimolecular reactant, up to MAX_PATHWAYS pathways in the order they were
+// added, their cumulative probabilities (bimolecular) or rates times the time step
+// (unimolecular), and up to two products each (-1 = none).
+constexpr int MAX_PATHWAYS = 4;
 struct ChemHost {
   uint32_t nsp = 0;
   double space_step[16] = {0};
-  double unimol_k[16];
-  int uni_prod[16][2];
-  double bimol_p[16][16];
-  int bimol_prod[16][16][2];
+  double unimol_k[16];                    // k_tot = last cumulative rate, < 0: none
+  int uni_npw[16];
+  double uni_cum[16][MAX_PATHWAYS];
+  int uni_prod[16][MAX_PATHWAYS][2];
+  double bimol_p[16][16];                 // max_fixed_p = last cumulative probability, < 0: none
+  int bimol_npw[16][16];
+  double bimol_cum[16][16][MAX_PATHWAYS];
+  int bimol_prod[16][16][MAX_PATHWAYS][2];
   ChemHost() {
     for (int a = 0; a < 16; a++) {
       unimol_k[a] = -1;
-      uni_prod[a][0] = uni_prod[a][1] = -1;
+      uni_npw[a] = 0;
+      for (int k = 0; k < MAX_PATHWAYS; k++) {
+        uni_cum[a][k] = 0;
+        uni_prod[a][k][0] = uni_prod[a][k][1] = -1;
+      }
       for (int b = 0; b < 16; b++) {
         bimol_p[a][b] = -1;
-        bimol_prod[a][b][0] = bimol_prod[a][b][1] = -1;
+        bimol_npw[a][b] = 0;
+        for (int k = 0; k < MAX_PATHWAYS; k++) {
+          bimol_cum[a][b][k] = 0;
+          bimol_prod[a][b][k][0] = bimol_prod[a][b][k][1] = -1;
+        }
       }
     }
+  }
+  // appends a pathway; false if the class is full
+  bool add_bimol(int a, int b, double p, int p0, int p1) {
+    const int k = bimol_npw[a][b];
+    if (k >= MAX_PATHWAYS) return false;
+    const double c = (k ? bimol_cum[a][b][k - 1] : 0.0) + p;
+    for (int pass = 0; pass < (a == b ? 1 : 2); pass++) {
+      const int x = pass ? b : a, y = pass ? a : b;
+      bimol_cum[x][y][k] = c;
+      bimol_prod[x][y][k][0] = p0;
+      bimol_prod[x][y][k][1] = p1;
+      bimol_npw[x][y] = k + 1;
+      bimol_p[x][y] = c;
+    }
+    return true;
+  }
+  bool add_unimol(int a, double k_tot, int p0, int p1) {
+    const int k = uni_npw[a];
+    if (k >= MAX_PATHWAYS) return false;
+    uni_cum[a][k] = (k ? uni_cum[a][k - 1] : 0.0) + k_tot;
+    uni_prod[a][k][0] = p0;
+    uni_prod[a][k][1] = p1;
+    uni_npw[a] = k + 1;
+    unimol_k[a] = uni_cum[a][k];
+    return true;
+  }
+  // species that are products of some reaction and reactants of a bimolecular one
+  // (their same-step reactions are outside the GPU path); returns a bit mask
+  uint32_t reactive_products() const {
+    uint32_t prod = 0, react = 0;
+    for (uint32_t a = 0; a < nsp; a++) {
+      for (int k = 0; k < uni_npw[a]; k++)
+        for (int q = 0; q < 2; q++)
+          if (uni_prod[a][k][q] >= 0) prod |= 1u << uni_prod[a][k][q];
+      for (uint32_t b = 0; b < nsp; b++) {
+        if (bimol_npw[a][b]) react |= 1u << a;
+        for (int k = 0; k < bimol_npw[a][b]; k++)
+          for (int q = 0; q < 2; q++)
+            if (bimol_prod[a][b][k][q] >= 0) prod |= 1u << bimol_prod[a][b][k][q];
+      }
+    }
+    return prod & react;
   }
 };
 
@@ -79,6 +139,9 @@ class DeviceEngine {
   // last iteration or upload ([nsp][n_counted]), and their trajectory
   virtual int counted_counts(uint32_t rep, uint64_t* out, std::string& err) = 0;
   virtual int counted_trajectory(uint32_t rep, uint32_t n, uint64_t* out, std::string& err) = 0;
+  // counts before the replica's first iteration: world[nsp], and inside[nsp][n_counted]
+  // (may be null) for its counted objects
+  virtual int initial_counts(uint32_t rep, uint64_t* world, uint64_t* inside, std::string& err) = 0;
   // iterations the replica has run (it freezes after its n_iterations)
   virtual int replica_iterations(uint32_t rep, uint64_t* done, std::string& err) = 0;
   // the replica's counted objects and the engine iterations since it was added (the
@@ -93,6 +156,11 @@ class DeviceEngine {
   virtual int trace_static(uint32_t n, const uint64_t* ids, const double* disp, const uint32_t* draws,
                            uint32_t ndraws, const double* rrf, const double* tst, double* out, std::string& err) = 0;
   virtual void stats(uint64_t* iterations, uint64_t* mol_steps, uint64_t* launches) = 0;
+  // exact fallbacks taken: [0] traces that refilled a full candidate page, [1] traces
+  // whose partner list overflowed (partners scanned along the walk)
+  virtual int fallbacks(uint64_t* out, std::string& err) = 0;
+  // test hook: capacities of a candidate page (<= 16) and of the partner list (<= 48)
+  virtual int set_trace_limits(int maxc, int maxset, std::string& err) = 0;
   virtual void set_options(int use_graphs, int profile) = 0;
   // diffuse-kernel shape: resident blocks per SM of the persistent grid (0 = as many as fit)
   virtual int set_diffuse_blocks_per_sm(int blocks, std::string& err) = 0;
@@ -106,6 +174,11 @@ class DeviceEngine {
 // test hook: the device allocation after `after` more successful ones fails as if the
 // device were out of memory (once); negative: off (mcg_inject_device_alloc_failure)
 void set_alloc_failure(long long after);
+
+// reaction decisions on injected draws (parity harness; kind 0 test_bimolecular, 1
+// which_unimolecular): cum[n][MAX_PATHWAYS], npw[n], scaling[n] (kind 0), draws[n]
+int rxn_decisions(int kind, uint32_t n, const double* cum, const uint32_t* npw, const double* scaling,
+                  const uint32_t* draws, int32_t* out, std::string& err);
 
 DeviceEngine* make_engine_f64();
 DeviceEngine* make_engine_f32();

@@ -50,8 +50,8 @@ struct Counters {
   uint32_t status;       // ST_* bits
   uint32_t iteration;
   unsigned long long mol_steps;
-  unsigned long long warn_coll_overflow;
-  unsigned long long warn_set_overflow;
+  unsigned long long warn_coll_overflow;  // traces that refilled a full candidate page
+  unsigned long long warn_set_overflow;   // traces that scanned partners along the walk
   // first escapes (diagnostics): uid, species, iteration, start xyz, displacement xyz, final xyz, replica
   uint32_t n_esc;
   double esc[8][13];
@@ -60,6 +60,7 @@ struct Counters {
 struct Proposal {
   uint32_t i, partner;
   uint32_t cv;  // counted-volume bits of the reactant at the collision (the products')
+  uint32_t pw;  // pathway of the reaction class that fired
   uint64_t key;
   double t_abs;
   double x, y, z;
@@ -82,6 +83,7 @@ struct State {
   uint64_t debug_uid;  // molecule whose steps are logged into debug_log (diagnostics)
   double* debug_log;   // [64 iterations][271] or null
   uint32_t cap, prod_cap, prop_cap, nkeys, traj_cap;
+  int maxc, maxset;  // candidate page and partner list capacities (MAXC, MAXSET; tests lower them)
   // current sorted molecules and the next iteration's
   P4<T>* a_pos;
   uint64_t* a_uid;
@@ -182,6 +184,13 @@ __device__ __forceinline__ uint32_t key_of_rec(const State<T>& s, const P4<T>& b
   return key_of(geo_of(s, m), v3<T>(b.x, b.y, b.z), m & META_SPECIES_MASK);
 }
 
+// exact fallbacks a trace took (rare), one count per trace
+template <typename T>
+__device__ __forceinline__ void count_fallbacks(const State<T>& s, uint32_t terr) {
+  if (terr & ST_COLL_OVERFLOW) atomicAdd(&s.cnt->warn_coll_overflow, 1ull);
+  if (terr & ST_SET_OVERFLOW) atomicAdd(&s.cnt->warn_set_overflow, 1ull);
+}
+
 template <typename T>
 __device__ void add_product(const State<T>& s, int species, uint32_t rep, uint32_t cv, V3<T> pos, double birth,
                             uint64_t uid) {
@@ -202,14 +211,17 @@ __device__ void add_product(const State<T>& s, int species, uint32_t rep, uint32
   s.prod[k] = p;
 }
 
-// unimolecular outcome: the molecule is destroyed, products appear at its position
-// (outcome_unimolecular, diffuse_react_event.cpp:2939). it: the replica's own iteration.
+// unimolecular outcome: the pathway (which_unimolecular, one more draw of the
+// molecule's stream when the class has several), the molecule is destroyed, products
+// appear at its position (react_unimol_single_molecule / outcome_unimolecular,
+// diffuse_react_event.cpp:1809-1813, :2939). it: the replica's own iteration.
 template <typename T>
 __device__ __noinline__ void unimol_products(const State<T>& s, const Geo<T>& g, int species, uint32_t cv, V3<T> pos,
-                                             double t, uint64_t uid, uint32_t it) {
+                                             double t, uint64_t uid, uint32_t it, PhiloxDraws& draws) {
   const Chem& ch = *g.chem;
+  const int pw = which_unimolecular(ch.uni_cum[species], ch.uni_npw[species], draws);
   for (int k = 0; k < 2; k++) {
-    int ps = ch.uni_prod[species][k];
+    int ps = ch.uni_prod[species][pw][k];
     if (ps >= 0)
       add_product(s, ps, g.rep, cv, pos, t, mix64(uid ^ ((uint64_t)(it + 1) << 40) ^ (0xA5ull << 32) ^ (uint64_t)k));
   }
@@ -247,7 +259,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   }
   if (tuni <= 0.0) {
     // scheduled at or before the start of the step: react first (diffuse_single_molecule :214-223)
-    unimol_products(s, g, species, meta_cv(meta), pos, 0.0, uid, it);
+    unimol_products(s, g, species, meta_cv(meta), pos, 0.0, uid, it, draws);
     return 2;
   }
   // get_max_time (:164-198) with the barrier at the end of the iteration
@@ -281,6 +293,8 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
     cells.uid = s.a_uid;
     cells.start = s.start;
     cells.dead = dead;
+    cells.maxc = s.maxc;
+    cells.maxset = s.maxset;
     if (LOG) {
       MaybeEvents ev;
       ev.out = nullptr;
@@ -308,6 +322,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
       NoEvents ev;  // production kernel: no event code in the hot path
       r = trace_molecule<T>(g, cells, i, pos, species, disp, r_rate_factor, t_steps, 0.0, draws, ev);
     }
+    if (r.err & (ST_COLL_OVERFLOW | ST_SET_OVERFLOW)) count_fallbacks(s, r.err);
     err |= r.err;
   } else {
     r.status = 0;
@@ -318,6 +333,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
     Proposal p;
     p.i = i;
     p.partner = r.partner;
+    p.pw = (uint32_t)r.pathway;
     float tf = (float)r.t_abs;
     // earliest reaction wins; the molecule index makes keys unique within the iteration
     p.key = ((uint64_t)__float_as_uint(tf < 0.f ? 0.f : tf) << 32) | i;
@@ -332,7 +348,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   if (r.status == 2) return 2;
   if (max_time < 1.0) {
     // the unimolecular reaction happens where the molecule stopped
-    unimol_products(s, g, species, meta_cv(meta) ^ r.flip, r.pos, tuni, uid, it);
+    unimol_products(s, g, species, meta_cv(meta) ^ r.flip, r.pos, tuni, uid, it, draws);
     return 2;
   }
   const bool escaped = !in_partition(g, r.pos);
@@ -401,9 +417,8 @@ __global__ void __launch_bounds__(TPB, MCG_DIFFUSE_MIN_BLOCKS) k_diffuse(State<T
     }
     warp_count(s.counts, key, active && kind == 0);
   }
-  if (err) atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
-  if (err & ST_COLL_OVERFLOW) atomicAdd(&s.cnt->warn_coll_overflow, 1ull);
-  if (err & ST_SET_OVERFLOW) atomicAdd(&s.cnt->warn_set_overflow, 1ull);
+  if (err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG))
+    atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
   if (steps) atomicAdd(&s.cnt->mol_steps, (unsigned long long)steps);
 }
 
@@ -425,7 +440,7 @@ __device__ void commit(const State<T>& s, const Proposal& p) {
   const int sb = (int)(meta_of(s.a_pos[p.partner]) & META_SPECIES_MASK);
   const uint64_t uid = s.a_uid[p.i];
   for (int k = 0; k < 2; k++) {
-    int ps = ch.bimol_prod[sa][sb][k];
+    int ps = ch.bimol_prod[sa][sb][p.pw][k];
     if (ps >= 0) {
       add_product(s, ps, g.rep, p.cv, v3<T>((T)p.x, (T)p.y, (T)p.z), p.t_abs,
                   mix64(uid ^ ((uint64_t)(it + 1) << 40) ^ (0x5Aull << 32) ^ (uint64_t)k));
@@ -515,7 +530,8 @@ __global__ void __launch_bounds__(TPB) k_redo_trace(State<T> s, int round) {
   if (lane < per)
     for (uint32_t l = (blockIdx.x * (TPB / 32) + threadIdx.x / 32) * per + lane; l < n; l += nwarps * per)
       redo_one(s, cur[l], &s.cnt->redo_np[round], err);
-  if (err) atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
+  if (err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG))
+    atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
 }
 
 template <typename T>
@@ -585,7 +601,8 @@ __global__ void __launch_bounds__(TPB) k_redo(State<T> s) {
     const uint32_t* cur = s.losers + (size_t)half * s.prop_cap;
     for (uint32_t l = threadIdx.x; l < n_cur; l += blockDim.x) s.st[cur[l]] = 2;
   }
-  if (err) atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
+  if (err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG))
+    atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
 }
 
 // Products diffuse the rest of the step from their birth time (the queue of new
@@ -624,7 +641,7 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
       uint32_t cv = meta_cv(meta);
       bool dead = false;
       if (max_time <= 0.0) {
-        unimol_products(s, g, species, meta_cv(meta), pos, unimol_time, p.uid, it);
+        unimol_products(s, g, species, meta_cv(meta), pos, unimol_time, p.uid, it, draws);
         dead = true;
       } else {
         double steps = 1.0, t_steps = 1.0;
@@ -652,9 +669,12 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
           cells.uid = s.a_uid;
           cells.start = s.start;
           cells.dead = s.st;
+          cells.maxc = s.maxc;
+          cells.maxset = s.maxset;
           NoEvents ev;
           TraceOut<T> r = trace_molecule<T>(g, cells, NONE, pos, species, disp, r_rate_factor, t_steps, p.birth,
                                             draws, ev, false);
+          if (r.err & (ST_COLL_OVERFLOW | ST_SET_OVERFLOW)) count_fallbacks(s, r.err);
           err |= r.err;
           cv ^= r.flip;
           if (r.status == 2) {
@@ -664,7 +684,7 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
           }
         }
         if (!dead && unimol_time < 1.0) {
-          unimol_products(s, g, species, cv, pos, unimol_time, p.uid, it);
+          unimol_products(s, g, species, cv, pos, unimol_time, p.uid, it, draws);
           dead = true;
         }
       }
@@ -687,7 +707,8 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
     warp_count(s.counts, key, active && survive);
   }
   __syncthreads();
-  if (err) atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
+  if (err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG))
+    atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
 }
 
 // window of products for the next pass: [done, hi) where hi is a snapshot taken
@@ -1046,8 +1067,11 @@ __global__ void k_trace_cases(State<T> s, uint32_t ncases, const uint32_t* idx, 
   cells.uid = s.a_uid;
   cells.start = s.start;
   cells.dead = nullptr;
+  cells.maxc = s.maxc;
+  cells.maxset = s.maxset;
   V3<T> dv = v3<T>((T)disp[3 * c], (T)disp[3 * c + 1], (T)disp[3 * c + 2]);
   TraceOut<T> r = trace_molecule<T>(g, cells, i, v3<T>(rec.x, rec.y, rec.z), species, dv, rrf[c], tst[c], 0.0, d, ev);
+  count_fallbacks(s, r.err);
   int status = r.status;
   if (d.over) status = 3;
   o[0] = status;

@@ -23,3 +23,26 @@ struct mcg_engine {
   uint64_t next_uid = 0;
   mcg::DeviceEngine* dev = nullptr;   // created on first use (mcg_prepare / mcg_step)
 };
+
+namespace mcg {
+
+// Model features outside the GPU path are refused, with no fallback. A product of
+// any reaction that is also a reactant of a bimolecular reaction would, in the
+// reference, diffuse the rest of its birth step with vol-vol reaction tests (the
+// queue of new diffuse actions, src4/diffuse_react_event.cpp:116-129, :2883-2886);
+// the GPU's products diffuse the rest of that step without them, so such models
+// are refused (MCG_ERR_UNSUPPORTED) rather than run with other semantics.
+inline int check_model_supported(const mcg_engine& m, std::string& why) {
+  const uint32_t rp = m.chem.reactive_products();
+  if (rp) {
+    uint32_t s = 0;
+    while (!((rp >> s) & 1u)) s++;
+    why = "species " + std::to_string(s) +
+          " is a reaction product and a bimolecular reactant: same-step reactions of products are not on the "
+          "GPU path";
+    return MCG_ERR_UNSUPPORTED;
+  }
+  return MCG_OK;
+}
+
+}  // namespace mcg

@@ -257,6 +257,10 @@ int mcg_serve_submit(mcg_server* s, const mcg_engine* model, uint32_t n_iteratio
   if (model->dev) return sfail(s, MCG_ERR_ARG, "a submitted model must not have been prepared or stepped");
   if (model->cfg.n_species != s->cfg.n_species) return sfail(s, MCG_ERR_ARG, "model species count differs");
   if (!model->species_set) return sfail(s, MCG_ERR_ARG, "model without mcg_set_species");
+  {
+    std::string why;
+    if (int rc = mcg::check_model_supported(*model, why)) return sfail(s, rc, why);
+  }
   Request r;
   r.model = *model;
   r.model.err.clear();

@@ -4,21 +4,14 @@
 // MCG_TRACE_STATIC_MAX_CASES and MCG_TRACE_STATIC_MAX_DRAWS (about 0.6 MB).
 #include "mcg_trace_static.h"
 
-#include <mutex>
-
 namespace mcg {
 
 namespace {
-
-constexpr int kMaxDevices = 64;
 
 // Every device context holds its own copy of this array. Nothing in it has to
 // start at zero: each call resets the index slots it uses and the trace kernel
 // writes every output double of every case it runs.
 static __device__ __align__(256) unsigned char g_trace_scratch[TraceStaticLayout::bytes];
-
-std::mutex g_mu;
-unsigned char* g_addr[kMaxDevices] = {};
 
 __global__ void k_find_ids(const uint64_t* uid, uint32_t n, const uint64_t* want, uint32_t nc, uint32_t* idx) {
   __shared__ uint64_t w[MCG_TRACE_STATIC_MAX_CASES];
@@ -34,27 +27,15 @@ __global__ void k_find_ids(const uint64_t* uid, uint32_t n, const uint64_t* want
 }  // namespace
 
 int trace_static_scratch(unsigned char** addr, std::string& err) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) {
-    err = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
+  // resolved per call (engines call it once, when they are created): an address
+  // cached across engines would go stale after a cudaDeviceReset in the process
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_trace_scratch);
+  if (e != cudaSuccess || !p) {
+    err = std::string("cudaGetSymbolAddress of the trace scratch: ") + cudaGetErrorString(e);
     return MCG_ERR_CUDA;
   }
-  if (dev < 0 || dev >= kMaxDevices) {
-    err = "mcg_trace_cases_static supports device ordinals below 64";
-    return MCG_ERR_ARG;
-  }
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_trace_scratch);
-    if (e != cudaSuccess || !p) {
-      err = std::string("cudaGetSymbolAddress of the trace scratch: ") + cudaGetErrorString(e);
-      return MCG_ERR_CUDA;
-    }
-    g_addr[dev] = static_cast<unsigned char*>(p);
-  }
-  *addr = g_addr[dev];
+  *addr = static_cast<unsigned char*>(p);
   return MCG_OK;
 }
 

@@ -28,9 +28,11 @@ struct TraceStaticLayout {
   static constexpr size_t bytes = trace_static_up(out + 8 * (size_t)MCG_TRACE_RESULT_SIZE * kCases);
 };
 
-// Device address of the scratch on the current device. The first call for a
-// device looks it up with cudaGetSymbolAddress (with that device current) and
-// caches it; later calls only read the cache. Returns an MCG_* code.
+// Device address of the scratch on the current device (cudaGetSymbolAddress with
+// that device current). The first call on a device also loads the module that
+// holds the array (CUDA loads modules lazily), which takes its device memory;
+// engines call it once, when they are created, and keep the address. Returns an
+// MCG_* code.
 int trace_static_scratch(unsigned char** addr, std::string& err);
 
 // idx[c] = position of the live molecule whose id is want[c]; slots of ids that

@@ -159,12 +159,23 @@ int write_counts(mcg::DeviceEngine* dev, uint32_t rep, uint32_t nsp, const char*
       if (rc) return rc;
     }
   }
+  std::vector<uint32_t> rows;
+  std::vector<double> times;
+  // a window that reaches back to the replica's start begins with the counts before
+  // its first iteration, at t = 0, as the reference's count event runs before the
+  // diffusion event in iteration 0 (row index n_it stands for it)
+  std::vector<uint64_t> world0(nsp), inside0((size_t)nsp * n_cv);
+  const bool row0 = n_it == ran && dev->initial_counts(rep, world0.data(), inside0.data(), err) == 0;
+  err.clear();
+  if (row0) {
+    rows.push_back(n_it);
+    times.push_back(0.0);
+  }
   auto value = [&](uint32_t k, uint32_t c) -> double {
+    if (k == n_it) return (double)(objects[c] < 0 ? world0[species[c]] : inside0[(size_t)species[c] * n_cv + (uint32_t)objects[c]]);
     if (objects[c] < 0) return (double)world[(size_t)k * nsp + species[c]];
     return (double)inside[((size_t)k * nsp + species[c]) * n_cv + (uint32_t)objects[c]];
   };
-  std::vector<uint32_t> rows;
-  std::vector<double> times;
   for (uint32_t k = 0; k < n_it; k++) {
     const uint64_t it = ran - n_it + k + 1;  // iterations run after row k
     if (it % every) continue;

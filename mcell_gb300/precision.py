@@ -86,16 +86,19 @@ def wall_hit_mismatch(model: W.Model, n_cases=100_000, near_ids=None, seed=5, ch
 
 def count_error(model: W.Model, n_iter=50, seed=3):
     """Species-count trajectories of fp32 and fp64 runs (same seed) and of a second
-    fp64 run (another seed): largest relative difference of the product count."""
-    traj = {}
+    fp64 run (another seed): largest relative difference of the product count. Also
+    the exact fallbacks each run took (mcg_get_fallbacks)."""
+    traj, fallbacks = {}, {}
     for tag, prec, sd in (("fp32", "fp32", seed), ("fp64", "fp64", seed), ("fp64_other_seed", "fp64", seed + 1)):
         e = W.engine_for(model, prec, seed=sd)
         e.step(n_iter)
         traj[tag] = e.trajectory(n_iter).astype(np.float64)
+        fallbacks[tag] = list(e.fallbacks())
         e.close()
     ref = np.maximum(traj["fp64"], 1.0)
     rel = np.abs(traj["fp32"] - traj["fp64"]) / ref
     noise = np.abs(traj["fp64_other_seed"] - traj["fp64"]) / ref
     return {"iterations": n_iter, "max_rel_error_fp32_vs_fp64": float(rel.max()),
             "max_rel_difference_two_fp64_seeds": float(noise.max()),
-            "final_counts": {k: [int(x) for x in v[-1]] for k, v in traj.items()}}
+            "final_counts": {k: [int(x) for x in v[-1]] for k, v in traj.items()},
+            "fallbacks_page_refills_walk_scans": fallbacks}

@@ -150,8 +150,12 @@ typedef struct {
   double* space_step;
   unsigned char* wall_class; /* [nw * nspecies] */
   int* can_volwall;          /* species has a non-reflective wall class */
-  double* bimol_p;           /* [nspecies * nspecies], < 0 = no reaction */
-  int* bimol_rxn;            /* [nspecies * nspecies] reaction index or -1 */
+  double* bimol_p;           /* [nspecies * nspecies] max_fixed_p, < 0 = no reaction */
+  /* reaction class per reactant pair (BNG::RxnClass): its pathways' cumulative
+     probabilities and the reaction index of each pathway, in the order added */
+  double* bimol_cum;         /* [nspecies * nspecies * ORC_MAX_PATHWAYS] */
+  int* bimol_npw;            /* [nspecies * nspecies] */
+  int* bimol_rxn;            /* [nspecies * nspecies * ORC_MAX_PATHWAYS] reaction index */
   int* can_vol_react;
   /* molecules and per-subpartition occupant lists (set semantics) */
   omol* mols;
@@ -448,23 +452,33 @@ static oscene* scene_build(const double* origin, double partition_edge, unsigned
     for (unsigned i = 0; i < nspecies; i++)
       if (s->wall_class[(size_t)w * nspecies + i]) s->can_volwall[i] = 1;
   s->bimol_p = (double*)malloc(sizeof(double) * nspecies * nspecies);
-  s->bimol_rxn = (int*)malloc(sizeof(int) * nspecies * nspecies);
-  for (unsigned i = 0; i < nspecies * nspecies; i++) {
-    s->bimol_p[i] = -1;
-    s->bimol_rxn[i] = -1;
-  }
+  s->bimol_cum = (double*)calloc((size_t)nspecies * nspecies * ORC_MAX_PATHWAYS, sizeof(double));
+  s->bimol_npw = (int*)calloc((size_t)nspecies * nspecies, sizeof(int));
+  s->bimol_rxn = (int*)malloc(sizeof(int) * nspecies * nspecies * ORC_MAX_PATHWAYS);
+  for (unsigned i = 0; i < nspecies * nspecies; i++) s->bimol_p[i] = -1;
+  for (unsigned i = 0; i < nspecies * nspecies * ORC_MAX_PATHWAYS; i++) s->bimol_rxn[i] = -1;
   s->can_vol_react = (int*)calloc(nspecies, sizeof(int));
   s->occ = (idvec*)calloc(s->nsub3, sizeof(idvec));
   return s;
 }
 
-static void scene_set_bimol(oscene* s, unsigned r, unsigned a, unsigned b, double p) {
-  s->bimol_p[a * s->nspecies + b] = p;
-  s->bimol_p[b * s->nspecies + a] = p;
-  s->bimol_rxn[a * s->nspecies + b] = (int)r;
-  s->bimol_rxn[b * s->nspecies + a] = (int)r;
+/* reaction r (probability p) of the pair (a, b): a further pathway of the pair's class;
+   returns 0, or -1 when the class is full */
+static int scene_set_bimol(oscene* s, unsigned r, unsigned a, unsigned b, double p) {
+  const unsigned ab = a * s->nspecies + b, ba = b * s->nspecies + a;
+  const int k = s->bimol_npw[ab];
+  if (k >= ORC_MAX_PATHWAYS) return -1;
+  const double c = (k ? s->bimol_cum[ab * ORC_MAX_PATHWAYS + k - 1] : 0.0) + p;
+  for (int pass = 0; pass < (ab == ba ? 1 : 2); pass++) {
+    const unsigned q = pass ? ba : ab;
+    s->bimol_cum[q * ORC_MAX_PATHWAYS + k] = c;
+    s->bimol_rxn[q * ORC_MAX_PATHWAYS + k] = (int)r;
+    s->bimol_npw[q] = k + 1;
+    s->bimol_p[q] = c;
+  }
   s->can_vol_react[a] = 1;
   s->can_vol_react[b] = 1;
+  return 0;
 }
 
 static void scene_free(oscene* s) {
@@ -480,6 +494,8 @@ static void scene_free(oscene* s) {
   free(s->wall_class);
   free(s->can_volwall);
   free(s->bimol_p);
+  free(s->bimol_cum);
+  free(s->bimol_npw);
   free(s->bimol_rxn);
   free(s->can_vol_react);
   free(s);
@@ -560,7 +576,7 @@ typedef struct {
   v3 pos;
   unsigned partner; /* molecule id (vol-vol) */
   unsigned wall;
-  double p;         /* max_fixed_p of the reaction (vol-vol) */
+  unsigned cls;     /* reaction class of the pair (vol-vol): index a * nspecies + b */
 } ocoll;
 
 #define MAX_COLL 256
@@ -881,7 +897,7 @@ static int ray_trace_vol(const oscene* s, unsigned id, v3* pos, unsigned* sp, un
           c->pos = cp;
           c->partner = pid;
           c->wall = IDX_INVALID;
-          c->p = p;
+          c->cls = species * s->nspecies + s->mols[pid].species;
         }
       }
     }
@@ -893,8 +909,21 @@ static int ray_trace_vol(const oscene* s, unsigned id, v3* pos, unsigned* sp, un
   return res;
 }
 
-/* test_bimolecular (rxn_utils.inl:336-414) for a single-pathway class */
-static int test_bimolecular(double max_fixed_p, double scaling, orng* rng) {
+/* binary_search_double (rxn_utils.inl:301-321) with mult = 1: the pathway a probability
+   selects from a class's cumulative probabilities (get_pathway_index_for_probability) */
+static int pathway_for(const double* cum, int npw, double match) {
+  int lo = 0, hi = npw - 1;
+  while (hi - lo > 1) {
+    int mid = (hi + lo) / 2;
+    if (match > cum[mid]) lo = mid;
+    else hi = mid;
+  }
+  return match > cum[lo] ? hi : lo;
+}
+
+/* test_bimolecular (rxn_utils.inl:336-414): the pathway that fires, or -2 */
+static int test_bimolecular(const double* cum, int npw, double scaling, orng* rng) {
+  double max_fixed_p = cum[npw - 1];
   double prob;
   if (max_fixed_p < scaling) {
     prob = rng_dbl(rng) * scaling;
@@ -910,8 +939,14 @@ static int test_bimolecular(double max_fixed_p, double scaling, orng* rng) {
       if (prob >= max_p) return -2;
     }
   }
-  (void)prob;
-  return 0; /* one pathway: binary search over one cumulative bound returns 0 */
+  return pathway_for(cum, npw, prob);
+}
+
+/* which_unimolecular (rxn_utils.inl:774-783): a draw only for several pathways */
+static int which_unimolecular(const double* cum, int npw, orng* rng) {
+  if (npw <= 1) return 0;
+  double match = rng_dbl(rng) * cum[npw - 1];
+  return pathway_for(cum, npw, match);
 }
 
 /* test_intersect (rxn_utils.inl:593-626) for an absorptive class (rate DBL_GIGANTIC) */
@@ -1206,6 +1241,7 @@ static double exact_disk(const oscene* s, v3 loc, v3 mv, double R, unsigned movi
 typedef struct {
   int status;       /* 0 finished, 1 reacted, 2 absorbed, 3 error */
   unsigned partner; /* reaction partner */
+  int pathway;      /* pathway of the pair's reaction class that fired */
   double rxn_time;  /* absolute time of the reaction / absorption */
   v3 rxn_pos;
   double elapsed, t_steps;
@@ -1252,13 +1288,15 @@ static ostep diffuse_vol(oscene* s, unsigned id, v3 disp, orng* rng, double r_ra
           continue;
         }
         double scaling = factor * r_rate_factor;
-        if (test_bimolecular(c->p, scaling, rng) < 0) {
+        int pw = test_bimolecular(&s->bimol_cum[c->cls * ORC_MAX_PATHWAYS], s->bimol_npw[c->cls], scaling, rng);
+        if (pw < 0) {
           put_event(out, 4, (int)c->partner, 0, c->time, t_abs, c->pos);
           continue;
         }
-        put_event(out, 5, (int)c->partner, 0, c->time, t_abs, c->pos);
+        put_event(out, 5, (int)c->partner, pw, c->time, t_abs, c->pos);
         was_defunct = 1;
         res.status = 1;
+        res.pathway = pw;
         res.partner = c->partner;
         res.rxn_time = t_abs;
         res.rxn_pos = c->pos;
@@ -1406,12 +1444,25 @@ double orc_exact_disk(void* sp, const double* loc, const double* mv, unsigned mo
 }
 
 int orc_test_bimolecular(double max_fixed_p, double scaling, unsigned draw) {
+  return orc_test_bimolecular_pw(&max_fixed_p, 1, scaling, draw);
+}
+
+int orc_test_bimolecular_pw(const double* cum, unsigned n, double scaling, unsigned draw) {
   orng rng;
   memset(&rng, 0, sizeof(rng));
   rng.injected = 1;
   rng.draws = &draw;
   rng.n = 1;
-  return test_bimolecular(max_fixed_p, scaling, &rng);
+  return test_bimolecular(cum, (int)n, scaling, &rng);
+}
+
+int orc_which_unimolecular(const double* cum, unsigned n, unsigned draw) {
+  orng rng;
+  memset(&rng, 0, sizeof(rng));
+  rng.injected = 1;
+  rng.draws = &draw;
+  rng.n = 1;
+  return which_unimolecular(cum, (int)n, &rng);
 }
 
 double orc_time_of_unimol(double k_tot, unsigned draw) {
@@ -1430,8 +1481,10 @@ typedef struct {
   orng rng;
   unsigned nbimol, nunimol;
   int* bimol_prod;     /* [nbimol * 2] */
-  int* unimol_of;      /* [nspecies] unimol rxn index or -1 */
-  double* unimol_k;    /* [nunimol] */
+  /* unimolecular class of each species: cumulative rates and reaction index per pathway */
+  int* uni_npw;        /* [nspecies] */
+  double* uni_cum;     /* [nspecies * ORC_MAX_PATHWAYS] */
+  int* uni_rxn;        /* [nspecies * ORC_MAX_PATHWAYS] */
   int* unimol_prod;    /* [nunimol * 2] */
   unsigned* queue;     /* new diffuse actions (ids), FIFO within an iteration */
   unsigned nqueue, capqueue;
@@ -1460,13 +1513,18 @@ void* orc_engine_new(const orc_engine_desc* d) {
     e->bimol_prod[2 * r + 1] = d->bimol_products[2 * r + 1];
   }
   e->nunimol = d->nunimol;
-  e->unimol_of = (int*)malloc(sizeof(int) * d->nspecies);
-  for (unsigned i = 0; i < d->nspecies; i++) e->unimol_of[i] = -1;
-  e->unimol_k = (double*)malloc(sizeof(double) * (d->nunimol ? d->nunimol : 1));
+  e->uni_npw = (int*)calloc(d->nspecies, sizeof(int));
+  e->uni_cum = (double*)calloc((size_t)d->nspecies * ORC_MAX_PATHWAYS, sizeof(double));
+  e->uni_rxn = (int*)calloc((size_t)d->nspecies * ORC_MAX_PATHWAYS, sizeof(int));
   e->unimol_prod = (int*)malloc(sizeof(int) * 2 * (d->nunimol ? d->nunimol : 1));
   for (unsigned r = 0; r < d->nunimol; r++) {
-    e->unimol_of[d->unimol_reactant[r]] = (int)r;
-    e->unimol_k[r] = d->unimol_k[r];
+    const unsigned a = d->unimol_reactant[r];
+    const int k = e->uni_npw[a];
+    if (k < ORC_MAX_PATHWAYS) {
+      e->uni_cum[a * ORC_MAX_PATHWAYS + k] = (k ? e->uni_cum[a * ORC_MAX_PATHWAYS + k - 1] : 0.0) + d->unimol_k[r];
+      e->uni_rxn[a * ORC_MAX_PATHWAYS + k] = (int)r;
+      e->uni_npw[a] = k + 1;
+    }
     e->unimol_prod[2 * r] = d->unimol_products[2 * r];
     e->unimol_prod[2 * r + 1] = d->unimol_products[2 * r + 1];
   }
@@ -1485,8 +1543,9 @@ void orc_engine_free(void* ep) {
   if (!e) return;
   scene_free(e->s);
   free(e->bimol_prod);
-  free(e->unimol_of);
-  free(e->unimol_k);
+  free(e->uni_npw);
+  free(e->uni_cum);
+  free(e->uni_rxn);
   free(e->unimol_prod);
   free(e->queue);
   free(e);
@@ -1515,12 +1574,12 @@ static void create_product(oengine* e, int species, v3 pos, double time) {
 
 /* pick_unimol_rxn_class_and_set_rxn_time (diffuse_react_event.cpp:1731-1760) */
 static void set_unimol_time(oengine* e, omol* m, double now) {
-  int r = e->unimol_of[m->species];
-  if (r < 0) {
+  const int npw = e->uni_npw[m->species];
+  if (npw == 0) {
     m->unimol_time = TIME_INVALID;
     return;
   }
-  m->unimol_time = now + time_of_unimol(e->unimol_k[r], &e->rng);
+  m->unimol_time = now + time_of_unimol(e->uni_cum[m->species * ORC_MAX_PATHWAYS + npw - 1], &e->rng);
 }
 
 /* DiffuseReactEvent::diffuse_single_molecule (diffuse_react_event.cpp:201-337) */
@@ -1531,8 +1590,10 @@ static void diffuse_single(oengine* e, unsigned id) {
   double start = m->diffusion_time;
   if (m->unimol_time != TIME_INVALID && m->unimol_time <= start) {
     /* react_unimol_single_molecule / outcome_unimolecular (:1764-1826, :2939) */
-    int r = e->unimol_of[m->species];
-    if (r >= 0) {
+    const int npw = e->uni_npw[m->species];
+    if (npw > 0) {
+      const double* cum = &e->uni_cum[m->species * ORC_MAX_PATHWAYS];
+      const int r = e->uni_rxn[m->species * ORC_MAX_PATHWAYS + which_unimolecular(cum, npw, &e->rng)];
       v3 pos = m->pos;
       double t = m->unimol_time;
       set_defunct(e, id);
@@ -1585,7 +1646,8 @@ static void diffuse_single(oengine* e, unsigned id) {
       /* outcome_bimolecular / outcome_products_random (:1833-1895, :2446-2933) */
       m->defunct = 1;
       unsigned partner = r.partner;
-      unsigned rx = (unsigned)s->bimol_rxn[m->species * s->nspecies + s->mols[partner].species];
+      unsigned rx =
+          (unsigned)s->bimol_rxn[(m->species * s->nspecies + s->mols[partner].species) * ORC_MAX_PATHWAYS + r.pathway];
       set_defunct(e, partner);
       create_product(e, e->bimol_prod[2 * rx], r.rxn_pos, r.rxn_time);
       create_product(e, e->bimol_prod[2 * rx + 1], r.rxn_pos, r.rxn_time);

@@ -27,6 +27,9 @@ extern "C" {
 #define ORC_EV_SIZE 8
 #define ORC_EV_MAX 32
 #define ORC_RES_SIZE (ORC_RES_HDR + ORC_EV_MAX * ORC_EV_SIZE)
+/* pathways of one reaction class (reactions of one reactant pair, or unimolecular
+   reactions of one species, in the order given) */
+#define ORC_MAX_PATHWAYS 4
 
 void* orc_scene_new(
     const double* origin, double partition_edge, unsigned nsub, double rxn_radius,
@@ -44,6 +47,10 @@ void orc_diffuse_case(
     double r_rate_factor, double t_steps, double* out);
 double orc_exact_disk(void* s, const double* loc, const double* mv, unsigned moving, unsigned target);
 int orc_test_bimolecular(double max_fixed_p, double scaling, unsigned draw);
+/* the same over a class of n pathways (cumulative probabilities); pathway or < 0 */
+int orc_test_bimolecular_pw(const double* cum, unsigned n, double scaling, unsigned draw);
+/* which_unimolecular over n pathways (cumulative rates); the draw is used for n > 1 */
+int orc_which_unimolecular(const double* cum, unsigned n, unsigned draw);
 double orc_time_of_unimol(double k_tot, unsigned draw);
 
 /* serial engine */
@@ -59,11 +66,11 @@ typedef struct orc_engine_desc {
   unsigned nspecies;
   const double* space_steps;          /* internal length units per time step */
   const unsigned char* wall_class;    /* [nw * nspecies]: 0 reflect, 1 transparent, 2 absorptive */
-  unsigned nbimol;
+  unsigned nbimol;                    /* reactions of one pair are the pathways of its class */
   const unsigned* bimol_reactants;    /* [nbimol * 2] */
-  const double* bimol_p;              /* max_fixed_p per reaction */
+  const double* bimol_p;              /* probability per reaction */
   const int* bimol_products;          /* [nbimol * 2], -1 = none */
-  unsigned nunimol;
+  unsigned nunimol;                   /* reactions of one species are the pathways of its class */
   const unsigned* unimol_reactant;    /* [nunimol] */
   const double* unimol_k;             /* rate * time_step (per iteration) */
   const int* unimol_products;         /* [nunimol * 2], -1 = none */

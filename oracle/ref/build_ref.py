@@ -18,7 +18,9 @@ the reference sources where they lie:
 It also compiles the reference's ISAAC64 and ziggurat generator
 (src/isaac64.c, src/rng.c through src/rng.h) into the same library.
 
-Usage: python oracle/ref/build_ref.py [--ref /root/reference]
+Usage: python oracle/ref/build_ref.py [--ref <reference checkout>]
+The checkout defaults to $MCELL_REFERENCE_ROOT, else a directory named
+"reference" beside this repository.
 Test infrastructure only; the product never loads oracle/_ref.
 """
 import argparse
@@ -54,6 +56,7 @@ FUNCS = [
     ("src4/rxn_utils.inl", "test_bimolecular", "MCell::RxnUtils"),
     ("src4/rxn_utils.inl", "test_intersect", "MCell::RxnUtils"),
     ("src4/rxn_utils.inl", "time_of_unimol", "MCell::RxnUtils"),
+    ("src4/rxn_utils.inl", "which_unimolecular", "MCell::RxnUtils"),
     ("src4/diffuse_react_event.cpp", "sort_collisions_by_time", "MCell"),
     ("src4/diffuse_react_event.cpp", "ray_trace_vol", "MCell"),
 ]
@@ -165,7 +168,7 @@ def compile_lib(ref: Path, pos_bytes: int, out: Path, verbose=False):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=os.environ.get("MCELL_REFERENCE_ROOT", "/root/reference"))
+    ap.add_argument("--ref", default=os.environ.get("MCELL_REFERENCE_ROOT", str(ORACLE.parent.parent / "reference")))
     ap.add_argument("-v", action="store_true")
     a = ap.parse_args()
     ref = Path(a.ref)

@@ -19,6 +19,9 @@
  *   then 32 events of 8 doubles: kind, index, side, t_rel, t_abs, x, y, z
  *   kinds: 1 reflect, 2 transparent, 3 absorbed, 4 partner tested (no rxn),
  *          5 partner rxn fired, 6 partner occluded by a wall (exact_disk < 0)
+ *   side: the wall side (1 front, 2 back) of wall events; the pathway of the
+ *   pair's reaction class for kind 5 (reactions given for one pair in
+ *   ref_scene_new are the pathways of its class, in that order)
  */
 #include <cstdio>
 
@@ -108,15 +111,23 @@ void* ref_scene_new(
   }
 
   s->can_vol_react.assign(nspecies, 0);
-  s->rxn_store.resize(nrxn);
-  for (unsigned r = 0; r < nrxn; r++) {
-    s->rxn_store[r].type = BNG::RxnType::Standard;
-    s->rxn_store[r].cum_probs.push_back(rxn_p[r]);
-  }
+  // one reaction class per reactant pair; the reactions of a pair are its pathways,
+  // with cumulative probabilities (BNG::RxnClass::cum_probs)
+  s->rxn_store.reserve(nrxn);
   for (unsigned r = 0; r < nrxn; r++) {
     unsigned a = rxn_ab[2 * r], b = rxn_ab[2 * r + 1];
-    p.rxns.bimol[std::make_pair(a, b)] = &s->rxn_store[r];
-    p.rxns.bimol[std::make_pair(b, a)] = &s->rxn_store[r];
+    auto it = p.rxns.bimol.find(std::make_pair(a, b));
+    if (it == p.rxns.bimol.end()) {
+      s->rxn_store.emplace_back();
+      BNG::RxnClass* rc = &s->rxn_store.back();
+      rc->type = BNG::RxnType::Standard;
+      rc->cum_probs.push_back(rxn_p[r]);
+      p.rxns.bimol[std::make_pair(a, b)] = rc;
+      p.rxns.bimol[std::make_pair(b, a)] = rc;
+    }
+    else {
+      it->second->cum_probs.push_back(it->second->cum_probs.back() + rxn_p[r]);
+    }
     s->can_vol_react[a] = 1;
     s->can_vol_react[b] = 1;
   }
@@ -250,7 +261,7 @@ void ref_diffuse_case(
           put_event(out, 4, collision.colliding_molecule_id, 0, collision.time, t_abs, collision.pos);
           continue;
         }
-        put_event(out, 5, collision.colliding_molecule_id, 0, collision.time, t_abs, collision.pos);
+        put_event(out, 5, collision.colliding_molecule_id, i, collision.time, t_abs, collision.pos);
         was_defunct = true;
         status = 1;
         break;
@@ -320,6 +331,29 @@ int ref_test_bimolecular(double max_fixed_p, double scaling, unsigned draw) {
   rng.draws = &draw;
   rng.n = 1;
   return RxnUtils::test_bimolecular(p, &rc, rng, a, b, scaling, 0, 0);
+}
+
+// test_bimolecular over a class of n pathways (cumulative probabilities): pathway or < 0
+int ref_test_bimolecular_pw(const double* cum, unsigned n, double scaling, unsigned draw) {
+  Partition p;
+  BNG::RxnClass rc;
+  rc.cum_probs.assign(cum, cum + n);
+  Molecule a, b;
+  ShimRng rng;
+  rng.draws = &draw;
+  rng.n = 1;
+  return RxnUtils::test_bimolecular(p, &rc, rng, a, b, scaling, 0, 0);
+}
+
+// which_unimolecular over a class of n pathways (cumulative rates)
+int ref_which_unimolecular(const double* cum, unsigned n, unsigned draw) {
+  BNG::RxnClass rc;
+  rc.cum_probs.assign(cum, cum + n);
+  Molecule m;
+  ShimRng rng;
+  rng.draws = &draw;
+  rng.n = 1;
+  return RxnUtils::which_unimolecular(m, &rc, rng);
 }
 
 double ref_time_of_unimol(double k_tot, unsigned draw) {

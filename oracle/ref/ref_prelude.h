@@ -16,25 +16,20 @@
 #define CHECK_STIME_MAX(x) do { } while (0)
 #endif
 
+namespace MCell {
+namespace RxnUtils {
+// the reference's own search, compiled further down from src4/rxn_utils.inl
+static int binary_search_double(const std::vector<double>& A, double match, int max_idx, double mult);
+}  // namespace RxnUtils
+}  // namespace MCell
+
 namespace BNG {
-// pathway for a probability drawn below max_fixed_p: first cumulative bound above it,
-// the same search MCell3 uses (binary_search_double, src4/rxn_utils.inl:301)
+// pathway for a probability drawn below max_fixed_p. libbng is not in the tree; MCell3's
+// test_bimolecular selects it with binary_search_double over the class's cumulative
+// probabilities up to index n_pathways - 1 (src/react_cond.c:166-172), and so does this
+// stand-in, with the reference's binary_search_double (src4/rxn_utils.inl:301)
 inline int RxnClass::get_pathway_index_for_probability(const double prob, const double mult) const {
-  int max_idx = (int)cum_probs.size() - 1;
-  int min_idx = 0;
-  while (max_idx - min_idx > 1) {
-    int mid = (max_idx + min_idx) / 2;
-    if (prob > cum_probs[mid] * mult) {
-      min_idx = mid;
-    }
-    else {
-      max_idx = mid;
-    }
-  }
-  if (prob > cum_probs[min_idx] * mult) {
-    return max_idx;
-  }
-  return min_idx;
+  return MCell::RxnUtils::binary_search_double(cum_probs, prob, (int)cum_probs.size() - 1, mult);
 }
 } // namespace BNG
 

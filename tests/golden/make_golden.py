@@ -88,6 +88,71 @@ def partner_cases(rng, sc: H.Scene, n):
     return cases
 
 
+def record_scene(ref64, rng, name, sc, cases):
+    """Runs the cases through the reference's routines and writes diffuse_<name>.npz."""
+    h = ref64.scene(sc)
+    mols = np.array([c[0] for c in cases], np.uint32)
+    disps = np.array([c[1] for c in cases], np.float64)
+    draws = rng.integers(0, 2 ** 32, size=(len(cases), NDRAWS), dtype=np.uint64).astype(np.uint32)
+    # a share of cases with draws that make reactions fire (small uniforms)
+    draws[::3, :] = (draws[::3, :] >> 6).astype(np.uint32)
+    res = np.array([h.diffuse_case(int(m), d, dr) for m, d, dr in zip(mols, disps, draws)])
+    nev = int(res[:, 6].max())
+    keep = H.RES_HDR + H.EV_SIZE * max(1, min(nev, H.EV_MAX))
+    info = h.info()
+    wc_ref = h.wall_consts(len(sc.tris))
+    counts, lst = h.walls_in_subparts(sc.nsub ** 3)
+    np.savez_compressed(
+        HERE / f"diffuse_{name}.npz",
+        origin=sc.origin, partition_edge=sc.partition_edge, nsub=sc.nsub, rxn_radius=sc.rxn_radius,
+        verts=sc.verts, tris=sc.tris, space_steps=sc.space_steps, wall_class=sc.wall_class,
+        rxn_ab=sc.rxn_ab, rxn_p=sc.rxn_p, mol_pos=sc.mol_pos, mol_species=sc.mol_species,
+        mols=mols, disps=disps, draws=draws, results=res[:, :keep],
+        info=info, wall_consts=wc_ref, wsp_counts=counts, wsp_list=lst)
+    return res
+
+
+def pathway_fixtures(ref64):
+    """Reaction classes with several pathways (BNG::RxnClass cum_probs): a closed cube
+    where A + B has three pathways and A + A two (kind-5 events record the pathway
+    that fired), and test_bimolecular / which_unimolecular on injected draws over
+    classes of 1-4 pathways, including the branch where the class's probability
+    cannot be scaled enough (max_fixed_p >= scaling)."""
+    rng = np.random.default_rng(20261204)
+    sc = H.cube_scene(rng, n_mol=1500, nsub=12, partition_um=1.2)
+    sc.rxn_ab = np.array([[0, 1], [0, 1], [0, 1], [0, 0], [0, 0]], np.uint32)
+    sc.rxn_p = np.array([0.15, 0.25, 0.1, 0.3, 0.2])
+    cases = [(m, d) for (m, d, _) in H.random_cases(rng, sc, 300, scale=2.0, near_wall_frac=0.3)]
+    cases += partner_cases(rng, sc, 700)
+    res = record_scene(ref64, rng, "pathways", sc, cases)
+    fired = res[:, H.RES_HDR::H.EV_SIZE] == 5
+    sides = res[:, H.RES_HDR + 2::H.EV_SIZE][fired]
+    print("pathways", len(cases), "cases; pathways fired", np.unique(sides, return_counts=True))
+    n = 800
+    npw = rng.integers(1, 5, n)
+    cum = np.zeros((n, 4))
+    for i in range(n):
+        p = rng.uniform(0, 0.6, npw[i]) * (4.0 if i % 5 == 0 else 1.0)
+        cum[i, :npw[i]] = np.cumsum(p)
+    scaling = rng.uniform(0, 1.5, n)
+    scaling[::7] = 1.0
+    U = rng.integers(0, 2 ** 32, size=n, dtype=np.uint64).astype(np.uint32)
+    U[::3] >>= 2
+    bim = np.array([ref64.test_bimolecular_pw(cum[i, :npw[i]], scaling[i], U[i]) for i in range(n)], np.int32)
+    m = 500
+    unpw = rng.integers(1, 5, m)
+    ucum = np.zeros((m, 4))
+    for i in range(m):
+        ucum[i, :unpw[i]] = np.cumsum(rng.uniform(0, 2e-3, unpw[i]))
+    Uu = rng.integers(0, 2 ** 32, size=m, dtype=np.uint64).astype(np.uint32)
+    Uu[:3] = [0, 1, 2 ** 32 - 1]
+    uni = np.array([ref64.which_unimolecular(ucum[i, :unpw[i]], Uu[i]) for i in range(m)], np.int32)
+    np.savez_compressed(HERE / "rxn_pathways.npz", cum=cum, npw=npw.astype(np.uint32), scaling=scaling, U=U,
+                        bimol=bim, ucum=ucum, unpw=unpw.astype(np.uint32), Uu=Uu, unimol=uni)
+    print("rxn pathways: bimolecular", np.unique(bim, return_counts=True), "unimolecular",
+          np.unique(uni, return_counts=True))
+
+
 def main():
     ref64 = H.reference(64)
     if ref64 is None:
@@ -99,25 +164,7 @@ def main():
             cases += add_edge_molecules(sc)
         cases += [(m, d) for (m, d, _) in H.random_cases(rng, sc, 700, scale=2.0, near_wall_frac=0.4)]
         cases += partner_cases(rng, sc, 500)
-        h = ref64.scene(sc)
-        mols = np.array([c[0] for c in cases], np.uint32)
-        disps = np.array([c[1] for c in cases], np.float64)
-        draws = rng.integers(0, 2 ** 32, size=(len(cases), NDRAWS), dtype=np.uint64).astype(np.uint32)
-        # a share of cases with draws that make reactions fire (small uniforms)
-        draws[::3, :] = (draws[::3, :] >> 6).astype(np.uint32)
-        res = np.array([h.diffuse_case(int(m), d, dr) for m, d, dr in zip(mols, disps, draws)])
-        nev = int(res[:, 6].max())
-        keep = H.RES_HDR + H.EV_SIZE * max(1, min(nev, H.EV_MAX))
-        info = h.info()
-        wc_ref = h.wall_consts(len(sc.tris))
-        counts, lst = h.walls_in_subparts(sc.nsub ** 3)
-        np.savez_compressed(
-            HERE / f"diffuse_{name}.npz",
-            origin=sc.origin, partition_edge=sc.partition_edge, nsub=sc.nsub, rxn_radius=sc.rxn_radius,
-            verts=sc.verts, tris=sc.tris, space_steps=sc.space_steps, wall_class=sc.wall_class,
-            rxn_ab=sc.rxn_ab, rxn_p=sc.rxn_p, mol_pos=sc.mol_pos, mol_species=sc.mol_species,
-            mols=mols, disps=disps, draws=draws, results=res[:, :keep],
-            info=info, wall_consts=wc_ref, wsp_counts=counts, wsp_list=lst)
+        res = record_scene(ref64, rng, name, sc, cases)
         kinds = np.unique(res[:, H.RES_HDR::H.EV_SIZE][res[:, H.RES_HDR::H.EV_SIZE] > 0], return_counts=True)
         print(name, len(cases), "cases, event kinds", dict(zip(kinds[0].astype(int).tolist(), kinds[1].tolist())),
               "status", np.unique(res[:, 0], return_counts=True))
@@ -136,6 +183,7 @@ def main():
     ref64.lib.ref_rng_gauss(ctypes.c_ulonglong(1), ctypes.c_uint(len(g)), H.ptr(g))
     np.savez_compressed(HERE / "rxn_tests.npz", P=P, S=S, U=U, bimol=tb, K=K, Uu=Uu, unimol=tu, ref_gauss=g)
     print("rxn tests", (tb >= 0).sum(), "fired of", len(tb))
+    pathway_fixtures(ref64)
 
 
 if __name__ == "__main__":

@@ -76,6 +76,8 @@ class Checker:
         self.fn("subpart_index").restype = _u
         self.fn("scene_walls_in_subparts").restype = _u
         self.fn("test_bimolecular").restype = ctypes.c_int
+        self.fn("test_bimolecular_pw").restype = ctypes.c_int
+        self.fn("which_unimolecular").restype = ctypes.c_int
         self.fn("time_of_unimol").restype = _d
 
     def fn(self, name):
@@ -90,6 +92,15 @@ class Checker:
 
     def time_of_unimol(self, k, draw):
         return self.fn("time_of_unimol")(_d(k), _u(draw))
+
+    def test_bimolecular_pw(self, cum, scaling, draw):
+        """test_bimolecular over a class of len(cum) pathways: pathway index, < 0 = none."""
+        c = np.ascontiguousarray(cum, np.float64)
+        return self.fn("test_bimolecular_pw")(ptr(c), _u(len(c)), _d(scaling), _u(draw))
+
+    def which_unimolecular(self, cum, draw):
+        c = np.ascontiguousarray(cum, np.float64)
+        return self.fn("which_unimolecular")(ptr(c), _u(len(c)), _u(draw))
 
 
 class _Handle:
@@ -242,7 +253,7 @@ def edge_cases(sc: Scene):
 
 
 GOLDEN = ROOT / "tests" / "golden"
-GOLDEN_SCENES = ["cube", "cube_dense", "cube_classes", "sphere"]
+GOLDEN_SCENES = ["cube", "cube_dense", "cube_classes", "sphere", "pathways"]
 
 
 def load_golden(name):

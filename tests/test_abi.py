@@ -40,10 +40,33 @@ def test_config_validation():
     with pytest.raises(_native.EngineError):
         e.add_bimol_rxn(0, 5, 0.1)                                  # bad species
     e.add_bimol_rxn(0, 1, 0.0368, (2, -1))
-    with pytest.raises(_native.EngineError):
-        e.add_bimol_rxn(1, 0, 0.1)                                  # second class for the same pair
+    for _ in range(_native.MAX_PATHWAYS - 1):
+        e.add_bimol_rxn(1, 0, 0.01)                                 # further pathways of the pair's class
+    with pytest.raises(_native.EngineError) as ex:
+        e.add_bimol_rxn(1, 0, 0.01)                                 # one pathway too many
+    assert ex.value.code == -6
     with pytest.raises(_native.EngineError):
         e.add_molecules(np.zeros((1, 3)), np.array([7]))
+
+
+def test_reactive_products_are_refused_without_a_device():
+    """A product that is also a bimolecular reactant would react in its birth step in
+    the reference; the GPU path refuses such models (MCG_ERR_UNSUPPORTED) before any
+    device work, for single models and for batches."""
+    def model(rxns):
+        e = _native.Engine("fp64", (-60, -60, -60), 120.0, 12, 0.5642, 4)
+        e.set_species([2.0, 2.0, 1.41, 1.0])
+        for a, b, prods in rxns:
+            e.add_bimol_rxn(a, b, 0.05, prods)
+        e.add_unimol_rxn(3, 1e-3, (2, -1))
+        return e
+    for rxns in ([(0, 1, (2, -1)), (2, 0, (3, -1))],    # C = A + B is a reactant of C + A
+                 [(0, 1, (3, -1)), (2, 1, (-1, -1))]):  # C = the product of D's decay reacts with B
+        e = model(rxns)
+        with pytest.raises(_native.EngineError) as ex:
+            e.prepare()
+        assert ex.value.code == -6 and "product" in str(ex.value)
+        e.close()
 
 
 def test_host_setup_matches_oracle_without_gpu():

@@ -127,7 +127,9 @@ def test_batch_count_files_follow_the_replica(tmp_path):
     t = b.trajectory(r, 10)
     lines = (tmp_path / "rep.gdat").read_text().splitlines()
     g = np.array([[float(x) for x in ln.split()] for ln in lines[1:]])
-    assert np.allclose(g[:, 0], [2e-6, 4e-6, 6e-6, 8e-6, 1e-5])
-    assert np.array_equal(g[:, 1], t[[1, 3, 5, 7, 9], 2].astype(float))
-    assert g[3, 1] == g[2, 1] == g[4, 1]  # frozen from iteration 6 on
+    # a t = 0 row (no C before the first iteration), then every second iteration
+    assert np.allclose(g[:, 0], [0.0, 2e-6, 4e-6, 6e-6, 8e-6, 1e-5])
+    assert g[0, 1] == 0.0
+    assert np.array_equal(g[1:, 1], t[[1, 3, 5, 7, 9], 2].astype(float))
+    assert g[4, 1] == g[3, 1] == g[5, 1]  # frozen from iteration 6 on
     b.close()

@@ -92,6 +92,8 @@ def test_count_files_in_the_reference_formats(tmp_path):
     h.set_wall_objects(obj)
     h.set_counted_objects([0])
     h.prepare()
+    world0 = h.counts()
+    inside0 = h.counted_counts()
     h.step(12)
     world = h.trajectory(12)
     inside = h.counted_trajectory(12)
@@ -99,18 +101,23 @@ def test_count_files_in_the_reference_formats(tmp_path):
     h.write_counts(tmp_path / "run", cols, n_iterations=12, every=3, time_step_s=1e-6, fmt="dat")
     h.write_counts(tmp_path / "run", cols, n_iterations=12, every=3, time_step_s=1e-6, fmt="gdat")
     h.close()
-    rows = [2, 5, 8, 11]  # iterations 3, 6, 9, 12
-    times = [3e-6, 6e-6, 9e-6, 1.2e-5]
-    want = {"A_world": world[rows, 0], "C_world": world[rows, 2], "A_in_sphere": inside[rows, 0, 0]}
+    # the window reaches back to the start: a t = 0 row of the counts before the first
+    # iteration (the reference's count event runs before diffusion in iteration 0),
+    # then iterations 3, 6, 9, 12
+    rows = [2, 5, 8, 11]
+    times = [0.0, 3e-6, 6e-6, 9e-6, 1.2e-5]
+    want = {"A_world": np.r_[world0[0], world[rows, 0]], "C_world": np.r_[world0[2], world[rows, 2]],
+            "A_in_sphere": np.r_[inside0[0, 0], inside[rows, 0, 0]]}
     for name, vals in want.items():
         lines = (tmp_path / f"run.{name}.dat").read_text().splitlines()
-        assert lines[0].split()[0] == "3e-06" and lines[3].split()[0] == "1.2e-05"
+        assert lines[0].split()[0] == "0" and lines[1].split()[0] == "3e-06" and lines[4].split()[0] == "1.2e-05"
         got = np.array([[float(x) for x in ln.split()] for ln in lines])
         assert np.allclose(got[:, 0], times) and np.array_equal(got[:, 1], vals.astype(float))
     text = (tmp_path / "run.gdat").read_text().splitlines()
     assert text[0] == "#" + "time".rjust(14) + "".join(n.rjust(16) for n in ("A_world", "C_world", "A_in_sphere"))
     first = text[1].split()
-    assert text[1].startswith(" 3.00000000e-06  ") and len(first) == 4
+    assert text[1].startswith(" 0.00000000e+00  ") and len(first) == 4
+    assert text[2].startswith(" 3.00000000e-06  ")
     g = np.array([[float(x) for x in ln.split()] for ln in text[1:]])
     for k, name in enumerate(("A_world", "C_world", "A_in_sphere")):
         assert np.array_equal(g[:, k + 1], want[name].astype(float))

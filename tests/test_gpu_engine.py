@@ -127,45 +127,6 @@ def test_absorptive_walls_remove_molecules():
     assert 0 < c[1] < nB0
 
 
-def _ensemble(make, runs, n_iter):
-    out = []
-    for s in range(runs):
-        out.append(make(s))
-    return np.array(out, dtype=float)
-
-
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_ensemble_matches_oracle(precision):
-    """A + B -> C in a closed reflective 1 um cube (the CPU-runnable configuration at
-    reduced size): the count of C after n iterations, GPU ensemble vs the oracle's
-    serial engine ensemble, means within 3 combined standard errors."""
-    n_iter, runs = 120, 8
-    lu = 0.01
-    p = 0.0368 * 4  # a faster reaction to resolve the mean in few runs
-
-    def scene(seed):
-        rng = np.random.default_rng(1000 + seed)
-        sc = H.cube_scene(rng, n_mol=4000)
-        sc.mol_species = np.repeat(np.array([0, 1], np.uint32), 2000)
-        return sc
-
-    def gpu(seed):
-        e = H.make_gpu_engine(scene(seed), precision, bimol=[(0, 1, p, (2, -1))], seed=seed + 1)
-        e.step(n_iter)
-        return e.counts()[2]
-
-    def cpu(seed):
-        e = H.make_oracle_engine(scene(seed), bimol=[(0, 1, p, (2, -1))], seed=seed + 1)
-        return e.run(n_iter)[-1, 2]
-
-    g = _ensemble(gpu, runs, n_iter)
-    c = _ensemble(cpu, runs, n_iter)
-    se = np.sqrt(g.var(ddof=1) / runs + c.var(ddof=1) / runs)
-    print(f"C after {n_iter} it: gpu {g.mean():.1f} +- {g.std(ddof=1):.1f}, oracle {c.mean():.1f} +- "
-          f"{c.std(ddof=1):.1f}, se {se:.1f}")
-    assert abs(g.mean() - c.mean()) < 3 * se + 1e-9
-
-
 def test_fp32_large_model_stays_confined():
     """1M molecules in fp32 around the 20,480-triangle sphere: fp32 rounding must not let
     any molecule through the reflective cube (the fp64 tie-breaks of the precision form)."""
@@ -259,3 +220,45 @@ def test_density_becomes_uniform_in_a_reflective_box(precision):
     print(f"chi2 {chi2:.1f} (511 dof)")
     assert chi2 < 511 + 5 * np.sqrt(2 * 511)
     e.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_pathway_branching_matches_oracle(precision):
+    """Reaction classes with several pathways in a running model: A + B -> C (p 0.06)
+    or D (p 0.03), and C -> 0 (k 4e-3) or E (k 12e-3). The products of each pathway,
+    over an ensemble, against the oracle's serial engine (means within 3 standard
+    errors) and against the branching ratios (2:1 and 1:3)."""
+    n_iter, runs = 60, 6
+
+    def scene(seed):
+        rng = np.random.default_rng(300 + seed)
+        sc = H.cube_scene(rng, n_mol=6000)
+        sc.mol_species = np.repeat(np.array([0, 1], np.uint32), 3000)
+        sc.space_steps = np.array([2.0, 2.0, 1.414, 1.414, 1.414])
+        sc.wall_class = np.zeros((len(sc.tris), 5), np.uint8)
+        return sc
+
+    bimol = [(0, 1, 0.06, (2, -1)), (0, 1, 0.03, (3, -1))]
+    unimol = [(2, 4e-3, (-1, -1)), (2, 12e-3, (4, -1))]
+
+    def gpu(seed):
+        e = H.make_gpu_engine(scene(seed), precision, bimol=bimol, unimol=unimol, seed=seed + 1)
+        e.step(n_iter)
+        c = e.counts().astype(float)
+        e.close()
+        return c
+
+    def cpu(seed):
+        e = H.make_oracle_engine(scene(seed), bimol=bimol, unimol=unimol, seed=seed + 1)
+        return e.run(n_iter)[-1].astype(float)
+
+    g = np.array([gpu(s) for s in range(runs)])
+    c = np.array([cpu(s) for s in range(runs)])
+    se = np.sqrt(g.var(0, ddof=1) / runs + c.var(0, ddof=1) / runs) + 1e-9
+    print("gpu", g.mean(0), "oracle", c.mean(0), "se", se)
+    assert (np.abs(g.mean(0) - c.mean(0)) < 3 * se + 1.0).all()
+    # C and D born 2:1; of C's decays 1 in 4 goes to nothing, 3 in 4 to E
+    born_c = g[:, 2] + g[:, 4] + (g[:, 4] / 3.0)
+    ratio = born_c.sum() / g[:, 3].sum()
+    assert 1.6 < ratio < 2.5, ratio
+    assert g[:, 4].sum() > 0

@@ -84,3 +84,98 @@ def test_fp32_wall_hit_mismatch_rate():
     err = np.abs(got[same, 1:4] - want[same, 1:4]).max()
     print(f"fp32 max final-position error on matching cases: {err:.3g} internal units")
     assert err < 0.1  # 1 nm (0.1 internal units); fp32 ulp at 150 internal units is 1.5e-5
+
+
+@pytest.mark.parametrize("name", H.GOLDEN_SCENES)
+def test_fallbacks_are_exact_with_small_pages(name):
+    """The candidate page (16 in production) and the partner list (48) have fixed sizes
+    where the reference's lists grow. With both cut to a few entries, the refilled
+    pages and the partner scan along the walk must still reproduce the reference's
+    routines on every golden case."""
+    sc, g = H.load_golden(name)
+    e = H.engine_from_scene(sc, "fp64")
+    e.set_trace_limits(1, 2)
+    got = _trace(e, sc, g["mols"], g["disps"], g["draws"])
+    bad = H.compare_results(got, g["results"], rel=0.0, scene=sc)
+    hard = [c for c in bad if H.compare_results(got[c:c + 1], g["results"][c:c + 1], rel=1e-9, scene=sc)]
+    fb = e.fallbacks()
+    print(name, "fallbacks (page refills, walk scans):", fb)
+    assert not hard, f"{len(hard)} of {len(got)} cases differ with small pages: {hard[:5]}"
+    assert fb[0] + fb[1] > 0
+    e.close()
+
+
+@pytest.mark.parametrize("dense", [False, True])
+def test_fallbacks_are_exact_on_random_cases(dense):
+    """Long steps on a fine grid (partner sets beyond the list), and in a crowded cube
+    (150,000 molecules: several candidates per step, pages refilled), with pages of
+    two candidates and lists of three subpartitions, against the oracle."""
+    rng = np.random.default_rng(17)
+    if dense:
+        sc = H.cube_scene(rng, n_mol=150_000, p_rxn=0.3)
+    else:
+        sc = H.sphere_in_cube_scene(rng, levels=3, n_mol=6000, radius_um=0.6, cube_um=1.5, p_rxn=0.3, nsub=30)
+    cases = H.random_cases(rng, sc, 3000, scale=6.0, near_wall_frac=0.5)
+    mols = [c[0] for c in cases]
+    disps = np.array([c[1] for c in cases])
+    draws = np.array([c[2] for c in cases])
+    draws[::4] >>= 4
+    orc = H.oracle().scene(sc)
+    want = np.array([orc.diffuse_case(m, d, dr) for m, d, dr in zip(mols, disps, draws)])
+    e = H.engine_from_scene(sc, "fp64")
+    full = _trace(e, sc, mols, disps, draws)
+    e.set_trace_limits(2, 3)
+    small = _trace(e, sc, mols, disps, draws)
+    fb = e.fallbacks()
+    print("fallbacks (page refills, walk scans):", fb)
+    for got in (full, small):
+        bad = H.compare_results(got, want, rel=0.0, scene=sc)
+        hard = [c for c in bad if H.compare_results(got[c:c + 1], want[c:c + 1], rel=1e-9, scene=sc)]
+        assert not hard, f"{len(hard)} cases differ: {hard[:5]}"
+    assert fb[0] > 0 if dense else fb[1] > 0
+    e.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_fallbacks_leave_the_trajectory_unchanged(precision):
+    """A dense cube with long steps on a fine grid (many candidates per trace, partner
+    sets larger than the 4x4x4 window): 20 iterations with the production capacities
+    and with pages of one candidate and lists of four subpartitions give the same
+    molecules, bit for bit."""
+    rng = np.random.default_rng(21)
+    sc = H.cube_scene(rng, n_mol=12000, nsub=24, p_rxn=0.2)
+    sc.space_steps = np.array([20.0, 20.0, 14.0])
+    runs = []
+    for limits in (None, (1, 4)):
+        e = H.make_gpu_engine(sc, precision, bimol=[(0, 1, 0.2, (2, -1))], seed=5)
+        if limits:
+            e.set_trace_limits(*limits)
+        e.step(20)
+        pos, sp, ids = e.molecules()
+        o = np.argsort(ids)
+        runs.append((pos[o], sp[o], ids[o], e.trajectory(20), e.fallbacks()))
+        e.close()
+    (p0, s0, i0, t0, f0), (p1, s1, i1, t1, f1) = runs
+    print("fallbacks: production", f0, "small", f1)
+    assert f1[0] > 0 and f1[1] > 0
+    assert np.array_equal(i0, i1) and np.array_equal(s0, s1) and np.array_equal(p0, p1)
+    assert np.array_equal(t0, t1)
+
+
+def test_reaction_decisions_match_reference_golden():
+    """The device's test_bimolecular and which_unimolecular on injected draws against
+    the reference's routines: fire / no-fire and the pathway chosen, bit for bit, over
+    classes of one (rxn_tests) and of 1-4 pathways (rxn_pathways), including the branch
+    where the class's probability cannot be scaled enough."""
+    from mcell_gb300 import _native
+    z = np.load(H.GOLDEN / "rxn_tests.npz")
+    got = _native.reaction_decisions("bimol", [[p] for p in z["P"]], z["S"], z["U"])
+    assert np.array_equal(got >= 0, z["bimol"] >= 0)
+    assert np.array_equal(got[got >= 0], z["bimol"][z["bimol"] >= 0])
+    z = np.load(H.GOLDEN / "rxn_pathways.npz")
+    cum = [z["cum"][i, :z["npw"][i]] for i in range(len(z["U"]))]
+    got = _native.reaction_decisions("bimol", cum, z["scaling"], z["U"])
+    assert np.array_equal(np.where(got < 0, -1, got), np.where(z["bimol"] < 0, -1, z["bimol"]))
+    ucum = [z["ucum"][i, :z["unpw"][i]] for i in range(len(z["Uu"]))]
+    got = _native.reaction_decisions("unimol", ucum, None, z["Uu"])
+    assert np.array_equal(got, z["unimol"])

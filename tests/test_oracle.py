@@ -39,7 +39,32 @@ def test_reaction_tests_match_golden():
     assert np.array_equal(tu, z["unimol"])
 
 
+def test_reaction_pathways_match_golden():
+    """Classes of 1-4 pathways: test_bimolecular's fire decision and pathway, and
+    which_unimolecular's pathway, against the reference's routines (golden)."""
+    z = np.load(H.GOLDEN / "rxn_pathways.npz")
+    orc = H.oracle()
+    tb = np.array([orc.test_bimolecular_pw(z["cum"][i, :z["npw"][i]], z["scaling"][i], z["U"][i])
+                   for i in range(len(z["U"]))])
+    assert np.array_equal(np.where(tb < 0, -1, tb), np.where(z["bimol"] < 0, -1, z["bimol"]))
+    tu = np.array([orc.which_unimolecular(z["ucum"][i, :z["unpw"][i]], z["Uu"][i]) for i in range(len(z["Uu"]))])
+    assert np.array_equal(tu, z["unimol"])
+    assert len(np.unique(z["bimol"])) >= 4 and len(np.unique(z["unimol"])) == 4
+
+
 REF = H.reference(64)
+
+
+@pytest.mark.skipif(REF is None, reason="reference routines not built here (no reference sources)")
+def test_oracle_pathways_match_reference_random():
+    rng = np.random.default_rng(13)
+    for _ in range(2000):
+        k = int(rng.integers(1, 5))
+        cum = np.cumsum(rng.uniform(0, 0.7, k)) * (3.0 if rng.random() < 0.2 else 1.0)
+        sc, u = float(rng.uniform(0, 2)), int(rng.integers(0, 2 ** 32))
+        a, b = H.oracle().test_bimolecular_pw(cum, sc, u), REF.test_bimolecular_pw(cum, sc, u)
+        assert (a < 0 and b < 0) or a == b
+        assert H.oracle().which_unimolecular(cum, u) == REF.which_unimolecular(cum, u)
 
 
 @pytest.mark.skipif(REF is None, reason="reference routines not built here (no reference sources)")

@@ -43,6 +43,30 @@ def test_static_trace_matches_allocating_trace(precision):
     e.close()
 
 
+def test_static_trace_takes_no_device_memory():
+    """The property the entry point exists for: with the next device allocation armed
+    to fail, a static call still succeeds (it makes none), and the device's free
+    memory is the same before and after the call."""
+    torch = pytest.importorskip("torch")
+    sc, ids, disps, draws = _scene_and_cases(13, 64)
+    e = H.engine_from_scene(sc, "fp32")
+    want = e.trace_cases_static(ids, disps, draws)
+    free0 = torch.cuda.mem_get_info(0)[0]
+    _native.inject_device_alloc_failure(0)
+    try:
+        got = e.trace_cases_static(ids, disps, draws)
+        free1 = torch.cuda.mem_get_info(0)[0]
+        # the armed failure is still pending (the static call made no allocation):
+        # the allocating trace, which allocates, meets it
+        with pytest.raises(_native.EngineError):
+            e.trace_cases(ids, disps, draws)
+    finally:
+        _native.inject_device_alloc_failure(None)
+    assert np.array_equal(got, want)
+    assert free1 == free0, f"free device memory changed by {free0 - free1} bytes across the call"
+    e.close()
+
+
 def test_static_trace_rejects_oversized_and_unknown_requests():
     sc, ids, disps, draws = _scene_and_cases(12, 8)
     e = H.engine_from_scene(sc, "fp64")
