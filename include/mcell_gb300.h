@@ -128,8 +128,11 @@ int mcg_inject_device_alloc_failure(int64_t after);
    whose partner subpartitions overflowed the fixed-size list (48), whose partners
    were then scanned along the walk with repeated candidates dropped. Both restate the
    growable lists of ray_trace_vol / collect_crossed_subparts
-   (src4/diffuse_react_event.cpp:627-780, src4/collision_utils_subparts.inl:127-300). */
-int mcg_get_fallbacks(mcg_engine* e, uint64_t* out /* [2] */);
+   (src4/diffuse_react_event.cpp:627-780, src4/collision_utils_subparts.inl:127-300).
+   out[2]: inside tests (counted-volume membership, releases into an object) whose ray
+   met a wall edge, where the reference's test stops (its must_redo_test); such a
+   molecule is counted outside, such a release point drawn again. */
+int mcg_get_fallbacks(mcg_engine* e, uint64_t* out /* [3] */);
 /* Test hook (no counterpart in the reference): smaller page and list capacities
    (1..16 candidates, 1..48 subpartitions) so that tests can drive the fallbacks. */
 int mcg_set_trace_limits(mcg_engine* e, uint32_t max_candidates, uint32_t max_subparts);
@@ -240,7 +243,7 @@ int mcg_batch_download_molecules(mcg_batch* b, uint32_t replica, uint64_t cap, d
 int mcg_batch_get_stats(mcg_batch* b, uint64_t* iterations, uint64_t* mol_steps, uint64_t* launches);
 int mcg_batch_set_options(mcg_batch* b, int use_graphs, int profile);
 /* As mcg_get_fallbacks, over all replicas. */
-int mcg_batch_get_fallbacks(mcg_batch* b, uint64_t* out /* [2] */);
+int mcg_batch_get_fallbacks(mcg_batch* b, uint64_t* out /* [3] */);
 int mcg_batch_get_profile(mcg_batch* b, double* out);
 /* Device bytes held by the batch, and the resident blocks per SM the diffuse
    kernel runs with (the autotuner's choice, or the maximum). */
@@ -316,7 +319,9 @@ int mcg_serve_get_stats(mcg_server* s, mcg_serve_stats* out);
    the counter-based generator keyed by release_seed, so positions are not the
    reference's; their distribution is. Molecule ids continue the model's. The
    region must lie inside the partition. Walls are assigned to objects with
-   mcg_set_wall_objects (before the first step). */
+   mcg_set_wall_objects (before the first step). The positions follow the reference's
+   arithmetic from the draws (mcg_release_positions gives them on injected draws); the
+   inside test is the reference's (mcg_inside_tests). */
 #define MCG_RELEASE_SPHERE 0
 #define MCG_RELEASE_CUBOID 1
 #define MCG_RELEASE_SHELL 2
@@ -327,13 +332,30 @@ int mcg_release(mcg_engine* e, uint32_t species, uint64_t n, int shape, const do
 int mcg_batch_release(mcg_batch* b, uint32_t replica, uint32_t species, uint64_t n, int shape, const double* center,
                       const double* diameter, uint32_t object, uint64_t release_seed);
 
+/* Parity harness of the inside tests (test infrastructure; the engine must have its
+   wall objects, and for kind 0 its counted objects): for each point, kind 0 the
+   counted-volume bits (bit q: inside counted object q; compute_counted_volume_for_pos,
+   src4/collision_utils.inl:1515-1545), kind 1 whether it lies inside geometry object
+   `object` (is_point_inside_region_no_waypoints, src4/collision_utils.inl:1484-1510);
+   0xFFFFFFFF where the ray met a wall edge. */
+int mcg_inside_tests(mcg_engine* e, uint32_t n, const double* pos, int kind, uint32_t object, uint32_t* out);
+/* Parity harness of the volume releases (no engine; test infrastructure): n positions
+   of ReleaseEvent::release_ellipsoid_or_rectcuboid (src4/release_event.cpp:953-1000)
+   for shape MCG_RELEASE_SPHERE / _CUBOID / _SHELL, drawing from one injected stream
+   of 32-bit draws as the reference's generator would; *draws_used = the draws it took
+   (0xFFFFFFFF if the stream ran out). */
+int mcg_release_positions(int shape, uint32_t n, const double* center, const double* diameter, const uint32_t* draws,
+                          uint32_t n_draws, double* pos, uint32_t* draws_used);
+
 /* ---- Counted volumes: molecules inside closed geometry objects, per species, for
    MolOrRxnCountEvent (src4/mol_or_rxn_count_event.cpp:707). As MCell4's counted-
    volume index, each molecule carries its membership (up to 7 counted objects per
    model), set at upload or release by the reference's ray-parity test
-   (compute_counted_volume_for_pos, src4/collision_utils.inl:1515-1545) and flipped
-   whenever it crosses a (transparent) wall of a counted object; products inherit
-   their reactant's. Objects are named by the ids of mcg_set_wall_objects; set
+   (compute_counted_volume_for_pos, src4/collision_utils.inl:1515-1545) and set at
+   every crossing of a (transparent) wall of a counted object: inside after a hit on
+   its front face, outside after a hit on its back face
+   (update_counted_volume_id_when_crossing_wall, src4/collision_utils.inl:1637-1694);
+   products inherit their reactant's. Objects are named by the ids of mcg_set_wall_objects; set
    before the first step. Counts: [n_species][n_counted] after the last iteration
    or upload; trajectory: [n][n_species][n_counted] for the last n iterations. */
 int mcg_set_counted_objects(mcg_engine* e, uint32_t n, const uint16_t* objects);

@@ -37,6 +37,7 @@ EXPORTS = [
     "mcg_set_wall_objects", "mcg_release", "mcg_batch_release", "mcg_set_counted_objects",
     "mcg_get_counted_volume_counts", "mcg_get_counted_volume_trajectory",
     "mcg_get_fallbacks", "mcg_set_trace_limits", "mcg_batch_get_fallbacks", "mcg_reaction_decisions",
+    "mcg_inside_tests", "mcg_release_positions",
 ]
 MAX_PATHWAYS = 4
 
@@ -157,6 +158,21 @@ def reaction_decisions(kind, cum, scaling, draws):
     return out
 
 
+def release_positions(shape, n, center, diameter, draws):
+    """Device release positions on an injected stream (mcg_release_positions): shape
+    "sphere", "cuboid" or "shell". Returns (positions [n, 3], draws used or None)."""
+    out = np.zeros((n, 3))
+    c = np.ascontiguousarray(center, np.float64)
+    d = np.ascontiguousarray(diameter, np.float64)
+    dr = np.ascontiguousarray(draws, np.uint32)
+    used = ctypes.c_uint32()
+    rc = lib().mcg_release_positions(ctypes.c_int({"sphere": 0, "cuboid": 1, "shell": 2}[shape]), ctypes.c_uint32(n),
+                                     _p(c), _p(d), _p(dr), ctypes.c_uint32(len(dr)), _p(out), ctypes.byref(used))
+    if rc:
+        raise EngineError(rc, "mcg_release_positions failed")
+    return out, (None if used.value == 0xFFFFFFFF else int(used.value))
+
+
 class Engine:
     """One GPU model: thin object over the C ABI (same calls a C++ host makes)."""
 
@@ -258,10 +274,20 @@ class Engine:
         self._chk(lib().mcg_set_options(self.h, ctypes.c_int(int(use_graphs)), ctypes.c_int(int(profile))))
 
     def fallbacks(self):
-        """(traces that refilled a full candidate page, traces that scanned partners along the walk)."""
-        out = np.zeros(2, np.uint64)
+        """(traces that refilled a full candidate page, traces that scanned partners along the
+        walk, inside tests whose ray met a wall edge)."""
+        out = np.zeros(3, np.uint64)
         self._chk(lib().mcg_get_fallbacks(self.h, _p(out)))
-        return int(out[0]), int(out[1])
+        return int(out[0]), int(out[1]), int(out[2])
+
+    def inside_tests(self, pos, kind, obj=0):
+        """mcg_inside_tests: kind "counted" (counted-volume bits) or "object" (inside obj)."""
+        p = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        out = np.zeros(len(p), np.uint32)
+        self._chk(lib().mcg_inside_tests(self.h, ctypes.c_uint32(len(p)), _p(p),
+                                         ctypes.c_int({"counted": 0, "object": 1}[kind]), ctypes.c_uint32(obj),
+                                         _p(out)))
+        return out
 
     def set_trace_limits(self, max_candidates, max_subparts):
         """Test hook: smaller candidate page / partner list capacities (drives the fallbacks)."""
@@ -494,9 +520,9 @@ class Batch:
         self._chk(lib().mcg_batch_set_options(self.h, int(use_graphs), int(profile)))
 
     def fallbacks(self):
-        out = np.zeros(2, np.uint64)
+        out = np.zeros(3, np.uint64)
         self._chk(lib().mcg_batch_get_fallbacks(self.h, _p(out)))
-        return int(out[0]), int(out[1])
+        return int(out[0]), int(out[1]), int(out[2])
 
     def profile(self):
         out = np.zeros(6)

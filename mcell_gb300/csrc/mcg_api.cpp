@@ -240,12 +240,30 @@ int mcg_reaction_decisions(int kind, uint32_t n, const double* cum, const uint32
 int mcg_get_fallbacks(mcg_engine* e, uint64_t* out) {
   if (!e || !out) return MCG_ERR_ARG;
   if (!e->dev) {
-    out[0] = out[1] = 0;
+    out[0] = out[1] = out[2] = 0;
     return MCG_OK;
   }
   std::string err;
   int rc = e->dev->fallbacks(out, err);
   return rc ? fail(e, rc, err) : MCG_OK;
+}
+
+int mcg_inside_tests(mcg_engine* e, uint32_t n, const double* pos, int kind, uint32_t object, uint32_t* out) {
+  if (!e || (n && (!pos || !out)) || (kind != 0 && kind != 1)) return MCG_ERR_ARG;
+  int rc = prepare(e);
+  if (rc) return rc;
+  std::string err;
+  rc = e->dev->inside_tests(0, n, pos, kind, object, out, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
+int mcg_release_positions(int shape, uint32_t n, const double* center, const double* diameter, const uint32_t* draws,
+                          uint32_t n_draws, double* pos, uint32_t* draws_used) {
+  if (shape < MCG_RELEASE_SPHERE || shape > MCG_RELEASE_SHELL || !center || !diameter || !draws_used ||
+      (n && !pos) || (n_draws && !draws))
+    return MCG_ERR_ARG;
+  std::string err;
+  return mcg::release_positions(shape, n, center, diameter, draws, n_draws, pos, draws_used, err);
 }
 
 int mcg_set_trace_limits(mcg_engine* e, uint32_t max_candidates, uint32_t max_subparts) {

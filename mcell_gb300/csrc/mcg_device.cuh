@@ -167,11 +167,13 @@ struct Geo {
   const uint16_t* wall_obj;   // geometry object of each wall (releases inside objects), or null
   uint32_t n_cv;              // counted objects (volumes whose contents are counted)
   uint16_t cv_obj[MAX_COUNTED];
+  // the grid in fp64 (the inside tests run in fp64 in both engines)
+  double origin64[3], sp_edge64, sp_rcp64;
 };
 
-// membership bits a crossing of wall wi flips (walls of counted objects only)
+// counted-object slots a wall belongs to (walls of counted objects only)
 template <typename T>
-__device__ __forceinline__ uint32_t cv_flip_of_wall(const Geo<T>& g, uint32_t wi) {
+__device__ __forceinline__ uint32_t cv_bits_of_wall(const Geo<T>& g, uint32_t wi) {
   if (!g.n_cv) return 0;
   const uint16_t o = g.wall_obj[wi];
   uint32_t f = 0;
@@ -201,8 +203,18 @@ struct TraceOut {
   V3<T> rxn_pos;
   double elapsed, t_steps;
   uint32_t err;
-  uint32_t flip;     // counted-volume bits flipped by transparent crossings (up to the reaction)
+  // counted-volume membership set by transparent crossings up to the reaction
+  // (update_counted_volume_id_when_crossing_wall, collision_utils.inl:1637-1694: a hit
+  // on a counted object's front face goes inside it, on its back face outside): the
+  // objects crossed and their membership after the last crossing
+  uint32_t cv_mask, cv_val;
 };
+
+// a molecule's counted-volume bits after the crossings of a trace
+template <typename T>
+__device__ __forceinline__ uint32_t cv_after(uint32_t cv, const TraceOut<T>& r) {
+  return (cv & ~r.cv_mask) | (r.cv_val & r.cv_mask);
+}
 
 // ------------------------------------------------------------------ draws
 
@@ -341,8 +353,9 @@ __device__ __forceinline__ uint32_t octants_touched(const Geo<T>& g, uint32_t sp
   int ix, iy, iz;
   decode_sp(g, sp, ix, iy, iz);
   const T h = g.sp_edge * (T)0.5;
-  const V3<T> mid = g.origin + cmul(v3<T>((T)ix, (T)iy, (T)iz), v3<T>(g.sp_edge, g.sp_edge, g.sp_edge)) +
-                    v3<T>(h, h, h);
+  const V3<T> mid = v3<T>(add_rn(add_rn(g.origin.x, mul_rn((T)ix, g.sp_edge)), h),
+                          add_rn(add_rn(g.origin.y, mul_rn((T)iy, g.sp_edge)), h),
+                          add_rn(add_rn(g.origin.z, mul_rn((T)iz, g.sp_edge)), h));
   const uint32_t ax = (lo.x < mid.x ? 1u : 0u) | (hi.x >= mid.x ? 2u : 0u);
   const uint32_t ay = (lo.y < mid.y ? 1u : 0u) | (hi.y >= mid.y ? 2u : 0u);
   const uint32_t az = (lo.z < mid.z ? 1u : 0u) | (hi.z >= mid.z ? 2u : 0u);
@@ -463,26 +476,28 @@ struct Walk {
   // advances to the next crossed subpartition; false when the walk is over
   __device__ bool next(const Geo<T>& g) {
     if (done) return false;
-    V3<T> len = v3<T>(g.sp_edge, g.sp_edge, g.sp_edge);
-    V3<T> edges = (g.origin + cmul(v3<T>((T)cx, (T)cy, (T)cz), len)) + cmul(v3<T>((T)dx, (T)dy, (T)dz), len);
+    const T e = g.sp_edge;
+    V3<T> edges = v3<T>(add_rn(add_rn(g.origin.x, mul_rn((T)cx, e)), mul_rn((T)dx, e)),
+                        add_rn(add_rn(g.origin.y, mul_rn((T)cy, e)), mul_rn((T)dy, e)),
+                        add_rn(add_rn(g.origin.z, mul_rn((T)cz, e)), mul_rn((T)dz, e)));
     V3<T> diff = edges - cp;
     V3<T> t = cmul(diff, rcp);
     if (t.x < t.y && t.x <= t.z) {
-      cp = cp + scale(disp, t.x);
+      cp = v3<T>(add_rn(cp.x, mul_rn(disp.x, t.x)), add_rn(cp.y, mul_rn(disp.y, t.x)), add_rn(cp.z, mul_rn(disp.z, t.x)));
       cx += ax;
       if (cx < 0 || cx >= g.nsub) {
         done = true;
         return false;
       }
     } else if (t.y <= t.z) {
-      cp = cp + scale(disp, t.y);
+      cp = v3<T>(add_rn(cp.x, mul_rn(disp.x, t.y)), add_rn(cp.y, mul_rn(disp.y, t.y)), add_rn(cp.z, mul_rn(disp.z, t.y)));
       cy += ay;
       if (cy < 0 || cy >= g.nsub) {
         done = true;
         return false;
       }
     } else {
-      cp = cp + scale(disp, t.z);
+      cp = v3<T>(add_rn(cp.x, mul_rn(disp.x, t.z)), add_rn(cp.y, mul_rn(disp.y, t.z)), add_rn(cp.z, mul_rn(disp.z, t.z)));
       cz += az;
       if (cz < 0 || cz >= g.nsub) {
         done = true;
@@ -542,7 +557,8 @@ struct SubMask {
 // instead of three keeps the diffuse kernel's instruction footprint smaller (the
 // kernel stalls on instruction fetch; measured 7 % faster).
 template <typename T, class Set>
-__device__ __noinline__ void collect_neighbors(const Geo<T>& g, V3<T> pos, int ix, int iy, int iz, T r, Set& st) {
+__device__ __forceinline__ void collect_neighbors_body(const Geo<T>& g, V3<T> pos, int ix, int iy, int iz, T r,
+                                                       Set& st) {
   T part_len = g.part_edge;
   V3<T> rel = pos - g.origin;
   V3<T> plus = rel + v3<T>(r, r, r);
@@ -552,21 +568,21 @@ __device__ __noinline__ void collect_neighbors(const Geo<T>& g, V3<T> pos, int i
   if (minus.x < b.x && minus.x > (T)0.0) {
     st.insert3(g, ix - 1, iy, iz);
     xd = -1;
-  } else if (plus.x > b.x + g.sp_edge && plus.x < part_len) {
+  } else if (plus.x > add_rn(b.x, g.sp_edge) && plus.x < part_len) {
     st.insert3(g, ix + 1, iy, iz);
     xd = 1;
   }
   if (minus.y < b.y && minus.y > (T)0.0) {
     st.insert3(g, ix, iy - 1, iz);
     yd = -1;
-  } else if (plus.y > b.y + g.sp_edge && plus.y < part_len) {
+  } else if (plus.y > add_rn(b.y, g.sp_edge) && plus.y < part_len) {
     st.insert3(g, ix, iy + 1, iz);
     yd = 1;
   }
   if (minus.z < b.z && minus.z > (T)0.0) {
     st.insert3(g, ix, iy, iz - 1);
     zd = -1;
-  } else if (plus.z > b.z + g.sp_edge && plus.z < part_len) {
+  } else if (plus.z > add_rn(b.z, g.sp_edge) && plus.z < part_len) {
     st.insert3(g, ix, iy, iz + 1);
     zd = 1;
   }
@@ -574,6 +590,30 @@ __device__ __noinline__ void collect_neighbors(const Geo<T>& g, V3<T> pos, int i
   if (xd && zd) st.insert3(g, ix + xd, iy, iz + zd);
   if (yd && zd) st.insert3(g, ix, iy + yd, iz + zd);
   if (xd && yd && zd) st.insert3(g, ix + xd, iy + yd, iz + zd);
+}
+template <typename T, class Set>
+__device__ __noinline__ void collect_neighbors(const Geo<T>& g, V3<T> pos, int ix, int iy, int iz, T r, Set& st) {
+  collect_neighbors_body<T, Set>(g, pos, ix, iy, iz, r, st);
+}
+
+// collect_neighbors for the mask, returning what it adds: the caller's mask is not
+// passed by reference to the out-of-line call, so it can stay in registers
+struct MaskAdd {
+  uint64_t bits;
+  bool bad;
+};
+template <typename T>
+__device__ __noinline__ MaskAdd neighbors_mask(const Geo<T>& g, V3<T> pos, int ix, int iy, int iz, T r, int x0, int y0,
+                                               int z0, uint32_t n3) {
+  SubMask m;
+  m.bits = 0;
+  m.x0 = x0;
+  m.y0 = y0;
+  m.z0 = z0;
+  m.n3 = n3;
+  m.bad = false;
+  collect_neighbors_body<T, SubMask>(g, pos, ix, iy, iz, r, m);
+  return MaskAdd{m.bits, m.bad};
 }
 
 // subpartitions whose occupants can collide with the segment: crossed ones and
@@ -589,10 +629,26 @@ __device__ __forceinline__ void collect_start(const Geo<T>& g, V3<T> pos, int sx
   st.insert3(g, sx, sy, sz);
   collect_neighbors(g, pos, sx, sy, sz, collect_radius(g), st);
 }
+template <typename T>
+__device__ __forceinline__ void add_neighbors(const Geo<T>& g, V3<T> pos, int ix, int iy, int iz, SubMask& st) {
+  const MaskAdd a = neighbors_mask(g, pos, ix, iy, iz, collect_radius(g), st.x0, st.y0, st.z0, st.n3);
+  st.bits |= a.bits;
+  st.bad = st.bad || a.bad;
+}
+template <typename T>
+__device__ __forceinline__ void collect_start(const Geo<T>& g, V3<T> pos, int sx, int sy, int sz, SubMask& st) {
+  st.insert3(g, sx, sy, sz);
+  add_neighbors(g, pos, sx, sy, sz, st);
+}
 template <typename T, class Set>
 __device__ __forceinline__ void collect_crossing(const Geo<T>& g, const Walk<T>& w, Set& st) {
   st.insert3(g, w.cx, w.cy, w.cz);
   collect_neighbors(g, w.cp, w.cx, w.cy, w.cz, collect_radius(g), st);
+}
+template <typename T>
+__device__ __forceinline__ void collect_crossing(const Geo<T>& g, const Walk<T>& w, SubMask& st) {
+  st.insert3(g, w.cx, w.cy, w.cz);
+  add_neighbors(g, w.cp, w.cx, w.cy, w.cz, st);
 }
 template <typename T, class Set>
 __device__ __forceinline__ void collect_end(const Geo<T>& g, V3<T> pos, V3<T> disp, Set& st) {
@@ -600,6 +656,13 @@ __device__ __forceinline__ void collect_end(const Geo<T>& g, V3<T> pos, V3<T> di
   int ex, ey, ez;
   sub3(g, dest, ex, ey, ez);
   collect_neighbors(g, dest, ex, ey, ez, collect_radius(g), st);
+}
+template <typename T>
+__device__ __forceinline__ void collect_end(const Geo<T>& g, V3<T> pos, V3<T> disp, SubMask& st) {
+  V3<T> dest = pos + disp;
+  int ex, ey, ez;
+  sub3(g, dest, ex, ey, ez);
+  add_neighbors(g, dest, ex, ey, ez, st);
 }
 template <typename T, class Set>
 __device__ void collect_for_molecules(const Geo<T>& g, V3<T> pos, uint32_t sp, V3<T> disp, Set& st) {
@@ -617,8 +680,9 @@ __device__ void collect_for_molecules(const Geo<T>& g, V3<T> pos, uint32_t sp, V
 enum : int { CT_MISS = 0, CT_REDO = 1, CT_FRONT = 2, CT_BACK = 3 };
 
 // jump_away_line (collision_utils.inl:568-603)
-template <typename T, class D>
-__device__ __noinline__ void jump_away_line(V3<T> p, T k, V3<T> A, V3<T> B, V3<T> n, D& draws, V3<T>& v) {
+// `u`: its one 32-bit draw (the sign of the jump); returns the new move
+template <typename T>
+__device__ __noinline__ V3<T> jump_away_line(V3<T> p, T k, V3<T> A, V3<T> B, V3<T> n, uint32_t u, V3<T> v) {
   V3<T> e = B - A;
   T elen2 = dot(e, e);
   T le_1 = (T)1.0 / sqrt(elen2);
@@ -633,10 +697,11 @@ __device__ __noinline__ void jump_away_line(V3<T> p, T k, V3<T> A, V3<T> B, V3<T
   } else {
     tiny = Eps<T>::pos_sqrt;  // fp32 branch of the reference
   }
-  if ((draws.u32() & 1) == 0) tiny = -tiny;
+  if ((u & 1) == 0) tiny = -tiny;
   v.x -= tiny * f.x;
   v.y -= tiny * f.y;
   v.z -= tiny * f.z;
+  return v;
 }
 
 enum : int { PT_MISS = 0, PT_PARALLEL = 1, PT_HIT = 2 };
@@ -694,15 +759,20 @@ __device__ __forceinline__ int tri_test(S b, S c, S uv1u, S uv2u, S uv2v, S eps)
 // position and move are exact in fp64): near the plane the fp32 side test can
 // have the wrong sign (its error grows with the coordinates), letting a molecule
 // moving outwards pass a reflective wall. Out of line: rarely taken.
+// (results returned by value: nothing of the caller is passed by reference to these
+// out-of-line calls, so its variables can stay in registers)
 template <typename T>
-__device__ __noinline__ int plane_test_fp64(const double* w64, V3<T> pos, V3<T> move, T& a, T& dv) {
+struct PlaneFp64 {
+  int pt;
+  T a, dv;
+};
+template <typename T>
+__device__ __noinline__ PlaneFp64<T> plane_test_fp64(const double* w64, V3<T> pos, V3<T> move) {
   const double ddd = (w64[0] * (double)pos.x + w64[1] * (double)pos.y + w64[2] * (double)pos.z) - w64[3];
   const double dvd = w64[0] * (double)move.x + w64[1] * (double)move.y + w64[2] * (double)move.z;
   double ad = 0;
   const int pt = plane_test<double>(ddd, dvd, (double)Eps<T>::pos, ad);
-  a = (T)ad;
-  dv = (T)dvd;
-  return pt;
+  return PlaneFp64<T>{pt, (T)ad, (T)dvd};
 }
 
 // fp32 tie-break near an edge or vertex: the float in-triangle test is within its
@@ -713,23 +783,27 @@ __device__ __noinline__ int plane_test_fp64(const double* w64, V3<T> pos, V3<T> 
 // edge is re-tried. Returns a TRI_* code (crossing time and point updated), or
 // -1 when the fp64 plane test misses. Out of line: rarely taken.
 template <typename T>
-__device__ __noinline__ int edge_test_fp64(const double* w64, V3<T> pos, V3<T> move, int tr, T& ct, V3<T>& cpos,
-                                           T& dv) {
+struct EdgeFp64 {
+  int tr;
+  T ct, dv;
+  V3<T> cpos;
+};
+template <typename T>
+__device__ __noinline__ EdgeFp64<T> edge_test_fp64(const double* w64, V3<T> pos, V3<T> move, int tr, T ct,
+                                                   V3<T> cpos, T dv) {
   const double px = pos.x, py = pos.y, pz = pos.z, mx = move.x, my = move.y, mz = move.z;
   const double ddd = (w64[0] * px + w64[1] * py + w64[2] * pz) - w64[3];
   const double dvd = w64[0] * mx + w64[1] * my + w64[2] * mz;
   double ad = 0;
   const int ptd = plane_test<double>(ddd, dvd, Eps<double>::pos, ad);
-  if (ptd == PT_MISS) return -1;
-  if (ptd != PT_HIT) return tr;
+  if (ptd == PT_MISS) return EdgeFp64<T>{-1, ct, dv, cpos};
+  if (ptd != PT_HIT) return EdgeFp64<T>{tr, ct, dv, cpos};
   const double cx = px + mx * ad, cy = py + my * ad, cz = pz + mz * ad;
   const double lx = cx - w64[10], ly = cy - w64[11], lz = cz - w64[12];
   const double bd = lx * w64[4] + ly * w64[5] + lz * w64[6];
   const double cd = lx * w64[7] + ly * w64[8] + lz * w64[9];
-  ct = (T)ad;
-  cpos = v3<T>((T)cx, (T)cy, (T)cz);
-  dv = (T)dvd;
-  return tri_test<double>(bd, cd, w64[13], w64[14], w64[15], Eps<double>::pos);
+  const int t2 = tri_test<double>(bd, cd, w64[13], w64[14], w64[15], Eps<double>::pos);
+  return EdgeFp64<T>{t2, (T)ad, (T)dvd, v3<T>((T)cx, (T)cy, (T)cz)};
 }
 
 // collide_wall (collision_utils.inl:629-812)
@@ -742,10 +816,14 @@ __device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V
   T dd = dp - rj.w;
   T a;
   int pt;
-  if (sizeof(T) == 4 && tabs(dd) < (T)1e-2)
-    pt = plane_test_fp64<T>(g.w64 + 16 * (size_t)wi, pos, move, a, dv);
-  else
+  if (sizeof(T) == 4 && tabs(dd) < (T)1e-2) {
+    const PlaneFp64<T> q = plane_test_fp64<T>(g.w64 + 16 * (size_t)wi, pos, move);
+    pt = q.pt;
+    a = q.a;
+    dv = q.dv;
+  } else {
     pt = plane_test<T>(dd, dv, Eps<T>::pos, a);
+  }
   if (pt == PT_MISS) return CT_MISS;
   if (pt == PT_PARALLEL) {
     a = (abs_max_2vec(pos, move) + (T)1.0) * Eps<T>::pos;
@@ -768,17 +846,21 @@ __device__ int collide_wall(const Geo<T>& g, V3<T> pos, uint32_t wi, D& draws, V
   }
   int tr = tri_test<T>(dot(local, w.u), dot(local, w.v), w.uv1u, w.uv2u, w.uv2v, teps);
   if (sizeof(T) == 4 && tr >= TRI_E12) {
-    tr = edge_test_fp64<T>(g.w64 + 16 * (size_t)wi, pos, move, tr, ct, cpos, dv);
+    const EdgeFp64<T> q = edge_test_fp64<T>(g.w64 + 16 * (size_t)wi, pos, move, tr, ct, cpos, dv);
+    tr = q.tr;
+    ct = q.ct;
+    cpos = q.cpos;
+    dv = q.dv;
     if (tr < 0) return CT_MISS;
   }
   if (tr == TRI_IN) return dv > 0 ? CT_BACK : CT_FRONT;
   if (tr == TRI_OUT) return CT_MISS;
   if (tr == TRI_E12)
-    jump_away_line(pos, ct, w.v1, w.v2, normal, draws, move);
+    move = jump_away_line(pos, ct, w.v1, w.v2, normal, draws.u32(), move);
   else if (tr == TRI_E20)
-    jump_away_line(pos, ct, w.v2, w.v0, normal, draws, move);
+    move = jump_away_line(pos, ct, w.v2, w.v0, normal, draws.u32(), move);
   else
-    jump_away_line(pos, ct, w.v0, w.v1, normal, draws, move);
+    move = jump_away_line(pos, ct, w.v0, w.v1, normal, draws.u32(), move);
   return CT_REDO;
 }
 
@@ -825,8 +907,9 @@ __device__ MCG_GUARD_INLINE void guard_sides(const Geo<T>& g, uint32_t sp, V3<T>
 
 // the same, out of line, for the rare sites (reflection and crossing points)
 template <typename T>
-__device__ __noinline__ void guard_sides_rare(const Geo<T>& g, uint32_t sp, V3<T>& pos, V3<T> ref, uint32_t skip) {
+__device__ __noinline__ V3<T> guard_sides_rare(const Geo<T>& g, uint32_t sp, V3<T> pos, V3<T> ref, uint32_t skip) {
   guard_sides(g, sp, pos, ref, skip);
+  return pos;
 }
 
 template <typename T>
@@ -913,66 +996,209 @@ __device__ __forceinline__ void wall_fp64(const Geo<T>& g, uint32_t wi, double* 
   }
 }
 
-// Is p inside closed object `obj`? The reference's test
-// (compute_counted_volume_for_pos, collision_utils.inl:1515-1545): a ray from p to
-// the partition's origin corner moved by (edge/11, edge/21, 0) subpartition edges,
-// an odd number of crossed walls of the object means inside. The ray walks the
-// subpartition grid; a wall listed in several subpartitions counts once, in the
-// subpartition that holds its crossing point. fp64 throughout.
-template <typename T>
-__device__ bool inside_object(const Geo<T>& g, V3<double> p, uint32_t obj) {
-  const double e = (double)g.sp_edge;
-  const V3<double> o = v3<double>((double)g.origin.x, (double)g.origin.y, (double)g.origin.z);
-  const V3<double> dst = v3<double>(o.x + e / 11.0, o.y + e / 21.0, o.z);
-  const V3<double> d = dst - p;
-  const double rcp = (double)g.sp_rcp;
-  auto cell = [&](double v, double ov) {
-    int c = (int)floor((v - ov) * rcp);
-    return c < 0 ? 0 : (c >= g.nsub ? g.nsub - 1 : c);
-  };
-  int cx = cell(p.x, o.x), cy = cell(p.y, o.y), cz = cell(p.z, o.z);
-  const int ex = cell(dst.x, o.x), ey = cell(dst.y, o.y), ez = cell(dst.z, o.z);
-  uint32_t crossed = 0;
-  for (int guard = 0; guard < 3 * g.nsub + 3; guard++) {
-    const uint32_t sp = (uint32_t)cx + (uint32_t)cy * g.nsub + (uint32_t)cz * g.nsub2;
-    for (uint32_t k = g.wsp_off[sp]; k < g.wsp_off[sp + 1]; k++) {
-      const uint32_t wi = g.wsp_list[k];
-      if (g.wall_obj[wi] != obj) continue;
-      double c[16];
-      wall_fp64(g, wi, c);
-      const double a = c[0] * p.x + c[1] * p.y + c[2] * p.z - c[3];
-      const double b = c[0] * dst.x + c[1] * dst.y + c[2] * dst.z - c[3];
-      if ((a > 0 && b > 0) || (a < 0 && b < 0) || a == b) continue;
-      const double t = a / (a - b);
-      const V3<double> x = p + scale(d, t);
-      if (cell(x.x, o.x) != cx || cell(x.y, o.y) != cy || cell(x.z, o.z) != cz) continue;
-      const double lx = x.x - c[10], ly = x.y - c[11], lz = x.z - c[12];
-      const int tr = tri_test<double>(lx * c[4] + ly * c[5] + lz * c[6], lx * c[7] + ly * c[8] + lz * c[9], c[13], c[14],
-                                      c[15], Eps<double>::pos);
-      if (tr != TRI_OUT) crossed++;
-    }
-    if (cx == ex && cy == ey && cz == ez) break;
-    // next cell along the ray: the axis whose cell boundary comes first
-    double tb[3];
-    const double pv[3] = {p.x, p.y, p.z}, dv[3] = {d.x, d.y, d.z}, ov[3] = {o.x, o.y, o.z};
-    const int cv[3] = {cx, cy, cz};
-    for (int k = 0; k < 3; k++) {
-      if (dv[k] == 0) {
-        tb[k] = 1e300;
-        continue;
-      }
-      const double bnd = ov[k] + e * (double)(cv[k] + (dv[k] > 0 ? 1 : 0));
-      tb[k] = (bnd - pv[k]) / dv[k];
-    }
-    if (tb[0] <= tb[1] && tb[0] <= tb[2])
-      cx += d.x > 0 ? 1 : -1;
-    else if (tb[1] <= tb[2])
-      cy += d.y > 0 ? 1 : -1;
-    else
-      cz += d.z > 0 ? 1 : -1;
-    if (cx < 0 || cy < 0 || cz < 0 || cx >= g.nsub || cy >= g.nsub || cz >= g.nsub) break;
+// The inside tests (counted-volume membership at upload and release, releases into a
+// closed object) count a ray's wall crossings as the reference does, in fp64 from the
+// walls' fp64 constants. The fp32 engine's translation unit allows fused multiply-adds,
+// so the arithmetic here is written with round-to-nearest intrinsics: both engines
+// reproduce the reference's fp64 decisions bit for bit.
+__device__ __forceinline__ double rn_dot3(double ax, double ay, double az, double bx, double by, double bz) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(ax, bx), __dmul_rn(ay, by)), __dmul_rn(az, bz));
+}
+__device__ __forceinline__ bool rn_distinguishable(double a, double b, double eps) {
+  const double c = fabs(__dsub_rn(a, b));
+  a = fabs(a);
+  if (a < 1) a = 1;
+  b = fabs(b);
+  eps = b < a ? __dmul_rn(eps, a) : __dmul_rn(eps, b);
+  return c > eps;
+}
+
+// collide_wall (collision_utils.inl:629-812) for the inside tests, with a wall's fp64
+// constants c[16] (wall_fp64): CT_MISS, CT_FRONT, CT_BACK, or CT_REDO where the
+// reference re-tries (a ray in the wall's plane or through an edge, which makes its
+// inside tests give up: must_redo_test)
+static __device__ __noinline__ int collide_wall_rn(const double* c, V3<double> pos, V3<double> move) {
+  const double dp = rn_dot3(c[0], c[1], c[2], pos.x, pos.y, pos.z);
+  const double dv = rn_dot3(c[0], c[1], c[2], move.x, move.y, move.z);
+  const double dd = __dsub_rn(dp, c[3]);
+  double a = 0;
+  const int pt = plane_test<double>(dd, dv, Eps<double>::pos, a);
+  if (pt == PT_MISS) return CT_MISS;
+  if (pt == PT_PARALLEL) return CT_REDO;
+  const double lx = __dsub_rn(__dadd_rn(pos.x, __dmul_rn(a, move.x)), c[10]);
+  const double ly = __dsub_rn(__dadd_rn(pos.y, __dmul_rn(a, move.y)), c[11]);
+  const double lz = __dsub_rn(__dadd_rn(pos.z, __dmul_rn(a, move.z)), c[12]);
+  const double b = rn_dot3(lx, ly, lz, c[4], c[5], c[6]);
+  double cc = rn_dot3(lx, ly, lz, c[7], c[8], c[9]);
+  const double uv1u = c[13], uv2u = c[14], uv2v = c[15];
+  double f;
+  if (uv2v < 0) {
+    cc = -cc;
+    f = -uv2v;
+  } else {
+    f = uv2v;
   }
-  return (crossed & 1) != 0;
+  if (cc > 0) {
+    const double gg = __dmul_rn(b, f), h = __dmul_rn(cc, uv2u);
+    if (gg > h) {
+      const double lhs = __dadd_rn(__dmul_rn(cc, uv1u), gg), rhs = __dadd_rn(h, __dmul_rn(uv1u, uv2v));
+      if (lhs < rhs) return dv > 0 ? CT_BACK : CT_FRONT;
+      return rn_distinguishable(lhs, rhs, Eps<double>::pos) ? CT_MISS : CT_REDO;
+    }
+    return rn_distinguishable(gg, h, Eps<double>::pos) ? CT_MISS : CT_REDO;
+  }
+  return rn_distinguishable(cc, 0.0, Eps<double>::pos) ? CT_MISS : CT_REDO;
+}
+
+// raycast_with_endpoints with compute_inputs_for_raycast_with_endpoints
+// (collision_utils.inl:138-244): the subpartitions a ray from p1 to p2 visits, in
+// order. Like the reference's, it ends as soon as the axis it would step along has
+// reached p2's subpartition, which can be before p2's subpartition on the others.
+struct RayCells {
+  int ix, iy, iz, ex, ey, ez, dx, dy, dz, n, n2;
+  double tx, ty, tz, gx, gy, gz;
+  uint32_t sp;
+  template <typename T>
+  __device__ void start(const Geo<T>& g, V3<double> p1, V3<double> p2, V3<double> d) {
+    n = g.nsub;
+    n2 = g.nsub2;
+    dx = d.x > 0 ? 1 : (d.x < 0 ? -1 : 0);
+    dy = d.y > 0 ? 1 : (d.y < 0 ? -1 : 0);
+    dz = d.z > 0 ? 1 : (d.z < 0 ? -1 : 0);
+    const double ax = d.x == 0 ? Eps<double>::pos : fabs(d.x), ay = d.y == 0 ? Eps<double>::pos : fabs(d.y),
+                 az = d.z == 0 ? Eps<double>::pos : fabs(d.z);
+    const double rx = 1.0 / ax, ry = 1.0 / ay, rz = 1.0 / az;
+    const double side = g.sp_edge64, rcp = g.sp_rcp64;
+    gx = __dmul_rn(side, rx);
+    gy = __dmul_rn(side, ry);
+    gz = __dmul_rn(side, rz);
+    ix = (int)__dmul_rn(__dsub_rn(p1.x, g.origin64[0]), rcp);
+    iy = (int)__dmul_rn(__dsub_rn(p1.y, g.origin64[1]), rcp);
+    iz = (int)__dmul_rn(__dsub_rn(p1.z, g.origin64[2]), rcp);
+    ex = (int)__dmul_rn(__dsub_rn(p2.x, g.origin64[0]), rcp);
+    ey = (int)__dmul_rn(__dsub_rn(p2.y, g.origin64[1]), rcp);
+    ez = (int)__dmul_rn(__dsub_rn(p2.z, g.origin64[2]), rcp);
+    sp = (uint32_t)(ix + iy * n + iz * n2);
+    // the cell boundaries are multiples of the cell side from 0 (the partition's corner is one)
+    const double mx = __dmul_rn(floor(__dmul_rn(p1.x, rcp)), side), my = __dmul_rn(floor(__dmul_rn(p1.y, rcp)), side),
+                 mz = __dmul_rn(floor(__dmul_rn(p1.z, rcp)), side);
+    tx = __dmul_rn(dx == -1 ? __dsub_rn(p1.x, mx) : __dsub_rn(__dadd_rn(mx, side), p1.x), rx);
+    ty = __dmul_rn(dy == -1 ? __dsub_rn(p1.y, my) : __dsub_rn(__dadd_rn(my, side), p1.y), ry);
+    tz = __dmul_rn(dz == -1 ? __dsub_rn(p1.z, mz) : __dsub_rn(__dadd_rn(mz, side), p1.z), rz);
+  }
+  // after visiting sp: to the next subpartition, false when the ray is done
+  __device__ bool next() {
+    if (tx <= ty && tx <= tz) {
+      if (ix == ex) return false;
+      tx = __dadd_rn(tx, gx);
+      ix += dx;
+      sp += (uint32_t)dx;
+    } else if (ty <= tz) {
+      if (iy == ey) return false;
+      ty = __dadd_rn(ty, gy);
+      iy += dy;
+      sp += (uint32_t)(dy * n);
+    } else {
+      if (iz == ez) return false;
+      tz = __dadd_rn(tz, gz);
+      iz += dz;
+      sp += (uint32_t)(dz * n2);
+    }
+    return true;
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ bool listed_in(const Geo<T>& g, uint32_t sp, uint32_t wi) {
+  if (sp >= g.n3) return false;
+  uint32_t lo = g.wsp_off[sp], hi = g.wsp_off[sp + 1];  // ascending wall indices
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    const uint32_t v = g.wsp_list[mid];
+    if (v == wi) return true;
+    if (v < wi)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return false;
+}
+
+// Crossings of a ray from p to dst (moved by -POS_EPS on every axis, as the reference
+// moves its displacement) with the walls of the objects `want` selects (a bit per
+// counted-object slot, or the object itself): each wall counts once, at the first
+// subpartition of the ray that lists it (get_num_crossed_walls_per_object /
+// get_num_crossed_region_walls, collision_utils.inl:1328-1465). Returns the crossings
+// per slot as parity bits, or NONE when the ray met an edge or lay in a wall's plane.
+// `region` >= 0: count the walls of that object into bit 0 instead of the slots.
+template <typename T>
+__device__ uint32_t ray_parity(const Geo<T>& g, V3<double> p, V3<double> dst, int region) {
+  const V3<double> d = v3<double>(__dsub_rn(__dsub_rn(dst.x, p.x), Eps<double>::pos),
+                                  __dsub_rn(__dsub_rn(dst.y, p.y), Eps<double>::pos),
+                                  __dsub_rn(__dsub_rn(dst.z, p.z), Eps<double>::pos));
+  RayCells rc;
+  rc.start(g, p, dst, d);
+  uint32_t parity = 0;
+  int k = 0;
+  for (int guard = 0; guard < 3 * g.nsub + 3; guard++, k++) {
+    const uint32_t sp = rc.sp;
+    if (sp < g.n3) {
+      for (uint32_t e = g.wsp_off[sp]; e < g.wsp_off[sp + 1]; e++) {
+        const uint32_t wi = g.wsp_list[e];
+        const uint32_t o = g.wall_obj[wi];
+        uint32_t bits;
+        if (region >= 0) {
+          bits = o == (uint32_t)region ? 1u : 0u;
+        } else {
+          bits = 0;
+          for (uint32_t q = 0; q < g.n_cv; q++)
+            if (g.cv_obj[q] == o) bits |= 1u << q;
+        }
+        if (!bits) continue;
+        double c[16];
+        wall_fp64(g, wi, c);
+        const int ct = collide_wall_rn(c, p, d);
+        if (ct == CT_REDO) return NONE;
+        if (ct == CT_MISS) continue;
+        // counted once: skip when an earlier subpartition of the ray lists the wall
+        bool seen = false;
+        RayCells r2;
+        r2.start(g, p, dst, d);
+        for (int j = 0; j < k && !seen; j++) {
+          seen = listed_in(g, r2.sp, wi);
+          if (!r2.next()) break;
+        }
+        if (!seen) parity ^= bits;
+      }
+    }
+    if (!rc.next()) break;
+  }
+  return parity;
+}
+
+// compute_counted_volume_for_pos (collision_utils.inl:1515-1545): the counted objects
+// (bit q for slot q of cv_obj) whose walls a ray from p to the partition's corner,
+// moved by (edge/11, edge/21, 0) subpartition edges, crosses an odd number of times;
+// NONE when the ray met an edge (the reference stops there)
+template <typename T>
+__device__ uint32_t counted_volume_bits(const Geo<T>& g, V3<double> p) {
+  const double e = g.sp_edge64;
+  const V3<double> dst = v3<double>(__dadd_rn(g.origin64[0], e / 11.0), __dadd_rn(g.origin64[1], e / 21.0),
+                                    g.origin64[2]);
+  return ray_parity(g, p, dst, -1);
+}
+
+// is_point_inside_region_no_waypoints (collision_utils.inl:1484-1510) for the closed
+// region made of object obj's walls, whose bounding box's low corner is llf: 1 inside,
+// 0 outside, NONE when the ray met an edge
+template <typename T>
+__device__ uint32_t inside_region(const Geo<T>& g, V3<double> p, uint32_t obj, const double* llf) {
+  const double e = g.sp_edge64;
+  V3<double> dst = v3<double>(__dsub_rn(llf[0], Eps<double>::pos), __dsub_rn(llf[1], Eps<double>::pos),
+                              __dsub_rn(llf[2], Eps<double>::pos));
+  dst.x = __dadd_rn(dst.x, e / 11.0);
+  dst.y = __dadd_rn(dst.y, e / 22.0);
+  return ray_parity(g, p, dst, (int)obj);
 }
 
 // ------------------------------------------------------------------ collisions with molecules
@@ -1096,11 +1322,11 @@ __device__ __forceinline__ void occupants_of(const Geo<T>& g, const Cells<T>& ce
           const uint32_t j = j4 + u;
           if (j >= j1) break;
           const V3<T> dir = v3<T>(q4[u].x, q4[u].y, q4[u].z) - pos;
-          const T d = dot(dir, disp);
+          const T d = dot_rn(dir, disp);
           if (d < 0) continue;
           if (d > movelen2) continue;
-          const T dirlen2 = dot(dir, dir);
-          if (movelen2 * dirlen2 - d * d > movelen2 * sigma2) continue;
+          const T dirlen2 = dot_rn(dir, dir);
+          if (sub_rn(mul_rn(movelen2, dirlen2), mul_rn(d, d)) > mul_rn(movelen2, sigma2)) continue;
           if (j == self) continue;
           if (cells.dead && cells.dead[j] == 2) continue;
           VV<T> c;
@@ -1118,11 +1344,11 @@ __device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, u
                                        V3<T> disp, const SubSet& st, C& out) {
   const Chem& ch = *g.chem;
   const uint32_t pmask = ch.partners[species];
-  const T movelen2 = dot(disp, disp);
-  const T sigma2 = g.R * g.R;
+  const T movelen2 = dot_rn(disp, disp);
+  const T sigma2 = mul_rn(g.R, g.R);
   // segment box grown by R plus a margin that covers rounding in the octant test
   const V3<T> e = pos + disp;
-  const T mg = g.R * (T)1.01 + g.sp_edge * (T)1e-3;
+  const T mg = add_rn(mul_rn(g.R, (T)1.01), mul_rn(g.sp_edge, (T)1e-3));
   const V3<T> lo = v3<T>(min(pos.x, e.x) - mg, min(pos.y, e.y) - mg, min(pos.z, e.z) - mg);
   const V3<T> hi = v3<T>(max(pos.x, e.x) + mg, max(pos.y, e.y) + mg, max(pos.z, e.z) + mg);
   for (int i = 0; i < st.n; i++) occupants_of(g, cells, self, pos, disp, pmask, movelen2, sigma2, lo, hi, st.s[i], out);
@@ -1135,11 +1361,11 @@ __device__ void collide_with_occupants(const Geo<T>& g, const Cells<T>& cells, u
                                        V3<T> disp, const SubMask& sm, C& out) {
   const Chem& ch = *g.chem;
   const uint32_t pmask = ch.partners[species];
-  const T movelen2 = dot(disp, disp);
-  const T sigma2 = g.R * g.R;
+  const T movelen2 = dot_rn(disp, disp);
+  const T sigma2 = mul_rn(g.R, g.R);
   // segment box grown by R plus a margin that covers rounding in the octant test
   const V3<T> e = pos + disp;
-  const T mg = g.R * (T)1.01 + g.sp_edge * (T)1e-3;
+  const T mg = add_rn(mul_rn(g.R, (T)1.01), mul_rn(g.sp_edge, (T)1e-3));
   const V3<T> lo = v3<T>(min(pos.x, e.x) - mg, min(pos.y, e.y) - mg, min(pos.z, e.z) - mg);
   const V3<T> hi = v3<T>(max(pos.x, e.x) + mg, max(pos.y, e.y) + mg, max(pos.z, e.z) + mg);
   for (uint64_t mb = sm.bits; mb; mb &= mb - 1) {
@@ -1170,9 +1396,11 @@ __device__ __forceinline__ void mask_box(const Geo<T>& g, V3<T> pos, V3<T> mdisp
 
 // the partner set of a segment cut short by a wall hit; out of line: rarely taken
 template <typename T>
-__device__ __noinline__ void recollect_mask(const Geo<T>& g, V3<T> pos, uint32_t sp, V3<T> mdisp, SubMask& sm) {
+__device__ __noinline__ SubMask recollect_mask(const Geo<T>& g, V3<T> pos, uint32_t sp, V3<T> mdisp) {
+  SubMask sm;
   mask_box(g, pos, mdisp, sm);
   if (!sm.bad) collect_for_molecules(g, pos, sp, mdisp, sm);
+  return sm;
 }
 
 // The partner set visited without storing it: every subpartition the collection
@@ -1223,10 +1451,10 @@ __device__ int partners_listed(const Geo<T>& g, const Cells<T>& cells, uint32_t 
   ss.n3 = (uint32_t)g.nsub2 * (uint32_t)g.nsub;
   ss.pos = pos;
   ss.disp = remaining;
-  ss.movelen2 = dot(remaining, remaining);
-  ss.sigma2 = g.R * g.R;
+  ss.movelen2 = dot_rn(remaining, remaining);
+  ss.sigma2 = mul_rn(g.R, g.R);
   const V3<T> e = pos + remaining;
-  const T mg = g.R * (T)1.01 + g.sp_edge * (T)1e-3;
+  const T mg = add_rn(mul_rn(g.R, (T)1.01), mul_rn(g.sp_edge, (T)1e-3));
   ss.lo = v3<T>(min(pos.x, e.x) - mg, min(pos.y, e.y) - mg, min(pos.z, e.z) - mg);
   ss.hi = v3<T>(max(pos.x, e.x) + mg, max(pos.y, e.y) + mg, max(pos.z, e.z) + mg);
   out.dedupe = true;
@@ -1238,15 +1466,17 @@ __device__ int partners_listed(const Geo<T>& g, const Cells<T>& cells, uint32_t 
 // the 4x4x4 mask (long moves, fine grids); out of line: rarely taken. Returns the
 // partner mode used (PM_LIST or PM_STREAM).
 template <typename T>
-__device__ __noinline__ int partners_by_list(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos,
+__device__ __noinline__ int partners_by_list(const Geo<T>& g, const Cells<T> cells, uint32_t self, V3<T> pos,
                                              uint32_t sp, V3<T> mdisp, int species, V3<T> remaining,
-                                             Colls<T>& colls, uint32_t& err) {
+                                             Colls<T>& colls) {
   CollsX<T> x{colls, false, false, (T)0, 0};
-  return partners_listed(g, cells, self, pos, sp, mdisp, species, remaining, PM_LIST, x, err);
+  uint32_t err = 0;
+  const int mode = partners_listed(g, cells, self, pos, sp, mdisp, species, remaining, PM_LIST, x, err);
+  return mode | (int)(err << 8);  // the mode, and ST_SET_OVERFLOW shifted into bits 8+
 }
 
 template <typename T>
-__device__ __noinline__ void save_refill(RefillState<T>* rs, const SubMask& sm, V3<T> mdisp, uint32_t sp, int mode) {
+__device__ __noinline__ void save_refill(RefillState<T>* rs, SubMask sm, V3<T> mdisp, uint32_t sp, int mode) {
   rs->sm = sm;
   rs->mdisp = mdisp;
   rs->sp = sp;
@@ -1256,16 +1486,19 @@ __device__ __noinline__ void save_refill(RefillState<T>* rs, const SubMask& sm, 
 // The next page of candidates after a page that overflowed: those after its last
 // one in time order, collected the way the first page was. Out of line: rare.
 template <typename T>
-__device__ __noinline__ void refill_colls(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos, int species,
-                                          V3<T> remaining, const RefillState<T>* rs, Colls<T>& colls, uint32_t& err) {
+__device__ __noinline__ uint32_t refill_colls(const Geo<T>& g, const Cells<T> cells, uint32_t self, V3<T> pos,
+                                              int species, V3<T> remaining, const RefillState<T>* rs,
+                                              Colls<T>& colls) {
   const VV<T> last = colls.c[colls.n - 1];
   CollsX<T> x{colls, true, false, last.t, cells.uid[last.idx]};
   colls.n = 0;
   colls.overflow = false;
+  uint32_t err = 0;
   if (rs->mode == PM_MASK)
     collide_with_occupants(g, cells, self, pos, species, remaining, rs->sm, x);
   else
     partners_listed(g, cells, self, pos, rs->sp, rs->mdisp, species, remaining, rs->mode, x, err);
+  return err;
 }
 
 // ------------------------------------------------------------------ exact disk
@@ -1588,20 +1821,22 @@ __device__ __forceinline__ int pathway_for(const double* cum, int npw, double ma
 
 // test_bimolecular (rxn_utils.inl:336-414): the pathway that fires, or -1. Out of
 // line (fp64 arithmetic, run for few candidates): a smaller diffuse kernel.
-template <class D>
-__device__ __noinline__ int test_bimolecular(const double* cum, int npw, double scaling, D& draws) {
+// `u`: the one 32-bit draw it takes (rng_dbl), drawn by the caller so that the
+// generator's state is not passed by reference to this out-of-line call
+static __device__ __noinline__ int test_bimolecular(const double* cum, int npw, double scaling, uint32_t u) {
   const double max_fixed_p = cum[npw - 1];
+  const double r = (double)u * (1.0 / 4294967296.0);
   double prob;
   if (max_fixed_p < scaling) {
-    prob = draw_dbl(draws) * scaling;
+    prob = r * scaling;
     if (prob >= max_fixed_p) return -1;
   } else {
     const float max_p = (float)max_fixed_p;
     if (max_p >= scaling) {
       // cannot scale enough: keep the proportions of the pathways
-      prob = draw_dbl(draws) * max_p;
+      prob = r * max_p;
     } else {
-      prob = draw_dbl(draws) * scaling;
+      prob = r * scaling;
       if (prob >= max_p) return -1;
     }
   }
@@ -1652,7 +1887,8 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
   TraceOut<T> res;
   res.status = 0;
   res.err = 0;
-  res.flip = 0;
+  res.cv_mask = 0;
+  res.cv_val = 0;
   res.partner = NONE;
   res.t_abs = 0;
   res.pathway = 0;
@@ -1723,7 +1959,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
       // falls outside) the list
       if (hit_wall && !hit_in_last) {
         mdisp = used_tentative ? up_to_init : hit.pos - pos;
-        recollect_mask(g, pos, sp, mdisp, sm);
+        sm = recollect_mask(g, pos, sp, mdisp);
       } else if (!sm.bad) {
         collect_end(g, pos, pdisp, sm);
       }
@@ -1731,7 +1967,9 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
       if (!sm.bad) {
         collide_with_occupants(g, cells, self, pos, species, remaining, sm, colls);
       } else {
-        pmode = partners_by_list(g, cells, self, pos, sp, mdisp, species, remaining, colls, res.err);
+        const int pm = partners_by_list(g, cells, self, pos, sp, mdisp, species, remaining, colls);
+        pmode = pm & 0xFF;
+        res.err |= (uint32_t)pm >> 8;
       }
       // a full page: how to collect the next one (rare)
       if (colls.overflow) save_refill(&rs, sm, mdisp, sp, pmode);
@@ -1756,7 +1994,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
       if (i == colls.n && colls.overflow) {
         // the page held only the earliest candidates: the next ones, in time order
         res.err |= ST_COLL_OVERFLOW;
-        refill_colls(g, cells, self, pos_at_start, species, remaining, &rs, colls, res.err);
+        res.err |= refill_colls(g, cells, self, pos_at_start, species, remaining, &rs, colls);
         i = -1;
         continue;
       }
@@ -1772,7 +2010,11 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
         const int kind = ch.can_volwall[species] ? g.wall_class[(size_t)hit.wall * g.nsp + species] : 0;
         const double t_abs = elapsed + t_steps * (double)hit.t;
         if (kind == 1) {
-          res.flip ^= cv_flip_of_wall(g, hit.wall);
+          if (g.n_cv) {
+            const uint32_t f = cv_bits_of_wall(g, hit.wall);
+            res.cv_mask |= f;
+            res.cv_val = hit.type == CT_FRONT ? (res.cv_val | f) : (res.cv_val & ~f);
+          }
           pos = hit.pos;
           sp = subpart_of(g, pos);
           double t_smash = (double)hit.t;
@@ -1786,7 +2028,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
           // triangle of the crossed edge is hit again at t ~ 0 and re-tried without end
           if (sizeof(T) == 4) {
             keep_side(g.wrej[hit.wall], hit.type == CT_FRONT ? -1.0 : 1.0, pos);
-            guard_sides_rare(g, sp, pos, pos_at_start, hit.wall);  // every other plane: the side it came from
+            pos = guard_sides_rare(g, sp, pos, pos_at_start, hit.wall);  // every other plane: the side it came from
             sp = subpart_of(g, pos);
           }
           ev.put(2, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
@@ -1816,7 +2058,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
           // edge of two faces rounds onto both planes)
           if (sizeof(T) == 4) {
             keep_side(rj, hit.type == CT_FRONT ? 1.0 : -1.0, pos);
-            guard_sides_rare(g, sp, pos, pos_at_start, hit.wall);
+            pos = guard_sides_rare(g, sp, pos, pos_at_start, hit.wall);
             sp = subpart_of(g, pos);
           }
           ev.put(1, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
@@ -1843,7 +2085,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
       }
       double scaling = (double)factor * r_rate_factor;
       const uint32_t ps = meta_of(q) & META_SPECIES_MASK;
-      const int pw = test_bimolecular(ch.bimol_cum[species][ps], ch.bimol_npw[species][ps], scaling, draws);
+      const int pw = test_bimolecular(ch.bimol_cum[species][ps], ch.bimol_npw[species][ps], scaling, draws.u32());
       if (pw < 0) {
         ev.put(4, cuid, 0, (double)c.t, t_abs, (double)cpos.x, (double)cpos.y, (double)cpos.z);
         continue;

@@ -674,6 +674,46 @@ class DeviceEngineT : public DeviceEngine {
     if (rc) return rc;
     out[0] = cnt_.warn_coll_overflow;
     out[1] = cnt_.warn_set_overflow;
+    out[2] = cnt_.warn_inside_redo;
+    return 0;
+  }
+
+  int inside_tests(uint32_t rep, uint32_t n, const double* pos, int kind, uint32_t obj, uint32_t* out,
+                   std::string& err) override {
+    int rc = sync(err);
+    if (rc) return rc;
+    if (rep >= max_rep_ || !reps_[rep].used) {
+      err = "no such replica";
+      return -1;
+    }
+    const Rep& R = reps_[rep];
+    double llf[3] = {0, 0, 0};
+    if (kind == 1) {
+      if (!R.has_obj || obj >= R.obj_llf.size() / 3 || R.obj_llf[3 * obj] > R.obj_urb[3 * obj]) {
+        err = "no walls of that object (mcg_set_wall_objects)";
+        return -1;
+      }
+      for (int a = 0; a < 3; a++) llf[a] = R.obj_llf[3 * obj + a];
+    } else if (!R.n_cv) {
+      err = "no counted objects in this model";
+      return -1;
+    } else if (!R.has_obj) {
+      err = "counted objects need wall objects";
+      return -1;
+    }
+    if (n == 0) return 0;
+    AllocSet tmp;
+    double *d_pos, *d_llf;
+    uint32_t* d_out;
+    MCG_CUDA(tmp.get(&d_pos, sizeof(double) * 3 * n));
+    MCG_CUDA(tmp.get(&d_llf, sizeof(double) * 3));
+    MCG_CUDA(tmp.get(&d_out, sizeof(uint32_t) * n));
+    MCG_CUDA(cudaMemcpyAsync(d_pos, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, stream_));
+    MCG_CUDA(cudaMemcpyAsync(d_llf, llf, sizeof(double) * 3, cudaMemcpyHostToDevice, stream_));
+    k_inside_tests<T><<<grid(n), TPB, 0, stream_>>>(state(parity_), rep, n, d_pos, kind, obj, d_llf, d_out);
+    launches_ += 1;
+    MCG_CUDA(cudaGetLastError());
+    MCG_CUDA(d2h(out, d_out, sizeof(uint32_t) * n));
     return 0;
   }
 
@@ -872,6 +912,9 @@ class DeviceEngineT : public DeviceEngine {
     g.n3 = hs.nsub * hs.nsub * hs.nsub;
     g.rcp_n = 1.0f / (float)hs.nsub;
     g.rcp_n2 = 1.0f / (float)(hs.nsub * hs.nsub);
+    for (int a = 0; a < 3; a++) g.origin64[a] = hs.origin[a];
+    g.sp_edge64 = hs.sp_edge;
+    g.sp_rcp64 = hs.sp_rcp;
     const uint64_t base_keys = (uint64_t)g.n3 * nsp_;
     // occupants are binned per subpartition octant while the key space stays small
     g.oct_shift = (sp.octants && base_keys * 8 <= (1ull << 26)) ? 3 : 0;

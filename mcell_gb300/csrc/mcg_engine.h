@@ -157,8 +157,13 @@ class DeviceEngine {
                            uint32_t ndraws, const double* rrf, const double* tst, double* out, std::string& err) = 0;
   virtual void stats(uint64_t* iterations, uint64_t* mol_steps, uint64_t* launches) = 0;
   // exact fallbacks taken: [0] traces that refilled a full candidate page, [1] traces
-  // whose partner list overflowed (partners scanned along the walk)
+  // whose partner list overflowed (partners scanned along the walk); [2] inside tests
+  // whose ray met a wall edge
   virtual int fallbacks(uint64_t* out, std::string& err) = 0;
+  // inside tests on points (parity harness): kind 0 counted-volume bits, 1 inside
+  // object obj; 0xFFFFFFFF where the ray met an edge
+  virtual int inside_tests(uint32_t rep, uint32_t n, const double* pos, int kind, uint32_t obj, uint32_t* out,
+                           std::string& err) = 0;
   // test hook: capacities of a candidate page (<= 16) and of the partner list (<= 48)
   virtual int set_trace_limits(int maxc, int maxset, std::string& err) = 0;
   virtual void set_options(int use_graphs, int profile) = 0;
@@ -179,6 +184,12 @@ void set_alloc_failure(long long after);
 // which_unimolecular): cum[n][MAX_PATHWAYS], npw[n], scaling[n] (kind 0), draws[n]
 int rxn_decisions(int kind, uint32_t n, const double* cum, const uint32_t* npw, const double* scaling,
                   const uint32_t* draws, int32_t* out, std::string& err);
+
+// release positions on an injected stream (parity harness of release_point): shape 0
+// ellipsoid, 1 cuboid, 2 ellipsoid shell; one stream for the whole release; *used = the
+// draws consumed (0xFFFFFFFF if they ran out)
+int release_positions(int shape, uint32_t n, const double* center, const double* diameter, const uint32_t* draws,
+                      uint32_t ndraws, double* out, uint32_t* used, std::string& err);
 
 DeviceEngine* make_engine_f64();
 DeviceEngine* make_engine_f32();

@@ -20,7 +20,7 @@ __global__ void k_rxn_decisions(int kind, uint32_t n, const double* cum, const u
   d.used = 0;
   d.over = false;
   const int np = (int)min(max(npw[c], 1u), (uint32_t)MAXPW);
-  out[c] = kind == 0 ? test_bimolecular(cum + (size_t)c * MAXPW, np, scaling[c], d)
+  out[c] = kind == 0 ? test_bimolecular(cum + (size_t)c * MAXPW, np, scaling[c], d.u32())
                      : which_unimolecular(cum + (size_t)c * MAXPW, np, d);
 }
 
@@ -47,4 +47,44 @@ int rxn_decisions(int kind, uint32_t n, const double* cum, const uint32_t* npw, 
   MCG_CUDA(cudaMemcpy(out, d_out, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
   return 0;
 }
+
+// one thread draws the whole release from the injected stream, as the reference's
+// single generator does
+__global__ void k_release_positions(int shape, uint32_t n, const double* c, const double* dia, const uint32_t* draws,
+                                    uint32_t ndraws, double* out, uint32_t* used) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  InjectedDraws d;
+  d.d = draws;
+  d.n = ndraws;
+  d.used = 0;
+  d.over = false;
+  for (uint32_t i = 0; i < n; i++) {
+    V3<double> p;
+    release_point(shape, c, dia, d, p);
+    out[3 * i] = p.x;
+    out[3 * i + 1] = p.y;
+    out[3 * i + 2] = p.z;
+  }
+  *used = d.over ? 0xFFFFFFFFu : d.used;
+}
+
+int release_positions(int shape, uint32_t n, const double* center, const double* diameter, const uint32_t* draws,
+                      uint32_t ndraws, double* out, uint32_t* used, std::string& err) {
+  AllocSet a;
+  double *d_c, *d_out;
+  uint32_t *d_dr, *d_used;
+  MCG_CUDA(a.get(&d_c, sizeof(double) * 6));
+  MCG_CUDA(a.get(&d_out, sizeof(double) * 3 * std::max<uint32_t>(n, 1)));
+  MCG_CUDA(a.get(&d_dr, sizeof(uint32_t) * std::max<uint32_t>(ndraws, 1)));
+  MCG_CUDA(a.get(&d_used, sizeof(uint32_t)));
+  const double cd[6] = {center[0], center[1], center[2], diameter[0], diameter[1], diameter[2]};
+  MCG_CUDA(cudaMemcpy(d_c, cd, sizeof(cd), cudaMemcpyHostToDevice));
+  if (ndraws) MCG_CUDA(cudaMemcpy(d_dr, draws, sizeof(uint32_t) * ndraws, cudaMemcpyHostToDevice));
+  k_release_positions<<<1, 1>>>(shape, n, d_c, d_c + 3, d_dr, ndraws, d_out, d_used);
+  MCG_CUDA(cudaGetLastError());
+  MCG_CUDA(cudaMemcpy(out, d_out, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost));
+  MCG_CUDA(cudaMemcpy(used, d_used, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
 }  // namespace mcg

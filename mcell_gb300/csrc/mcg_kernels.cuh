@@ -52,6 +52,7 @@ struct Counters {
   unsigned long long mol_steps;
   unsigned long long warn_coll_overflow;  // traces that refilled a full candidate page
   unsigned long long warn_set_overflow;   // traces that scanned partners along the walk
+  unsigned long long warn_inside_redo;    // inside tests whose ray met an edge (see counted_volume_bits)
   // first escapes (diagnostics): uid, species, iteration, start xyz, displacement xyz, final xyz, replica
   uint32_t n_esc;
   double esc[8][13];
@@ -217,7 +218,7 @@ __device__ void add_product(const State<T>& s, int species, uint32_t rep, uint32
 // diffuse_react_event.cpp:1809-1813, :2939). it: the replica's own iteration.
 template <typename T>
 __device__ __noinline__ void unimol_products(const State<T>& s, const Geo<T>& g, int species, uint32_t cv, V3<T> pos,
-                                             double t, uint64_t uid, uint32_t it, PhiloxDraws& draws) {
+                                             double t, uint64_t uid, uint32_t it, PhiloxDraws draws) {
   const Chem& ch = *g.chem;
   const int pw = which_unimolecular(ch.uni_cum[species], ch.uni_npw[species], draws);
   for (int k = 0; k < 2; k++) {
@@ -327,7 +328,8 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   } else {
     r.status = 0;
     r.pos = pos;
-    r.flip = 0;
+    r.cv_mask = 0;
+    r.cv_val = 0;
   }
   if (r.status == 1) {
     Proposal p;
@@ -338,7 +340,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
     // earliest reaction wins; the molecule index makes keys unique within the iteration
     p.key = ((uint64_t)__float_as_uint(tf < 0.f ? 0.f : tf) << 32) | i;
     p.t_abs = r.t_abs;
-    p.cv = meta_cv(meta) ^ r.flip;
+    p.cv = cv_after(meta_cv(meta), r);
     p.x = (double)r.rxn_pos.x;
     p.y = (double)r.rxn_pos.y;
     p.z = (double)r.rxn_pos.z;
@@ -348,7 +350,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   if (r.status == 2) return 2;
   if (max_time < 1.0) {
     // the unimolecular reaction happens where the molecule stopped
-    unimol_products(s, g, species, meta_cv(meta) ^ r.flip, r.pos, tuni, uid, it, draws);
+    unimol_products(s, g, species, cv_after(meta_cv(meta), r), r.pos, tuni, uid, it, draws);
     return 2;
   }
   const bool escaped = !in_partition(g, r.pos);
@@ -372,7 +374,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   out.y = r.pos.y;
   out.z = r.pos.z;
   // schedule flag consumed; counted-volume bits as left by the crossings
-  set_meta(out, make_meta((uint32_t)species, g.rep, (meta_cv(meta) ^ r.flip) << META_CV_SHIFT));
+  set_meta(out, make_meta((uint32_t)species, g.rep, cv_after(meta_cv(meta), r) << META_CV_SHIFT));
   s.b_pos[i] = out;
   if (meta & META_SCHEDULE_UNIMOL) s.a_tuni[i] = (T)tuni;  // keep the drawn time for the scatter
   return 0;
@@ -676,7 +678,7 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
                                             draws, ev, false);
           if (r.err & (ST_COLL_OVERFLOW | ST_SET_OVERFLOW)) count_fallbacks(s, r.err);
           err |= r.err;
-          cv ^= r.flip;
+          cv = cv_after(cv, r);
           if (r.status == 2) {
             dead = true;
           } else {
@@ -918,10 +920,13 @@ __global__ void k_cv_init(State<T> s, uint32_t n_staged) {
     const uint32_t m = meta_of(p.pos);
     const Geo<T>& g = geo_of(s, m);
     if (!g.n_cv) continue;
-    uint32_t cv = 0;
     const V3<double> x = v3<double>((double)p.pos.x, (double)p.pos.y, (double)p.pos.z);
-    for (uint32_t o = 0; o < g.n_cv; o++)
-      if (inside_object(g, x, g.cv_obj[o])) cv |= 1u << o;
+    uint32_t cv = counted_volume_bits(g, x);
+    if (cv == NONE) {
+      // the ray met an edge, where the reference stops: counted outside every object
+      atomicAdd(&s.cnt->warn_inside_redo, 1ull);
+      cv = 0;
+    }
     set_meta(p.pos, (m & ~(0x7Fu << META_CV_SHIFT)) | (cv << META_CV_SHIFT));
     s.prod[k].pos = p.pos;
   }
@@ -997,47 +1002,89 @@ struct ReleaseDesc {
   uint64_t seed, uid0;
 };
 
+// one molecule of ReleaseEvent::release_ellipsoid_or_rectcuboid (release_event.cpp:953-
+// 1000): a point of the unit cube around 0, kept (spheroidal shapes) inside the ball of
+// radius 0.5, on a shell moved onto the sphere, scaled by the diameter and moved to the
+// center; fp64 without fused multiply-adds, so that injected draws give the
+// reference's positions. False when 1024 tries gave no point.
+template <class D>
+__device__ bool release_point(int shape, const double* center, const double* diameter, D& d, V3<double>& out) {
+  const bool spheroidal = shape == REL_SPHERE || shape == REL_SHELL;
+  V3<double> q = v3<double>(0, 0, 0);
+  bool ok = false;
+  for (int attempt = 0; attempt < 1024 && !ok; attempt++) {
+    q.x = __dsub_rn(draw_dbl(d), 0.5);
+    q.y = __dsub_rn(draw_dbl(d), 0.5);
+    q.z = __dsub_rn(draw_dbl(d), 0.5);
+    ok = !spheroidal || rn_dot3(q.x, q.y, q.z, q.x, q.y, q.z) < 0.25;
+  }
+  if (shape == REL_SHELL) {
+    const double r = __dmul_rn(sqrt(rn_dot3(q.x, q.y, q.z, q.x, q.y, q.z)), 2.0);
+    q = r == 0 ? v3<double>(0, 0, 0.5) : v3<double>(q.x / r, q.y / r, q.z / r);
+  }
+  out = v3<double>(__dadd_rn(__dmul_rn(q.x, diameter[0]), center[0]), __dadd_rn(__dmul_rn(q.y, diameter[1]), center[1]),
+                   __dadd_rn(__dmul_rn(q.z, diameter[2]), center[2]));
+  return ok;
+}
+
+// one molecule of ReleaseEvent::release_inside_regions (release_event.cpp:904-952): a
+// point of the object's bounding box, kept if inside the object (the reference's ray
+// test; a ray through an edge, where the reference's test would fail, draws again)
+template <typename T, class D>
+__device__ bool release_inside_point(const Geo<T>& g, uint32_t obj, const double* llf, const double* urb, D& d,
+                                     V3<double>& out, uint32_t& redo) {
+  for (int attempt = 0; attempt < 1024; attempt++) {
+    out.x = __dadd_rn(llf[0], __dmul_rn(__dsub_rn(urb[0], llf[0]), draw_dbl(d)));
+    out.y = __dadd_rn(llf[1], __dmul_rn(__dsub_rn(urb[1], llf[1]), draw_dbl(d)));
+    out.z = __dadd_rn(llf[2], __dmul_rn(__dsub_rn(urb[2], llf[2]), draw_dbl(d)));
+    const uint32_t in = inside_region(g, out, obj, llf);
+    if (in == NONE) {
+      redo++;
+      continue;
+    }
+    if (in) return true;
+  }
+  return false;
+}
+
 template <typename T>
 __global__ void k_release(State<T> s, ReleaseDesc r) {
   const Geo<T>& g = s.geos[r.rep];
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < r.n; i += gridDim.x * blockDim.x) {
     PhiloxDraws d;
     d.ph.init(r.seed, i, 0, 7);
-    auto uni = [&d]() { return ((double)d.u32() + 0.5) * (1.0 / 4294967296.0); };
     V3<double> p = v3<double>(0, 0, 0);
-    bool ok = false;
-    for (int attempt = 0; attempt < 1024 && !ok; attempt++) {
-      if (r.shape == REL_INSIDE) {
-        p = v3<double>(r.llf[0] + (r.urb[0] - r.llf[0]) * uni(), r.llf[1] + (r.urb[1] - r.llf[1]) * uni(),
-                       r.llf[2] + (r.urb[2] - r.llf[2]) * uni());
-        ok = inside_object(g, p, r.object);
-      } else {
-        // unit cube around 0, spheroidal shapes keep only the unit ball (radius 0.5)
-        V3<double> q = v3<double>(uni() - 0.5, uni() - 0.5, uni() - 0.5);
-        const double r2 = dot(q, q);
-        if ((r.shape == REL_SPHERE || r.shape == REL_SHELL) && r2 >= 0.25) continue;
-        if (r.shape == REL_SHELL) {
-          const double rr = sqrt(r2) * 2;
-          q = rr == 0 ? v3<double>(0, 0, 0.5) : scale(q, 1.0 / rr);
-        }
-        p = v3<double>(q.x * r.diameter[0] + r.center[0], q.y * r.diameter[1] + r.center[1],
-                       q.z * r.diameter[2] + r.center[2]);
-        ok = true;
-      }
-    }
+    uint32_t redo = 0;
+    const bool ok = r.shape == REL_INSIDE ? release_inside_point(g, r.object, r.llf, r.urb, d, p, redo)
+                                          : release_point(r.shape, r.center, r.diameter, d, p);
     if (!ok) atomicOr(&s.cnt->status, ST_WATCHDOG);
     Product<T> m;
     m.pos.x = (T)p.x;
     m.pos.y = (T)p.y;
     m.pos.z = (T)p.z;
-    uint32_t cv = 0;
-    for (uint32_t o = 0; o < g.n_cv; o++)
-      if (inside_object(g, p, g.cv_obj[o])) cv |= 1u << o;
+    uint32_t cv = g.n_cv ? counted_volume_bits(g, p) : 0u;
+    if (cv == NONE) {
+      redo++;
+      cv = 0;
+    }
+    if (redo) atomicAdd(&s.cnt->warn_inside_redo, (unsigned long long)redo);
     set_meta(m.pos, make_meta(r.species, r.rep, META_SCHEDULE_UNIMOL | (cv << META_CV_SHIFT)));
     m.birth = 0;
     m.uid = r.uid0 + i;
     m.tuni = TIME_FOREVER;
     s.prod[i] = m;
+  }
+}
+
+// inside tests on given points (parity harness): kind 0 the counted-volume bits, kind 1
+// inside object obj (bounding box low corner llf); NONE where the ray met an edge
+template <typename T>
+__global__ void k_inside_tests(State<T> s, uint32_t rep, uint32_t n, const double* pos, int kind, uint32_t obj,
+                               const double* llf, uint32_t* out) {
+  const Geo<T>& g = s.geos[rep];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const V3<double> p = v3<double>(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    out[i] = kind == 0 ? counted_volume_bits(g, p) : inside_region(g, p, obj, llf);
   }
 }
 

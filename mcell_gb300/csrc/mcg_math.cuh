@@ -53,6 +53,23 @@ template <typename T>
 __host__ __device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {
   return v3<T>(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
 }
+// Round-to-nearest products and sums that the compiler may not fuse into a
+// multiply-add. The fp32 translation unit allows fused multiply-adds; the partner
+// geometry (walk crossings, neighbour tests, octant bounds, the closest-approach test)
+// is written with these, so that every code path that builds a segment's candidates —
+// the fast mask, the list, the refilled pages of the exact fallbacks — rounds alike.
+// (In the fp64 unit, built without fused multiply-adds, they are the plain operations.)
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+template <typename T>
+__device__ __forceinline__ T dot_rn(V3<T> a, V3<T> b) {
+  return add_rn(add_rn(mul_rn(a.x, b.x), mul_rn(a.y, b.y)), mul_rn(a.z, b.z));
+}
+
 template <typename T>
 __host__ __device__ __forceinline__ T tmax(T a, T b) {
   return a > b ? a : b;

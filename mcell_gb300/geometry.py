@@ -79,6 +79,17 @@ def create_icosphere(radius: float, levels: int, center=(0.0, 0.0, 0.0)) -> Tupl
     return verts.astype(np.float64), faces.astype(np.uint32)
 
 
+def create_star_sphere(radius: float, levels: int, bump: float = 0.35, center=(0.0, 0.0, 0.0)):
+    """A closed, non-convex mesh: an icosphere whose vertices sit at radius
+    r(theta, phi) = radius * (1 + bump * sin(3 phi) * sin(2 theta)) (deep lobes and
+    dents; outward-facing normals as the icosphere's)."""
+    v, w = create_icosphere(1.0, levels)
+    th = np.arccos(np.clip(v[:, 2], -1.0, 1.0))
+    ph = np.arctan2(v[:, 1], v[:, 0])
+    r = radius * (1.0 + bump * np.sin(3.0 * ph) * np.sin(2.0 * th))
+    return (v * r[:, None] + np.asarray(center, dtype=np.float64)).astype(np.float64), w
+
+
 def create_bumpy_tube(radius: float = 0.2, length: float = 10.0, bump: float = 0.05,
                       n_theta: int = 200, n_z: int = 500, axial_waves: float = 20.0,
                       angular_waves: int = 4) -> Tuple[np.ndarray, np.ndarray]:

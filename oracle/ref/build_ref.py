@@ -52,6 +52,15 @@ FUNCS = [
     ("src4/collision_utils.inl", "is_immediate_collision", "MCell::CollisionUtils"),
     ("src4/collision_utils.inl", "get_closest_wall_collision", "MCell::CollisionUtils"),
     ("src4/collision_utils.inl", "reflect_from_wall", "MCell::CollisionUtils"),
+    ("src4/collision_utils.inl", "raycast_with_endpoints", "MCell::CollisionUtils"),
+    ("src4/collision_utils.inl", "compute_inputs_for_raycast_with_endpoints", "MCell::CollisionUtils"),
+    ("src4/collision_utils.inl", "get_crossed_subparts_for_walls", "MCell::CollisionUtils"),
+    ("src4/collision_utils.inl", "get_num_crossed_region_walls", "MCell::CollisionUtils"),
+    ("src4/collision_utils.inl", "get_num_crossed_walls_per_object", "MCell::CollisionUtils"),
+    ("src4/collision_utils.inl", "is_point_inside_region_no_waypoints", "MCell::CollisionUtils"),
+    ("src4/collision_utils.inl", "compute_counted_volume_for_pos", "MCell::CollisionUtils"),
+    ("src4/wall.cpp", "Region::compute_bounding_box", "MCell"),
+    ("src4/release_event.cpp", "ReleaseEvent::release_ellipsoid_or_rectcuboid", "MCell"),
     ("src4/rxn_utils.inl", "binary_search_double", "MCell::RxnUtils"),
     ("src4/rxn_utils.inl", "test_bimolecular", "MCell::RxnUtils"),
     ("src4/rxn_utils.inl", "test_intersect", "MCell::RxnUtils"),

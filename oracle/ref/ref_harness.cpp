@@ -37,6 +37,7 @@ struct Scene {
   Partition p;
   std::vector<BNG::RxnClass> rxn_store;
   std::vector<int> can_vol_react;
+  std::map<unsigned, Region> regions;  // closed regions, one per geometry object
 };
 
 void put_event(double* out, int kind, int index, int side, double t_rel, double t_abs, const Vec3& pos) {
@@ -319,6 +320,99 @@ void ref_diffuse_case(
   out[7] = elapsed_molecule_time;
   out[8] = t_steps;
   p.molecules[mol] = saved;
+}
+
+// geometry objects: the object of each wall and which objects are counted volumes
+void ref_scene_set_objects(void* sp, unsigned nobj, const unsigned* object_of_wall, const unsigned char* counted) {
+  Scene* s = (Scene*)sp;
+  Partition& p = s->p;
+  p.geometry_objects.assign(nobj, GeometryObject());
+  for (unsigned k = 0; k < nobj; k++) {
+    p.geometry_objects[k].index = k;
+    p.geometry_objects[k].id = k;
+    p.geometry_objects[k].counted = counted[k] != 0;
+  }
+  for (size_t w = 0; w < p.walls.size(); w++) {
+    p.walls[w].object_index = object_of_wall[w];
+    p.walls[w].object_id = object_of_wall[w];
+  }
+  s->regions.clear();
+}
+
+// compute_counted_volume_for_pos (collision_utils.inl:1515-1545): bit k set when pos is
+// inside counted object k; bit 31 when the ray met a wall edge (the reference's
+// release_assert on must_redo_test), tested with the same ray through
+// get_num_crossed_walls_per_object
+unsigned ref_counted_volume_for_pos(void* sp, const double* pos) {
+  Partition& p = ((Scene*)sp)->p;
+  const Vec3 v((pos_t)pos[0], (pos_t)pos[1], (pos_t)pos[2]);
+  const counted_volume_index_t i = CollisionUtils::compute_counted_volume_for_pos(p, v);
+  unsigned mask = 0;
+  for (geometry_object_index_t o: p.counted_volumes[i].contained_in_objects) {
+    mask |= 1u << o;
+  }
+  Vec3 dst = p.get_origin_corner();
+  dst.x += p.config.subpart_edge_length / (pos_t)11;
+  dst.y += p.config.subpart_edge_length / (pos_t)21;
+  std::map<geometry_object_index_t, uint> crossed;
+  bool redo = false;
+  CollisionUtils::get_num_crossed_walls_per_object(p, v, dst, true, crossed, redo);
+  return redo ? (mask | (1u << 31)) : mask;
+}
+
+// is_point_inside_region_no_waypoints (collision_utils.inl:1484-1510) for the closed
+// region made of object obj's walls: 0 outside, 1 inside, 2 the ray met a wall edge
+int ref_inside_region(void* sp, unsigned obj, const double* pos) {
+  Scene* s = (Scene*)sp;
+  Partition& p = s->p;
+  auto it = s->regions.find(obj);
+  if (it == s->regions.end()) {
+    Region reg;
+    for (size_t w = 0; w < p.walls.size(); w++) {
+      if (p.walls[w].object_index == obj) {
+        reg.walls_and_edges[(wall_index_t)w];
+      }
+    }
+    // walls per subpartition of the region (Region::initialize_wall_subpart_mapping_if_needed)
+    for (size_t sub = 0; sub < p.walls_per_subpart.size(); sub++) {
+      for (wall_index_t w: p.walls_per_subpart[sub]) {
+        if (p.walls[w].object_index == obj) {
+          reg.walls_per_subpart[(subpart_index_t)sub].push_back(w);
+        }
+      }
+    }
+    reg.compute_bounding_box(p, reg.bounding_box_llf, reg.bounding_box_urb);
+    it = s->regions.emplace(obj, reg).first;
+  }
+  const Vec3 v((pos_t)pos[0], (pos_t)pos[1], (pos_t)pos[2]);
+  bool redo = false;
+  const bool in = CollisionUtils::is_point_inside_region_no_waypoints(p, v, it->second, redo);
+  return redo ? 2 : (in ? 1 : 0);
+}
+
+// ReleaseEvent::release_ellipsoid_or_rectcuboid (release_event.cpp:953-1000) with the
+// random stream injected: shape 0 sphere (ellipsoid), 1 cuboid, 2 spherical shell; the
+// positions of the n molecules in release order; returns the draws used
+unsigned ref_release_ellipsoid_or_rectcuboid(int shape, unsigned n, const double* location, const double* diameter,
+                                              const unsigned* draws, unsigned ndraws, double* out) {
+  WorldShim world;
+  world.species.species.resize(1);
+  world.rng.draws = draws;
+  world.rng.n = ndraws;
+  ReleaseEvent ev;
+  ev.world = &world;
+  ev.release_shape = shape == 0 ? ReleaseShape::SPHERICAL
+                                : (shape == 2 ? ReleaseShape::SPHERICAL_SHELL : ReleaseShape::REGION);
+  ev.location = Vec3((pos_t)location[0], (pos_t)location[1], (pos_t)location[2]);
+  ev.diameter = Vec3((pos_t)diameter[0], (pos_t)diameter[1], (pos_t)diameter[2]);
+  ev.release_ellipsoid_or_rectcuboid((int)n);
+  const std::vector<Molecule>& m = world.partition.molecules;
+  for (size_t i = 0; i < m.size() && i < n; i++) {
+    out[3 * i] = m[i].v.pos.x;
+    out[3 * i + 1] = m[i].v.pos.y;
+    out[3 * i + 2] = m[i].v.pos.z;
+  }
+  return world.rng.overrun ? 0xFFFFFFFFu : (unsigned)world.rng.used;
 }
 
 // reaction tests on injected uniforms

@@ -12,6 +12,7 @@
  *   Wall / rejection   src4/wall.h:200-350
  *   Collision          src4/collision_structs.h:29-140
  *   SimulationConfig   src4/simulation_config.h:28-135
+ *   CountedVolume, GeometryObject, Region   src4/geometry.h:39-320
  * The bodies are this project's own. Test infrastructure only: this header is
  * compiled into oracle/_ref and is never part of the product.
  */
@@ -19,6 +20,7 @@
 #define ORACLE_REF_SHIM_H
 
 #include <map>
+#include <set>
 #include <vector>
 #include <cstring>
 #include <cstdint>
@@ -88,17 +90,28 @@ public:
 
 namespace MCell {
 
+using std::map;  // the reference's headers bring std names into MCell
+
 const uint MOLECULE_FLAG_DEFUNCT = 1u << 31;
+const uint MOLECULE_FLAG_VOL = 1u << 1;
+const uint MOLECULE_FLAG_SCHEDULE_UNIMOL_RXN = 1u << 8;
 
 class Molecule {
 public:
+  Molecule() = default;
+  Molecule(const molecule_id_t id_, const species_id_t species_id_, const Vec3& pos_, const double time_)
+    : id(id_), species_id(species_id_), birthday(time_) {
+    v.pos = pos_;
+  }
   molecule_id_t id = MOLECULE_ID_INVALID;
   species_id_t species_id = BNG::SPECIES_ID_INVALID;
   uint flags = 0;
+  double birthday = 0;
   struct {
     Vec3 pos;
     subpart_index_t subpart_index = SUBPART_INDEX_INVALID;
   } v;
+  void set_flag(const uint f) { flags |= f; }
   bool is_defunct() const { return (flags & MOLECULE_FLAG_DEFUNCT) != 0; }
   bool is_vol() const { return true; }
   bool is_surf() const { return false; }
@@ -123,6 +136,8 @@ public:
   Vec2 uv_vert2;
   Vec3 unit_u, unit_v;
   uint surf_class_of_species_mask = 0; // unused by the routines
+  geometry_object_index_t object_index = 0;
+  geometry_object_id_t object_id = 0;
   bool exists_in_partition() const { return id != WALL_ID_NOT_IN_PARTITION; }
   bool is_overlapped_wall() const { return false; }
   void initialize_wall_constants(const Partition& p);
@@ -184,6 +199,36 @@ public:
   void init_subpartition_edge_length();
 };
 
+// the set of geometry objects a position is inside (src4/geometry.h:39)
+class CountedVolume {
+public:
+  counted_volume_index_t index = COUNTED_VOLUME_INDEX_INVALID;
+  uint_set<geometry_object_index_t> contained_in_objects;
+};
+
+class GeometryObject {
+public:
+  geometry_object_index_t index = 0;
+  geometry_object_id_t id = 0;
+  bool counted = false;  // a counted volume (is_counted_volume_or_compartment)
+  bool is_counted_volume_or_compartment() const { return counted; }
+};
+
+template<typename T> using small_vector = boost::container::small_vector<T, BASE_CONTAINER_ALLOC>;
+typedef std::map<subpart_index_t, small_vector<wall_index_t>> WallsPerSubpartMap;
+
+// a closed region made of the walls of one geometry object (src4/geometry.h:186-320)
+class Region {
+public:
+  std::map<wall_index_t, std::set<edge_index_t>> walls_and_edges;
+  WallsPerSubpartMap walls_per_subpart;
+  Vec3 bounding_box_llf, bounding_box_urb;
+  void initialize_volume_info_if_needed(const Partition&) { }
+  const Vec3& get_bounding_box_llf() const { return bounding_box_llf; }
+  const WallsPerSubpartMap& get_walls_per_subpart() const { return walls_per_subpart; }
+  void compute_bounding_box(const Partition& p, Vec3& llf, Vec3& urb);
+};
+
 class SimulationStats {
 public:
   void inc_ray_voxel_tests() const { }
@@ -227,6 +272,26 @@ public:
   SpeciesContainerShim all_species;
   // surface class kind per (wall, species): 0 reflect, 1 transparent, 2 absorptive
   std::map<std::pair<wall_index_t, species_id_t>, int> wall_class;
+  std::vector<GeometryObject> geometry_objects;
+  std::vector<CountedVolume> counted_volumes;
+  mutable ShimRng aux_rng;  // no draws: the routines that use it return on a re-try
+
+  const GeometryObject& get_geometry_object(const geometry_object_index_t i) const { return geometry_objects[i]; }
+  Molecule& add_volume_molecule(const Molecule& vm, const double) {
+    molecules.push_back(vm);
+    molecules.back().id = (molecule_id_t)(molecules.size() - 1);
+    return molecules.back();
+  }
+  counted_volume_index_t find_or_add_counted_volume(const CountedVolume& cv) {
+    for (size_t k = 0; k < counted_volumes.size(); k++) {
+      if (counted_volumes[k].contained_in_objects == cv.contained_in_objects) {
+        return (counted_volume_index_t)k;
+      }
+    }
+    counted_volumes.push_back(cv);
+    counted_volumes.back().index = (counted_volume_index_t)(counted_volumes.size() - 1);
+    return counted_volumes.back().index;
+  }
 
   const Vec3& get_origin_corner() const { return origin_corner; }
   bool in_this_partition(const Vec3& pos) const {
@@ -288,6 +353,32 @@ public:
   const RxnContainerShim& get_all_rxns() const { return rxns; }
   const SpeciesContainerShim& get_all_species() const { return all_species; }
   const BNG::Species& get_species(const species_id_t id) const { return all_species.get(id); }
+};
+
+// the parts of the World and of ReleaseEvent (src4/release_event.h:35-260) that
+// ReleaseEvent::release_ellipsoid_or_rectcuboid uses
+enum class ReleaseShape { UNDEFINED = -1, SPHERICAL, SPHERICAL_SHELL, REGION, LIST, INITIAL_SURF_REGION };
+
+
+class WorldShim {
+public:
+  Partition partition;
+  SpeciesContainerShim species;
+  ShimRng rng;
+  Partition& get_partition(const int) { return partition; }
+  const SpeciesContainerShim& get_all_species() const { return species; }
+};
+
+class ReleaseEvent {
+public:
+  WorldShim* world = nullptr;
+  ReleaseShape release_shape = ReleaseShape::SPHERICAL;
+  Vec3 location, diameter;
+  species_id_t species_id = 0;
+  double event_time = 0;
+  double get_release_delay_time() const { return 0; }
+  void schedule_for_immediate_diffusion_if_needed(const molecule_id_t) { }
+  void release_ellipsoid_or_rectcuboid(int computed_release_number);
 };
 
 } // namespace MCell

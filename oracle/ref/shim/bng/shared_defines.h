@@ -32,6 +32,7 @@
 #endif
 
 typedef unsigned int uint;
+const uint UINT_INVALID = 0xFFFFFFFFu;  // libbng's invalid value of an unsigned count
 
 const uint ID_INVALID = UINT_MAX;
 const uint INDEX_INVALID = UINT_MAX;
@@ -147,6 +148,7 @@ public:
   void clear() { s.clear(); }
   const_iterator begin() const { return s.begin(); }
   const_iterator end() const { return s.end(); }
+  bool operator==(const uint_set& o) const { return s == o.s; }
 private:
   std::set<T> s;
 };

@@ -153,6 +153,61 @@ def pathway_fixtures(ref64):
           np.unique(uni, return_counts=True))
 
 
+def inside_fixtures(ref64):
+    """Inside decisions on a closed non-convex object (the star-shaped sphere of
+    H.star_scene, object 0, in a cube, object 1; both counted volumes):
+    compute_counted_volume_for_pos (the counted-volume membership of a position) and
+    is_point_inside_region_no_waypoints (the inside test of a release into a region),
+    on points uniform in the cube and points within 1e-4-0.5 internal units of the
+    object's faces, edges and vertices; and ReleaseEvent::release_ellipsoid_or_
+    rectcuboid on injected random streams (sphere, cuboid, spherical shell)."""
+    rng = np.random.default_rng(20261205)
+    sc = H.star_scene(rng)
+    h = ref64.scene(sc)
+    h.set_objects(sc.obj, [1, 1])
+    half = 60.0
+    pts = [rng.uniform(-half, half, size=(3000, 3))]
+    # near the star's surface: points of its triangles (vertices, edges, interiors) moved
+    # along the face normal by a small signed offset
+    sw = np.nonzero(sc.obj == 0)[0]
+    tri = sc.tris[rng.choice(sw, 2000)]
+    a, b, c = sc.verts[tri[:, 0]], sc.verts[tri[:, 1]], sc.verts[tri[:, 2]]
+    u = rng.uniform(0, 1, (2000, 1))
+    wv = rng.uniform(0, 1, (2000, 1))
+    kind = rng.integers(0, 3, 2000)
+    bary = np.where(kind[:, None] == 0, a, np.where(kind[:, None] == 1, a + (b - a) * u,
+                                                     a + (b - a) * u * (1 - wv) + (c - a) * wv * (1 - u)))
+    nrm = np.cross(b - a, c - a)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    off = np.exp(rng.uniform(np.log(1e-4), np.log(0.5), (2000, 1))) * rng.choice([-1.0, 1.0], (2000, 1))
+    pts.append(bary + nrm * off)
+    pts = np.concatenate(pts)
+    cv = np.array([h.counted_volume_for_pos(p) for p in pts], np.uint32)
+    reg = np.array([[h.inside_region(o, p) for o in (0, 1)] for p in pts], np.int32)
+    # releases on injected streams
+    n_rel = 60
+    shapes = rng.integers(0, 3, n_rel).astype(np.int32)
+    counts = rng.integers(1, 40, n_rel).astype(np.uint32)
+    loc = rng.uniform(-30, 30, (n_rel, 3))
+    dia = rng.uniform(1, 40, (n_rel, 3))
+    nd = 512
+    draws = rng.integers(0, 2 ** 32, size=(n_rel, nd), dtype=np.uint64).astype(np.uint32)
+    rel_pos = np.zeros((n_rel, 40, 3))
+    used = np.zeros(n_rel, np.int64)
+    for k in range(n_rel):
+        pos, u_ = ref64.release_ellipsoid_or_rectcuboid(int(shapes[k]), int(counts[k]), loc[k], dia[k], draws[k])
+        assert u_ is not None
+        rel_pos[k, :counts[k]] = pos
+        used[k] = u_
+    np.savez_compressed(
+        HERE / "inside_star.npz",
+        origin=sc.origin, partition_edge=sc.partition_edge, nsub=sc.nsub, rxn_radius=sc.rxn_radius, verts=sc.verts,
+        tris=sc.tris, obj=sc.obj, points=pts, counted=cv, inside_region=reg, rel_shape=shapes, rel_n=counts,
+        rel_loc=loc, rel_dia=dia, rel_draws=draws, rel_pos=rel_pos, rel_used=used)
+    print("inside: points", len(pts), "in star", int(((cv & 1) > 0).sum()), "in cube", int(((cv & 2) > 0).sum()),
+          "edge re-tries", int(((cv >> 31) & 1).sum()), "region tests", np.unique(reg, return_counts=True))
+
+
 def main():
     ref64 = H.reference(64)
     if ref64 is None:
@@ -184,6 +239,7 @@ def main():
     np.savez_compressed(HERE / "rxn_tests.npz", P=P, S=S, U=U, bimol=tb, K=K, Uu=Uu, unimol=tu, ref_gauss=g)
     print("rxn tests", (tb >= 0).sum(), "fired of", len(tb))
     pathway_fixtures(ref64)
+    inside_fixtures(ref64)
 
 
 if __name__ == "__main__":

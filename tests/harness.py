@@ -93,6 +93,18 @@ class Checker:
     def time_of_unimol(self, k, draw):
         return self.fn("time_of_unimol")(_d(k), _u(draw))
 
+    def release_ellipsoid_or_rectcuboid(self, shape, n, location, diameter, draws):
+        """Positions [n, 3] of a release (shape 0 sphere, 1 cuboid, 2 shell) drawing from
+        `draws`, and the draws used (None if they ran out)."""
+        out = np.zeros((n, 3))
+        loc = np.ascontiguousarray(location, np.float64)
+        dia = np.ascontiguousarray(diameter, np.float64)
+        dr = np.ascontiguousarray(draws, np.uint32)
+        f = self.fn("release_ellipsoid_or_rectcuboid")
+        f.restype = _u
+        used = f(ctypes.c_int(shape), _u(n), ptr(loc), ptr(dia), ptr(dr), _u(len(dr)), ptr(out))
+        return out, (None if used == 0xFFFFFFFF else int(used))
+
     def test_bimolecular_pw(self, cum, scaling, draw):
         """test_bimolecular over a class of len(cum) pathways: pathway index, < 0 = none."""
         c = np.ascontiguousarray(cum, np.float64)
@@ -132,6 +144,26 @@ class _Handle:
     def subpart_index(self, pos):
         p = np.ascontiguousarray(pos, np.float64)
         return self.c.fn("subpart_index")(self.h, ptr(p))
+
+    def set_objects(self, object_of_wall, counted):
+        """Geometry objects: the object index of each wall; counted[k] marks counted volumes."""
+        ow = np.ascontiguousarray(object_of_wall, np.uint32)
+        cn = np.ascontiguousarray(counted, np.uint8)
+        self.c.fn("scene_set_objects")(self.h, _u(len(cn)), ptr(ow), ptr(cn))
+
+    def counted_volume_for_pos(self, pos):
+        """Bit mask of the counted objects containing pos; bit 31: the ray met an edge."""
+        p = np.ascontiguousarray(pos, np.float64)
+        f = self.c.fn("counted_volume_for_pos")
+        f.restype = _u
+        return f(self.h, ptr(p))
+
+    def inside_region(self, obj, pos):
+        """0 outside / 1 inside the closed region of object obj; 2: the ray met an edge."""
+        p = np.ascontiguousarray(pos, np.float64)
+        f = self.c.fn("inside_region")
+        f.restype = ctypes.c_int
+        return f(self.h, _u(obj), ptr(p))
 
     def diffuse_case(self, mol, disp, draws, r_rate_factor=1.0, t_steps=1.0):
         out = np.zeros(RES_SIZE)
@@ -254,6 +286,25 @@ def edge_cases(sc: Scene):
 
 GOLDEN = ROOT / "tests" / "golden"
 GOLDEN_SCENES = ["cube", "cube_dense", "cube_classes", "sphere", "pathways"]
+
+
+def star_scene(rng, n_mol=200, levels=3):
+    """A closed non-convex object (geometry.create_star_sphere, radius 0.45 um, object 0,
+    transparent to A) in a reflective 1.2 um cube (object 1); objects per wall in .obj."""
+    lu = conversion.length_unit_um()
+    sv, sw = geometry.create_star_sphere(0.45, levels)
+    bv, bw = geometry.create_box(edge_dimension=1.2)
+    v, w, obj = geometry.merge_meshes((sv, sw), (bv, bw))
+    lay = conversion.partition_layout(v.min(0), v.max(0), partition_dimension_um=1.3, subpartition_dimension_um=0.1)
+    wc = np.zeros((len(w), 3), np.uint8)
+    wc[obj == 0, 0] = 1
+    half = 0.6 / lu
+    pos = rng.uniform(-half, half, size=(n_mol, 3))
+    sp = rng.integers(0, 2, size=n_mol).astype(np.uint32)
+    sc = Scene(np.array(lay.origin), lay.edge, lay.nsub, conversion.default_rxn_radius_um() / lu, v / lu, w,
+               np.array([2.0, 2.0, 1.414213562373095]), wc, np.array([[0, 1]], np.uint32), np.array([0.0]), pos, sp)
+    sc.obj = np.asarray(obj, np.uint32)
+    return sc
 
 
 def load_golden(name):

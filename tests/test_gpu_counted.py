@@ -1,4 +1,4 @@
-"""Counted volumes: molecules inside a closed object, kept per molecule and flipped
+"""Counted volumes: molecules inside a closed object, kept per molecule and set
 at crossings, must equal a recount of the downloaded positions (the icosphere is
 convex: inside = behind every face plane) — exactly in fp64."""
 import numpy as np
