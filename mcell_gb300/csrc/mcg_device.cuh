@@ -159,6 +159,11 @@ struct Geo {
   const uint32_t* wsp_off;    // CSR: walls per subpartition (ascending wall index)
   const uint32_t* wsp_list;   // wall indices
   const uint64_t* wsp_cells;  // per entry: cells of the subpartition's 4x4x4 grid the wall reaches
+  // per subpartition listing 1-64 walls: the block (of 64) of wsp_cellent holding, per
+  // cell of its 4x4x4 grid, the bit mask of its entries that reach the cell; NONE
+  // for other subpartitions
+  const uint32_t* wsp_cm;
+  const uint64_t* wsp_cellent;
   const uint8_t* wall_class;  // [wall * nsp + species]: 0 reflect, 1 transparent, 2 absorptive
   const Chem* chem;
   // fp32 engines: the wall constants in fp64 for the tie-breaks, 16 per wall (normal
@@ -881,6 +886,51 @@ __device__ bool keep_side(const P4<T>& rj, double side, V3<T>& pos, bool near_on
   return true;
 }
 
+// The entries of subpartition sp whose wall reaches a cell of `om`, in ascending order
+// (the order the reference tests its wall list in). For a subpartition of at most 64
+// walls the candidates come from the per-cell entry masks (one load per touched cell);
+// otherwise every entry's cell mask is tested.
+template <typename T>
+struct WallEntries {
+  uint32_t b, e, k;
+  uint64_t cand, om;
+  bool masked;
+  __device__ __forceinline__ void start(const Geo<T>& g, uint32_t sp, uint64_t cells) {
+    b = g.wsp_off[sp];
+    e = g.wsp_off[sp + 1];
+    om = cells;
+    const uint32_t cm = g.wsp_cm[sp];
+    masked = cm != NONE;
+    k = b;
+    cand = 0;
+    if (masked) {
+      if (cells == ~0ull) {
+        cand = (e - b) >= 64 ? ~0ull : ((1ull << (e - b)) - 1);
+      } else {
+        const uint64_t* ce = g.wsp_cellent + (size_t)cm * 64;
+        for (uint64_t m = cells; m; m &= m - 1) cand |= __ldg(ce + (__ffsll((long long)m) - 1));
+      }
+    }
+  }
+  // the next entry index, false when there is none
+  __device__ __forceinline__ bool next(const Geo<T>& g, uint32_t& entry) {
+    if (masked) {
+      if (!cand) return false;
+      entry = b + (uint32_t)(__ffsll((long long)cand) - 1);
+      cand &= cand - 1;
+      return true;
+    }
+    while (k < e) {
+      const uint32_t q = k++;
+      if (g.wsp_cells[q] & om) {
+        entry = q;
+        return true;
+      }
+    }
+    return false;
+  }
+};
+
 // fp32: moves `pos` off any wall plane of subpartition sp that it lies on (within
 // keep_side's margin) to the side `ref` is on; `skip` is left alone. The point
 // reached a rounded position on a segment from `ref` that crossed none of these
@@ -891,8 +941,10 @@ __device__ MCG_GUARD_INLINE void guard_sides(const Geo<T>& g, uint32_t sp, V3<T>
   V3<T> glo, ghi;
   seg_box(pos, v3<T>(0, 0, 0), (T)2e-2, glo, ghi);
   const uint64_t gm = cells_touched(g, sp, glo, ghi);
-  for (uint32_t k = g.wsp_off[sp]; k < g.wsp_off[sp + 1]; k++) {
-    if (!(g.wsp_cells[k] & gm)) continue;
+  WallEntries<T> it;
+  it.start(g, sp, gm);
+  uint32_t k;
+  while (it.next(g, k)) {
     const uint32_t wi = g.wsp_list[k];
     if (wi == skip) continue;
     const P4<T> rj = g.wrej[wi];
@@ -942,9 +994,10 @@ restart:
   seg_box(pos, disp, g.sp_edge * (T)1e-3, lo, hi);
   const uint64_t om =
       (disp.x == 0 || disp.y == 0 || disp.z == 0) ? ~0ull : cells_touched(g, sp, lo, hi);
-  const uint32_t b = g.wsp_off[sp], e = g.wsp_off[sp + 1];
-  for (uint32_t k = b; k < e; k++) {
-    if (!(g.wsp_cells[k] & om)) continue;
+  WallEntries<T> it;
+  it.start(g, sp, om);
+  uint32_t k;
+  while (it.next(g, k)) {
     const uint32_t wi = g.wsp_list[k];
     if (wi == last_hit) continue;
     T t;
@@ -1667,8 +1720,10 @@ __device__ __noinline__ T exact_disk(const Geo<T>& g, V3<T> loc, V3<T> mv, int m
   V3<T> blo, bhi;
   seg_box(loc, v3<T>(0, 0, 0), R * (T)1.01 + g.sp_edge * (T)1e-3, blo, bhi);
   const uint64_t om = cells_touched(g, sp, blo, bhi);
-  for (uint32_t k = g.wsp_off[sp]; k < g.wsp_off[sp + 1]; k++) {
-    if (!(g.wsp_cells[k] & om)) continue;
+  WallEntries<T> it;
+  it.start(g, sp, om);
+  uint32_t k;
+  while (it.next(g, k)) {
     const uint32_t wi = g.wsp_list[k];
     const P4<T> rj = g.wrej[wi];
     V3<T> wn = v3<T>(rj.x, rj.y, rj.z);

@@ -808,6 +808,8 @@ class DeviceEngineT : public DeviceEngine {
     uint32_t* wsp_off = nullptr;
     uint32_t* wsp_list = nullptr;
     uint64_t* wsp_cells = nullptr;
+    uint32_t* wsp_cm = nullptr;
+    uint64_t* wsp_cellent = nullptr;
     uint8_t* wclass = nullptr;
     Chem* chem = nullptr;
     double* w64 = nullptr;  // fp32 engines: fp64 wall constants for the tie-breaks
@@ -952,6 +954,22 @@ class DeviceEngineT : public DeviceEngine {
       ent[k] = hs.wsp_list[k];
       cells[k] = hs.wsp_cells[k];
     }
+    // per-cell entry masks of the subpartitions that list 1-64 walls: the wall search
+    // then loads one mask per cell its segment touches instead of testing every entry
+    const uint32_t n3h = hs.nsub * hs.nsub * hs.nsub;
+    std::vector<uint32_t> cm(n3h, NONE);
+    std::vector<uint64_t> cellent;
+    for (uint32_t sp = 0; sp < n3h; sp++) {
+      const uint32_t b = hs.wsp_off[sp], e = hs.wsp_off[sp + 1];
+      if (e == b || e - b > 64) continue;
+      cm[sp] = (uint32_t)(cellent.size() / 64);
+      cellent.resize(cellent.size() + 64, 0);
+      uint64_t* blk = &cellent[cellent.size() - 64];
+      for (uint32_t k = b; k < e; k++)
+        for (int c = 0; c < 64; c++)
+          if ((hs.wsp_cells[k] >> c) & 1ull) blk[c] |= 1ull << (k - b);
+    }
+    if (cellent.empty()) cellent.assign(64, 0);
     Chem c;
     std::memset(&c, 0, sizeof(c));
     static_assert(MAXPW == MAX_PATHWAYS, "pathway tables of host and device differ");
@@ -982,7 +1000,8 @@ class DeviceEngineT : public DeviceEngine {
     R.used = true;  // from here on free_replica() releases what was allocated
     if (alloc_copy(&R.wrej, rej, R.bytes, err) || alloc_copy(&R.wface, face, R.bytes, err) ||
         alloc_copy(&R.wsp_off, hs.wsp_off, R.bytes, err) || alloc_copy(&R.wsp_list, ent, R.bytes, err) ||
-        alloc_copy(&R.wsp_cells, cells, R.bytes, err) ||
+        alloc_copy(&R.wsp_cells, cells, R.bytes, err) || alloc_copy(&R.wsp_cm, cm, R.bytes, err) ||
+        alloc_copy(&R.wsp_cellent, cellent, R.bytes, err) ||
         alloc_copy(&R.wclass, wall_class.empty() ? std::vector<uint8_t>(1, 0) : wall_class, R.bytes, err) ||
         alloc_copy(&R.chem, std::vector<Chem>(1, c), R.bytes, err))
       return -2;
@@ -991,6 +1010,8 @@ class DeviceEngineT : public DeviceEngine {
     g.wsp_off = R.wsp_off;
     g.wsp_list = R.wsp_list;
     g.wsp_cells = R.wsp_cells;
+    g.wsp_cm = R.wsp_cm;
+    g.wsp_cellent = R.wsp_cellent;
     g.wall_class = R.wclass;
     g.chem = R.chem;
     g.w64 = nullptr;
@@ -1062,6 +1083,8 @@ class DeviceEngineT : public DeviceEngine {
     cudaFree(R.wsp_off);
     cudaFree(R.wsp_list);
     cudaFree(R.wsp_cells);
+    cudaFree(R.wsp_cm);
+    cudaFree(R.wsp_cellent);
     cudaFree(R.wclass);
     cudaFree(R.chem);
     cudaFree(R.w64);

@@ -139,7 +139,8 @@ __device__ __forceinline__ void warp_count(uint32_t* counts, uint32_t key, bool 
 // Box-Muller pairs from 4 draws -> 3 standard normals
 template <typename T>
 __device__ __forceinline__ V3<T> gauss3(PhiloxDraws& d) {
-  uint32_t a = d.u32(), b = d.u32(), c = d.u32(), e = d.u32();
+  const uint4 w = d.ph.next4();
+  const uint32_t a = w.x, b = w.y, c = w.z, e = w.w;
   if (sizeof(T) == 8) {
     double u1 = ((double)a + 0.5) * (1.0 / 4294967296.0), u2 = (double)b * (1.0 / 4294967296.0);
     double u3 = ((double)c + 0.5) * (1.0 / 4294967296.0), u4 = (double)e * (1.0 / 4294967296.0);

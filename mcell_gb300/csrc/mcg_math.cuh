@@ -84,12 +84,40 @@ __host__ __device__ __forceinline__ T tabs(T a) {
 // as 1, 2, 3", SC 2011): a counter-based generator, so every molecule-step owns
 // an independent stream addressed by (molecule id, iteration, phase, block) and
 // any draw can be replayed without storing generator state.
+// One block of the generator: four 32-bit words for key (k0, k1) and counter
+// (c0, c1, c2, c3).
+__device__ __forceinline__ uint4 philox_block(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t c2,
+                                              uint32_t c3) {
+  uint32_t x0 = c0, x1 = c1, x2 = c2, x3 = c3;
+  uint32_t a = k0, b = k1;
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    uint32_t hi0 = __umulhi(0xD2511F53u, x0), lo0 = 0xD2511F53u * x0;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, x2), lo1 = 0xCD9E8D57u * x2;
+    uint32_t y0 = hi1 ^ x1 ^ a, y1 = lo1, y2 = hi0 ^ x3 ^ b, y3 = lo0;
+    x0 = y0;
+    x1 = y1;
+    x2 = y2;
+    x3 = y3;
+    a += 0x9E3779B9u;
+    b += 0xBB67AE85u;
+  }
+  return make_uint4(x0, x1, x2, x3);
+}
+// the same out of line, for the rare draws after the first block
+__device__ __noinline__ static uint4 philox_block_rare(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1,
+                                                       uint32_t c2, uint32_t c3) {
+  return philox_block(k0, k1, c0, c1, c2, c3);
+}
+
+// The stream of one molecule-step: key = seed, counter = (id low, id high, iteration,
+// phase << 24 | block). It holds no buffer, only the index of the next draw: a draw
+// computes its block (the first four, the displacement's, are taken together by
+// first4), so the state is six registers and the stream is the same as a buffered one.
 struct Philox {
   uint32_t k0, k1;      // key = seed
   uint32_t c0, c1, c2;  // counter words: id low, id high, iteration
-  uint32_t c3;          // phase << 24 | block
-  uint32_t buf[4];
-  int left;
+  uint32_t n;           // phase << 24 | index of the next draw
 
   __device__ __forceinline__ void init(uint64_t seed, uint64_t id, uint32_t iteration, uint32_t phase) {
     k0 = (uint32_t)seed;
@@ -97,34 +125,27 @@ struct Philox {
     c0 = (uint32_t)id;
     c1 = (uint32_t)(id >> 32);
     c2 = iteration;
-    c3 = phase << 24;
-    left = 0;
+    n = phase << 24;
   }
-  __device__ __forceinline__ void block() {
-    uint32_t x0 = c0, x1 = c1, x2 = c2, x3 = c3;
-    uint32_t a = k0, b = k1;
-#pragma unroll
-    for (int r = 0; r < 10; r++) {
-      uint32_t hi0 = __umulhi(0xD2511F53u, x0), lo0 = 0xD2511F53u * x0;
-      uint32_t hi1 = __umulhi(0xCD9E8D57u, x2), lo1 = 0xCD9E8D57u * x2;
-      uint32_t y0 = hi1 ^ x1 ^ a, y1 = lo1, y2 = hi0 ^ x3 ^ b, y3 = lo0;
-      x0 = y0;
-      x1 = y1;
-      x2 = y2;
-      x3 = y3;
-      a += 0x9E3779B9u;
-      b += 0xBB67AE85u;
-    }
-    buf[0] = x0;
-    buf[1] = x1;
-    buf[2] = x2;
-    buf[3] = x3;
-    c3++;
-    left = 4;
+  // the next four draws (the displacement's): one block, or two when a draw was taken
+  // before them (a newborn molecule's unimolecular time)
+  __device__ __forceinline__ uint4 next4() {
+    const uint32_t idx = n & 0xFFFFFFu, ph = n & 0xFF000000u;
+    n += 4;
+    const uint4 w0 = philox_block(k0, k1, c0, c1, c2, ph | (idx >> 2));
+    const uint32_t off = idx & 3u;
+    if (off == 0) return w0;
+    const uint4 w1 = philox_block_rare(k0, k1, c0, c1, c2, ph | ((idx >> 2) + 1));
+    if (off == 1) return make_uint4(w0.y, w0.z, w0.w, w1.x);
+    if (off == 2) return make_uint4(w0.z, w0.w, w1.x, w1.y);
+    return make_uint4(w0.w, w1.x, w1.y, w1.z);
   }
   __device__ __forceinline__ uint32_t next_u32() {
-    if (left == 0) block();
-    return buf[4 - left--];
+    const uint32_t idx = n & 0xFFFFFFu;
+    const uint4 w = philox_block_rare(k0, k1, c0, c1, c2, (n & 0xFF000000u) | (idx >> 2));
+    n++;
+    const uint32_t q = idx & 3u;
+    return q == 0 ? w.x : (q == 1 ? w.y : (q == 2 ? w.z : w.w));
   }
 };
 
