@@ -234,10 +234,12 @@ struct StepDecision {
   int kind;  // 0 survivor, 1 proposal, 2 dead
 };
 
-// returns 0 survivor, 1 proposal, 2 dead, 3 survivor of a frozen replica (not stepped).
+// returns 0 survivor, 1 proposal, 2 dead, 3 survivor of a frozen replica (not stepped);
+// key: the next iteration's sort key of a survivor.
 // LOG: the build that can log one molecule's events (mcg_debug_molecule)
 template <typename T, bool LOG = true>
-__device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, Proposal* prop_out, uint32_t& err) {
+__device__ __forceinline__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, Proposal* prop_out,
+                                            uint32_t& err, uint32_t& key) {
   P4<T> rec = s.a_pos[i];
   uint32_t meta = meta_of(rec);
   const Geo<T>& g = geo_of(s, meta);
@@ -245,6 +247,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   if (mode != REP_RUN) {
     if (mode == REP_DROP) return 2;
     s.b_pos[i] = rec;  // frozen: stays as it is until the replica is collected
+    key = key_of(g, v3<T>(rec.x, rec.y, rec.z), meta & META_SPECIES_MASK);
     return 3;
   }
   const Chem& ch = *g.chem;
@@ -377,6 +380,7 @@ __device__ int run_molecule(const State<T>& s, uint32_t i, const uint8_t* dead, 
   // schedule flag consumed; counted-volume bits as left by the crossings
   set_meta(out, make_meta((uint32_t)species, g.rep, cv_after(meta_cv(meta), r) << META_CV_SHIFT));
   s.b_pos[i] = out;
+  key = key_of(g, r.pos, (uint32_t)species);
   if (meta & META_SCHEDULE_UNIMOL) s.a_tuni[i] = (T)tuni;  // keep the drawn time for the scatter
   return 0;
 }
@@ -399,7 +403,7 @@ __global__ void __launch_bounds__(TPB, MCG_DIFFUSE_MIN_BLOCKS) k_diffuse(State<T
     uint32_t key = 0;
     if (active) {
       Proposal p;
-      kind = run_molecule<T, LOG>(s, i, nullptr, &p, err);
+      kind = run_molecule<T, LOG>(s, i, nullptr, &p, err, key);
       if (kind == 3)
         kind = 0;  // frozen replica: kept, not stepped
       else
@@ -414,8 +418,6 @@ __global__ void __launch_bounds__(TPB, MCG_DIFFUSE_MIN_BLOCKS) k_diffuse(State<T
         } else {
           err |= ST_CAPACITY;
         }
-      } else if (kind == 0) {
-        key = key_of_rec(s, s.b_pos[i]);
       }
     }
     warp_count(s.counts, key, active && kind == 0);
@@ -505,7 +507,8 @@ __device__ __forceinline__ uint32_t lanes_per_warp(uint32_t n, uint32_t nwarps) 
 template <typename T>
 __device__ __forceinline__ void redo_one(const State<T>& s, uint32_t i, uint32_t* n_props, uint32_t& err) {
   Proposal p;
-  int kind = run_molecule(s, i, s.st, &p, err);
+  uint32_t key = 0;
+  int kind = run_molecule(s, i, s.st, &p, err, key);
   if (kind == 1) {
     s.st[i] = 1;
     uint32_t k = atomicAdd(n_props, 1u);
@@ -514,7 +517,7 @@ __device__ __forceinline__ void redo_one(const State<T>& s, uint32_t i, uint32_t
     atomicMin((unsigned long long*)&s.claim[p.partner], (unsigned long long)p.key);
   } else if (kind == 0 || kind == 3) {
     s.st[i] = 0;
-    atomicAdd(&s.counts[key_of_rec(s, s.b_pos[i])], 1u);
+    atomicAdd(&s.counts[key], 1u);
   } else {
     s.st[i] = (uint8_t)kind;
   }
