@@ -203,10 +203,10 @@ struct TraceOut {
   V3<T> pos;
   uint32_t subpart;
   uint32_t partner;  // index into Cells
-  double t_abs;      // time of the reaction / absorption
+  T t_abs;           // time of the reaction / absorption
   int pathway;       // pathway of the reaction class that fired (status 1)
   V3<T> rxn_pos;
-  double elapsed, t_steps;
+  T elapsed, t_steps;
   uint32_t err;
   // counted-volume membership set by transparent crossings up to the reaction
   // (update_counted_volume_id_when_crossing_wall, collision_utils.inl:1637-1694: a hit
@@ -1952,8 +1952,8 @@ __device__ __forceinline__ double time_of_unimol(double k_tot, D& draws) {
 // ray trace, sort, collisions in time order, wall interactions; loops while walls are hit.
 template <typename T, class D, class E>
 __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, uint32_t self, V3<T> pos, int species,
-                                      V3<T> disp, double r_rate_factor, double t_steps, double start_time, D& draws,
-                                      E& ev, bool allow_vv = true) {
+                                      V3<T> disp, T r_rate_factor, T t_steps, T start_time, D& draws, E& ev,
+                                      bool allow_vv = true) {
   TraceOut<T> res;
   res.status = 0;
   res.err = 0;
@@ -1967,7 +1967,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
   const bool can_vol_react = allow_vv && ch.partners[species] != 0;
   uint32_t sp = subpart_of(g, pos);
   uint32_t last_hit = NONE;
-  double elapsed = start_time;
+  T elapsed = start_time;
   V3<T> remaining = disp;
   int bounces = 0;
   bool was_defunct = false;
@@ -2078,7 +2078,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
       if (take_wall) {
         const int side = hit.type == CT_FRONT ? 1 : 2;
         const int kind = ch.can_volwall[species] ? g.wall_class[(size_t)hit.wall * g.nsp + species] : 0;
-        const double t_abs = elapsed + t_steps * (double)hit.t;
+        const T t_abs = elapsed + t_steps * hit.t;
         if (kind == 1) {
           if (g.n_cv) {
             const uint32_t f = cv_bits_of_wall(g, hit.wall);
@@ -2087,12 +2087,12 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
           }
           pos = hit.pos;
           sp = subpart_of(g, pos);
-          double t_smash = (double)hit.t;
-          T f = (T)(1.0 - t_smash);
+          const T t_smash = hit.t;
+          const T f = (T)1 - t_smash;
           remaining = cmul(remaining, v3<T>(f, f, f));
           elapsed += t_steps * t_smash;
-          t_steps *= (1.0 - t_smash);
-          if (t_steps < EPS) t_steps = EPS;
+          t_steps *= f;
+          if (t_steps < (T)EPS) t_steps = (T)EPS;
           last_hit = hit.wall;
           // fp32: make sure the crossing point lies on the far side, else the neighbouring
           // triangle of the crossed edge is hit again at t ~ 0 and re-tried without end
@@ -2101,26 +2101,28 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
             pos = guard_sides_rare(g, sp, pos, pos_at_start, hit.wall);  // every other plane: the side it came from
             sp = subpart_of(g, pos);
           }
-          ev.put(2, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
-        } else if (kind == 2 && test_intersect_absorb(r_rate_factor, draws)) {
-          ev.put(3, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
+          ev.put(2, hit.wall, side, (double)hit.t, (double)t_abs, (double)hit.pos.x, (double)hit.pos.y,
+                 (double)hit.pos.z);
+        } else if (kind == 2 && test_intersect_absorb((double)r_rate_factor, draws)) {
+          ev.put(3, hit.wall, side, (double)hit.t, (double)t_abs, (double)hit.pos.x, (double)hit.pos.y,
+                 (double)hit.pos.z);
           was_defunct = true;
           res.status = 2;
           res.t_abs = t_abs;
           res.rxn_pos = hit.pos;
         } else {
           // reflect_from_wall (collision_utils.inl:1711-1747)
-          elapsed += t_steps * (double)hit.t;
+          elapsed += t_steps * hit.t;
           const P4<T> rj = g.wrej[hit.wall];
           V3<T> n = v3<T>(rj.x, rj.y, rj.z);
-          double t_reflect = (double)hit.t;
+          T t_reflect = hit.t;
           pos = hit.pos;
           sp = subpart_of(g, pos);
-          t_steps *= (double)((T)1.0 - (T)t_reflect);
+          t_steps *= (T)1 - t_reflect;
           last_hit = hit.wall;
           T rf = (T)-2.0 * dot(remaining, n);
-          if (sizeof(T) == 4 && 1.0 - t_reflect < (double)Eps<T>::pos_sqrt) t_reflect -= (double)Eps<T>::pos_sqrt;
-          T f = (T)(1.0 - t_reflect);
+          if (sizeof(T) == 4 && (T)1 - t_reflect < Eps<T>::pos_sqrt) t_reflect -= Eps<T>::pos_sqrt;
+          const T f = (T)1 - t_reflect;
           remaining = cmul(remaining + cmul(v3<T>(rf, rf, rf), n), v3<T>(f, f, f));
           // fp32: the rounded reflection point must stay on the side the molecule came
           // from, else a coplanar neighbour triangle can reflect it outwards
@@ -2131,7 +2133,8 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
             pos = guard_sides_rare(g, sp, pos, pos_at_start, hit.wall);
             sp = subpart_of(g, pos);
           }
-          ev.put(1, hit.wall, side, (double)hit.t, t_abs, (double)hit.pos.x, (double)hit.pos.y, (double)hit.pos.z);
+          ev.put(1, hit.wall, side, (double)hit.t, (double)t_abs, (double)hit.pos.x, (double)hit.pos.y,
+                 (double)hit.pos.z);
         }
         wall_done = true;
         break;
@@ -2139,7 +2142,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
       if (i == colls.n) break;
       const VV<T> c = colls.c[i];
       if (c.t < Eps<T>::stime) continue;  // is_immediate_collision
-      const double t_abs = elapsed + t_steps * (double)c.t;
+      const T t_abs = elapsed + t_steps * c.t;
       const P4<T> q = cells.pos[c.idx];
       const uint64_t cuid = cells.uid[c.idx];
       const V3<T> cpos = pos_at_start + scale(remaining, c.t);  // collide_mol's rel_collision_pos
@@ -2150,17 +2153,17 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
                            ? (T)1
                            : exact_disk(g, cpos, remaining, species, v3<T>(q.x, q.y, q.z));
       if (factor < 0) {
-        ev.put(6, cuid, 0, (double)c.t, t_abs, (double)cpos.x, (double)cpos.y, (double)cpos.z);
+        ev.put(6, cuid, 0, (double)c.t, (double)t_abs, (double)cpos.x, (double)cpos.y, (double)cpos.z);
         continue;
       }
-      double scaling = (double)factor * r_rate_factor;
+      const double scaling = (double)factor * (double)r_rate_factor;
       const uint32_t ps = meta_of(q) & META_SPECIES_MASK;
       const int pw = test_bimolecular(ch.bimol_cum[species][ps], ch.bimol_npw[species][ps], scaling, draws.u32());
       if (pw < 0) {
-        ev.put(4, cuid, 0, (double)c.t, t_abs, (double)cpos.x, (double)cpos.y, (double)cpos.z);
+        ev.put(4, cuid, 0, (double)c.t, (double)t_abs, (double)cpos.x, (double)cpos.y, (double)cpos.z);
         continue;
       }
-      ev.put(5, cuid, pw, (double)c.t, t_abs, (double)cpos.x, (double)cpos.y, (double)cpos.z);
+      ev.put(5, cuid, pw, (double)c.t, (double)t_abs, (double)cpos.x, (double)cpos.y, (double)cpos.z);
       was_defunct = true;
       res.status = 1;
       res.pathway = pw;

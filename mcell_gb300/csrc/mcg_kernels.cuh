@@ -254,45 +254,47 @@ __device__ __forceinline__ int run_molecule(const State<T>& s, uint32_t i, const
   const uint32_t it = s.cnt->iteration - g.it0;  // the replica's own iteration
   const uint64_t uid = s.a_uid[i];
   const int species = (int)(meta & META_SPECIES_MASK);
-  double tuni = (double)s.a_tuni[i];
+  // the step's time bookkeeping runs in T: fp32 keeps the FP64 pipe out of the common path
+  T tuni = s.a_tuni[i];
   V3<T> pos = v3<T>(rec.x, rec.y, rec.z);
   PhiloxDraws draws;
   draws.ph.init(g.seed, uid, it, 0);
   // pick_unimol_rxn_class_and_set_rxn_time (diffuse_react_event.cpp:1731) on first diffusion
   if (meta & META_SCHEDULE_UNIMOL) {
-    tuni = ch.unimol_k[species] >= 0 ? time_of_unimol(ch.unimol_k[species], draws) : TIME_FOREVER;
+    tuni = (T)(ch.unimol_k[species] >= 0 ? time_of_unimol(ch.unimol_k[species], draws) : TIME_FOREVER);
   }
-  if (tuni <= 0.0) {
+  if (tuni <= (T)0) {
     // scheduled at or before the start of the step: react first (diffuse_single_molecule :214-223)
     unimol_products(s, g, species, meta_cv(meta), pos, 0.0, uid, it, draws);
     return 2;
   }
   // get_max_time (:164-198) with the barrier at the end of the iteration
-  double max_time = 1.0;
+  T max_time = 1;
   if (tuni < max_time) max_time = tuni;
   // compute_vol_displacement (diffusion_utils.inl:366-432), time_step = 1
-  double steps = 1.0, t_steps = 1.0;
+  T steps = 1, t_steps = 1;
   if (t_steps > max_time) {
     t_steps = max_time;
     steps = max_time;
   }
-  if (steps < EPS) {
-    steps = EPS;
-    t_steps = EPS;
+  if (steps < (T)EPS) {
+    steps = (T)EPS;
+    t_steps = (T)EPS;
   }
-  double scl = ch.space_step[species];
-  double r_rate_factor = 1.0;
-  if (steps != 1.0) {
-    double rate_factor = sqrt(steps);
-    r_rate_factor = 1.0 / rate_factor;
-    scl = rate_factor * ch.space_step[species];
+  const T space_step = (T)ch.space_step[species];
+  T scl = space_step;
+  T r_rate_factor = 1;
+  if (steps != (T)1) {
+    T rate_factor = sqrt(steps);
+    r_rate_factor = (T)1 / rate_factor;
+    scl = rate_factor * space_step;
   }
   TraceOut<T> r;
   V3<T> disp = v3<T>(0, 0, 0);
-  if (scl != 0.0) {
+  if (scl != (T)0) {
     V3<T> gz = gauss3<T>(draws);
-    disp = v3<T>((T)(scl * (double)gz.x * 0.70710678118654752440), (T)(scl * (double)gz.y * 0.70710678118654752440),
-                       (T)(scl * (double)gz.z * 0.70710678118654752440));
+    const T rsqrt2 = (T)0.70710678118654752440;
+    disp = v3<T>(scl * gz.x * rsqrt2, scl * gz.y * rsqrt2, scl * gz.z * rsqrt2);
     Cells<T> cells;
     cells.pos = s.a_pos;
     cells.uid = s.a_uid;
@@ -314,7 +316,7 @@ __device__ __forceinline__ int run_molecule(const State<T>& s, uint32_t i, const
         ev.out[269] = (double)disp.y;
         ev.out[270] = (double)disp.z;
       }
-      r = trace_molecule<T>(g, cells, i, pos, species, disp, r_rate_factor, t_steps, 0.0, draws, ev);
+      r = trace_molecule<T>(g, cells, i, pos, species, disp, r_rate_factor, t_steps, (T)0, draws, ev);
       if (ev.out) {
         ev.out[0] = r.status;
         ev.out[1] = (double)r.pos.x;
@@ -325,7 +327,7 @@ __device__ __forceinline__ int run_molecule(const State<T>& s, uint32_t i, const
       }
     } else {
       NoEvents ev;  // production kernel: no event code in the hot path
-      r = trace_molecule<T>(g, cells, i, pos, species, disp, r_rate_factor, t_steps, 0.0, draws, ev);
+      r = trace_molecule<T>(g, cells, i, pos, species, disp, r_rate_factor, t_steps, (T)0, draws, ev);
     }
     if (r.err & (ST_COLL_OVERFLOW | ST_SET_OVERFLOW)) count_fallbacks(s, r.err);
     err |= r.err;
@@ -340,10 +342,10 @@ __device__ __forceinline__ int run_molecule(const State<T>& s, uint32_t i, const
     p.i = i;
     p.partner = r.partner;
     p.pw = (uint32_t)r.pathway;
-    float tf = (float)r.t_abs;
+    const float tf = (float)r.t_abs;
     // earliest reaction wins; the molecule index makes keys unique within the iteration
     p.key = ((uint64_t)__float_as_uint(tf < 0.f ? 0.f : tf) << 32) | i;
-    p.t_abs = r.t_abs;
+    p.t_abs = (double)r.t_abs;
     p.cv = cv_after(meta_cv(meta), r);
     p.x = (double)r.rxn_pos.x;
     p.y = (double)r.rxn_pos.y;
@@ -352,9 +354,9 @@ __device__ __forceinline__ int run_molecule(const State<T>& s, uint32_t i, const
     return 1;
   }
   if (r.status == 2) return 2;
-  if (max_time < 1.0) {
+  if (max_time < (T)1) {
     // the unimolecular reaction happens where the molecule stopped
-    unimol_products(s, g, species, cv_after(meta_cv(meta), r), r.pos, tuni, uid, it, draws);
+    unimol_products(s, g, species, cv_after(meta_cv(meta), r), r.pos, (double)tuni, uid, it, draws);
     return 2;
   }
   const bool escaped = !in_partition(g, r.pos);
@@ -381,7 +383,7 @@ __device__ __forceinline__ int run_molecule(const State<T>& s, uint32_t i, const
   set_meta(out, make_meta((uint32_t)species, g.rep, cv_after(meta_cv(meta), r) << META_CV_SHIFT));
   s.b_pos[i] = out;
   key = key_of(g, r.pos, (uint32_t)species);
-  if (meta & META_SCHEDULE_UNIMOL) s.a_tuni[i] = (T)tuni;  // keep the drawn time for the scatter
+  if (meta & META_SCHEDULE_UNIMOL) s.a_tuni[i] = tuni;  // keep the drawn time for the scatter
   return 0;
 }
 
@@ -678,8 +680,8 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
           cells.maxc = s.maxc;
           cells.maxset = s.maxset;
           NoEvents ev;
-          TraceOut<T> r = trace_molecule<T>(g, cells, NONE, pos, species, disp, r_rate_factor, t_steps, p.birth,
-                                            draws, ev, false);
+          TraceOut<T> r = trace_molecule<T>(g, cells, NONE, pos, species, disp, (T)r_rate_factor, (T)t_steps,
+                                            (T)p.birth, draws, ev, false);
           if (r.err & (ST_COLL_OVERFLOW | ST_SET_OVERFLOW)) count_fallbacks(s, r.err);
           err |= r.err;
           cv = cv_after(cv, r);
@@ -1121,7 +1123,8 @@ __global__ void k_trace_cases(State<T> s, uint32_t ncases, const uint32_t* idx, 
   cells.maxc = s.maxc;
   cells.maxset = s.maxset;
   V3<T> dv = v3<T>((T)disp[3 * c], (T)disp[3 * c + 1], (T)disp[3 * c + 2]);
-  TraceOut<T> r = trace_molecule<T>(g, cells, i, v3<T>(rec.x, rec.y, rec.z), species, dv, rrf[c], tst[c], 0.0, d, ev);
+  TraceOut<T> r =
+      trace_molecule<T>(g, cells, i, v3<T>(rec.x, rec.y, rec.z), species, dv, (T)rrf[c], (T)tst[c], (T)0, d, ev);
   count_fallbacks(s, r.err);
   int status = r.status;
   if (d.over) status = 3;
