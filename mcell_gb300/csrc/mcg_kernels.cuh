@@ -128,6 +128,18 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
 
+// slot in a list filled through a counter, with one atomic per group of lanes that
+// arrive together (a counter hit by every thread on its own serialises at its cache
+// line: on GB300 that costs more than the work of a short kernel)
+__device__ __forceinline__ uint32_t warp_slot(uint32_t* counter) {
+  const unsigned am = __activemask();
+  const int leader = __ffs(am) - 1;
+  uint32_t b = 0;
+  if ((int)lane_id() == leader) b = atomicAdd(counter, (uint32_t)__popc(am));
+  b = __shfl_sync(am, b, leader);
+  return b + (uint32_t)__popc(am & ((1u << lane_id()) - 1u));
+}
+
 // histogram add with one atomic per distinct key in the warp
 __device__ __forceinline__ void warp_count(uint32_t* counts, uint32_t key, bool active) {
   unsigned mask = __ballot_sync(0xffffffffu, active);
@@ -197,7 +209,7 @@ template <typename T>
 __device__ void add_product(const State<T>& s, int species, uint32_t rep, uint32_t cv, V3<T> pos, double birth,
                             uint64_t uid) {
   if (species < 0) return;
-  uint32_t k = atomicAdd(&s.cnt->n_prod, 1u);
+  const uint32_t k = warp_slot(&s.cnt->n_prod);
   if (k >= s.prod_cap) {
     atomicOr(&s.cnt->status, ST_CAPACITY);
     return;
@@ -412,7 +424,7 @@ __global__ void __launch_bounds__(TPB, MCG_DIFFUSE_MIN_BLOCKS) k_diffuse(State<T
         steps++;
       s.st[i] = (uint8_t)kind;
       if (kind == 1) {
-        uint32_t k = atomicAdd(&s.cnt->n_props, 1u);
+        const uint32_t k = warp_slot(&s.cnt->n_props);
         if (k < s.prop_cap) {
           s.props[k] = p;
           atomicMin((unsigned long long*)&s.claim[i], (unsigned long long)p.key);
@@ -426,7 +438,9 @@ __global__ void __launch_bounds__(TPB, MCG_DIFFUSE_MIN_BLOCKS) k_diffuse(State<T
   }
   if (err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG))
     atomicOr(&s.cnt->status, err & (ST_CAPACITY | ST_ESCAPE | ST_WATCHDOG));
-  if (steps) atomicAdd(&s.cnt->mol_steps, (unsigned long long)steps);
+  // the warps leave the loop together: one molecule-step count per warp
+  steps = __reduce_add_sync(0xffffffffu, steps);
+  if (lane_id() == 0 && steps) atomicAdd(&s.cnt->mol_steps, (unsigned long long)steps);
 }
 
 // a winning proposal: both reactants die, products appear at the collision point
@@ -470,8 +484,7 @@ __global__ void k_collect_losers(State<T> s) {
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const Proposal p = s.props[k];
     if (s.st[p.i] == 1) {
-      uint32_t m = atomicAdd(&s.cnt->redo_n[0], 1u);
-      s.losers[m] = p.i;  // losers <= n_props <= prop_cap
+      s.losers[warp_slot(&s.cnt->redo_n[0])] = p.i;  // losers <= n_props <= prop_cap
     }
   }
 }
@@ -513,7 +526,7 @@ __device__ __forceinline__ void redo_one(const State<T>& s, uint32_t i, uint32_t
   int kind = run_molecule(s, i, s.st, &p, err, key);
   if (kind == 1) {
     s.st[i] = 1;
-    uint32_t k = atomicAdd(n_props, 1u);
+    const uint32_t k = warp_slot(n_props);
     s.redo_props[k] = p;  // k < number of losers <= prop_cap
     atomicMin((unsigned long long*)&s.claim[i], (unsigned long long)p.key);
     atomicMin((unsigned long long*)&s.claim[p.partner], (unsigned long long)p.key);
@@ -558,7 +571,7 @@ __global__ void k_redo_next(State<T> s, int round) {
   uint32_t* next = s.losers + (size_t)((round + 1) & 1) * s.prop_cap;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const Proposal p = s.redo_props[k];
-    if (s.st[p.i] == 1) next[atomicAdd(&s.cnt->redo_n[round + 1], 1u)] = p.i;
+    if (s.st[p.i] == 1) next[warp_slot(&s.cnt->redo_n[round + 1])] = p.i;
     s.claim[p.i] = CLAIM_FREE;
     s.claim[p.partner] = CLAIM_FREE;
   }
