@@ -1988,10 +1988,16 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
     // kept unless a wall is hit before the last subpartition (then re-collected below).
     SubMask sm;
     sm.bad = true;
+    // collide_mol divides by the squared length of the move: a move of zero length
+    // (what a wall met exactly at the end of the move, t = 1, leaves for the next
+    // segment), or one whose square underflows in fp32, meets no molecule. The
+    // reference asserts a non-zero length there; its release build would take every
+    // occupant scanned as a collision at t = 0/0.
+    const bool scan = can_vol_react && dot_rn(remaining, remaining) > (T)0;
     {
       Walk<T> w;
       w.start(g, pos, sp, pdisp);
-      if (can_vol_react) {
+      if (scan) {
         mask_box(g, pos, pdisp, sm);
         if (!sm.bad) collect_start(g, pos, w.cx, w.cy, w.cz, sm);
       }
@@ -2020,7 +2026,7 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
     Colls<T> colls;
     colls.n = 0;
     colls.overflow = false;
-    if (can_vol_react) {
+    if (scan) {
       // ray_trace_vol keeps the set of the first collection unless a wall was hit
       // before the last crossed subpartition, then re-collects up to the hit
       V3<T> mdisp = pdisp;
@@ -2172,7 +2178,6 @@ __device__ TraceOut<T> trace_molecule(const Geo<T>& g, const Cells<T>& cells, ui
       res.rxn_pos = cpos;
       break;
     }
-    (void)wall_done;
     if (draws.overrun() || ++bounces > MAX_BOUNCES) {
       res.err |= ST_WATCHDOG;
       res.status = 3;

@@ -246,6 +246,23 @@ struct StepDecision {
   int kind;  // 0 survivor, 1 proposal, 2 dead
 };
 
+// anomaly log for the host (the first 8 of an iteration): uid, species + 1000 * kind
+// (1 escape, 2 watchdog), iteration, start xyz, displacement xyz, final xyz, replica
+template <typename T>
+__device__ __noinline__ void log_anomaly(const State<T>& s, const Geo<T>& g, uint64_t uid, int species, bool escaped,
+                                         uint32_t it, V3<T> start, V3<T> disp, V3<T> end) {
+  const uint32_t k = atomicAdd(&s.cnt->n_esc, 1u);
+  if (k >= 8) return;
+  const double rec[13] = {(double)uid,    (double)species + 1000.0 * (escaped ? 1 : 2),
+                          (double)it,     (double)start.x,
+                          (double)start.y, (double)start.z,
+                          (double)disp.x, (double)disp.y,
+                          (double)disp.z, (double)end.x,
+                          (double)end.y,  (double)end.z,
+                          (double)g.rep};
+  for (int q = 0; q < 13; q++) s.cnt->esc[k][q] = rec[q];
+}
+
 // returns 0 survivor, 1 proposal, 2 dead, 3 survivor of a frozen replica (not stepped);
 // key: the next iteration's sort key of a survivor.
 // LOG: the build that can log one molecule's events (mcg_debug_molecule)
@@ -372,17 +389,7 @@ __device__ __forceinline__ int run_molecule(const State<T>& s, uint32_t i, const
     return 2;
   }
   const bool escaped = !in_partition(g, r.pos);
-  if (escaped || (r.err & ST_WATCHDOG)) {
-    // anomaly log for the host: kind 1 escape, 2 watchdog (field 1 = species + 1000 * kind)
-    uint32_t k = atomicAdd(&s.cnt->n_esc, 1u);
-    if (k < 8) {
-      const double rec_[12] = {(double)uid, (double)species + 1000.0 * (escaped ? 1 : 2), (double)it,
-                               (double)pos.x, (double)pos.y, (double)pos.z, (double)disp.x, (double)disp.y,
-                               (double)disp.z, (double)r.pos.x, (double)r.pos.y, (double)r.pos.z};
-      for (int q = 0; q < 12; q++) s.cnt->esc[k][q] = rec_[q];
-      s.cnt->esc[k][12] = (double)g.rep;
-    }
-  }
+  if (escaped || (r.err & ST_WATCHDOG)) log_anomaly(s, g, uid, species, escaped, it, pos, disp, r.pos);
   if (escaped) {
     err |= ST_ESCAPE;  // the reference stops with a fatal error; here the molecule is dropped
     return 2;
@@ -659,6 +666,9 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
       double max_time = 1.0 - p.birth;
       if (unimol_time < p.birth + max_time) max_time = unimol_time - p.birth;
       V3<T> pos = v3<T>(p.pos.x, p.pos.y, p.pos.z);
+      const V3<T> start = pos;
+      V3<T> disp = v3<T>(0, 0, 0);
+      uint32_t werr = 0;
       uint32_t cv = meta_cv(meta);
       bool dead = false;
       if (max_time <= 0.0) {
@@ -682,9 +692,9 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
         }
         if (scl != 0.0) {
           V3<T> gz = gauss3<T>(draws);
-          V3<T> disp = v3<T>((T)(scl * (double)gz.x * 0.70710678118654752440),
-                             (T)(scl * (double)gz.y * 0.70710678118654752440),
-                             (T)(scl * (double)gz.z * 0.70710678118654752440));
+          disp = v3<T>((T)(scl * (double)gz.x * 0.70710678118654752440),
+                       (T)(scl * (double)gz.y * 0.70710678118654752440),
+                       (T)(scl * (double)gz.z * 0.70710678118654752440));
           Cells<T> cells;
           cells.pos = s.a_pos;
           cells.uid = s.a_uid;
@@ -697,6 +707,7 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
                                             (T)p.birth, draws, ev, false);
           if (r.err & (ST_COLL_OVERFLOW | ST_SET_OVERFLOW)) count_fallbacks(s, r.err);
           err |= r.err;
+          werr = r.err & ST_WATCHDOG;
           cv = cv_after(cv, r);
           if (r.status == 2) {
             dead = true;
@@ -709,7 +720,9 @@ __global__ void __launch_bounds__(TPB) k_products(State<T> s) {
           dead = true;
         }
       }
-      if (!dead && !in_partition(g, pos)) {
+      const bool escaped = !dead && !in_partition(g, pos);
+      if (escaped || werr) log_anomaly(s, g, p.uid, species, escaped, it, start, disp, pos);
+      if (escaped) {
         err |= ST_ESCAPE;
         dead = true;
       }
