@@ -1354,31 +1354,14 @@ __device__ __forceinline__ void occupants_of(const Geo<T>& g, const Cells<T>& ce
   while (m) {
     const int b = __ffs(m) - 1;
     m &= m - 1;
-    // the octants of (subpartition, species) are consecutive keys: load their starts
-    // together (independent loads, one or two cache lines), then scan the wanted ones
+    // the octants of (subpartition, species) are consecutive keys, so a run of
+    // consecutive octants is one range of occupants
     const uint32_t base = g.kbase + (((uint32_t)b * g.n3 + sp) << g.oct_shift);
-    uint32_t s9[9];
-    if (g.oct_shift == 3 && (g.kbase & 7u) == 0) {
-      // 8 octant starts at a multiple of 8 keys: two aligned 16-byte loads and the end
-      const uint4 lo = __ldg(reinterpret_cast<const uint4*>(cells.start + base));
-      const uint4 hi = __ldg(reinterpret_cast<const uint4*>(cells.start + base + 4));
-      s9[0] = lo.x;
-      s9[1] = lo.y;
-      s9[2] = lo.z;
-      s9[3] = lo.w;
-      s9[4] = hi.x;
-      s9[5] = hi.y;
-      s9[6] = hi.z;
-      s9[7] = hi.w;
-      s9[8] = __ldg(cells.start + base + 8);
-    } else {
-      const uint32_t noct = 1u << g.oct_shift;
-#pragma unroll
-      for (int o = 0; o < 9; o++) s9[o] = (o <= (int)noct) ? __ldg(cells.start + base + o) : 0u;
-    }
-    for (uint32_t oo = om; oo; oo &= oo - 1) {
+    for (uint32_t oo = om; oo;) {
       const uint32_t o = (uint32_t)(__ffs(oo) - 1);
-      const uint32_t j0 = s9[o], j1 = s9[o + 1];
+      const uint32_t run = (uint32_t)(__ffs(~(oo >> o)) - 1);
+      oo &= ~(((1u << run) - 1u) << o);
+      const uint32_t j0 = __ldg(cells.start + base + o), j1 = __ldg(cells.start + base + o + run);
       // MCG_OCC_BATCH occupants per round: their loads are issued together (latency overlap)
       for (uint32_t j4 = j0; j4 < j1; j4 += MCG_OCC_BATCH) {
         P4<T> q4[MCG_OCC_BATCH];

@@ -263,6 +263,16 @@ __device__ __noinline__ void log_anomaly(const State<T>& s, const Geo<T>& g, uin
   for (int q = 0; q < 13; q++) s.cnt->esc[k][q] = rec[q];
 }
 
+// Items a warp takes at a time when a pass has n items (molecules, products, losers)
+// for nwarps warps: the fewest lanes (a power of two) that still cover all items in
+// one round. Scattered items diverge, so a full warp of them costs nearly 32 traces
+// in a row; spread thin, the pass costs about one.
+__device__ __forceinline__ uint32_t lanes_per_warp(uint32_t n, uint32_t nwarps) {
+  uint32_t per = 32;
+  while (per > 1 && (uint64_t)nwarps * (per / 2) >= n) per >>= 1;
+  return per;
+}
+
 // returns 0 survivor, 1 proposal, 2 dead, 3 survivor of a frozen replica (not stepped);
 // key: the next iteration's sort key of a survivor.
 // LOG: the build that can log one molecule's events (mcg_debug_molecule)
@@ -411,15 +421,21 @@ __global__ void __launch_bounds__(TPB, MCG_DIFFUSE_MIN_BLOCKS) k_diffuse(State<T
   const uint32_t n = s.cnt->n_live;
   uint32_t err = 0;
   uint32_t steps = 0;
-  // persistent warps: each warp takes the next 32 molecules (in sorted order) until
-  // none are left, so long-running warps near walls do not leave SMs idle at the end
+  // persistent warps: each warp takes the next `per` molecules (in sorted order) until
+  // none are left, so long-running warps near walls do not leave SMs idle at the end.
+  // A warp's lanes diverge and run largely one after another, so a warp's batch costs
+  // about its lanes' traces in a row: in fp32 a model with fewer molecules than 32 per
+  // warp spreads them thinner (its step then takes a few traces' time, not 32). fp64
+  // keeps full warps: a warp instruction holds GB300's narrow FP64 pipe as long with
+  // 2 lanes as with 32.
+  const uint32_t per = sizeof(T) == 4 ? lanes_per_warp(n, gridDim.x * (TPB / 32)) : 32u;
   for (;;) {
     uint32_t base = 0;
-    if (lane_id() == 0) base = atomicAdd(&s.cnt->work, 32u);
+    if (lane_id() == 0) base = atomicAdd(&s.cnt->work, per);
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= n) break;
     uint32_t i = base + lane_id();
-    bool active = i < n;
+    bool active = lane_id() < per && i < n;
     int kind = 2;
     uint32_t key = 0;
     if (active) {
@@ -514,16 +530,6 @@ __global__ void k_reset_claims(State<T> s) {
 // models at high rates lose a large share of their proposals), the rest in one
 // CTA. Round r reads its losers from half (r & 1) of the loser buffer and
 // their count from redo_n[r], and appends the next round's to the other half.
-
-// Items a warp takes at a time when a pass has n scattered items (products, losers)
-// for nwarps warps: the fewest lanes (a power of two) that still cover all items in
-// one round. Scattered items diverge, so a full warp of them costs nearly 32 traces
-// in a row; spread thin, the pass costs about one.
-__device__ __forceinline__ uint32_t lanes_per_warp(uint32_t n, uint32_t nwarps) {
-  uint32_t per = 32;
-  while (per > 1 && (uint64_t)nwarps * (per / 2) >= n) per >>= 1;
-  return per;
-}
 
 // one loser re-traced: a new proposal (counted in *n_props) or a final state
 template <typename T>

@@ -48,6 +48,8 @@ def test_crossing_at_the_end_of_the_move_meets_no_partner(precision):
     n_ev = int(got[6])
     ev = got[9:9 + 8 * n_ev].reshape(-1, 8)
     assert n_ev == 1 and ev[0, 0] == 2  # one event: the transparent crossing
-    tol = 1e-12 if precision == "fp64" else 1e-4  # the crossing point, as collide_wall computes it
+    # the crossing point; the zero move lies in the plane of the square's other triangle,
+    # whose re-try (jump_away_line) may move it by the fp64 jump
+    tol = 1e-9 if precision == "fp64" else 1e-4
     assert np.allclose(got[1:4], [3.0, 0.3, 0.2], rtol=0, atol=tol)
     e.close()
