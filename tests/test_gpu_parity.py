@@ -63,7 +63,9 @@ def test_fp64_matches_oracle_random(seed):
 
 def test_fp32_wall_hit_mismatch_rate():
     """fp32 geometry against the fp64 oracle: wall-hit identity must agree on nearly
-    every case; positions within 1e-4 internal units (~1 pm)."""
+    every case, and final positions closely. Bounds at about 3x what was measured here
+    (0 of 4,000 mismatches; 12 per 100,000 on the 10M-molecule precision tube, i.e. 1.4
+    expected at 3x that rate; largest position error 0.028 internal units)."""
     rng = np.random.default_rng(7)
     sc = H.sphere_in_cube_scene(rng, levels=3, n_mol=3000, radius_um=0.6, cube_um=1.5, p_rxn=0.0)
     cases = H.random_cases(rng, sc, 4000, scale=3.0, near_wall_frac=0.6)
@@ -79,11 +81,11 @@ def test_fp32_wall_hit_mismatch_rate():
     mism = sum(a != b for a, b in zip(walls_g, walls_w))
     rate = mism / len(got)
     print(f"fp32 wall-hit identity mismatch rate: {rate:.5f} ({mism}/{len(got)})")
-    assert rate < 0.01
+    assert mism <= 2
     same = [c for c in range(len(got)) if walls_g[c] == walls_w[c]]
     err = np.abs(got[same, 1:4] - want[same, 1:4]).max()
     print(f"fp32 max final-position error on matching cases: {err:.3g} internal units")
-    assert err < 0.1  # 1 nm (0.1 internal units); fp32 ulp at 150 internal units is 1.5e-5
+    assert err < 0.08  # internal units (0.8 nm); fp32 ulp at 150 internal units is 1.5e-5
 
 
 @pytest.mark.parametrize("name", H.GOLDEN_SCENES)
