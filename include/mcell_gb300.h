@@ -347,6 +347,65 @@ int mcg_inside_tests(mcg_engine* e, uint32_t n, const double* pos, int kind, uin
 int mcg_release_positions(int shape, uint32_t n, const double* center, const double* diameter, const uint32_t* draws,
                           uint32_t n_draws, double* pos, uint32_t* draws_used);
 
+/* ---- Releases into region expressions, by concentration, and vacuum releases
+   (ReleaseEvent::release_inside_regions, src4/release_event.cpp:904-952, with
+   is_point_inside_region_expr_recursively :785-810, num_vol_mols_from_conc :826-856,
+   vacuum_inside_regions :864-896, randomly_remove_molecules :578-597).
+   A region expression is a postfix program of at most 15 tokens: a geometry object
+   index (>= 0, objects as given to mcg_set_wall_objects) or one of the operators
+   below, which combine the two results before it; e.g. {1, 0, MCG_REGION_DIFFERENCE}
+   is "inside object 1 and not inside object 0". */
+#define MCG_REGION_UNION (-1)
+#define MCG_REGION_INTERSECT (-2)
+#define MCG_REGION_DIFFERENCE (-3)
+#define MCG_RELEASE_BY_NUMBER 0
+#define MCG_RELEASE_BY_CONCENTRATION 1
+/* Volume of the closed object `object` of a mesh (Region::initialize_volume_info_if_needed,
+   src4/geometry.cpp:860-897: tetrahedra of its faces, in wall order, with the center of
+   its bounding box; internal units cubed). Host only. */
+int mcg_object_volume(uint32_t n_verts, const double* verts, uint32_t n_walls, const uint32_t* walls,
+                      const uint16_t* object_of_wall, uint32_t object, double* volume);
+/* Bounding box of a region expression (compute_region_expr_bounding_box,
+   src4/geometry.cpp:1180-1265): union widens, intersection narrows, difference keeps the
+   left operand's box. Host only. */
+int mcg_region_expr_bbox(uint32_t n_verts, const double* verts, uint32_t n_walls, const uint32_t* walls,
+                         const uint16_t* object_of_wall, const int32_t* expr, uint32_t n_expr, double* llf,
+                         double* urb);
+/* Molecules a release of a molar concentration into a sphere of the given diameter
+   (internal units) places (calculate_number_to_release, src4/release_event.cpp:509-553);
+   length_unit_um = microns per internal unit. Host only. */
+int mcg_release_number_from_concentration(const double* diameter, double concentration_molar, double length_unit_um,
+                                          uint64_t* n);
+/* The vacuum's choice (randomly_remove_molecules) of n_remove of m candidates, in
+   candidate order, drawing from an injected stream of 32-bit draws (one per candidate);
+   removed[i] = 1 for the chosen. Parity harness and host logic; host only. */
+int mcg_vacuum_select(uint32_t m, uint32_t n_remove, const uint32_t* draws, uint32_t n_draws, uint8_t* removed,
+                      uint32_t* draws_used);
+/* Release into, or vacuum from, a region expression of the model's closed objects.
+   method MCG_RELEASE_BY_NUMBER: number > 0 places that many molecules of the species,
+   uniform in the expression (rejection in its bounding box with the reference's inside
+   tests, a point whose ray meets a wall edge drawn again); number < 0 removes up to
+   -number molecules of the species that lie inside (candidates in id order, the
+   reference's choice; the draws come from a generator keyed by release_seed).
+   method MCG_RELEASE_BY_CONCENTRATION: the count is the reference's from the molar
+   concentration: for a single object from its volume, and all those molecules are
+   placed; for an expression from its bounding box's volume, each of those draws placing
+   a molecule only if it falls inside (as the reference's approximate count does).
+   *done = molecules placed, or removed (negative). Molecule ids continue the model's. */
+int mcg_release_region(mcg_engine* e, uint32_t species, int method, int64_t number, double concentration_molar,
+                       double length_unit_um, const int32_t* expr, uint32_t n_expr, uint64_t release_seed,
+                       int64_t* done);
+/* Parity harness of release_inside_regions (test infrastructure): the positions the
+   release above would place, computed in one device thread from one injected stream of
+   32-bit draws as the reference's generator would be consumed (number < 0: the indices,
+   in id order, of the molecules the vacuum removes, in `removed`, nothing changed).
+   *n_pos / *n_removed = how many were written; *draws_used (0xFFFFFFFF if the stream
+   ran out). */
+int mcg_release_region_harness(mcg_engine* e, uint32_t species, int method, int64_t number,
+                               double concentration_molar, double length_unit_um, const int32_t* expr,
+                               uint32_t n_expr, const uint32_t* draws, uint32_t n_draws, double* pos, uint32_t cap,
+                               uint32_t* n_pos, uint64_t* removed, uint32_t* n_removed, uint32_t* draws_used);
+
 /* ---- Counted volumes: molecules inside closed geometry objects, per species, for
    MolOrRxnCountEvent (src4/mol_or_rxn_count_event.cpp:707). As MCell4's counted-
    volume index, each molecule carries its membership (up to 7 counted objects per

@@ -38,7 +38,10 @@ EXPORTS = [
     "mcg_get_counted_volume_counts", "mcg_get_counted_volume_trajectory",
     "mcg_get_fallbacks", "mcg_set_trace_limits", "mcg_batch_get_fallbacks", "mcg_reaction_decisions",
     "mcg_inside_tests", "mcg_release_positions",
+    "mcg_object_volume", "mcg_region_expr_bbox", "mcg_release_number_from_concentration", "mcg_vacuum_select",
+    "mcg_release_region", "mcg_release_region_harness",
 ]
+REGION_OPS = {"union": -1, "intersect": -2, "difference": -3}
 MAX_PATHWAYS = 4
 
 
@@ -171,6 +174,64 @@ def release_positions(shape, n, center, diameter, draws):
     if rc:
         raise EngineError(rc, "mcg_release_positions failed")
     return out, (None if used.value == 0xFFFFFFFF else int(used.value))
+
+
+def _mesh_args(verts, walls, object_of_wall):
+    v = np.ascontiguousarray(verts, np.float64)
+    w = np.ascontiguousarray(walls, np.uint32)
+    o = np.ascontiguousarray(object_of_wall, np.uint16)
+    return (v, w, o), (ctypes.c_uint32(len(v)), _p(v), ctypes.c_uint32(len(w)), _p(w), _p(o))
+
+
+def region_expr(tokens):
+    """A region expression as the C ABI's postfix program: object indices and the
+    operator names "union", "intersect", "difference"."""
+    return np.array([REGION_OPS[t] if isinstance(t, str) else int(t) for t in tokens], np.int32)
+
+
+def object_volume(verts, walls, object_of_wall, obj):
+    """Volume of a closed object of a mesh (mcg_object_volume; host only)."""
+    keep, args = _mesh_args(verts, walls, object_of_wall)
+    out = ctypes.c_double()
+    rc = lib().mcg_object_volume(*args, ctypes.c_uint32(obj), ctypes.byref(out))
+    if rc:
+        raise EngineError(rc, "mcg_object_volume failed")
+    return out.value
+
+
+def region_expr_bbox(verts, walls, object_of_wall, tokens):
+    """(llf, urb) of a region expression (mcg_region_expr_bbox; host only)."""
+    keep, args = _mesh_args(verts, walls, object_of_wall)
+    ex = region_expr(tokens)
+    lo, hi = np.zeros(3), np.zeros(3)
+    rc = lib().mcg_region_expr_bbox(*args, _p(ex), ctypes.c_uint32(len(ex)), _p(lo), _p(hi))
+    if rc:
+        raise EngineError(rc, "mcg_region_expr_bbox failed")
+    return lo, hi
+
+
+def release_number_from_concentration(diameter, concentration, length_unit_um):
+    """Molecules a molar concentration places in a sphere (mcg_release_number_from_concentration)."""
+    d = np.ascontiguousarray(diameter, np.float64)
+    n = ctypes.c_uint64()
+    rc = lib().mcg_release_number_from_concentration(_p(d), ctypes.c_double(concentration),
+                                                     ctypes.c_double(length_unit_um), ctypes.byref(n))
+    if rc:
+        raise EngineError(rc, "mcg_release_number_from_concentration failed")
+    return n.value
+
+
+def vacuum_select(m, n_remove, draws):
+    """The vacuum's choice of n_remove of m candidates on injected draws (mcg_vacuum_select):
+    (0/1 per candidate, draws used or None)."""
+    dr = np.ascontiguousarray(draws, np.uint32)
+    out = np.zeros(max(m, 1), np.uint8)
+    used = ctypes.c_uint32()
+    rc = lib().mcg_vacuum_select(ctypes.c_uint32(m), ctypes.c_uint32(n_remove), _p(dr), ctypes.c_uint32(len(dr)),
+                                 _p(out), ctypes.byref(used))
+    if rc:
+        raise EngineError(rc, "mcg_vacuum_select failed")
+    return out[:m], (None if used.value == 0xFFFFFFFF else int(used.value))
 
 
 class Engine:
@@ -351,6 +412,35 @@ class Engine:
         d = np.ascontiguousarray(diameter, np.float64)
         self._chk(lib().mcg_release(self.h, ctypes.c_uint32(species), ctypes.c_uint64(n), ctypes.c_int(shapes[shape]),
                                     _p(c), _p(d), ctypes.c_uint32(obj), ctypes.c_uint64(seed)))
+
+    def release_region(self, species, tokens, number=0, concentration=None, length_unit_um=0.01, seed=1):
+        """Release into (number > 0, or a molar concentration) or vacuum from (number < 0)
+        a region expression (mcg_release_region). Returns molecules placed (removed < 0)."""
+        ex = region_expr(tokens)
+        method = 0 if concentration is None else 1
+        done = ctypes.c_int64()
+        self._chk(lib().mcg_release_region(self.h, ctypes.c_uint32(species), ctypes.c_int(method),
+                                           ctypes.c_int64(number), ctypes.c_double(concentration or 0.0),
+                                           ctypes.c_double(length_unit_um), _p(ex), ctypes.c_uint32(len(ex)),
+                                           ctypes.c_uint64(seed), ctypes.byref(done)))
+        return done.value
+
+    def release_region_harness(self, species, tokens, draws, number=0, concentration=None, length_unit_um=0.01,
+                               cap=100000):
+        """Parity harness (mcg_release_region_harness): (positions [k, 3], removed ids, draws used or None)."""
+        ex = region_expr(tokens)
+        dr = np.ascontiguousarray(draws, np.uint32)
+        pos = np.zeros((cap, 3))
+        rem = np.zeros(cap, np.uint64)
+        n_pos, n_rem, used = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        method = 0 if concentration is None else 1
+        self._chk(lib().mcg_release_region_harness(
+            self.h, ctypes.c_uint32(species), ctypes.c_int(method), ctypes.c_int64(number),
+            ctypes.c_double(concentration or 0.0), ctypes.c_double(length_unit_um), _p(ex), ctypes.c_uint32(len(ex)),
+            _p(dr), ctypes.c_uint32(len(dr)), _p(pos), ctypes.c_uint32(cap), ctypes.byref(n_pos), _p(rem),
+            ctypes.byref(n_rem), ctypes.byref(used)))
+        return (pos[:min(cap, n_pos.value)], rem[:min(cap, n_rem.value)],
+                None if used.value == 0xFFFFFFFF else int(used.value))
 
     def export_state(self):
         """Checkpoint: dict of pos, species, ids, unimol_time, flags and the iteration."""

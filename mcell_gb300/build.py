@@ -8,6 +8,7 @@ Translation units are compiled in parallel:
   mcg_batch.cpp C ABI of batches (replicas) and the batch autotuner
   mcg_serve.cpp C ABI of the serving loop (continuous batching on a worker thread)
   mcg_viz.cpp   visualisation files (ASCII / CellBlender) from device state
+  mcg_region.cpp  region releases: object volumes, expression boxes, concentration counts, vacuum choice
   mcg_trace_static.cu  fixed device scratch of mcg_trace_cases_static
 Usage: python -m mcell_gb300.build [--force] [-v]
 """
@@ -48,6 +49,7 @@ def _units():
         ("mcg_batch.cpp", ["-x", "c++"] + host),
         ("mcg_serve.cpp", ["-x", "c++"] + host),
         ("mcg_viz.cpp", ["-x", "c++"] + host),
+        ("mcg_region.cpp", ["-x", "c++"] + host),
     ]
 
 

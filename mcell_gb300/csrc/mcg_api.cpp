@@ -402,6 +402,35 @@ int mcg_release(mcg_engine* e, uint32_t species, uint64_t n, int shape, const do
   return MCG_OK;
 }
 
+int mcg_release_region(mcg_engine* e, uint32_t species, int method, int64_t number, double concentration_molar,
+                       double length_unit_um, const int32_t* expr, uint32_t n_expr, uint64_t release_seed,
+                       int64_t* done) {
+  if (!e || !expr || !done) return MCG_ERR_ARG;
+  if (!e->pend_species.empty() || !e->dev) {
+    int rc = prepare(e);  // pending host molecules are uploaded first
+    if (rc) return rc;
+  }
+  std::string err;
+  int rc = e->dev->release_region(0, species, method, number, concentration_molar, length_unit_um, expr, n_expr,
+                                  release_seed, done, err);
+  if (rc) return fail(e, rc, err);
+  return MCG_OK;
+}
+
+int mcg_release_region_harness(mcg_engine* e, uint32_t species, int method, int64_t number,
+                               double concentration_molar, double length_unit_um, const int32_t* expr,
+                               uint32_t n_expr, const uint32_t* draws, uint32_t n_draws, double* pos, uint32_t cap,
+                               uint32_t* n_pos, uint64_t* removed, uint32_t* n_removed, uint32_t* draws_used) {
+  if (!e || !expr || !n_pos || !n_removed || !draws_used || (n_draws && !draws) || (cap && (!pos || !removed)))
+    return MCG_ERR_ARG;
+  int rc = prepare(e);
+  if (rc) return rc;
+  std::string err;
+  rc = e->dev->release_region_harness(0, species, method, number, concentration_molar, length_unit_um, expr, n_expr,
+                                      draws, n_draws, pos, cap, n_pos, removed, n_removed, draws_used, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
 int mcg_export_state(mcg_engine* e, uint64_t cap, double* pos, uint32_t* species, uint64_t* ids, double* tuni,
                      uint8_t* flags, uint64_t* n_out, uint64_t* iteration) {
   if (!e || !n_out || !iteration || (cap && (!pos || !species || !ids || !tuni || !flags))) return MCG_ERR_ARG;

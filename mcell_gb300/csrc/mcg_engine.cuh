@@ -19,8 +19,11 @@
 #include <thread>
 #include <unordered_map>
 
+#include <random>
+
 #include "mcg_engine.h"
 #include "mcg_kernels.cuh"
+#include "mcg_region.h"
 #include "mcg_trace_static.h"
 
 namespace mcg {
@@ -433,7 +436,10 @@ class DeviceEngineT : public DeviceEngine {
       for (int a = 0; a < 3; a++) {
         d.llf[a] = lo[a] = R.obj_llf[3 * object + a];
         d.urb[a] = hi[a] = R.obj_urb[3 * object + a];
+        d.leaf_llf[0][a] = d.llf[a];
       }
+      d.expr[0] = (int32_t)object;
+      d.n_expr = 1;
     } else {
       for (int a = 0; a < 3; a++) {
         d.center[a] = center[a];
@@ -458,6 +464,217 @@ class DeviceEngineT : public DeviceEngine {
     MCG_CUDA(cudaGetLastError());
     reps_[rep].next_uid += n;
     return rebin(nullptr, n, err);
+  }
+
+  // the descriptor of a release into a region expression: its program, the box of each
+  // leaf object, the expression's box (inside the partition), and the count (method
+  // and number or concentration, the reference's rules; single_draw for an
+  // expression's approximate concentration count)
+  int region_desc(uint32_t rep, uint32_t species, int method, int64_t number, double concentration,
+                  double length_unit, const int32_t* expr, uint32_t n_expr, ReleaseDesc& d, int64_t& count,
+                  std::string& err) {
+    if (rep >= max_rep_ || !reps_[rep].used) {
+      err = "no such replica";
+      return -1;
+    }
+    const Rep& R = reps_[rep];
+    if (species >= nsp_ || (method != 0 && method != 1)) {
+      err = "invalid release";
+      return -1;
+    }
+    if (!R.has_obj) {
+      err = "region releases need the walls' objects (mcg_set_wall_objects)";
+      return -1;
+    }
+    const uint32_t nobj = (uint32_t)(R.obj_llf.size() / 3);
+    if (!region_expr_valid(expr, n_expr, nobj)) {
+      err = "invalid region expression (postfix program of objects and operators, at most 15 tokens)";
+      return -1;
+    }
+    d = ReleaseDesc{};
+    d.rep = rep;
+    d.species = species;
+    d.shape = REL_INSIDE;
+    d.n_expr = n_expr;
+    for (uint32_t k = 0; k < n_expr; k++) {
+      d.expr[k] = expr[k];
+      if (expr[k] < 0) continue;
+      const uint32_t o = (uint32_t)expr[k];
+      if (R.obj_llf[3 * o] > R.obj_urb[3 * o]) {
+        err = "region expression: an object without walls";
+        return -1;
+      }
+      for (int a = 0; a < 3; a++) d.leaf_llf[k][a] = R.obj_llf[3 * o + a];
+    }
+    region_expr_bbox(expr, n_expr, R.obj_llf.data(), R.obj_urb.data(), d.llf, d.urb);
+    const Geo<T>& g = geos_h_[rep];
+    const double o[3] = {(double)g.origin.x, (double)g.origin.y, (double)g.origin.z};
+    const double q[3] = {(double)g.opposite.x, (double)g.opposite.y, (double)g.opposite.z};
+    for (int a = 0; a < 3; a++)
+      if (!(d.llf[a] >= o[a] && d.urb[a] < q[a])) {
+        err = "release region outside the partition";
+        return -4;
+      }
+    if (method == 1) {
+      // num_vol_mols_from_conc (release_event.cpp:826-856): one object's volume, exact;
+      // an expression's bounding box, approximate (each draw counts)
+      if (!(concentration >= 0) || !(length_unit > 0)) {
+        err = "invalid concentration or length unit";
+        return -1;
+      }
+      double vol;
+      if (n_expr == 1) {
+        vol = R.obj_vol[(uint32_t)expr[0]];
+      } else {
+        vol = (d.urb[0] - d.llf[0]) * (d.urb[1] - d.llf[1]) * (d.urb[2] - d.llf[2]);
+        d.single_draw = 1;
+      }
+      const double num = concentration_number(concentration, vol, length_unit);
+      if (!(num >= 0) || num > 2147483647.0) {  // check_max_release_count (:497-506)
+        err = "concentration release of more than INT_MAX molecules";
+        return -1;
+      }
+      count = (int64_t)(uint32_t)num;
+    } else {
+      count = number;
+    }
+    if (count > (int64_t)0xFFFFFFF0ll || count < -(int64_t)0xFFFFFFF0ll) {
+      err = "invalid release";
+      return -1;
+    }
+    return 0;
+  }
+
+  // the molecules of d.species inside d's region, in id order
+  int vacuum_candidates(const ReleaseDesc& d, std::vector<std::pair<uint64_t, uint32_t>>& cand, std::string& err) {
+    if (read_counters(err)) return -2;
+    const uint32_t n = cnt_.n_live;
+    cand.clear();
+    if (n == 0) return 0;
+    AllocSet tmp;
+    uint64_t* d_ids;
+    uint32_t *d_idx, *d_cnt;
+    MCG_CUDA(tmp.get(&d_ids, sizeof(uint64_t) * n));
+    MCG_CUDA(tmp.get(&d_idx, sizeof(uint32_t) * n));
+    MCG_CUDA(tmp.get(&d_cnt, sizeof(uint32_t)));
+    MCG_CUDA(cudaMemsetAsync(d_cnt, 0, sizeof(uint32_t), stream_));
+    k_vacuum_candidates<T><<<grid(n), TPB, 0, stream_>>>(state(parity_), d, d_ids, d_idx, d_cnt);
+    launches_ += 1;
+    MCG_CUDA(cudaGetLastError());
+    uint32_t m = 0;
+    MCG_CUDA(d2h(&m, d_cnt, sizeof(uint32_t)));
+    std::vector<uint64_t> ids(m);
+    std::vector<uint32_t> idx(m);
+    if (m) {
+      MCG_CUDA(d2h(ids.data(), d_ids, sizeof(uint64_t) * m));
+      MCG_CUDA(d2h(idx.data(), d_idx, sizeof(uint32_t) * m));
+    }
+    cand.resize(m);
+    for (uint32_t k = 0; k < m; k++) cand[k] = {ids[k], idx[k]};
+    std::sort(cand.begin(), cand.end());
+    return 0;
+  }
+
+  int release_region(uint32_t rep, uint32_t species, int method, int64_t number, double concentration,
+                     double length_unit, const int32_t* expr, uint32_t n_expr, uint64_t seed, int64_t* done,
+                     std::string& err) override {
+    ReleaseDesc d;
+    int64_t count = 0;
+    int rc = region_desc(rep, species, method, number, concentration, length_unit, expr, n_expr, d, count, err);
+    if (rc) return rc;
+    *done = 0;
+    if (count == 0) return 0;
+    if (count < 0) {
+      // vacuum_inside_regions: the candidates in id order, each removed with the
+      // probability of the removals left over the candidates left
+      std::vector<std::pair<uint64_t, uint32_t>> cand;
+      if ((rc = vacuum_candidates(d, cand, err))) return rc;
+      std::vector<uint8_t> chosen(cand.size());
+      std::mt19937_64 gen(seed);
+      const int removed = select_for_removal((uint32_t)cand.size(), (uint32_t)(-count), [&]() {
+        return (double)(uint32_t)(gen() >> 32) * (1.0 / 4294967296.0);
+      }, chosen.data());
+      if (removed == 0) return 0;
+      const uint32_t n = cnt_.n_live;
+      std::vector<uint8_t> mask(n, 0);
+      for (size_t k = 0; k < cand.size(); k++)
+        if (chosen[k]) mask[cand[k].second] = 1;
+      AllocSet tmp;
+      uint8_t* d_mask;
+      MCG_CUDA(tmp.get(&d_mask, n));
+      MCG_CUDA(cudaMemcpyAsync(d_mask, mask.data(), n, cudaMemcpyHostToDevice, stream_));
+      if ((rc = rebin(nullptr, 0, err, false, d_mask))) return rc;
+      *done = -(int64_t)removed;
+      return 0;
+    }
+    if (read_counters(err)) return -2;
+    const uint64_t live = cnt_.n_live, n = (uint64_t)count;
+    if (live + n > cap_ && ensure_capacity(std::max<uint64_t>((live + n) * 3 / 2, 1024), err)) return -2;
+    if (n > base_.prod_cap && ensure_prod(n, err)) return -2;
+    d.n = (uint32_t)n;
+    d.seed = seed;
+    d.uid0 = reps_[rep].next_uid;
+    k_release<T><<<grid(n), TPB, 0, stream_>>>(state(parity_), d);
+    launches_ += 1;
+    MCG_CUDA(cudaGetLastError());
+    reps_[rep].next_uid += n;
+    if ((rc = rebin(nullptr, n, err, false, nullptr, 1))) return rc;
+    *done = (int64_t)cnt_.n_live - (int64_t)live;
+    return 0;
+  }
+
+  int release_region_harness(uint32_t rep, uint32_t species, int method, int64_t number, double concentration,
+                             double length_unit, const int32_t* expr, uint32_t n_expr, const uint32_t* draws,
+                             uint32_t n_draws, double* pos, uint32_t cap, uint32_t* n_pos, uint64_t* removed,
+                             uint32_t* n_removed, uint32_t* used, std::string& err) override {
+    ReleaseDesc d;
+    int64_t count = 0;
+    int rc = region_desc(rep, species, method, number, concentration, length_unit, expr, n_expr, d, count, err);
+    if (rc) return rc;
+    *n_pos = 0;
+    *n_removed = 0;
+    *used = 0;
+    if (count < 0) {
+      std::vector<std::pair<uint64_t, uint32_t>> cand;
+      if ((rc = vacuum_candidates(d, cand, err))) return rc;
+      std::vector<uint8_t> chosen(cand.size());
+      uint32_t k = 0;
+      bool over = false;
+      select_for_removal((uint32_t)cand.size(), (uint32_t)(-count), [&]() {
+        if (k >= n_draws) {
+          over = true;
+          return 0.0;
+        }
+        return (double)draws[k++] * (1.0 / 4294967296.0);
+      }, chosen.data());
+      uint32_t nr = 0;
+      for (size_t q = 0; q < cand.size(); q++)
+        if (chosen[q]) {
+          if (nr < cap) removed[nr] = cand[q].first;
+          nr++;
+        }
+      *n_removed = nr;
+      *used = over ? 0xFFFFFFFFu : k;
+      return 0;
+    }
+    d.n = (uint32_t)count;
+    AllocSet tmp;
+    uint32_t *d_draws, *d_out_n;
+    double* d_pos;
+    MCG_CUDA(tmp.get(&d_draws, sizeof(uint32_t) * std::max<uint32_t>(n_draws, 1)));
+    MCG_CUDA(tmp.get(&d_pos, sizeof(double) * 3 * std::max<uint32_t>(cap, 1)));
+    MCG_CUDA(tmp.get(&d_out_n, sizeof(uint32_t) * 2));
+    if (n_draws) MCG_CUDA(cudaMemcpyAsync(d_draws, draws, sizeof(uint32_t) * n_draws, cudaMemcpyHostToDevice, stream_));
+    k_release_region_harness<T><<<1, 32, 0, stream_>>>(state(parity_), d, d_draws, n_draws, d_pos, cap, d_out_n,
+                                                        d_out_n + 1);
+    launches_ += 1;
+    MCG_CUDA(cudaGetLastError());
+    uint32_t out2[2];
+    MCG_CUDA(d2h(out2, d_out_n, sizeof(out2)));
+    *n_pos = out2[0];
+    *used = out2[1];
+    if (out2[0] && cap) MCG_CUDA(d2h(pos, d_pos, sizeof(double) * 3 * std::min(cap, out2[0])));
+    return 0;
   }
 
   int import_state(uint32_t rep, uint64_t n, const double* pos, const uint32_t* species, const uint64_t* ids,
@@ -821,6 +1038,7 @@ class DeviceEngineT : public DeviceEngine {
     // per species in the world, and per species and counted object
     std::vector<uint64_t> init_world, init_cv;
     std::vector<double> obj_llf, obj_urb;  // bounding box of each object's walls
+    std::vector<double> obj_vol;           // volume of each closed object
     // host copies for placing fp32 molecules: wall planes (n xyz, d), walls per
     // subpartition, and the grid
     std::vector<double> planes;
@@ -1049,6 +1267,18 @@ class DeviceEngineT : public DeviceEngine {
             R.obj_urb[3 * ob + a] = std::max(R.obj_urb[3 * ob + a], x);
           }
       }
+      // the objects' volumes (concentration releases), from the walls' vertices
+      std::vector<double> vx(9 * (size_t)nw);
+      std::vector<uint32_t> tri(3 * (size_t)nw);
+      for (uint32_t w = 0; w < nw; w++)
+        for (int v = 0; v < 3; v++) {
+          tri[3 * (size_t)w + v] = 3 * w + v;
+          for (int a = 0; a < 3; a++) vx[9 * (size_t)w + 3 * v + a] = hs.wall[(size_t)w * 24 + 13 + 3 * v + a];
+        }
+      const MeshView mv{3 * nw, vx.data(), nw, tri.data(), sp.wall_obj->data()};
+      R.obj_vol.assign(nobj, 0.0);
+      for (uint32_t ob = 0; ob < nobj; ob++)
+        if (R.obj_llf[3 * ob] <= R.obj_urb[3 * ob]) object_volume(mv, ob, &R.obj_vol[ob]);
     }
     g.n_cv = 0;
     if (!sp.counted.empty()) {
@@ -1190,7 +1420,8 @@ class DeviceEngineT : public DeviceEngine {
 
   // re-sorts the live molecules plus the staged ones into the other sorted arrays
   // (molecules of dropped replicas are left out); counters must be fresh
-  int rebin(const Product<T>* stage, uint64_t n, std::string& err, bool init_cv = false) {
+  int rebin(const Product<T>* stage, uint64_t n, std::string& err, bool init_cv = false,
+            const uint8_t* d_remove = nullptr, int staged_status = 0) {
     const uint64_t live = cnt_.n_live;
     if (live + n > 0xFFFFFFF0ull) {
       err = "too many molecules for 32-bit indices";
@@ -1219,7 +1450,7 @@ class DeviceEngineT : public DeviceEngine {
       k_cv_init<T><<<grid(n), TPB, 0, stream_>>>(s, (uint32_t)n);
       launches_ += 1;
     }
-    k_rebin_count<T><<<grid(live + n), TPB, 0, stream_>>>(s, (uint32_t)n);
+    k_rebin_count<T><<<grid(live + n), TPB, 0, stream_>>>(s, (uint32_t)n, d_remove, staged_status);
     k_scan_tiles<T><<<ntiles_, TPB, 0, stream_>>>(s);
     k_scan_top<T><<<1, TPB, 0, stream_>>>(s, ntiles_);
     k_scan_apply<T><<<ntiles_, TPB, 0, stream_>>>(s);

@@ -135,6 +135,16 @@ class DeviceEngine {
   // inside geometry object `object`); ids continue the replica's
   virtual int release(uint32_t rep, uint32_t species, uint64_t n, int shape, const double* center,
                       const double* diameter, uint32_t object, uint64_t seed, std::string& err) = 0;
+  // release into / vacuum from a region expression (mcg_release_region); draws != null:
+  // the parity harness (nothing changes; positions or removed ids are returned)
+  virtual int release_region(uint32_t rep, uint32_t species, int method, int64_t number, double concentration,
+                             double length_unit, const int32_t* expr, uint32_t n_expr, uint64_t seed,
+                             int64_t* done, std::string& err) = 0;
+  virtual int release_region_harness(uint32_t rep, uint32_t species, int method, int64_t number,
+                                     double concentration, double length_unit, const int32_t* expr, uint32_t n_expr,
+                                     const uint32_t* draws, uint32_t n_draws, double* pos, uint32_t cap,
+                                     uint32_t* n_pos, uint64_t* removed, uint32_t* n_removed, uint32_t* used,
+                                     std::string& err) = 0;
   // counted volumes: molecules of each species inside each counted object after the
   // last iteration or upload ([nsp][n_counted]), and their trajectory
   virtual int counted_counts(uint32_t rep, uint64_t* out, std::string& err) = 0;

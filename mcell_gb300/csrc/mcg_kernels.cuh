@@ -996,8 +996,11 @@ __global__ void k_end(State<T> s) {
 // re-binning (uploads): existing molecules keep their position (b = a, status
 // survivor) and staged ones sit in the product list; both are counted here and
 // moved by k_scatter
+// remove: molecules (by index) that leave with this re-binning (a vacuum release), or
+// null; staged_status: the staged molecules' status was written by their producer (a
+// release whose single draws may place nothing), else every staged molecule is placed
 template <typename T>
-__global__ void k_rebin_count(State<T> s, uint32_t n_staged) {
+__global__ void k_rebin_count(State<T> s, uint32_t n_staged, const uint8_t* remove, int staged_status) {
   const uint32_t n = s.cnt->n_live;
   for (uint32_t base = blockIdx.x * TPB; base < n; base += gridDim.x * TPB) {
     uint32_t i = base + threadIdx.x;
@@ -1007,7 +1010,7 @@ __global__ void k_rebin_count(State<T> s, uint32_t n_staged) {
       P4<T> p = s.a_pos[i];
       s.b_pos[i] = p;
       // molecules of a dropped replica leave with this re-binning
-      active = geo_of(s, meta_of(p)).mode != REP_DROP;
+      active = geo_of(s, meta_of(p)).mode != REP_DROP && !(remove && remove[i]);
       s.st[i] = active ? 0 : 2;
       if (active) key = key_of_rec(s, p);
     }
@@ -1018,13 +1021,17 @@ __global__ void k_rebin_count(State<T> s, uint32_t n_staged) {
     bool active = k < n_staged;
     uint32_t key = 0;
     if (active) {
-      P4<T> p = s.prod[k].pos;
-      s.pst[k] = 0;
-      key = key_of_rec(s, p);
+      if (staged_status) {
+        active = s.pst[k] == 0;
+      } else {
+        s.pst[k] = 0;
+      }
+      if (active) key = key_of_rec(s, s.prod[k].pos);
     }
     warp_count(s.counts, key, active);
   }
 }
+
 
 // ---- volume releases on the device (ReleaseEvent::release_ellipsoid_or_rectcuboid,
 // release_inside_regions; release_event.cpp:904-1006): new molecules written into
@@ -1032,12 +1039,21 @@ __global__ void k_rebin_count(State<T> s, uint32_t n_staged) {
 
 constexpr int REL_SPHERE = 0, REL_CUBOID = 1, REL_SHELL = 2, REL_INSIDE = 3;
 
+constexpr int REGION_EXPR_MAX = 15;  // tokens of a region expression
 struct ReleaseDesc {
   uint32_t rep, species, n, object;
   int shape;
   double center[3], diameter[3];  // ellipsoid / cuboid / shell
-  double llf[3], urb[3];          // sampling box of a release inside an object
+  double llf[3], urb[3];          // sampling box of a release inside a region
   uint64_t seed, uid0;
+  // REL_INSIDE: the region, a postfix program of objects (>= 0) and operators (-1
+  // union, -2 intersection, -3 difference); the low corner of each leaf object's box
+  int32_t expr[REGION_EXPR_MAX];
+  uint32_t n_expr;
+  double leaf_llf[REGION_EXPR_MAX][3];
+  // each molecule's point is drawn once and kept only if inside (the reference's
+  // approximate count of a concentration release into an expression)
+  int single_draw;
 };
 
 // one molecule of ReleaseEvent::release_ellipsoid_or_rectcuboid (release_event.cpp:953-
@@ -1065,22 +1081,52 @@ __device__ bool release_point(int shape, const double* center, const double* dia
   return ok;
 }
 
+// is_point_inside_region_expr_recursively (release_event.cpp:785-810) over the postfix
+// program: every leaf's inside test (the reference evaluates both operands of every
+// operator), combined by union, intersection or difference; NONE when a leaf's ray met
+// a wall edge
+template <typename T>
+__device__ uint32_t inside_expr(const Geo<T>& g, V3<double> p, const ReleaseDesc& r) {
+  uint32_t st = 0;  // results, the last one in bit 0
+  for (uint32_t k = 0; k < r.n_expr; k++) {
+    const int32_t t = r.expr[k];
+    if (t >= 0) {
+      const uint32_t in = inside_region(g, p, (uint32_t)t, r.leaf_llf[k]);
+      if (in == NONE) return NONE;
+      st = (st << 1) | in;
+    } else {
+      const uint32_t b = st & 1u, a = (st >> 1) & 1u;
+      const uint32_t v = t == -1 ? (a | b) : (t == -2 ? (a & b) : (a & (b ^ 1u)));
+      st = ((st >> 2) << 1) | v;
+    }
+  }
+  return st & 1u;
+}
+
+// a point of the region's bounding box (release_inside_regions, release_event.cpp:923-926)
+template <class D>
+__device__ __forceinline__ V3<double> box_point(const double* llf, const double* urb, D& d) {
+  V3<double> out;
+  out.x = __dadd_rn(llf[0], __dmul_rn(__dsub_rn(urb[0], llf[0]), draw_dbl(d)));
+  out.y = __dadd_rn(llf[1], __dmul_rn(__dsub_rn(urb[1], llf[1]), draw_dbl(d)));
+  out.z = __dadd_rn(llf[2], __dmul_rn(__dsub_rn(urb[2], llf[2]), draw_dbl(d)));
+  return out;
+}
+
 // one molecule of ReleaseEvent::release_inside_regions (release_event.cpp:904-952): a
-// point of the object's bounding box, kept if inside the object (the reference's ray
-// test; a ray through an edge, where the reference's test would fail, draws again)
+// point of the region's bounding box, kept if inside the region (the reference's ray
+// tests; a ray through an edge, where the reference's test would fail, draws again).
+// single_draw: one point only, kept if inside (false when it is not)
 template <typename T, class D>
-__device__ bool release_inside_point(const Geo<T>& g, uint32_t obj, const double* llf, const double* urb, D& d,
-                                     V3<double>& out, uint32_t& redo) {
+__device__ bool release_inside_point(const Geo<T>& g, const ReleaseDesc& r, D& d, V3<double>& out, uint32_t& redo) {
   for (int attempt = 0; attempt < 1024; attempt++) {
-    out.x = __dadd_rn(llf[0], __dmul_rn(__dsub_rn(urb[0], llf[0]), draw_dbl(d)));
-    out.y = __dadd_rn(llf[1], __dmul_rn(__dsub_rn(urb[1], llf[1]), draw_dbl(d)));
-    out.z = __dadd_rn(llf[2], __dmul_rn(__dsub_rn(urb[2], llf[2]), draw_dbl(d)));
-    const uint32_t in = inside_region(g, out, obj, llf);
+    out = box_point(r.llf, r.urb, d);
+    const uint32_t in = inside_expr(g, out, r);
     if (in == NONE) {
       redo++;
       continue;
     }
-    if (in) return true;
+    if (in || r.single_draw) return in != 0;
   }
   return false;
 }
@@ -1093,9 +1139,11 @@ __global__ void k_release(State<T> s, ReleaseDesc r) {
     d.ph.init(r.seed, i, 0, 7);
     V3<double> p = v3<double>(0, 0, 0);
     uint32_t redo = 0;
-    const bool ok = r.shape == REL_INSIDE ? release_inside_point(g, r.object, r.llf, r.urb, d, p, redo)
+    const bool ok = r.shape == REL_INSIDE ? release_inside_point(g, r, d, p, redo)
                                           : release_point(r.shape, r.center, r.diameter, d, p);
-    if (!ok) atomicOr(&s.cnt->status, ST_WATCHDOG);
+    // a single draw outside the region places nothing; else no point in 1024 tries
+    s.pst[i] = ok ? 0 : 2;
+    if (!ok && !r.single_draw) atomicOr(&s.cnt->status, ST_WATCHDOG);
     Product<T> m;
     m.pos.x = (T)p.x;
     m.pos.y = (T)p.y;
@@ -1112,6 +1160,72 @@ __global__ void k_release(State<T> s, ReleaseDesc r) {
     m.tuni = TIME_FOREVER;
     s.prod[i] = m;
   }
+}
+
+// the molecules of a species of replica rep inside a region (vacuum_inside_regions,
+// release_event.cpp:864-896: the species, the region's bounding box, then the region's
+// inside tests): their ids and indices, in no particular order
+template <typename T>
+__global__ void k_vacuum_candidates(State<T> s, ReleaseDesc r, uint64_t* ids, uint32_t* idx, uint32_t* count) {
+  const Geo<T>& g = s.geos[r.rep];
+  const uint32_t n = s.cnt->n_live;
+  uint32_t redo = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const P4<T> p = s.a_pos[i];
+    const uint32_t meta = meta_of(p);
+    if (meta_rep(meta) != r.rep || (meta & META_SPECIES_MASK) != r.species) continue;
+    const V3<double> q = v3<double>((double)p.x, (double)p.y, (double)p.z);
+    if (!(q.x >= r.llf[0] && q.x <= r.urb[0] && q.y >= r.llf[1] && q.y <= r.urb[1] && q.z >= r.llf[2] &&
+          q.z <= r.urb[2]))
+      continue;
+    const uint32_t in = inside_expr(g, q, r);
+    if (in == NONE) {
+      redo++;  // counted outside
+      continue;
+    }
+    if (!in) continue;
+    const uint32_t k = warp_slot(count);
+    ids[k] = s.a_uid[i];
+    idx[k] = i;
+  }
+  if (redo) atomicAdd(&s.cnt->warn_inside_redo, (unsigned long long)redo);
+}
+
+// Parity harness of release_inside_regions (release_event.cpp:904-952), one thread:
+// `n` molecules drawn in turn from one injected stream; with single_draw each draw is
+// one of the n (kept if inside), else draws repeat until inside. NONE (a ray through an
+// edge) draws again. out: positions; *n_out placed; *used draws (0xFFFFFFFF overrun)
+template <typename T>
+__global__ void k_release_region_harness(State<T> s, ReleaseDesc r, const uint32_t* draws, uint32_t ndraws,
+                                         double* out, uint32_t cap, uint32_t* n_out, uint32_t* used) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const Geo<T>& g = s.geos[r.rep];
+  InjectedDraws d;
+  d.d = draws;
+  d.n = ndraws;
+  d.used = 0;
+  d.over = false;
+  uint32_t placed = 0;
+  int64_t left = r.n;
+  uint32_t guard = 0;
+  while (left > 0 && !d.over && ++guard < (1u << 22)) {
+    const V3<double> p = box_point(r.llf, r.urb, d);
+    const uint32_t in = d.over ? 0u : inside_expr(g, p, r);
+    if (in == NONE) continue;
+    if (!in) {
+      if (r.single_draw) left--;
+      continue;
+    }
+    if (placed < cap) {
+      out[3 * placed] = p.x;
+      out[3 * placed + 1] = p.y;
+      out[3 * placed + 2] = p.z;
+    }
+    placed++;
+    left--;
+  }
+  *n_out = placed;
+  *used = d.over ? 0xFFFFFFFFu : d.used;
 }
 
 // inside tests on given points (parity harness): kind 0 the counted-volume bits, kind 1

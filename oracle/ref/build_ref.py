@@ -61,6 +61,16 @@ FUNCS = [
     ("src4/collision_utils.inl", "compute_counted_volume_for_pos", "MCell::CollisionUtils"),
     ("src4/wall.cpp", "Region::compute_bounding_box", "MCell"),
     ("src4/release_event.cpp", "ReleaseEvent::release_ellipsoid_or_rectcuboid", "MCell"),
+    ("src4/geometry.cpp", "tetrahedral_volume", "MCell"),
+    ("src4/geometry.cpp", "Region::initialize_volume_info_if_needed", "MCell"),
+    ("src4/geometry.cpp", "compute_region_expr_bounding_box", "MCell"),
+    ("src4/release_event.cpp", "check_max_release_count", "MCell"),
+    ("src4/release_event.cpp", "ReleaseEvent::calculate_number_to_release", "MCell"),
+    ("src4/release_event.cpp", "ReleaseEvent::num_vol_mols_from_conc", "MCell"),
+    ("src4/release_event.cpp", "ReleaseEvent::randomly_remove_molecules", "MCell"),
+    ("src4/release_event.cpp", "ReleaseEvent::is_point_inside_region_expr_recursively", "MCell"),
+    ("src4/release_event.cpp", "ReleaseEvent::vacuum_inside_regions", "MCell"),
+    ("src4/release_event.cpp", "ReleaseEvent::release_inside_regions", "MCell"),
     ("src4/rxn_utils.inl", "binary_search_double", "MCell::RxnUtils"),
     ("src4/rxn_utils.inl", "test_bimolecular", "MCell::RxnUtils"),
     ("src4/rxn_utils.inl", "test_intersect", "MCell::RxnUtils"),

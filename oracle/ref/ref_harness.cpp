@@ -37,7 +37,6 @@ struct Scene {
   Partition p;
   std::vector<BNG::RxnClass> rxn_store;
   std::vector<int> can_vol_react;
-  std::map<unsigned, Region> regions;  // closed regions, one per geometry object
 };
 
 void put_event(double* out, int kind, int index, int side, double t_rel, double t_abs, const Vec3& pos) {
@@ -336,7 +335,7 @@ void ref_scene_set_objects(void* sp, unsigned nobj, const unsigned* object_of_wa
     p.walls[w].object_index = object_of_wall[w];
     p.walls[w].object_id = object_of_wall[w];
   }
-  s->regions.clear();
+  p.regions_by_id.clear();
 }
 
 // compute_counted_volume_for_pos (collision_utils.inl:1515-1545): bit k set when pos is
@@ -360,20 +359,19 @@ unsigned ref_counted_volume_for_pos(void* sp, const double* pos) {
   return redo ? (mask | (1u << 31)) : mask;
 }
 
-// is_point_inside_region_no_waypoints (collision_utils.inl:1484-1510) for the closed
-// region made of object obj's walls: 0 outside, 1 inside, 2 the ray met a wall edge
-int ref_inside_region(void* sp, unsigned obj, const double* pos) {
-  Scene* s = (Scene*)sp;
+// the closed region made of object obj's walls (walls_and_edges ordered by wall index,
+// walls per subpartition as Region::initialize_wall_subpart_mapping_if_needed makes
+// them), registered as the object's encompassing region
+static Region& region_of(Scene* s, unsigned obj) {
   Partition& p = s->p;
-  auto it = s->regions.find(obj);
-  if (it == s->regions.end()) {
+  auto it = p.regions_by_id.find(obj);
+  if (it == p.regions_by_id.end()) {
     Region reg;
     for (size_t w = 0; w < p.walls.size(); w++) {
       if (p.walls[w].object_index == obj) {
         reg.walls_and_edges[(wall_index_t)w];
       }
     }
-    // walls per subpartition of the region (Region::initialize_wall_subpart_mapping_if_needed)
     for (size_t sub = 0; sub < p.walls_per_subpart.size(); sub++) {
       for (wall_index_t w: p.walls_per_subpart[sub]) {
         if (p.walls[w].object_index == obj) {
@@ -382,12 +380,137 @@ int ref_inside_region(void* sp, unsigned obj, const double* pos) {
       }
     }
     reg.compute_bounding_box(p, reg.bounding_box_llf, reg.bounding_box_urb);
-    it = s->regions.emplace(obj, reg).first;
+    it = p.regions_by_id.emplace(obj, reg).first;
+    if (obj < p.geometry_objects.size()) {
+      p.geometry_objects[obj].encompassing_region_id = obj;
+    }
   }
+  return it->second;
+}
+
+bool Region::is_point_inside(Partition& p, const Vec3& pos) {
+  bool redo = false;
+  return CollisionUtils::is_point_inside_region_no_waypoints(p, pos, *this, redo);
+}
+
+// is_point_inside_region_no_waypoints (collision_utils.inl:1484-1510) for the closed
+// region made of object obj's walls: 0 outside, 1 inside, 2 the ray met a wall edge
+int ref_inside_region(void* sp, unsigned obj, const double* pos) {
+  Scene* s = (Scene*)sp;
+  Region& reg = region_of(s, obj);
   const Vec3 v((pos_t)pos[0], (pos_t)pos[1], (pos_t)pos[2]);
   bool redo = false;
-  const bool in = CollisionUtils::is_point_inside_region_no_waypoints(p, v, it->second, redo);
+  const bool in = CollisionUtils::is_point_inside_region_no_waypoints(s->p, v, reg, redo);
   return redo ? 2 : (in ? 1 : 0);
+}
+
+// Region::initialize_volume_info_if_needed (geometry.cpp:860-897): object obj's volume
+double ref_region_volume(void* sp, unsigned obj) {
+  Scene* s = (Scene*)sp;
+  Region& reg = region_of(s, obj);
+  reg.volume_info_initialized = false;
+  reg.initialize_volume_info_if_needed(s->p);
+  return reg.get_volume();
+}
+
+// A region expression from a postfix program: tokens >= 0 are objects, -1 union,
+// -2 intersection, -3 difference (the node pool lives as long as the call)
+static RegionExprNode* expr_from_postfix(Scene* s, const int* tok, unsigned n, std::vector<RegionExprNode>& pool) {
+  pool.assign(n, RegionExprNode());
+  std::vector<RegionExprNode*> st;
+  for (unsigned k = 0; k < n; k++) {
+    RegionExprNode* e = &pool[k];
+    if (tok[k] >= 0) {
+      region_of(s, (unsigned)tok[k]);
+      e->op = RegionExprOperator::LEAF_GEOMETRY_OBJECT;
+      e->geometry_object_id = (geometry_object_id_t)tok[k];
+    } else {
+      e->op = tok[k] == -1 ? RegionExprOperator::UNION
+                           : (tok[k] == -2 ? RegionExprOperator::INTERSECT : RegionExprOperator::DIFFERENCE);
+      e->right = st.back();
+      st.pop_back();
+      e->left = st.back();
+      st.pop_back();
+    }
+    st.push_back(e);
+  }
+  return st.empty() ? nullptr : st.back();
+}
+
+// compute_region_expr_bounding_box (geometry.cpp:1180-1265)
+void ref_region_expr_bbox(void* sp, const int* tok, unsigned n, double* llf, double* urb) {
+  Scene* s = (Scene*)sp;
+  std::vector<RegionExprNode> pool;
+  RegionExprNode* root = expr_from_postfix(s, tok, n, pool);
+  World world;
+  world.outer = &s->p;
+  Vec3 lo, hi;
+  compute_region_expr_bounding_box(&world, root, lo, hi);
+  llf[0] = lo.x; llf[1] = lo.y; llf[2] = lo.z;
+  urb[0] = hi.x; urb[1] = hi.y; urb[2] = hi.z;
+}
+
+// ReleaseEvent::calculate_number_to_release (release_event.cpp:509-575) by
+// concentration (molar) for a spherical release of the given diameter
+unsigned ref_number_from_concentration(const double* diameter, double concentration, double length_unit) {
+  World world;
+  world.config.length_unit = length_unit;
+  ReleaseEvent ev;
+  ev.world = &world;
+  ev.release_shape = ReleaseShape::SPHERICAL;
+  ev.release_number_method = ReleaseNumberMethod::CONCENTRATION_NUM;
+  ev.concentration = concentration;
+  ev.diameter = Vec3((pos_t)diameter[0], (pos_t)diameter[1], (pos_t)diameter[2]);
+  return ev.calculate_number_to_release();
+}
+
+// ReleaseEvent::release_inside_regions (release_event.cpp:904-952) into the region
+// expression `tok` with the random stream injected. method 0: `number` molecules
+// (CONST_NUM; a negative number removes molecules of `species`, vacuum_inside_regions
+// :864-896); method 1: by concentration (num_vol_mols_from_conc :826-856). Released
+// positions go to pos (up to cap), removed molecule indices to removed; the scene's
+// molecules are left as they were. Returns the computed release number; draws_used =
+// draws taken (0xFFFFFFFF if the stream ran out).
+int ref_release_inside_regions(void* sp, const int* tok, unsigned ntok, int method, int number, unsigned species,
+                               double concentration, double length_unit, const unsigned* draws, unsigned ndraws,
+                               double* pos, unsigned cap, unsigned* n_pos, unsigned* removed, unsigned* n_removed,
+                               unsigned* draws_used) {
+  Scene* s = (Scene*)sp;
+  Partition& p = s->p;
+  std::vector<RegionExprNode> pool;
+  World world;
+  world.outer = &p;
+  world.config.length_unit = length_unit;
+  world.rng.draws = draws;
+  world.rng.n = ndraws;
+  ReleaseEvent ev;
+  ev.world = &world;
+  ev.release_shape = ReleaseShape::REGION;
+  ev.release_number_method = method == 1 ? ReleaseNumberMethod::CONCENTRATION_NUM : ReleaseNumberMethod::CONST_NUM;
+  ev.release_number = (uint)(number < 0 ? 0 : number);
+  ev.concentration = concentration;
+  ev.species_id = species;
+  ev.region_expr.root = expr_from_postfix(s, tok, ntok, pool);
+  compute_region_expr_bounding_box(&world, ev.region_expr.root, ev.region_llf, ev.region_urb);
+  const std::vector<Molecule> saved = p.molecules;
+  int computed = number;
+  ev.release_inside_regions(computed);
+  unsigned np = 0, nr = 0;
+  for (size_t i = saved.size(); i < p.molecules.size() && np < cap; i++, np++) {
+    pos[3 * np] = p.molecules[i].v.pos.x;
+    pos[3 * np + 1] = p.molecules[i].v.pos.y;
+    pos[3 * np + 2] = p.molecules[i].v.pos.z;
+  }
+  for (size_t i = 0; i < saved.size(); i++) {
+    if (p.molecules[i].is_defunct() && !saved[i].is_defunct()) {
+      removed[nr++] = (unsigned)i;
+    }
+  }
+  p.molecules = saved;
+  *n_pos = np;
+  *n_removed = nr;
+  *draws_used = world.rng.overrun ? 0xFFFFFFFFu : (unsigned)world.rng.used;
+  return computed;
 }
 
 // ReleaseEvent::release_ellipsoid_or_rectcuboid (release_event.cpp:953-1000) with the
@@ -395,7 +518,7 @@ int ref_inside_region(void* sp, unsigned obj, const double* pos) {
 // positions of the n molecules in release order; returns the draws used
 unsigned ref_release_ellipsoid_or_rectcuboid(int shape, unsigned n, const double* location, const double* diameter,
                                               const unsigned* draws, unsigned ndraws, double* out) {
-  WorldShim world;
+  World world;
   world.species.species.resize(1);
   world.rng.draws = draws;
   world.rng.n = ndraws;

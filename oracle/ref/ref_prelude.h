@@ -8,6 +8,20 @@
 #define ORACLE_REF_PRELUDE_H
 
 #include <cstdio>
+#include <cfloat>
+#include <ostream>
+#include <sstream>
+
+// logging and fatal errors of the release and region routines
+#define mcell_error(...) do { fprintf(stderr, __VA_ARGS__); } while (0)
+inline std::ostream& perf() {
+  static std::ostringstream sink;
+  sink.str("");
+  return sink;
+}
+#ifndef FLT_INVALID
+#define FLT_INVALID FLT_MAX
+#endif
 
 #define INLINE_ATTR __attribute__((always_inline))
 // only reached from find_boundaries_occluding_disk, which is dead with use_expanded_list

@@ -196,6 +196,7 @@ public:
   bool use_expanded_list = true;
   double length_unit = 0.01;
   double rcp_length_unit = 100;
+  double grid_density = 10000;
   void init_subpartition_edge_length();
 };
 
@@ -211,6 +212,7 @@ public:
   geometry_object_index_t index = 0;
   geometry_object_id_t id = 0;
   bool counted = false;  // a counted volume (is_counted_volume_or_compartment)
+  region_id_t encompassing_region_id = 0;
   bool is_counted_volume_or_compartment() const { return counted; }
 };
 
@@ -220,10 +222,21 @@ typedef std::map<subpart_index_t, small_vector<wall_index_t>> WallsPerSubpartMap
 // a closed region made of the walls of one geometry object (src4/geometry.h:186-320)
 class Region {
 public:
+  std::string name;
   std::map<wall_index_t, std::set<edge_index_t>> walls_and_edges;
   WallsPerSubpartMap walls_per_subpart;
   Vec3 bounding_box_llf, bounding_box_urb;
-  void initialize_volume_info_if_needed(const Partition&) { }
+  pos_t volume = 0;
+  bool volume_info_initialized = false;
+  bool region_is_manifold = true;
+  // the reference's (geometry.cpp:860), compiled from its source
+  void initialize_volume_info_if_needed(const Partition& p);
+  bool is_manifold() const { return region_is_manifold; }
+  pos_t get_volume() const { return volume; }
+  // the reference's waypoint test falls back to is_point_inside_region_no_waypoints
+  // where its ray meets an edge (geometry.cpp:1048-1090); the stand-in is that test,
+  // which decides the same for points that are not on the region's walls
+  bool is_point_inside(Partition& p, const Vec3& pos);
   const Vec3& get_bounding_box_llf() const { return bounding_box_llf; }
   const WallsPerSubpartMap& get_walls_per_subpart() const { return walls_per_subpart; }
   void compute_bounding_box(const Partition& p, Vec3& llf, Vec3& urb);
@@ -277,6 +290,12 @@ public:
   mutable ShimRng aux_rng;  // no draws: the routines that use it return on a re-try
 
   const GeometryObject& get_geometry_object(const geometry_object_index_t i) const { return geometry_objects[i]; }
+  GeometryObject& get_geometry_object(const geometry_object_index_t i) { return geometry_objects[i]; }
+  GeometryObject& get_geometry_object_by_id(const geometry_object_id_t id) { return geometry_objects[id]; }
+  std::map<region_id_t, Region> regions_by_id;
+  Region& get_region_by_id(const region_id_t id) { return regions_by_id.at(id); }
+  std::vector<Molecule>& get_molecules() { return molecules; }
+  void set_molecule_as_defunct(Molecule& m) { m.set_flag(MOLECULE_FLAG_DEFUNCT); }
   Molecule& add_volume_molecule(const Molecule& vm, const double) {
     molecules.push_back(vm);
     molecules.back().id = (molecule_id_t)(molecules.size() - 1);
@@ -360,25 +379,57 @@ public:
 enum class ReleaseShape { UNDEFINED = -1, SPHERICAL, SPHERICAL_SHELL, REGION, LIST, INITIAL_SURF_REGION };
 
 
-class WorldShim {
+class World {
 public:
   Partition partition;
+  Partition* outer = nullptr;  // a scene's partition instead of the own one
   SpeciesContainerShim species;
   ShimRng rng;
-  Partition& get_partition(const int) { return partition; }
+  SimulationConfig config;
+  Partition& get_partition(const int) { return outer ? *outer : partition; }
   const SpeciesContainerShim& get_all_species() const { return species; }
 };
 
+// boolean expressions of closed objects for releases (src4/region_expr.h:23-90)
+enum class RegionExprOperator { INVALID, UNION, INTERSECT, DIFFERENCE, LEAF_SURFACE_REGION, LEAF_GEOMETRY_OBJECT };
+class RegionExprNode {
+public:
+  RegionExprOperator op = RegionExprOperator::INVALID;
+  region_id_t region_id = 0;
+  geometry_object_id_t geometry_object_id = 0;
+  RegionExprNode* left = nullptr;
+  RegionExprNode* right = nullptr;
+};
+class RegionExpr {
+public:
+  RegionExprNode* root = nullptr;
+};
+
+enum class ReleaseNumberMethod { INVALID, CONST_NUM, GAUSS_NUM, VOL_NUM, CONCENTRATION_NUM, DENSITY_NUM };
+
 class ReleaseEvent {
 public:
-  WorldShim* world = nullptr;
+  World* world = nullptr;
+  std::string release_site_name = "release";
   ReleaseShape release_shape = ReleaseShape::SPHERICAL;
+  ReleaseNumberMethod release_number_method = ReleaseNumberMethod::CONST_NUM;
+  uint release_number = 0;
+  double concentration = 0;
+  std::vector<CummAreaPWallIndexPair> cumm_area_and_pwall_index_pairs;
+  RegionExpr region_expr;
+  Vec3 region_llf, region_urb;
   Vec3 location, diameter;
   species_id_t species_id = 0;
   double event_time = 0;
   double get_release_delay_time() const { return 0; }
   void schedule_for_immediate_diffusion_if_needed(const molecule_id_t) { }
   void release_ellipsoid_or_rectcuboid(int computed_release_number);
+  uint calculate_number_to_release();
+  uint num_vol_mols_from_conc(bool& exact_number);
+  int randomly_remove_molecules(Partition& p, const MoleculeIdsVector& mol_ids_in_region, int number_to_remove);
+  int vacuum_inside_regions(int number_to_remove);
+  bool is_point_inside_region_expr_recursively(Partition& p, const Vec3& pos, const RegionExprNode* region_expr_node);
+  void release_inside_regions(int& computed_release_number);
 };
 
 } // namespace MCell

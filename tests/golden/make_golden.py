@@ -208,10 +208,80 @@ def inside_fixtures(ref64):
           "edge re-tries", int(((cv >> 31) & 1).sum()), "region tests", np.unique(reg, return_counts=True))
 
 
+def region_fixtures(ref64):
+    """Releases into region expressions on H.regions_scene (star, box, small cube;
+    closed objects 0-2): Region::initialize_volume_info_if_needed (object volumes),
+    compute_region_expr_bounding_box, calculate_number_to_release by concentration, and
+    ReleaseEvent::release_inside_regions on injected streams: a number of molecules into
+    each expression of H.REGION_EXPRS, concentration releases into one object (exact)
+    and into expressions (approximate count), and vacuums (negative numbers) of species
+    0 from expressions (removed molecule indices)."""
+    rng = np.random.default_rng(20261206)
+    sc = H.regions_scene(rng)
+    h = ref64.scene(sc)
+    h.set_objects(sc.obj, [0, 0, 0])
+    vol = np.array([h.region_volume(o) for o in range(3)])
+    ex = H.REGION_EXPRS
+    tok = np.full((len(ex), 15), 99, np.int32)
+    for k, e in enumerate(ex):
+        tok[k, :len(e)] = e
+    ntok = np.array([len(e) for e in ex], np.int32)
+    bbox = np.array([np.concatenate(h.region_expr_bbox(e)) for e in ex])
+    dia = rng.uniform(1, 60, (40, 3))
+    conc = np.exp(rng.uniform(np.log(1e-6), np.log(1e-2), 40))
+    conc_n = np.array([ref64.number_from_concentration(d, c, 0.01) for d, c in zip(dia, conc)], np.int64)
+    # releases: (expression, method, number, concentration)
+    cases = [(k, 0, int(rng.integers(1, 60)), 0.0) for k in range(len(ex))]
+    cases += [(1, 1, 0, 2e-6), (0, 1, 0, 3e-7)]                      # one object: exact count
+    cases += [(3, 1, 0, 4e-7), (2, 1, 0, 1e-7), (6, 1, 0, 1e-7)]      # expressions: approximate
+    cases += [(2, 0, -150, 0.0), (5, 0, -40, 0.0), (0, 0, -100000, 0.0), (4, 0, -7, 0.0)]  # vacuums
+    nd = 40000
+    draws = rng.integers(0, 2 ** 32, size=(len(cases), nd), dtype=np.uint64).astype(np.uint32)
+    cap = 4000
+    r_pos = np.zeros((len(cases), cap, 3))
+    r_npos = np.zeros(len(cases), np.int64)
+    r_rem = np.zeros((len(cases), cap), np.int64)
+    r_nrem = np.zeros(len(cases), np.int64)
+    r_used = np.zeros(len(cases), np.int64)
+    r_computed = np.zeros(len(cases), np.int64)
+    for c, (k, method, number, cc) in enumerate(cases):
+        computed, pos, rem, used = h.release_inside_regions(ex[k], draws[c], number=number, species=0,
+                                                            concentration=cc if method else None)
+        assert used is not None and len(pos) <= cap and len(rem) <= cap, (c, used, len(pos))
+        r_computed[c] = computed
+        r_pos[c, :len(pos)] = pos
+        r_npos[c] = len(pos)
+        r_rem[c, :len(rem)] = rem
+        r_nrem[c] = len(rem)
+        r_used[c] = used
+    # the vacuums' candidates in order: a vacuum of more than there are removes them all
+    r_cand = np.zeros((len(cases), cap), np.int64)
+    r_ncand = np.zeros(len(cases), np.int64)
+    for c, (k, method, number, cc) in enumerate(cases):
+        if number < 0:
+            _, _, rem, _ = h.release_inside_regions(ex[k], draws[c], number=-(1 << 30), species=0)
+            r_cand[c, :len(rem)] = rem
+            r_ncand[c] = len(rem)
+    draws = draws[:, :int(r_used.max()) + 16]  # the draws the reference took, and a few more
+    case_arr = np.array([[k, m, n] for (k, m, n, _) in cases], np.int64)
+    case_conc = np.array([cc for (_, _, _, cc) in cases])
+    np.savez_compressed(
+        HERE / "regions.npz",
+        origin=sc.origin, partition_edge=sc.partition_edge, nsub=sc.nsub, rxn_radius=sc.rxn_radius, verts=sc.verts,
+        tris=sc.tris, obj=sc.obj, mol_pos=sc.mol_pos, mol_species=sc.mol_species, volumes=vol, expr=tok,
+        n_expr=ntok, bbox=bbox, conc_dia=dia, conc=conc, conc_n=conc_n, cases=case_arr, case_conc=case_conc,
+        draws=draws, computed=r_computed, pos=r_pos, n_pos=r_npos, removed=r_rem, n_removed=r_nrem, used=r_used,
+        candidates=r_cand, n_candidates=r_ncand)
+    print("regions: volumes", vol, "placed", r_npos.tolist(), "removed", r_nrem.tolist())
+
+
 def main():
     ref64 = H.reference(64)
     if ref64 is None:
         raise SystemExit("oracle/_ref/libmcell_ref64.so missing: run python oracle/ref/build_ref.py")
+    if sys.argv[1:] == ["regions"]:
+        region_fixtures(ref64)
+        return
     rng = np.random.default_rng(20261203)
     for name, sc in scenes(rng).items():
         cases = []
@@ -240,6 +310,7 @@ def main():
     print("rxn tests", (tb >= 0).sum(), "fired of", len(tb))
     pathway_fixtures(ref64)
     inside_fixtures(ref64)
+    region_fixtures(ref64)
 
 
 if __name__ == "__main__":

@@ -114,6 +114,13 @@ class Checker:
         c = np.ascontiguousarray(cum, np.float64)
         return self.fn("which_unimolecular")(ptr(c), _u(len(c)), _u(draw))
 
+    def number_from_concentration(self, diameter, concentration, length_unit_um):
+        """ReleaseEvent::calculate_number_to_release for a spherical concentration release."""
+        d = np.ascontiguousarray(diameter, np.float64)
+        f = self.fn("number_from_concentration")
+        f.restype = _u
+        return f(ptr(d), _d(concentration), _d(length_unit_um))
+
 
 class _Handle:
     def __init__(self, chk: Checker, h):
@@ -164,6 +171,37 @@ class _Handle:
         f = self.c.fn("inside_region")
         f.restype = ctypes.c_int
         return f(self.h, _u(obj), ptr(p))
+
+    def region_volume(self, obj):
+        """Region::initialize_volume_info_if_needed: the closed object's volume."""
+        f = self.c.fn("region_volume")
+        f.restype = _d
+        return f(self.h, _u(obj))
+
+    def region_expr_bbox(self, tokens):
+        """compute_region_expr_bounding_box of a postfix program (objects, -1 union,
+        -2 intersection, -3 difference): (llf, urb)."""
+        t = np.ascontiguousarray(tokens, np.int32)
+        lo, hi = np.zeros(3), np.zeros(3)
+        self.c.fn("region_expr_bbox")(self.h, ptr(t), _u(len(t)), ptr(lo), ptr(hi))
+        return lo, hi
+
+    def release_inside_regions(self, tokens, draws, number=0, species=0, concentration=None, length_unit_um=0.01,
+                               cap=100000):
+        """ReleaseEvent::release_inside_regions on injected draws: (computed number,
+        positions, removed molecule indices, draws used or None)."""
+        t = np.ascontiguousarray(tokens, np.int32)
+        dr = np.ascontiguousarray(draws, np.uint32)
+        pos = np.zeros((cap, 3))
+        rem = np.zeros(cap, np.uint32)
+        n_pos, n_rem, used = _u(), _u(), _u()
+        f = self.c.fn("release_inside_regions")
+        f.restype = ctypes.c_int
+        computed = f(self.h, ptr(t), _u(len(t)), ctypes.c_int(0 if concentration is None else 1),
+                     ctypes.c_int(number), _u(species), _d(concentration or 0.0), _d(length_unit_um), ptr(dr),
+                     _u(len(dr)), ptr(pos), _u(cap), ctypes.byref(n_pos), ptr(rem), ctypes.byref(n_rem),
+                     ctypes.byref(used))
+        return (computed, pos[:n_pos.value], rem[:n_rem.value], None if used.value == 0xFFFFFFFF else used.value)
 
     def diffuse_case(self, mol, disp, draws, r_rate_factor=1.0, t_steps=1.0):
         out = np.zeros(RES_SIZE)
@@ -305,6 +343,31 @@ def star_scene(rng, n_mol=200, levels=3):
                np.array([2.0, 2.0, 1.414213562373095]), wc, np.array([[0, 1]], np.uint32), np.array([0.0]), pos, sp)
     sc.obj = np.asarray(obj, np.uint32)
     return sc
+
+
+def regions_scene(rng, n_mol=3000):
+    """Three closed objects for region releases: the non-convex star (object 0, radius
+    0.45 um), the 1.2 um reflective box (object 1) and a 0.4 um cube centred at
+    (0.2531, 0.2017, 0.1493) um (object 2) that overlaps the star; molecules uniform in the box."""
+    lu = conversion.length_unit_um()
+    sv, sw = geometry.create_star_sphere(0.45, 3)
+    bv, bw = geometry.create_box(edge_dimension=1.2)
+    cv, cw = geometry.create_box(edge_dimension=0.4)
+    cv = cv + np.array([0.2531, 0.2017, 0.1493])
+    v, w, obj = geometry.merge_meshes((sv, sw), (bv, bw), (cv, cw))
+    lay = conversion.partition_layout(v.min(0), v.max(0), partition_dimension_um=1.3, subpartition_dimension_um=0.1)
+    wc = np.zeros((len(w), 3), np.uint8)
+    half = 0.6 / lu
+    pos = rng.uniform(-half, half, size=(n_mol, 3))
+    sp = rng.integers(0, 2, size=n_mol).astype(np.uint32)
+    sc = Scene(np.array(lay.origin), lay.edge, lay.nsub, conversion.default_rxn_radius_um() / lu, v / lu, w,
+               np.array([2.0, 2.0, 1.414213562373095]), wc, np.array([[0, 1]], np.uint32), np.array([0.0]), pos, sp)
+    sc.obj = np.asarray(obj, np.uint32)
+    return sc
+
+
+# region expressions of the region fixture (postfix; -1 union, -2 intersection, -3 difference)
+REGION_EXPRS = [[0], [2], [1, 0, -3], [0, 2, -1], [0, 2, -2], [2, 0, -3], [1, 0, -3, 2, -1]]
 
 
 def load_golden(name):
