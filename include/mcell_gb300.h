@@ -395,6 +395,10 @@ int mcg_vacuum_select(uint32_t m, uint32_t n_remove, const uint32_t* draws, uint
 int mcg_release_region(mcg_engine* e, uint32_t species, int method, int64_t number, double concentration_molar,
                        double length_unit_um, const int32_t* expr, uint32_t n_expr, uint64_t release_seed,
                        int64_t* done);
+/* The same for one replica of a batch (the objects of that replica's model). */
+int mcg_batch_release_region(mcg_batch* b, uint32_t replica, uint32_t species, int method, int64_t number,
+                             double concentration_molar, double length_unit_um, const int32_t* expr, uint32_t n_expr,
+                             uint64_t release_seed, int64_t* done);
 /* Parity harness of release_inside_regions (test infrastructure): the positions the
    release above would place, computed in one device thread from one injected stream of
    32-bit draws as the reference's generator would be consumed (number < 0: the indices,

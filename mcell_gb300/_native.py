@@ -39,7 +39,7 @@ EXPORTS = [
     "mcg_get_fallbacks", "mcg_set_trace_limits", "mcg_batch_get_fallbacks", "mcg_reaction_decisions",
     "mcg_inside_tests", "mcg_release_positions",
     "mcg_object_volume", "mcg_region_expr_bbox", "mcg_release_number_from_concentration", "mcg_vacuum_select",
-    "mcg_release_region", "mcg_release_region_harness",
+    "mcg_release_region", "mcg_release_region_harness", "mcg_batch_release_region",
 ]
 REGION_OPS = {"union": -1, "intersect": -2, "difference": -3}
 MAX_PATHWAYS = 4
@@ -648,6 +648,25 @@ class Batch:
         n = ctypes.c_uint32()
         self._chk(lib().mcg_batch_get_escapes(self.h, ctypes.c_uint32(8), _p(out), ctypes.byref(n)))
         return out[:min(n.value, 8)], n.value
+
+    def release(self, rep, species, n, shape="sphere", center=(0, 0, 0), diameter=(1, 1, 1), obj=0, seed=1):
+        """mcg_batch_release into replica rep."""
+        shapes = {"sphere": 0, "cuboid": 1, "shell": 2, "inside": 3}
+        c = np.ascontiguousarray(center, np.float64)
+        d = np.ascontiguousarray(diameter, np.float64)
+        self._chk(lib().mcg_batch_release(self.h, ctypes.c_uint32(rep), ctypes.c_uint32(species), ctypes.c_uint64(n),
+                                          ctypes.c_int(shapes[shape]), _p(c), _p(d), ctypes.c_uint32(obj),
+                                          ctypes.c_uint64(seed)))
+
+    def release_region(self, rep, species, tokens, number=0, concentration=None, length_unit_um=0.01, seed=1):
+        """mcg_batch_release_region into (or a vacuum from) replica rep's region expression."""
+        ex = region_expr(tokens)
+        done = ctypes.c_int64()
+        self._chk(lib().mcg_batch_release_region(
+            self.h, ctypes.c_uint32(rep), ctypes.c_uint32(species), ctypes.c_int(0 if concentration is None else 1),
+            ctypes.c_int64(number), ctypes.c_double(concentration or 0.0), ctypes.c_double(length_unit_um), _p(ex),
+            ctypes.c_uint32(len(ex)), ctypes.c_uint64(seed), ctypes.byref(done)))
+        return done.value
 
     def diffuse_blocks_per_sm(self):
         v = ctypes.c_int()

@@ -357,6 +357,17 @@ int mcg_batch_release(mcg_batch* b, uint32_t replica, uint32_t species, uint64_t
   return rc ? bfail(b, rc, err) : MCG_OK;
 }
 
+int mcg_batch_release_region(mcg_batch* b, uint32_t replica, uint32_t species, int method, int64_t number,
+                             double concentration_molar, double length_unit_um, const int32_t* expr, uint32_t n_expr,
+                             uint64_t release_seed, int64_t* done) {
+  if (!b || !expr || !done) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  std::string err;
+  int rc = b->dev->release_region(replica, species, method, number, concentration_molar, length_unit_um, expr, n_expr,
+                                  release_seed, done, err);
+  return rc ? bfail(b, rc, err) : MCG_OK;
+}
+
 int mcg_batch_get_escapes(mcg_batch* b, uint32_t cap, double* out, uint32_t* n) {
   if (!b || !n || (cap && !out)) return MCG_ERR_ARG;
   if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");

@@ -129,3 +129,33 @@ def test_invalid_region_release_is_refused():
     with pytest.raises(_native.EngineError):
         e.release_region(7, [0], number=10)  # no such species
     e.close()
+
+
+def _handle(precision, seed):
+    h = _native.Engine(precision, G["origin"], float(G["partition_edge"]), int(G["nsub"]), float(G["rxn_radius"]), 3,
+                       seed=seed)
+    h.set_species([2.0, 2.0, 1.414213562373095])
+    h.upload_mesh(G["verts"], G["tris"], np.zeros((len(G["tris"]), 3), np.uint8))
+    h.set_wall_objects(G["obj"])
+    h.add_molecules(G["mol_pos"], G["mol_species"])
+    return h
+
+
+def test_batch_release_into_one_replica():
+    b = _native.Batch("fp32", 3, 2)
+    hs = [_handle("fp32", 1), _handle("fp32", 2)]
+    ids = b.add(hs)
+    for h in hs:
+        h.close()
+    def species_counts(r):
+        return np.bincount(b.molecules(r)[1], minlength=3)
+
+    c0, c1 = species_counts(ids[0]), species_counts(ids[1])
+    assert b.release_region(ids[1], 2, [1, 0, -3], number=300, seed=5) == 300
+    removed = -b.release_region(ids[0], 0, [2, 0, -3], number=-5, seed=6)
+    assert removed == 5
+    assert (species_counts(ids[1]) - c1).tolist() == [0, 0, 300]
+    assert (c0 - species_counts(ids[0])).tolist() == [5, 0, 0]
+    b.step(2)
+    b.sync()
+    b.close()
