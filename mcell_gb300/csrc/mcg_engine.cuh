@@ -272,14 +272,18 @@ class DeviceEngineT : public DeviceEngine {
     if (cap_ == 0 && ensure_capacity(1024, err)) return -2;
     uint32_t done = 0;
     while (done < n) {
-      if (n - done >= 2 && use_graphs_ && !profile_) {
-        cudaGraphExec_t& ge = graph_[parity_];
+      if (use_graphs_ && !profile_) {
+        // two iterations return to the same parity; a single one (a caller stepping one
+        // iteration at a time) flips it
+        const int k = n - done >= 2 ? 2 : 1;
+        cudaGraphExec_t& ge = graph_[parity_ + 2 * (k - 1)];
         if (!ge) {
-          if (capture(parity_, err)) return -2;
+          if (capture(parity_, k, err)) return -2;
         }
         MCG_CUDA(cudaGraphLaunch(ge, stream_));
-        launches_ += 2 * kernels_per_iteration_;
-        done += 2;  // two iterations return to the same parity
+        launches_ += (uint64_t)k * kernels_per_iteration_;
+        done += k;
+        if (k == 1) parity_ ^= 1;
       } else {
         launch_iteration(state(parity_), profile_);
         MCG_CUDA(cudaGetLastError());
@@ -1693,21 +1697,22 @@ class DeviceEngineT : public DeviceEngine {
     launches_ += kernels_per_iteration_;
   }
 
-  int capture(int parity, std::string& err) {
+  // graph of `iters` (1 or 2) iterations starting at `parity`
+  int capture(int parity, int iters, std::string& err) {
     cudaGraph_t gr;
     MCG_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     uint64_t l0 = launches_;
     launch_iteration(state(parity));
-    launch_iteration(state(parity ^ 1));
+    if (iters == 2) launch_iteration(state(parity ^ 1));
     launches_ = l0;
     MCG_CUDA(cudaStreamEndCapture(stream_, &gr));
-    MCG_CUDA(cudaGraphInstantiate(&graph_[parity], gr, 0));
+    MCG_CUDA(cudaGraphInstantiate(&graph_[parity + 2 * (iters - 1)], gr, 0));
     cudaGraphDestroy(gr);
     return 0;
   }
 
   void invalidate_graphs() {
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < 4; k++) {
       if (graph_[k]) cudaGraphExecDestroy(graph_[k]);
       graph_[k] = nullptr;
     }
@@ -1755,7 +1760,7 @@ class DeviceEngineT : public DeviceEngine {
   bool use_graphs_ = true;
   bool profile_ = false;
   std::vector<std::array<cudaEvent_t, 5>> prof_;
-  cudaGraphExec_t graph_[2] = {nullptr, nullptr};
+  cudaGraphExec_t graph_[4] = {nullptr, nullptr, nullptr, nullptr};  // [parity + 2 * (iterations - 1)]
   uint32_t nsp_ = 0, max_rep_ = 0, nkeys_ = 0, key_alloc_ = 0, ntiles_ = 0, traj_cap_ = 65536;
   uint64_t cap_ = 0, iterations_ = 0, launches_ = 0;
   uint64_t rebin_it_ = 0;  // engine iteration of the last re-sort (counts then come from the starts)
