@@ -160,8 +160,10 @@ class DeviceEngineT : public DeviceEngine {
     }
     uint64_t n_new = 0;
     for (uint32_t k = 0; k < n; k++) n_new += specs[k].n_mol;
-    std::unique_ptr<Product<T>[]> stage(new Product<T>[n_new]);  // filled below (no zeroing of 40 B/molecule)
-    uint64_t staged = 0;
+    if (cnt_.n_live + n_new > 0xFFFFFFF0ull) {
+      err = "too many molecules for 32-bit indices";
+      return -3;
+    }
     // any failure before the re-sort leaves the engine as it was: the new slots are
     // freed and the key space laid out again without them (it needs no new memory then)
     auto undo = [&](int rc) {
@@ -174,9 +176,6 @@ class DeviceEngineT : public DeviceEngine {
       const ReplicaSpec& sp = specs[k];
       const uint32_t r = slots[k];
       int rc = upload_replica(sp, r, err);
-      if (rc) return undo(rc);
-      rc = stage_molecules(r, sp.n_mol, sp.pos, sp.species, 0, stage.get() + staged, err);
-      staged += sp.n_mol;
       if (rc) return undo(rc);
       reps_[r].next_uid = sp.n_mol;
       out_reps[k] = r;
@@ -198,7 +197,14 @@ class DeviceEngineT : public DeviceEngine {
     }
     int rc = layout_keys(err);
     if (rc) return undo(rc);
-    return rebin(stage.get(), n_new, err, true);
+    // the molecules, staged on the device once the replicas' grids are there
+    uint64_t staged = 0;
+    for (uint32_t k = 0; k < n; k++) {
+      rc = stage_on_device(slots[k], specs[k].n_mol, specs[k].pos, specs[k].species, 0, staged, err);
+      if (rc) return undo(rc);
+      staged += specs[k].n_mol;
+    }
+    return rebin(nullptr, n_new, err, true);
   }
 
   // counted-volume count arrays (allocated when the first replica counts a volume)
@@ -254,12 +260,49 @@ class DeviceEngineT : public DeviceEngine {
       err = "no such replica";
       return -1;
     }
-    std::unique_ptr<Product<T>[]> stage(new Product<T>[n]);  // filled by stage_molecules
-    int rc = stage_molecules(rep, n, pos, species, uid0, stage.get(), err);
+    if (read_counters(err)) return -2;
+    if (cnt_.n_live + n > 0xFFFFFFF0ull) {
+      err = "too many molecules for 32-bit indices";
+      return -3;
+    }
+    if (cnt_.n_live + n > cap_ && ensure_capacity(std::max<uint64_t>((cnt_.n_live + n) * 3 / 2, 1024), err))
+      return -2;
+    if (n > base_.prod_cap && ensure_prod(n, err)) return -2;
+    int rc = stage_on_device(rep, n, pos, species, uid0, 0, err);
     if (rc) return rc;
     reps_[rep].next_uid = std::max<uint64_t>(reps_[rep].next_uid, uid0 + n);
-    if (read_counters(err)) return -2;
-    return rebin(stage.get(), n, err, true);
+    return rebin(nullptr, n, err, true);
+  }
+
+  // host molecule arrays staged into the product list at `offset` on the device
+  // (k_stage_upload); the input is checked before anything is kept
+  int stage_on_device(uint32_t r, uint64_t n, const double* pos, const uint32_t* species, uint64_t uid0,
+                      uint64_t offset, std::string& err) {
+    if (n == 0) return 0;
+    AllocSet tmp;
+    double* d_pos;
+    uint32_t *d_sp, *d_err;
+    MCG_CUDA(tmp.get(&d_pos, sizeof(double) * 3 * n));
+    MCG_CUDA(tmp.get(&d_sp, sizeof(uint32_t) * n));
+    MCG_CUDA(tmp.get(&d_err, sizeof(uint32_t)));
+    MCG_CUDA(cudaMemcpyAsync(d_pos, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, stream_));
+    MCG_CUDA(cudaMemcpyAsync(d_sp, species, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, stream_));
+    MCG_CUDA(cudaMemsetAsync(d_err, 0, sizeof(uint32_t), stream_));
+    k_stage_upload<T><<<grid(n), TPB, 0, stream_>>>(state(parity_), r, (uint32_t)n, d_pos, d_sp, uid0,
+                                                     (uint32_t)offset, nsp_, d_err);
+    launches_ += 1;
+    MCG_CUDA(cudaGetLastError());
+    uint32_t bad = 0;
+    MCG_CUDA(d2h(&bad, d_err, sizeof(uint32_t)));
+    if (bad & 1u) {
+      err = "species index out of range";
+      return -1;
+    }
+    if (bad & 2u) {
+      err = "molecule outside the partition";
+      return -4;
+    }
+    return 0;
   }
 
   int step(uint32_t n, std::string& err) override {

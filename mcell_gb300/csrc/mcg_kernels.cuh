@@ -1162,6 +1162,61 @@ __global__ void k_release(State<T> s, ReleaseDesc r) {
   }
 }
 
+// Molecules uploaded from host arrays (positions in fp64, species), staged into the
+// product list at `offset` for the re-binning: checked (species, inside the partition),
+// and in fp32 moved off any wall plane of their subpartition they lie within
+// max(1e-4, 8 fp32 ulps of the coordinates) of, to that distance on their own side
+// (twice, for edges and corners), in fp64 without fused multiply-adds. err bit 0: a
+// species out of range, bit 1: a molecule outside the partition.
+template <typename T>
+__global__ void k_stage_upload(State<T> s, uint32_t rep, uint32_t n, const double* pos, const uint32_t* species,
+                               uint64_t uid0, uint32_t offset, uint32_t nsp, uint32_t* err) {
+  const Geo<T>& g = s.geos[rep];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t sp = species[i];
+    double p[3] = {pos[3 * (size_t)i], pos[3 * (size_t)i + 1], pos[3 * (size_t)i + 2]};
+    if (sp >= nsp) {
+      atomicOr(err, 1u);
+      continue;
+    }
+    if (!(p[0] >= (double)g.origin.x && p[1] >= (double)g.origin.y && p[2] >= (double)g.origin.z &&
+          p[0] < (double)g.opposite.x && p[1] < (double)g.opposite.y && p[2] < (double)g.opposite.z)) {
+      atomicOr(err, 2u);
+      continue;
+    }
+    if (sizeof(T) == 4 && g.w64) {
+      int ix[3];
+      for (int a = 0; a < 3; a++)
+        ix[a] = min(max((int)__dmul_rn(__dsub_rn(p[a], g.origin64[a]), g.sp_rcp64), 0), g.nsub - 1);
+      const uint32_t c = (uint32_t)ix[0] + (uint32_t)ix[1] * (uint32_t)g.nsub + (uint32_t)ix[2] * (uint32_t)g.nsub2;
+      const double mag = fmax(fabs(p[0]), fmax(fabs(p[1]), fabs(p[2])));
+      const double margin = fmax(1e-4, __dmul_rn(__dmul_rn(8.0, mag), 1.1920928955078125e-07));
+      for (int pass = 0; pass < 2; pass++) {
+        bool moved = false;
+        for (uint32_t k = g.wsp_off[c]; k < g.wsp_off[c + 1]; k++) {
+          const double* pl = g.w64 + 16 * (size_t)g.wsp_list[k];
+          const double dd = __dsub_rn(
+              __dadd_rn(__dadd_rn(__dmul_rn(pl[0], p[0]), __dmul_rn(pl[1], p[1])), __dmul_rn(pl[2], p[2])), pl[3]);
+          if (fabs(dd) >= margin) continue;
+          const double shift = __dsub_rn(dd >= 0 ? margin : -margin, dd);
+          for (int a = 0; a < 3; a++) p[a] = __dadd_rn(p[a], __dmul_rn(shift, pl[a]));
+          moved = true;
+        }
+        if (!moved) break;
+      }
+    }
+    Product<T> m;
+    m.pos.x = (T)p[0];
+    m.pos.y = (T)p[1];
+    m.pos.z = (T)p[2];
+    set_meta(m.pos, make_meta(sp, rep, META_SCHEDULE_UNIMOL));
+    m.birth = 0;
+    m.uid = uid0 + i;
+    m.tuni = TIME_FOREVER;
+    s.prod[offset + i] = m;
+  }
+}
+
 // the molecules of a species of replica rep inside a region (vacuum_inside_regions,
 // release_event.cpp:864-896: the species, the region's bounding box, then the region's
 // inside tests): their ids and indices, in no particular order
