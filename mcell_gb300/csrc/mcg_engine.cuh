@@ -335,23 +335,46 @@ class DeviceEngineT : public DeviceEngine {
       }
     }
     iterations_ += n;
+    pending_iters_ += n;
     return 0;
   }
 
   int sync(std::string& err) override {
-    MCG_CUDA(cudaStreamSynchronize(stream_));
+    // the counters' copy is ordered after all queued work and waited for: one round trip
     if (read_counters(err)) return -2;
     return status_to_error(cnt_.status, err);
   }
 
   int counts(uint32_t rep, uint64_t* out, std::string& err) override {
-    int rc = sync(err);
-    if (rc) return rc;
     if (rep >= max_rep_ || !reps_[rep].used) {
       err = "no such replica";
       return -1;
     }
     const Geo<T>& g = geos_h_[rep];
+    {
+      // one round trip: the counters and the row the queued iterations will have
+      // written (each iteration advances the engine's iteration by one), then checked
+      const uint64_t it = (uint64_t)cnt_.iteration + pending_iters_;
+      if (it > g.it0 && it > rebin_it_ && it <= 0xFFFFFFFFull) {
+        const uint64_t row = (it - 1) % traj_cap_;
+        unsigned long long h[MAXSP];
+        Counters c;
+        MCG_CUDA(cudaMemcpyAsync(&c, d_cnt_, sizeof(Counters), cudaMemcpyDeviceToHost, stream_));
+        MCG_CUDA(cudaMemcpyAsync(h, d_traj_ + (row * max_rep_ + rep) * nsp_, sizeof(unsigned long long) * nsp_,
+                                 cudaMemcpyDeviceToHost, stream_));
+        MCG_CUDA(cudaStreamSynchronize(stream_));
+        cnt_ = c;
+        pending_iters_ = 0;
+        int rc = status_to_error(cnt_.status, err);
+        if (rc) return rc;
+        if (cnt_.iteration == it) {
+          for (uint32_t a = 0; a < nsp_; a++) out[a] = h[a];
+          return 0;
+        }
+      }
+    }
+    int rc = sync(err);
+    if (rc) return rc;
     if (cnt_.iteration > g.it0 && cnt_.iteration > rebin_it_) {
       // species counts of the last finished iteration (k_end)
       const uint64_t row = (cnt_.iteration - 1) % traj_cap_;
@@ -1573,6 +1596,7 @@ class DeviceEngineT : public DeviceEngine {
 
   int read_counters(std::string& err) {
     MCG_CUDA(d2h(&cnt_, d_cnt_, sizeof(Counters)));
+    pending_iters_ = 0;
     return 0;
   }
 
@@ -1804,6 +1828,7 @@ class DeviceEngineT : public DeviceEngine {
   bool profile_ = false;
   std::vector<std::array<cudaEvent_t, 5>> prof_;
   cudaGraphExec_t graph_[4] = {nullptr, nullptr, nullptr, nullptr};  // [parity + 2 * (iterations - 1)]
+  uint64_t pending_iters_ = 0;  // iterations queued since the counters were last read
   uint32_t nsp_ = 0, max_rep_ = 0, nkeys_ = 0, key_alloc_ = 0, ntiles_ = 0, traj_cap_ = 65536;
   uint64_t cap_ = 0, iterations_ = 0, launches_ = 0;
   uint64_t rebin_it_ = 0;  // engine iteration of the last re-sort (counts then come from the starts)
