@@ -1191,15 +1191,26 @@ __global__ void k_stage_upload(State<T> s, uint32_t rep, uint32_t n, const doubl
       const uint32_t c = (uint32_t)ix[0] + (uint32_t)ix[1] * (uint32_t)g.nsub + (uint32_t)ix[2] * (uint32_t)g.nsub2;
       const double mag = fmax(fabs(p[0]), fmax(fabs(p[1]), fabs(p[2])));
       const double margin = fmax(1e-4, __dmul_rn(__dmul_rn(8.0, mag), 1.1920928955078125e-07));
+      // fp32 screen first (GB300's FP64 rate is low): the fp32 distance is within
+      // 1e-4 + 1e-6 * |p| of the fp64 one, so a wall farther than that beyond the margin
+      // cannot be within it
+      const float screen = (float)(margin + 1e-3 + 1e-5 * mag);
       for (int pass = 0; pass < 2; pass++) {
         bool moved = false;
+        float px = (float)p[0], py = (float)p[1], pz = (float)p[2];
         for (uint32_t k = g.wsp_off[c]; k < g.wsp_off[c + 1]; k++) {
-          const double* pl = g.w64 + 16 * (size_t)g.wsp_list[k];
+          const uint32_t wi = g.wsp_list[k];
+          const P4<T> rj = g.wrej[wi];
+          if (fabsf((float)rj.x * px + (float)rj.y * py + (float)rj.z * pz - (float)rj.w) > screen) continue;
+          const double* pl = g.w64 + 16 * (size_t)wi;
           const double dd = __dsub_rn(
               __dadd_rn(__dadd_rn(__dmul_rn(pl[0], p[0]), __dmul_rn(pl[1], p[1])), __dmul_rn(pl[2], p[2])), pl[3]);
           if (fabs(dd) >= margin) continue;
           const double shift = __dsub_rn(dd >= 0 ? margin : -margin, dd);
           for (int a = 0; a < 3; a++) p[a] = __dadd_rn(p[a], __dmul_rn(shift, pl[a]));
+          px = (float)p[0];
+          py = (float)p[1];
+          pz = (float)p[2];
           moved = true;
         }
         if (!moved) break;
