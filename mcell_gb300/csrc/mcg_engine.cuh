@@ -324,7 +324,7 @@ class DeviceEngineT : public DeviceEngine {
           if (capture(parity_, k, err)) return -2;
         }
         MCG_CUDA(cudaGraphLaunch(ge, stream_));
-        launches_ += (uint64_t)k * kernels_per_iteration_;
+        launches_ += (uint64_t)k * kernels_per_iteration();
         done += k;
         if (k == 1) parity_ ^= 1;
       } else {
@@ -1081,7 +1081,8 @@ class DeviceEngineT : public DeviceEngine {
     if (launches) *launches = launches_;
   }
 
-  static constexpr int kernels_per_iteration_ = 15 + 3 * GRID_REDO_ROUNDS;
+  int kernels_per_iteration() const { return (prod_chain_ ? 15 : 13) + 3 * GRID_REDO_ROUNDS; }
+  bool prod_chain_ = true;  // two products passes (layout_keys decides)
 
  private:
   // host view of one replica slot
@@ -1109,6 +1110,7 @@ class DeviceEngineT : public DeviceEngine {
     std::vector<uint64_t> init_world, init_cv;
     std::vector<double> obj_llf, obj_urb;  // bounding box of each object's walls
     std::vector<double> obj_vol;           // volume of each closed object
+    bool uni_products = false;             // some unimolecular reaction has products
     // host copies for placing fp32 molecules: wall planes (n xyz, d), walls per
     // subpartition, and the grid
     std::vector<double> planes;
@@ -1285,6 +1287,11 @@ class DeviceEngineT : public DeviceEngine {
     for (uint32_t w = 0; w < nw; w++)
       for (uint32_t a = 0; a < ch.nsp; a++)
         if (wall_class[(size_t)w * ch.nsp + a]) c.can_volwall[a] = 1;
+    // a unimolecular reaction with products: a product can make products in its birth step
+    R.uni_products = false;
+    for (uint32_t a = 0; a < ch.nsp; a++)
+      for (int k = 0; k < (int)ch.uni_npw[a]; k++)
+        if (ch.uni_prod[a][k][0] >= 0 || ch.uni_prod[a][k][1] >= 0) R.uni_products = true;
     R.used = true;  // from here on free_replica() releases what was allocated
     if (alloc_copy(&R.wrej, rej, R.bytes, err) || alloc_copy(&R.wface, face, R.bytes, err) ||
         alloc_copy(&R.wsp_off, hs.wsp_off, R.bytes, err) || alloc_copy(&R.wsp_list, ent, R.bytes, err) ||
@@ -1442,6 +1449,10 @@ class DeviceEngineT : public DeviceEngine {
   // first in the key space: the persistent diffuse warps take molecules in key
   // order, so the slow ones start early instead of forming the kernel's tail.
   int layout_keys(std::string& err) {
+    // the second products pass (products of products' unimolecular reactions in their
+    // birth step) only where some replica's chemistry can make them
+    prod_chain_ = false;
+    for (uint32_t r = 0; r < max_rep_; r++) prod_chain_ = prod_chain_ || (reps_[r].used && reps_[r].uni_products);
     std::vector<uint32_t> order;
     for (uint32_t r = 0; r < max_rep_; r++) order.push_back(r);
     std::stable_sort(order.begin(), order.end(), [this](uint32_t a, uint32_t b) {
@@ -1752,8 +1763,10 @@ class DeviceEngineT : public DeviceEngine {
     k_prod_window<T><<<1, 1, 0, stream_>>>(s);
     k_products<T><<<2 * gs, TPB, 0, stream_>>>(s);
     k_prod_window<T><<<1, 1, 0, stream_>>>(s);
-    k_products<T><<<2 * gs, TPB, 0, stream_>>>(s);
-    k_prod_window<T><<<1, 1, 0, stream_>>>(s);
+    if (prod_chain_) {
+      k_products<T><<<2 * gs, TPB, 0, stream_>>>(s);
+      k_prod_window<T><<<1, 1, 0, stream_>>>(s);
+    }
     mark(3, prof);
     k_scan_tiles<T><<<ntiles_, TPB, 0, stream_>>>(s);
     k_scan_top<T><<<1, TPB, 0, stream_>>>(s, ntiles_);
@@ -1761,7 +1774,7 @@ class DeviceEngineT : public DeviceEngine {
     k_scatter<T><<<g, TPB, 0, stream_>>>(s, 1);
     k_end<T><<<1, TPB, 0, stream_>>>(s);
     mark(4, prof);
-    launches_ += kernels_per_iteration_;
+    launches_ += kernels_per_iteration();
   }
 
   // graph of `iters` (1 or 2) iterations starting at `parity`
