@@ -1377,7 +1377,7 @@ __device__ __forceinline__ void occupants_of(const Geo<T>& g, const Cells<T>& ce
           if (d < 0) continue;
           if (d > movelen2) continue;
           const T dirlen2 = dot_rn(dir, dir);
-          if (sub_rn(mul_rn(movelen2, dirlen2), mul_rn(d, d)) > mul_rn(movelen2, sigma2)) continue;
+          if (misses_disk(movelen2, dirlen2, d, sigma2)) continue;
           if (j == self) continue;
           if (cells.dead && cells.dead[j] == 2) continue;
           VV<T> c;

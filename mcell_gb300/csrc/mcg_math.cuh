@@ -53,21 +53,32 @@ template <typename T>
 __host__ __device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {
   return v3<T>(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
 }
-// Round-to-nearest products and sums that the compiler may not fuse into a
-// multiply-add. The fp32 translation unit allows fused multiply-adds; the partner
-// geometry (walk crossings, neighbour tests, octant bounds, the closest-approach test)
-// is written with these, so that every code path that builds a segment's candidates —
+// Round-to-nearest products and sums that the compiler may not fuse or reassociate on
+// its own. The fp32 translation unit allows fused multiply-adds; the partner geometry
+// (walk crossings, neighbour tests, octant bounds, the closest-approach test) is
+// written with these, so that every code path that builds a segment's candidates —
 // the fast mask, the list, the refilled pages of the exact fallbacks — rounds alike.
-// (In the fp64 unit, built without fused multiply-adds, they are the plain operations.)
+// In fp32 the dot product and the closest-approach test fuse explicitly (fewer
+// instructions, one rounding per fused step); in fp64 (the unit built without fused
+// multiply-adds) every operation rounds on its own, as the reference's do.
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
-template <typename T>
-__device__ __forceinline__ T dot_rn(V3<T> a, V3<T> b) {
-  return add_rn(add_rn(mul_rn(a.x, b.x), mul_rn(a.y, b.y)), mul_rn(a.z, b.z));
+__device__ __forceinline__ float dot_rn(V3<float> a, V3<float> b) {
+  return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x)));
+}
+__device__ __forceinline__ double dot_rn(V3<double> a, V3<double> b) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), __dmul_rn(a.z, b.z));
+}
+// collide_mol's miss test movelen2 * dirlen2 - d * d > movelen2 * sigma2
+__device__ __forceinline__ bool misses_disk(float movelen2, float dirlen2, float d, float sigma2) {
+  return __fmaf_rn(movelen2, dirlen2, -__fmul_rn(d, d)) > __fmul_rn(movelen2, sigma2);
+}
+__device__ __forceinline__ bool misses_disk(double movelen2, double dirlen2, double d, double sigma2) {
+  return __dsub_rn(__dmul_rn(movelen2, dirlen2), __dmul_rn(d, d)) > __dmul_rn(movelen2, sigma2);
 }
 
 template <typename T>
