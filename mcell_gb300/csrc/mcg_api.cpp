@@ -414,6 +414,8 @@ int mcg_release_region(mcg_engine* e, uint32_t species, int method, int64_t numb
   int rc = e->dev->release_region(0, species, method, number, concentration_molar, length_unit_um, expr, n_expr,
                                   release_seed, done, err);
   if (rc) return fail(e, rc, err);
+  // the ids the release gave out (one per draw of a single-draw release, placed or not)
+  e->next_uid = std::max<uint64_t>(e->next_uid, e->dev->next_molecule_id(0));
   return MCG_OK;
 }
 

@@ -693,6 +693,10 @@ class DeviceEngineT : public DeviceEngine {
     return 0;
   }
 
+  uint64_t next_molecule_id(uint32_t rep) override {
+    return rep < max_rep_ && reps_[rep].used ? reps_[rep].next_uid : 0;
+  }
+
   int release_region_harness(uint32_t rep, uint32_t species, int method, int64_t number, double concentration,
                              double length_unit, const int32_t* expr, uint32_t n_expr, const uint32_t* draws,
                              uint32_t n_draws, double* pos, uint32_t cap, uint32_t* n_pos, uint64_t* removed,

@@ -140,6 +140,8 @@ class DeviceEngine {
   virtual int release_region(uint32_t rep, uint32_t species, int method, int64_t number, double concentration,
                              double length_unit, const int32_t* expr, uint32_t n_expr, uint64_t seed,
                              int64_t* done, std::string& err) = 0;
+  // the id the replica's next new molecule gets
+  virtual uint64_t next_molecule_id(uint32_t rep) = 0;
   virtual int release_region_harness(uint32_t rep, uint32_t species, int method, int64_t number,
                                      double concentration, double length_unit, const int32_t* expr, uint32_t n_expr,
                                      const uint32_t* draws, uint32_t n_draws, double* pos, uint32_t cap,

@@ -95,6 +95,10 @@ def test_release_into_an_expression(precision):
     before = len(e.molecules()[2])
     done = e.release_region(0, _expr(k), concentration=float(G["case_conc"][c]), seed=5)
     assert 0 < done <= n_draws and len(e.molecules()[2]) == before + done
+    # molecules added afterwards get ids of their own
+    e.add_molecules(G["mol_pos"][:10], G["mol_species"][:10])
+    ids = e.molecules()[2]
+    assert len(np.unique(ids)) == len(ids)
     e.step(3)
     e.sync()
     e.close()
