@@ -57,3 +57,20 @@ def test_invalid_region_expressions_are_refused():
             _native.region_expr_bbox(v, w, o, bad)
     with pytest.raises(_native.EngineError):
         _native.release_number_from_concentration([10, 10, 10], -1.0, 0.01)
+
+
+def test_region_entry_points_check_their_arguments():
+    import ctypes
+    L = _native.lib()
+    n = ctypes.c_uint32()
+    assert L.mcg_vacuum_select(ctypes.c_uint32(3), ctypes.c_uint32(1), None, ctypes.c_uint32(0), None,
+                               ctypes.byref(n)) == -1
+    done = ctypes.c_int64()
+    ex = np.array([0], np.int32)
+    assert L.mcg_release_region(None, 0, 0, ctypes.c_int64(5), ctypes.c_double(0), ctypes.c_double(0.01),
+                                ex.ctypes.data_as(ctypes.c_void_p), 1, ctypes.c_uint64(1), ctypes.byref(done)) == -1
+    assert L.mcg_batch_release_region(None, 0, 0, 0, ctypes.c_int64(5), ctypes.c_double(0), ctypes.c_double(0.01),
+                                      ex.ctypes.data_as(ctypes.c_void_p), 1, ctypes.c_uint64(1),
+                                      ctypes.byref(done)) == -1
+    vol = ctypes.c_double()
+    assert L.mcg_object_volume(0, None, 0, None, None, 0, ctypes.byref(vol)) == -1
