@@ -208,6 +208,21 @@ def inside_fixtures(ref64):
           "edge re-tries", int(((cv >> 31) & 1).sum()), "region tests", np.unique(reg, return_counts=True))
 
 
+def star_fixture(ref64):
+    """Diffusion cases on a closed non-convex object: the star-shaped sphere of
+    H.star_scene (object 0, deep lobes, transparent to A, reflective to B) in a
+    reflective cube, A + B -> C; random moves (half near walls) and moves aimed past a
+    reacting partner."""
+    rng = np.random.default_rng(20261207)
+    sc = H.star_scene(rng, n_mol=1500, levels=3)
+    sc.rxn_p = np.array([0.4])
+    cases = [(m, d) for (m, d, _) in H.random_cases(rng, sc, 700, scale=3.0, near_wall_frac=0.5)]
+    cases += partner_cases(rng, sc, 500)
+    res = record_scene(ref64, rng, "star", sc, cases)
+    kinds = np.unique(res[:, H.RES_HDR::H.EV_SIZE][res[:, H.RES_HDR::H.EV_SIZE] > 0], return_counts=True)
+    print("star", len(cases), "cases, event kinds", dict(zip(kinds[0].astype(int).tolist(), kinds[1].tolist())))
+
+
 def region_fixtures(ref64):
     """Releases into region expressions on H.regions_scene (star, box, small cube;
     closed objects 0-2): Region::initialize_volume_info_if_needed (object volumes),
@@ -282,6 +297,9 @@ def main():
     if sys.argv[1:] == ["regions"]:
         region_fixtures(ref64)
         return
+    if sys.argv[1:] == ["star"]:
+        star_fixture(ref64)
+        return
     rng = np.random.default_rng(20261203)
     for name, sc in scenes(rng).items():
         cases = []
@@ -311,6 +329,7 @@ def main():
     pathway_fixtures(ref64)
     inside_fixtures(ref64)
     region_fixtures(ref64)
+    star_fixture(ref64)
 
 
 if __name__ == "__main__":

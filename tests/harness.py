@@ -323,7 +323,7 @@ def edge_cases(sc: Scene):
 
 
 GOLDEN = ROOT / "tests" / "golden"
-GOLDEN_SCENES = ["cube", "cube_dense", "cube_classes", "sphere", "pathways"]
+GOLDEN_SCENES = ["cube", "cube_dense", "cube_classes", "sphere", "pathways", "star"]
 
 
 def star_scene(rng, n_mol=200, levels=3):
