@@ -147,6 +147,12 @@ int compute_setup(const double* origin, double partition_edge, uint32_t nsub, do
     err = "subparts_per_edge must be in 1..300 and partition_edge > 0";
     return -1;
   }
+  // the neighbour collection reaches one subpartition across a face, edge or corner,
+  // so R * sqrt(2) must stay below half an edge (mcell4_converter.cpp:121-127)
+  if (!(rxn_radius * 1.41421356238 < partition_edge / (double)nsub / 2.0)) {
+    err = "reaction radius times sqrt(2) must be less than half of the subpartition edge";
+    return -1;
+  }
   hs.nsub = nsub;
   hs.sp_edge = partition_edge / (double)nsub;
   hs.sp_rcp = 1.0 / hs.sp_edge;

@@ -47,6 +47,14 @@ def test_config_validation():
     assert ex.value.code == -6
     with pytest.raises(_native.EngineError):
         e.add_molecules(np.zeros((1, 3)), np.array([7]))
+    # R * sqrt(2) must stay below half a subpartition edge (mcell4_converter.cpp:121):
+    # 120 / 100 = 1.2 units against 0.5642 * sqrt(2) = 0.798; refused before any device work
+    f = _native.Engine("fp64", (-60, -60, -60), 120.0, 100, 0.5642, 3)
+    f.set_species([2.0, 2.0, 1.41])
+    with pytest.raises(_native.EngineError) as ex:
+        f.prepare()
+    assert ex.value.code == -1 and "subpartition edge" in str(ex.value)
+    f.close()
 
 
 def test_reactive_products_are_refused_without_a_device():
