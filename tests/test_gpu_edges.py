@@ -1,0 +1,86 @@
+"""Edge cases of the whole step: the subpartition grid, and ragged or empty replicas.
+
+The subpartition grid only decides which walls and partners a move examines. On any
+grid the reaction radius allows (R * sqrt(2) below half an edge), every wall a move
+can hit and every partner within R of it is examined, collisions are ordered by time
+and then partner id, and every draw is keyed by molecule id and iteration; so the
+trajectories of a model cut into a coarse grid, into its own 0.1 um grid and into the
+finest grid the radius allows (where occupants are binned per subpartition instead of
+per octant, the key space being too large for octants) are the same, molecule for
+molecule. Replicas of 0, 1, 31 and 33 molecules (empty, one lane, either side of a
+warp) beside a larger one step exactly as they do alone.
+"""
+import numpy as np
+import pytest
+
+from mcell_gb300 import _native
+from mcell_gb300 import workloads as W
+from tests import harness as H
+
+pytestmark = pytest.mark.gpu
+
+NSP = 3
+
+
+def _finest_grid(sc):
+    # largest n with R * sqrt(2) < (edge / n) / 2
+    n = int(np.floor(sc.partition_edge / (2.0 * 1.41421356238 * sc.rxn_radius)))
+    while n > 1 and not sc.rxn_radius * 1.41421356238 < sc.partition_edge / n / 2.0:
+        n -= 1
+    return min(n, 300)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_trajectory_does_not_depend_on_the_subpartition_grid(precision):
+    rng = np.random.default_rng(31)
+    sc = H.sphere_in_cube_scene(rng, levels=2, n_mol=6000, p_rxn=0.3)
+    grids = [sc.nsub, 7, _finest_grid(sc)]
+    assert grids[2] > 2 * grids[0] and grids[2] ** 3 * NSP * 8 > (1 << 26)  # octants off on the finest
+    iters = 20
+    runs = []
+    for n in grids:
+        sc.nsub = n
+        e = H.make_gpu_engine(sc, precision, bimol=[(0, 1, 0.3, (2, -1))], unimol=[(2, 0.05, (-1, -1))], seed=17)
+        e.step(iters)
+        tr = e.trajectory(iters)
+        pos, sp, ids = e.molecules()
+        o = np.argsort(ids)
+        runs.append((tr, pos[o], sp[o], ids[o]))
+        e.close()
+    assert runs[0][0][-1, 2] > 0  # reactions happened
+    for n, r in zip(grids[1:], runs[1:]):
+        for a, b, what in zip(runs[0], r, ("counts", "positions", "species", "ids")):
+            assert np.array_equal(a, b), f"{what} differ between {grids[0]} and {n} subpartitions per edge"
+
+
+def _alone(model, precision, seed, iters):
+    e = W.engine_for(model, precision, seed=seed)
+    e.step(iters)
+    t = e.trajectory(iters)
+    pos, sp, ids = e.molecules()
+    o = np.argsort(ids)
+    e.close()
+    return t, pos[o], sp[o]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_ragged_and_empty_replicas_step_as_they_do_alone(precision):
+    ms = W.replica_models(5, seed=41, n_range=(2_000, 6_000), edge_range_um=(0.5, 1.0), levels=(2, 3))
+    for m, n in zip(ms, (0, 1, 31, 33)):
+        m.pos, m.species = m.pos[:n], m.species[:n]
+    iters = 25
+    want = [_alone(m, precision, 500 + k, iters) for k, m in enumerate(ms)]
+    b = _native.Batch(precision, NSP, len(ms))
+    hs = [W.model_handle(m, precision, seed=500 + k) for k, m in enumerate(ms)]
+    ids = b.add(hs)
+    for h in hs:
+        h.close()
+    b.step(iters)
+    for k, r in enumerate(ids):
+        t = b.trajectory(r, iters)
+        assert np.array_equal(t, want[k][0]), f"replica {k}"
+        pos, sp, uid = b.molecules(r)
+        o = np.argsort(uid)
+        assert np.array_equal(pos[o], want[k][1]) and np.array_equal(sp[o], want[k][2]), f"replica {k}"
+    assert int(b.counts(ids[0]).sum()) == 0
+    b.close()

@@ -1,5 +1,7 @@
 """Precision form on a reduced bumpy tube (2 um long, 40,400 triangles, 200k
-molecules, 5% within 1 nm of mesh edges and vertices, dt = 0.1 us): the fp32
+molecules, 5% within 1 nm of mesh edges and vertices, dt = 0.1 us, 100
+subpartitions per edge: 0.022 um, above the 2 * sqrt(2) * R = 0.016 um the reaction
+radius needs, and close to the full tube's 0.034 um): the fp32
 engine against the fp64 engine (which follows the reference routines bit for bit).
 
 Bars: wall-hit identity mismatch rate below 1e-3 (half of the cases start next
@@ -17,7 +19,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.fixture(scope="module")
 def tube():
-    return W.bumpy_tube(n_mol=200_000, length_um=2.0, n_z=100)
+    return W.bumpy_tube(n_mol=200_000, length_um=2.0, n_z=100, subparts_per_edge=100)
 
 
 def test_fp32_wall_hits_match_fp64_near_edges(tube):
