@@ -416,9 +416,10 @@ def run_precision(args):
     wall-hit identity on 100,000 traced cases of the full model (10M molecules,
     200,400 triangles; half of the cases start within 1 nm of an edge or vertex),
     once with each engine at its own stored positions and once with the fp64 engine
-    at the fp32 engine's (trace arithmetic alone), and the count trajectories of a
-    1M-molecule tube over args.precision_iters iterations (the full model runs ~3 s per fp64
-    iteration)."""
+    at the fp32 engine's (trace arithmetic alone), and the count trajectories of a tube
+    of args.precision_count_molecules molecules over args.precision_iters iterations (the
+    full model, 10M x 500, takes the fp64 engine about 0.5 s per iteration, several
+    minutes per run, so the default run counts on 1M molecules over 100)."""
     import numpy as np
 
     from mcell_gb300 import precision
@@ -429,15 +430,21 @@ def run_precision(args):
     near = np.arange(n - int(round(0.05 * n)), n)
     mism = precision.wall_hit_mismatch(m, n_cases=100_000, near_ids=near)
     mism_same = precision.wall_hit_mismatch(m, n_cases=100_000, near_ids=near, same_start=True)
-    del m
-    small = W.bumpy_tube(n_mol=1_000_000, seed=2)
-    cnt = precision.count_error(small, n_iter=args.precision_iters)
-    return {"workload": "bumpy tube r = 0.2 um (+-0.05 um), 10 um, 200,400 reflective triangles, 5% of the molecules "
-                        "within 1 nm of edges/vertices, A+B->C, dt 0.1 us",
-            "wall_hit_mismatch_10M": mism, "wall_hit_mismatch_10M_same_start": mism_same,
-            f"count_error_1M_{args.precision_iters}_iterations": cnt,
-            "reduction": f"count error on a 1M-molecule tube over {args.precision_iters} iterations, not 10M x 500: "
-                         "the fp64 engine takes ~3 s per iteration of the full model (about 25 minutes for 500)"}
+    nc = args.precision_count_molecules
+    if nc != n:
+        del m
+        m = W.bumpy_tube(n_mol=nc, seed=2)
+    cnt = precision.count_error(m, n_iter=args.precision_iters)
+    out = {"workload": "bumpy tube r = 0.2 um (+-0.05 um), 10 um, 200,400 reflective triangles, 5% of the molecules "
+                       "within 1 nm of edges/vertices, A+B->C, dt 0.1 us",
+           "wall_hit_mismatch_10M": mism, "wall_hit_mismatch_10M_same_start": mism_same,
+           f"count_error_{nc // 1_000_000}M_{args.precision_iters}_iterations": cnt}
+    if (nc, args.precision_iters) != (n, 500):
+        out["reduction"] = (f"count error on a {nc:,}-molecule tube over {args.precision_iters} iterations, not "
+                            "10M x 500: the fp64 engine takes about 0.5 s per iteration of the full model, and two "
+                            "fp64 runs of 500 iterations do not fit a run of a few minutes (--precision-count-molecules "
+                            "10000000 --precision-iters 500 runs the configuration as stated)")
+    return out
 
 
 # ---------------------------------------------------------------- serving form
@@ -532,6 +539,8 @@ def main():
     ap.add_argument("--sustained-rate", type=float, default=10.0)
     ap.add_argument("--sustained-seconds", type=float, default=60.0, help="0 skips the sustained serving run")
     ap.add_argument("--precision-iters", type=int, default=100)
+    ap.add_argument("--precision-count-molecules", type=int, default=1_000_000,
+                    help="molecules of the tube whose count trajectories are compared (10M: the model as configured)")
     args = ap.parse_args()
     rank, world, _ = _rank_env()
     procs = args.cpu_procs or os.cpu_count() or 1
