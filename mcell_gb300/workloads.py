@@ -102,7 +102,8 @@ def bumpy_tube(n_mol=10_000_000, seed=1, length_um=10.0, radius_um=0.2, bump_um=
     200,400 triangles at the defaults) holding n_mol molecules, A:B 1:1; a fraction
     near_edge_frac of them sits within near_nm nm of a mesh edge or vertex (moved
     inwards from a random point of a random side edge, or from a random side
-    vertex), the rest uniform inside (at least 2 nm from the analytic surface, so
+    vertex, away from the two rows of triangles that meet the end caps), the rest
+    uniform inside (at least 2 nm from the analytic surface, so
     inside the triangulated one). A + B -> C at 1e8 M^-1 s^-1, D = 1e-6 cm^2/s
     (C: 5e-7), dt = 1e-7 s. The partition is the cube around the tube with
     subparts_per_edge subpartitions per edge."""
@@ -127,7 +128,10 @@ def bumpy_tube(n_mol=10_000_000, seed=1, length_um=10.0, radius_um=0.2, bump_um=
     # moved towards the axis by up to near_nm, plus a jitter of the same size along it
     n_side = n_theta * (n_z + 1)
     half = n_near // 2
-    sw = rng.integers(0, 2 * n_theta * n_z, half)  # side triangles come first
+    # side triangles come first, row by row; the first and last rows are left out: their
+    # edges reach the end rings, where the surface narrows towards the cap within one
+    # row, and a point there kept below the cap by the clip below can lie outside it
+    sw = rng.integers(2 * n_theta, 2 * n_theta * (n_z - 1), half)
     k = rng.integers(0, 3, half)
     a = v[w[sw, k]]
     b = v[w[sw, (k + 1) % 3]]
