@@ -417,9 +417,9 @@ def run_precision(args):
     200,400 triangles; half of the cases start within 1 nm of an edge or vertex),
     once with each engine at its own stored positions and once with the fp64 engine
     at the fp32 engine's (trace arithmetic alone), and the count trajectories of a tube
-    of args.precision_count_molecules molecules over args.precision_iters iterations (the
-    full model, 10M x 500, takes the fp64 engine about 0.5 s per iteration, several
-    minutes per run, so the default run counts on 1M molecules over 100)."""
+    of args.precision_count_molecules molecules over args.precision_iters iterations
+    (by default the model as configured, 10M x 500: about a minute for the three runs,
+    the fp64 ones slowest while most molecules are still unreacted)."""
     import numpy as np
 
     from mcell_gb300 import precision
@@ -440,10 +440,7 @@ def run_precision(args):
            "wall_hit_mismatch_10M": mism, "wall_hit_mismatch_10M_same_start": mism_same,
            f"count_error_{nc // 1_000_000}M_{args.precision_iters}_iterations": cnt}
     if (nc, args.precision_iters) != (n, 500):
-        out["reduction"] = (f"count error on a {nc:,}-molecule tube over {args.precision_iters} iterations, not "
-                            "10M x 500: the fp64 engine takes about 0.5 s per iteration of the full model, and two "
-                            "fp64 runs of 500 iterations do not fit a run of a few minutes (--precision-count-molecules "
-                            "10000000 --precision-iters 500 runs the configuration as stated)")
+        out["reduction"] = f"count error on a {nc:,}-molecule tube over {args.precision_iters} iterations, not 10M x 500"
     return out
 
 
@@ -538,8 +535,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="the overload burst's duration")
     ap.add_argument("--sustained-rate", type=float, default=10.0)
     ap.add_argument("--sustained-seconds", type=float, default=60.0, help="0 skips the sustained serving run")
-    ap.add_argument("--precision-iters", type=int, default=100)
-    ap.add_argument("--precision-count-molecules", type=int, default=1_000_000,
+    ap.add_argument("--precision-iters", type=int, default=500)
+    ap.add_argument("--precision-count-molecules", type=int, default=10_000_000,
                     help="molecules of the tube whose count trajectories are compared (10M: the model as configured)")
     args = ap.parse_args()
     rank, world, _ = _rank_env()
