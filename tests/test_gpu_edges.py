@@ -84,3 +84,29 @@ def test_ragged_and_empty_replicas_step_as_they_do_alone(precision):
         assert np.array_equal(pos[o], want[k][1]) and np.array_equal(sp[o], want[k][2]), f"replica {k}"
     assert int(b.counts(ids[0]).sum()) == 0
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_sixteen_species(precision):
+    """The largest species count (16), each species with its own diffusion step: seven
+    pairs A_k + B_k -> P with products 14 and 15. Each reaction takes one of each
+    reactant and makes one product, and no molecule leaves the box."""
+    rng = np.random.default_rng(43)
+    nsp = 16
+    sc = H.cube_scene(rng, n_mol=30000, nsub=24)
+    sc.mol_species = rng.integers(0, 14, size=30000).astype(np.uint32)
+    sc.space_steps = np.linspace(1.0, 2.5, nsp)
+    sc.wall_class = np.zeros((len(sc.tris), nsp), np.uint8)
+    bimol = [(2 * k, 2 * k + 1, 0.2 + 0.05 * k, (14 + k % 2, -1)) for k in range(7)]
+    init = np.bincount(sc.mol_species, minlength=nsp).astype(np.int64)
+    e = H.make_gpu_engine(sc, precision, bimol=bimol, seed=4)
+    e.step(30)
+    c = e.counts().astype(np.int64)
+    for k in range(7):
+        assert c[2 * k] - c[2 * k + 1] == init[2 * k] - init[2 * k + 1], k
+    assert (init[:14] - c[:14]).sum() == 2 * (c[14] + c[15])
+    assert c[14] > 0 and c[15] > 0
+    pos, sp, ids = e.molecules()
+    assert len(ids) == int(c.sum()) and (np.abs(pos) <= 50 + 1e-3).all()
+    assert np.array_equal(np.bincount(sp, minlength=nsp), c)
+    e.close()

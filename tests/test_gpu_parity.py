@@ -45,8 +45,10 @@ def test_fp64_matches_reference_golden(name):
 @pytest.mark.parametrize("seed", [5, 6])
 def test_fp64_matches_oracle_random(seed):
     rng = np.random.default_rng(seed)
+    star = H.star_scene(rng, n_mol=3000)
+    star.rxn_p = np.array([0.4])
     for sc in [H.cube_scene(rng, n_mol=3000, p_rxn=0.4),
-               H.sphere_in_cube_scene(rng, levels=3, n_mol=4000, radius_um=0.6, cube_um=1.5, p_rxn=0.4)]:
+               H.sphere_in_cube_scene(rng, levels=3, n_mol=4000, radius_um=0.6, cube_um=1.5, p_rxn=0.4), star]:
         cases = H.random_cases(rng, sc, 3000, scale=3.0, near_wall_frac=0.5)
         mols = [c[0] for c in cases]
         disps = np.array([c[1] for c in cases])
