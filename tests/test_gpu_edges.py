@@ -8,7 +8,8 @@ trajectories of a model cut into a coarse grid, into its own 0.1 um grid and int
 finest grid the radius allows (where occupants are binned per subpartition instead of
 per octant, the key space being too large for octants) are the same, molecule for
 molecule. Replicas of 0, 1, 31 and 33 molecules (empty, one lane, either side of a
-warp) beside a larger one step exactly as they do alone.
+warp) beside a larger one step exactly as they do alone. A model with the largest
+species count (16) keeps its reaction bookkeeping.
 """
 import numpy as np
 import pytest
