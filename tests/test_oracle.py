@@ -71,8 +71,10 @@ def test_oracle_pathways_match_reference_random():
 @pytest.mark.parametrize("seed", [11, 12])
 def test_oracle_matches_reference_random(seed):
     rng = np.random.default_rng(seed)
+    star = H.star_scene(rng, n_mol=2000)
+    star.rxn_p = np.array([0.3])
     for sc in [H.cube_scene(rng, n_mol=1500, p_rxn=0.3),
-               H.sphere_in_cube_scene(rng, levels=3, n_mol=2000, radius_um=0.6, cube_um=1.5, p_rxn=0.3)]:
+               H.sphere_in_cube_scene(rng, levels=3, n_mol=2000, radius_um=0.6, cube_um=1.5, p_rxn=0.3), star]:
         o, r = H.oracle().scene(sc), REF.scene(sc)
         assert np.array_equal(o.wall_consts(len(sc.tris)), r.wall_consts(len(sc.tris)))
         n3 = sc.nsub ** 3
