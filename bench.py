@@ -14,7 +14,8 @@ summed over the timed steps, over the device time of those steps.
          flushed (a 512 MB write) before every timed step
   e2e    the same metric through the C ABI with host buffers: the molecule
          upload from host memory and, every step, mcg_step + a device-to-host
-         read of the species counts, timed on the host
+         read of the species counts (mcg_request_counts after the step, waited
+         for once the next step is queued), timed on the host
 Arms:
   default            the CUDA engine (mcell_gb300)
   --impl reference   the reference algorithm on the host cores: the oracle's
@@ -245,10 +246,16 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     e2.add_molecules(pos, sp)
-    counts = None
+    # every step's counts are read, one step late: the copy is queued behind the step
+    # and waited for while the device runs the next one
+    counts, prev = None, None
     for _ in range(args.steps):
         e2.step(1)
-        counts = e2.counts()
+        t = e2.request_counts()
+        if prev is not None:
+            counts = e2.wait_counts(prev)
+        prev = t
+    counts = e2.wait_counts(prev)
     e2_s = time.perf_counter() - t0
     _, e2_steps, _ = e2.stats()
     e2.close()

@@ -102,6 +102,17 @@ int mcg_sync(mcg_engine* e);
 /* Live molecule count per species after the last iteration
    (replaces counting molecules for MolOrRxnCountEvent, src4/mol_or_rxn_count_event.cpp:707). */
 int mcg_get_counts(mcg_engine* e, uint64_t* counts /* [n_species] */);
+/* Non-blocking counts (no reference counterpart: MolOrRxnCountEvent counts the
+   molecules in place). mcg_request_counts queues, after the work queued so far, a
+   copy of the counts mcg_get_counts would return now and returns a ticket at once;
+   mcg_wait_counts waits for that copy alone, not for iterations queued after the
+   request, and returns the counts (device-side errors as mcg_sync reports them).
+   A host that requests after each mcg_step and waits for the previous ticket reads
+   every iteration's counts while the device runs the next one. Eight tickets can be
+   outstanding: a request takes the slot of the ticket eight before it, whose wait
+   then fails with MCG_ERR_ARG. */
+int mcg_request_counts(mcg_engine* e, uint64_t* ticket);
+int mcg_wait_counts(mcg_engine* e, uint64_t ticket, uint64_t* counts /* [n_species] */);
 /* Count trajectory: counts after each of the last n iterations run, oldest first
    ([n * n_species]); n <= iterations run since the last mcg_create. */
 int mcg_get_count_trajectory(mcg_engine* e, uint32_t n, uint64_t* counts);

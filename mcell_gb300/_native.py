@@ -23,7 +23,7 @@ TRACE_RESULT_SIZE = 265
 EXPORTS = [
     "mcg_create", "mcg_destroy", "mcg_last_error", "mcg_set_species", "mcg_upload_mesh", "mcg_add_bimol_rxn",
     "mcg_add_unimol_rxn", "mcg_add_molecules", "mcg_step", "mcg_sync", "mcg_get_counts",
-    "mcg_get_count_trajectory", "mcg_download_molecules", "mcg_get_stats", "mcg_prepare", "mcg_trace_cases",
+    "mcg_request_counts", "mcg_wait_counts", "mcg_get_count_trajectory", "mcg_download_molecules", "mcg_get_stats", "mcg_prepare", "mcg_trace_cases",
     "mcg_wall_consts", "mcg_walls_in_subparts", "mcg_set_options", "mcg_inject_device_alloc_failure", "mcg_get_profile",
     "mcg_get_escapes", "mcg_debug_molecule", "mcg_get_debug_log", "mcg_trace_cases_static",
     "mcg_batch_create", "mcg_batch_destroy", "mcg_batch_last_error", "mcg_batch_add", "mcg_batch_remove",
@@ -314,6 +314,18 @@ class Engine:
     def trajectory(self, n):
         out = np.zeros((n, self.n_species), np.uint64)
         self._chk(lib().mcg_get_count_trajectory(self.h, ctypes.c_uint32(n), _p(out)))
+        return out
+
+    def request_counts(self):
+        """Queue a copy of the counts after the work queued so far; returns a ticket at once."""
+        t = ctypes.c_uint64()
+        self._chk(lib().mcg_request_counts(self.h, ctypes.byref(t)))
+        return t.value
+
+    def wait_counts(self, ticket):
+        """The counts of a request, waiting for its copy only (not for later iterations)."""
+        out = np.zeros(self.n_species, np.uint64)
+        self._chk(lib().mcg_wait_counts(self.h, ctypes.c_uint64(ticket), _p(out)))
         return out
 
     def molecules(self, cap=None):

@@ -196,6 +196,22 @@ int mcg_get_counts(mcg_engine* e, uint64_t* counts) {
   return rc ? fail(e, rc, err) : MCG_OK;
 }
 
+int mcg_request_counts(mcg_engine* e, uint64_t* ticket) {
+  if (!e || !ticket) return MCG_ERR_ARG;
+  int rc = prepare(e);
+  if (rc) return rc;
+  std::string err;
+  rc = e->dev->request_counts(0, ticket, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
+int mcg_wait_counts(mcg_engine* e, uint64_t ticket, uint64_t* counts) {
+  if (!e || !counts || !e->dev) return MCG_ERR_ARG;
+  std::string err;
+  int rc = e->dev->wait_counts(ticket, counts, err);
+  return rc ? fail(e, rc, err) : MCG_OK;
+}
+
 int mcg_get_count_trajectory(mcg_engine* e, uint32_t n, uint64_t* counts) {
   if (!e || !counts || !e->dev) return MCG_ERR_ARG;
   std::string err;

@@ -395,6 +395,67 @@ class DeviceEngineT : public DeviceEngine {
     return 0;
   }
 
+  // Non-blocking counts. The copy of the counters and of the row the queued iterations
+  // will have written goes on the stream after them, into pinned slots, followed by an
+  // event; the wait is on that event alone, so iterations queued after the request keep
+  // running while the host reads. Before a replica's first iteration since its
+  // molecules were added the counts come from the start offsets, read at once.
+  int request_counts(uint32_t rep, uint64_t* ticket, std::string& err) override {
+    if (rep >= max_rep_ || !reps_[rep].used) {
+      err = "no such replica";
+      return -1;
+    }
+    if (!cslot_host_) {
+      MCG_CUDA(cudaMallocHost(&cslot_host_, sizeof(CountSlotHost) * NCSLOT));
+      for (int k = 0; k < NCSLOT; k++) {
+        MCG_CUDA(cudaEventCreateWithFlags(&cslot_ev_[k], cudaEventDisableTiming));
+        cslot_ticket_[k] = 0;
+      }
+    }
+    const uint64_t t = next_ticket_;
+    const int k = (int)(t % NCSLOT);
+    CountSlotHost& h = cslot_host_[k];
+    const Geo<T>& g = geos_h_[rep];
+    const uint64_t it = (uint64_t)cnt_.iteration + pending_iters_;
+    if (it > g.it0 && it > rebin_it_ && it <= 0xFFFFFFFFull) {
+      const uint64_t row = (it - 1) % traj_cap_;
+      MCG_CUDA(cudaMemcpyAsync(&h.c, d_cnt_, sizeof(Counters), cudaMemcpyDeviceToHost, stream_));
+      MCG_CUDA(cudaMemcpyAsync(h.n, d_traj_ + (row * max_rep_ + rep) * nsp_, sizeof(unsigned long long) * nsp_,
+                               cudaMemcpyDeviceToHost, stream_));
+      cslot_it_[k] = it;
+    } else {
+      uint64_t out[MAXSP];
+      int rc = counts(rep, out, err);
+      if (rc) return rc;
+      for (uint32_t a = 0; a < nsp_; a++) h.n[a] = out[a];
+      h.c = cnt_;
+      cslot_it_[k] = cnt_.iteration;
+    }
+    MCG_CUDA(cudaEventRecord(cslot_ev_[k], stream_));
+    cslot_ticket_[k] = t;
+    next_ticket_++;
+    *ticket = t;
+    return 0;
+  }
+
+  int wait_counts(uint64_t ticket, uint64_t* out, std::string& err) override {
+    const int k = (int)(ticket % NCSLOT);
+    if (!cslot_host_ || ticket == 0 || cslot_ticket_[k] != ticket) {
+      err = "unknown ticket, or one whose slot a later request took";
+      return -1;
+    }
+    MCG_CUDA(cudaEventSynchronize(cslot_ev_[k]));
+    const CountSlotHost& h = cslot_host_[k];
+    int rc = status_to_error(h.c.status, err);
+    if (rc) return rc;
+    if (h.c.iteration != cslot_it_[k]) {
+      err = "the counts of the requested iteration were not written";
+      return -2;
+    }
+    for (uint32_t a = 0; a < nsp_; a++) out[a] = h.n[a];
+    return 0;
+  }
+
   int trajectory(uint32_t rep, uint32_t n, uint64_t* out, std::string& err) override {
     int rc = sync(err);
     if (rc) return rc;
@@ -1830,6 +1891,11 @@ class DeviceEngineT : public DeviceEngine {
     cudaFree(d_cv_count_);
     cudaFree(d_cv_now_);
     cudaFree(d_cv_traj_);
+    if (cslot_host_) {
+      for (int k = 0; k < NCSLOT; k++) cudaEventDestroy(cslot_ev_[k]);
+      cudaFreeHost(cslot_host_);
+      cslot_host_ = nullptr;
+    }
     if (stream_) cudaStreamDestroy(stream_);
   }
 
@@ -1846,6 +1912,17 @@ class DeviceEngineT : public DeviceEngine {
   std::vector<std::array<cudaEvent_t, 5>> prof_;
   cudaGraphExec_t graph_[4] = {nullptr, nullptr, nullptr, nullptr};  // [parity + 2 * (iterations - 1)]
   uint64_t pending_iters_ = 0;  // iterations queued since the counters were last read
+  // pinned slots of the non-blocking counts (request_counts / wait_counts)
+  struct CountSlotHost {
+    Counters c;
+    unsigned long long n[MAXSP];
+  };
+  static constexpr int NCSLOT = 8;
+  CountSlotHost* cslot_host_ = nullptr;
+  cudaEvent_t cslot_ev_[NCSLOT] = {};
+  uint64_t cslot_ticket_[NCSLOT] = {};
+  uint64_t cslot_it_[NCSLOT] = {};
+  uint64_t next_ticket_ = 1;
   uint32_t nsp_ = 0, max_rep_ = 0, nkeys_ = 0, key_alloc_ = 0, ntiles_ = 0, traj_cap_ = 65536;
   uint64_t cap_ = 0, iterations_ = 0, launches_ = 0;
   uint64_t rebin_it_ = 0;  // engine iteration of the last re-sort (counts then come from the starts)

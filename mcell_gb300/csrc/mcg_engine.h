@@ -122,6 +122,9 @@ class DeviceEngine {
   virtual int step(uint32_t n, std::string& err) = 0;
   virtual int sync(std::string& err) = 0;
   virtual int counts(uint32_t rep, uint64_t* out, std::string& err) = 0;
+  // non-blocking counts: a copy queued after the work queued so far, read by ticket
+  virtual int request_counts(uint32_t rep, uint64_t* ticket, std::string& err) = 0;
+  virtual int wait_counts(uint64_t ticket, uint64_t* out, std::string& err) = 0;
   virtual int trajectory(uint32_t rep, uint32_t n, uint64_t* out, std::string& err) = 0;
   virtual int download(uint32_t rep, uint64_t cap, double* pos, uint32_t* species, uint64_t* ids, uint64_t* n_out,
                        std::string& err) = 0;

@@ -146,6 +146,13 @@ def test_output_and_test_hook_entry_points_check_their_arguments():
     assert L.mcg_write_counts(null, b"x", 0, 1, 1, ctypes.c_double(1e-6), 1, null, null, null) == -1
     assert L.mcg_batch_write_counts(null, 0, b"x", 0, 1, 1, ctypes.c_double(1e-6), 1, null, null, null) == -1
     assert L.mcg_write_viz(null, b"x", 0, null, ctypes.c_uint64(0), ctypes.c_uint64(1), ctypes.c_double(0.01)) == -1
+    # the non-blocking counts refuse a missing handle, ticket output or engine without a device
+    assert L.mcg_request_counts(null, null) == -1
+    assert L.mcg_wait_counts(null, ctypes.c_uint64(1), null) == -1
+    e = _native.Engine("fp64", (-60, -60, -60), 120.0, 12, 0.5642, 3)
+    out = np.zeros(3, np.uint64)
+    assert L.mcg_wait_counts(e.h, ctypes.c_uint64(1), out.ctypes.data_as(ctypes.c_void_p)) == -1
+    e.close()
     # the out-of-memory hook arms and disarms without a device
     assert L.mcg_inject_device_alloc_failure(ctypes.c_int64(5)) == 0
     assert L.mcg_inject_device_alloc_failure(ctypes.c_int64(-1)) == 0

@@ -111,3 +111,33 @@ def test_sixteen_species(precision):
     assert len(ids) == int(c.sum()) and (np.abs(pos) <= 50 + 1e-3).all()
     assert np.array_equal(np.bincount(sp, minlength=nsp), c)
     e.close()
+
+
+def test_counts_read_while_the_next_iteration_runs():
+    """mcg_request_counts / mcg_wait_counts: the counts of every iteration, read one
+    iteration late (the device runs the next meanwhile), equal the count trajectory;
+    a request before the first iteration gives the uploaded counts; a slot taken by a
+    later request makes the old ticket's wait fail."""
+    rng = np.random.default_rng(8)
+    sc = H.cube_scene(rng, n_mol=20000)
+    e = H.make_gpu_engine(sc, "fp32", bimol=[(0, 1, 0.3, (2, -1))], seed=3)
+    t0 = e.request_counts()
+    assert np.array_equal(e.wait_counts(t0), e.counts())
+    prev, seen = None, []
+    for _ in range(6):
+        e.step(1)
+        t = e.request_counts()
+        if prev is not None:
+            seen.append(e.wait_counts(prev))
+        prev = t
+    seen.append(e.wait_counts(prev))
+    assert np.array_equal(np.array(seen), e.trajectory(6))
+    assert seen[-1][2] > 0
+    e.step(2)
+    tickets = [e.request_counts() for _ in range(8)]
+    assert np.array_equal(e.wait_counts(tickets[0]), e.counts())
+    e.request_counts()
+    with pytest.raises(_native.EngineError):
+        e.wait_counts(tickets[0])
+    assert np.array_equal(e.wait_counts(tickets[1]), e.counts())
+    e.close()
