@@ -78,6 +78,18 @@ class GpuDiffuseReactEvent {
     check(mcg_get_counts(engine_, c.data()), "mcg_get_counts");
     return c;
   }
+  // the same counts without waiting now: a ticket for a copy queued behind the
+  // iterations run so far, redeemed later (a count buffer's flush)
+  uint64_t request_counts() {
+    uint64_t t = 0;
+    check(mcg_request_counts(engine_, &t), "mcg_request_counts");
+    return t;
+  }
+  std::vector<uint64_t> wait_counts(uint64_t ticket, uint32_t n_species) {
+    std::vector<uint64_t> c(n_species);
+    check(mcg_wait_counts(engine_, ticket, c.data()), "mcg_wait_counts");
+    return c;
+  }
   void molecules(std::vector<double>& pos, std::vector<uint32_t>& species, std::vector<uint64_t>& ids) {
     uint64_t n = 0;
     check(mcg_download_molecules(engine_, 0, nullptr, nullptr, nullptr, &n), "mcg_download_molecules");

@@ -49,6 +49,26 @@ int main() {
         return 1;
       }
     }
+    // a count buffer that takes a ticket at each barrier and reads it one barrier later
+    uint64_t prev = 0;
+    for (int it = 0; it < 20; it++) {
+      ev.set_barrier_time_for_next_execution(1.0);
+      ev.step();
+      ev.update_event_time_for_next_scheduled_time();
+      const uint64_t t = ev.request_counts();
+      if (prev) {
+        std::vector<uint64_t> c = ev.wait_counts(prev, 3);
+        if (c[0] + c[2] != (uint64_t)n / 2 || c[1] + c[2] != (uint64_t)n / 2) {
+          std::printf("mass balance broken in the counts read late at iteration %d\n", it);
+          return 1;
+        }
+      }
+      prev = t;
+    }
+    if (ev.wait_counts(prev, 3) != ev.counts(3)) {
+      std::printf("the last ticket's counts differ from the counts now\n");
+      return 1;
+    }
     std::vector<double> p;
     std::vector<uint32_t> s;
     std::vector<uint64_t> ids;
