@@ -66,8 +66,8 @@ def test_fp64_matches_oracle_random(seed):
 def test_fp32_wall_hit_mismatch_rate():
     """fp32 geometry against the fp64 oracle: wall-hit identity must agree on nearly
     every case, and final positions closely. Bounds at about 3x what was measured here
-    (0 of 4,000 mismatches; 12 per 100,000 on the 10M-molecule precision tube, i.e. 1.4
-    expected at 3x that rate; largest position error 0.028 internal units)."""
+    (0 of 4,000 mismatches; 9-12 per 100,000 on the 10M-molecule precision tube, i.e.
+    1.1-1.4 expected at 3x that rate; largest position error 0.028 internal units)."""
     rng = np.random.default_rng(7)
     sc = H.sphere_in_cube_scene(rng, levels=3, n_mol=3000, radius_um=0.6, cube_um=1.5, p_rxn=0.0)
     cases = H.random_cases(rng, sc, 4000, scale=3.0, near_wall_frac=0.6)
