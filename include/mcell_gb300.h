@@ -305,6 +305,11 @@ int mcg_serve_create(const mcg_server_config* cfg, mcg_server** out);
 /* Stops the worker (open requests are abandoned) and frees everything. */
 void mcg_serve_destroy(mcg_server* s);
 const char* mcg_serve_last_error(const mcg_server* s);
+/* Queues a copy of the model for n_iterations. The host half of its admission (its
+   subpartition grid, autotuned when the server autotunes, and its wall constants
+   and lists: milliseconds for a mesh of thousands of walls) is done here, in the
+   caller's thread, so that the worker keeps the device busy; a request's time to
+   result starts at this call. */
 int mcg_serve_submit(mcg_server* s, const mcg_engine* model, uint32_t n_iterations, uint64_t* ticket);
 /* State of a request and seconds from submission to its result (or until now). */
 int mcg_serve_poll(mcg_server* s, uint64_t ticket, int* state, double* seconds);

@@ -162,6 +162,62 @@ int tune_diffuse(mcg_batch* b, uint32_t* used, uint32_t budget, std::string& err
 
 }  // namespace
 
+int batch_prepare_replica(const mcg_engine* m, bool autotune, ReplicaPrep& out, std::string& err) {
+  if (!m) {
+    err = "null model";
+    return MCG_ERR_ARG;
+  }
+  if (m->dev) {
+    err = "a model added to a batch must not have been prepared or stepped";
+    return MCG_ERR_ARG;
+  }
+  if (!m->species_set) {
+    err = "model without mcg_set_species";
+    return MCG_ERR_ARG;
+  }
+  if (m->wclass.empty() && !m->walls.empty()) {
+    err = "mesh without wall classes";
+    return MCG_ERR_ARG;
+  }
+  if (int rc = mcg::check_model_supported(*m, err)) return rc;
+  out.octants = true;
+  out.nsub = autotune ? choose_subparts(m, &out.octants) : m->cfg.subparts_per_edge;
+  if (mcg::compute_setup(m->cfg.partition_origin, m->cfg.partition_edge, out.nsub, m->cfg.rxn_radius,
+                         (uint32_t)(m->verts.size() / 3), m->verts.data(), (uint32_t)(m->walls.size() / 3),
+                         m->walls.data(), out.hs, err))
+    return MCG_ERR_ARG;
+  return MCG_OK;
+}
+
+int batch_add_prepared(mcg_batch* b, uint32_t n, mcg_engine* const* models, ReplicaPrep* const* preps,
+                       const uint32_t* n_iterations, uint32_t* ids) {
+  if (!b || (n && (!models || !preps || !ids))) return MCG_ERR_ARG;
+  if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  std::vector<mcg::ReplicaSpec> specs(n);
+  for (uint32_t k = 0; k < n; k++) {
+    const mcg_engine* m = models[k];
+    if (!m || !preps[k]) return bfail(b, MCG_ERR_ARG, "null model");
+    if (m->cfg.n_species != b->cfg.n_species) return bfail(b, MCG_ERR_ARG, "model species count differs from the batch");
+    mcg::ReplicaSpec& sp = specs[k];
+    sp.hs = &preps[k]->hs;
+    sp.chem = &m->chem;
+    sp.wall_class = &m->wclass;
+    sp.wall_obj = m->wall_obj.empty() ? nullptr : &m->wall_obj;
+    sp.counted = m->counted;
+    sp.seed = m->cfg.seed;
+    sp.n_mol = m->pend_species.size();
+    sp.pos = m->pend_pos.data();
+    sp.species = m->pend_species.data();
+    sp.n_iterations = n_iterations ? n_iterations[k] : 0;
+    sp.octants = preps[k]->octants;
+  }
+  std::string err;
+  int rc = b->dev->add_replicas(specs.data(), n, ids, err);
+  if (rc) return bfail(b, rc, err);
+  for (uint32_t k = 0; k < n; k++) b->nsub[ids[k]] = preps[k]->nsub;
+  return MCG_OK;
+}
+
 extern "C" {
 
 int mcg_batch_create(const mcg_batch_config* cfg, mcg_batch** out) {
@@ -201,45 +257,14 @@ int mcg_batch_add(mcg_batch* b, uint32_t n, mcg_engine* const* models, const uin
                   uint32_t* ids) {
   if (!b || (n && (!models || !ids))) return MCG_ERR_ARG;
   if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
-  std::vector<mcg::HostSetup> hs(n);
-  std::vector<mcg::ReplicaSpec> specs(n);
-  std::vector<uint32_t> nsub(n);
+  std::vector<ReplicaPrep> prep(n);
+  std::vector<ReplicaPrep*> pp(n);
   for (uint32_t k = 0; k < n; k++) {
-    const mcg_engine* m = models[k];
-    if (!m) return bfail(b, MCG_ERR_ARG, "null model");
-    if (m->dev) return bfail(b, MCG_ERR_ARG, "a model added to a batch must not have been prepared or stepped");
-    if (m->cfg.n_species != b->cfg.n_species) return bfail(b, MCG_ERR_ARG, "model species count differs from the batch");
-    if (!m->species_set) return bfail(b, MCG_ERR_ARG, "model without mcg_set_species");
-    if (m->wclass.empty() && !m->walls.empty()) return bfail(b, MCG_ERR_ARG, "mesh without wall classes");
-    {
-      std::string why;
-      if (int rc = mcg::check_model_supported(*m, why)) return bfail(b, rc, why);
-    }
-    bool oct = true;
-    nsub[k] = b->cfg.autotune ? choose_subparts(m, &oct) : m->cfg.subparts_per_edge;
     std::string err;
-    if (mcg::compute_setup(m->cfg.partition_origin, m->cfg.partition_edge, nsub[k], m->cfg.rxn_radius,
-                           (uint32_t)(m->verts.size() / 3), m->verts.data(), (uint32_t)(m->walls.size() / 3),
-                           m->walls.data(), hs[k], err))
-      return bfail(b, MCG_ERR_ARG, err);
-    mcg::ReplicaSpec& sp = specs[k];
-    sp.hs = &hs[k];
-    sp.chem = &m->chem;
-    sp.wall_class = &m->wclass;
-    sp.wall_obj = m->wall_obj.empty() ? nullptr : &m->wall_obj;
-    sp.counted = m->counted;
-    sp.seed = m->cfg.seed;
-    sp.n_mol = m->pend_species.size();
-    sp.pos = m->pend_pos.data();
-    sp.species = m->pend_species.data();
-    sp.n_iterations = n_iterations ? n_iterations[k] : 0;
-    sp.octants = oct;
+    if (int rc = batch_prepare_replica(models[k], b->cfg.autotune != 0, prep[k], err)) return bfail(b, rc, err);
+    pp[k] = &prep[k];
   }
-  std::string err;
-  int rc = b->dev->add_replicas(specs.data(), n, ids, err);
-  if (rc) return bfail(b, rc, err);
-  for (uint32_t k = 0; k < n; k++) b->nsub[ids[k]] = nsub[k];
-  return MCG_OK;
+  return batch_add_prepared(b, n, models, pp.data(), n_iterations, ids);
 }
 
 int mcg_batch_remove(mcg_batch* b, uint32_t n, const uint32_t* ids) {

@@ -4,11 +4,14 @@
 // slots and the device-memory budget allow (first come, first served), runs the
 // block for every admitted request at once, collects the requests that reached
 // their iteration count and frees their slots. A request's state stays resident
-// on the device from admission to its last iteration.
+// on the device from admission to its last iteration. The host half of an
+// admission (grid, wall constants and lists) is done at submission, in the
+// submitting thread: in the worker it held the device idle (about 30 ms a request).
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <unordered_map>
@@ -31,6 +34,9 @@ struct Request {
   Clock::time_point t_submit, t_done;
   std::vector<uint64_t> traj;   // [iterations][n_species], harvested block by block
   std::string err;              // why the request failed
+  // host half of the admission (grid, wall constants and lists), made at submission
+  // so that the worker, which the device waits on, only does the device half
+  std::unique_ptr<ReplicaPrep> prep;
 };
 
 }  // namespace
@@ -64,9 +70,9 @@ int sfail(mcg_server* s, int code, const std::string& msg) {
 // device bytes a request needs while resident: its mesh and wall lists, its sort
 // keys, and its molecules (both sorted copies and per-iteration scratch, with
 // room for products)
-uint64_t estimate_bytes(const mcg_engine& m, int precision) {
+uint64_t estimate_bytes(const mcg_engine& m, int precision, uint32_t subparts_per_edge) {
   const uint64_t nw = m.walls.size() / 3;
-  const uint64_t n = m.cfg.subparts_per_edge;
+  const uint64_t n = subparts_per_edge;
   const uint64_t keys = (uint64_t)m.cfg.n_species * n * n * n * 8;
   const uint64_t per_wall = precision == MCG_PRECISION_FP64 ? 232 : 120;
   const uint64_t per_mol = precision == MCG_PRECISION_FP64 ? 330 : 240;
@@ -89,14 +95,18 @@ int serve_once(mcg_server* s, std::unique_lock<std::mutex>& lk) {
   }
   if (admit.empty() && s->running.empty()) return MCG_OK;
   std::vector<mcg_engine*> models;
+  std::vector<ReplicaPrep*> preps;
   std::vector<uint32_t> iters;
   for (uint64_t t : admit) {
     models.push_back(&s->reqs[t].model);
+    preps.push_back(s->reqs[t].prep.get());
     iters.push_back(s->reqs[t].n_iterations);
   }
   lk.unlock();
   std::vector<uint32_t> ids(admit.size());
-  int rc = admit.empty() ? MCG_OK : mcg_batch_add(s->batch, (uint32_t)admit.size(), models.data(), iters.data(), ids.data());
+  int rc = admit.empty() ? MCG_OK
+                         : batch_add_prepared(s->batch, (uint32_t)admit.size(), models.data(), preps.data(),
+                                              iters.data(), ids.data());
   if (rc && mcg_batch_sync(s->batch) == MCG_OK) {
     // the admission failed (device memory, a model the batch rejects) but left the
     // batch as it was: those requests fail, the running ones go on
@@ -121,6 +131,7 @@ int serve_once(mcg_server* s, std::unique_lock<std::mutex>& lk) {
     r.model.pend_pos.shrink_to_fit();
     r.model.pend_species.clear();
     r.model.pend_species.shrink_to_fit();
+    r.prep.reset();
     s->running.push_back(admit[k]);
   }
   s->reserved += extra;
@@ -257,16 +268,17 @@ int mcg_serve_submit(mcg_server* s, const mcg_engine* model, uint32_t n_iteratio
   if (model->dev) return sfail(s, MCG_ERR_ARG, "a submitted model must not have been prepared or stepped");
   if (model->cfg.n_species != s->cfg.n_species) return sfail(s, MCG_ERR_ARG, "model species count differs");
   if (!model->species_set) return sfail(s, MCG_ERR_ARG, "model without mcg_set_species");
+  Request r;
+  r.t_submit = Clock::now();  // the time to result includes the preparation below
+  r.prep.reset(new ReplicaPrep());
   {
     std::string why;
-    if (int rc = mcg::check_model_supported(*model, why)) return sfail(s, rc, why);
+    if (int rc = batch_prepare_replica(model, s->cfg.autotune != 0, *r.prep, why)) return sfail(s, rc, why);
   }
-  Request r;
   r.model = *model;
   r.model.err.clear();
   r.n_iterations = n_iterations;
-  r.est_bytes = estimate_bytes(*model, s->cfg.precision);
-  r.t_submit = Clock::now();
+  r.est_bytes = estimate_bytes(*model, s->cfg.precision, r.prep->nsub);
   std::lock_guard<std::mutex> lk(s->mu);
   if (s->failed) return sfail(s, MCG_ERR_CUDA, "server stopped after a device error: " + s->err);
   if (r.est_bytes > s->cfg.hbm_budget_bytes)
