@@ -1,9 +1,11 @@
 // C ABI of batches (declared in include/mcell_gb300.h): many independent models
 // as replicas of one device engine, plus the batch autotuner.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -257,11 +259,27 @@ int mcg_batch_add(mcg_batch* b, uint32_t n, mcg_engine* const* models, const uin
                   uint32_t* ids) {
   if (!b || (n && (!models || !ids))) return MCG_ERR_ARG;
   if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
+  // the host halves only read their models: prepared on several threads (256 replicas
+  // of the batching workload take about 30 ms each on one core)
   std::vector<ReplicaPrep> prep(n);
   std::vector<ReplicaPrep*> pp(n);
+  std::vector<int> rcs(n, MCG_OK);
+  std::vector<std::string> errs(n);
+  const bool tune = b->cfg.autotune != 0;
+  const uint32_t nt = std::min<uint32_t>(n, std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
+  std::atomic<uint32_t> next{0};
+  auto work = [&] {
+    for (uint32_t k; (k = next.fetch_add(1)) < n;) rcs[k] = batch_prepare_replica(models[k], tune, prep[k], errs[k]);
+  };
+  if (nt <= 1) {
+    work();
+  } else {
+    std::vector<std::thread> th;
+    for (uint32_t t = 0; t < nt; t++) th.emplace_back(work);
+    for (auto& x : th) x.join();
+  }
   for (uint32_t k = 0; k < n; k++) {
-    std::string err;
-    if (int rc = batch_prepare_replica(models[k], b->cfg.autotune != 0, prep[k], err)) return bfail(b, rc, err);
+    if (rcs[k]) return bfail(b, rcs[k], errs[k]);
     pp[k] = &prep[k];
   }
   return batch_add_prepared(b, n, models, pp.data(), n_iterations, ids);
