@@ -77,34 +77,64 @@ uint32_t choose_subparts(const mcg_engine* m, bool* octants) {
   uint32_t best_n = n_user;
   bool best_oct = true;
   double best = 1e300;
+  std::vector<uint32_t> dense;  // samples per subpartition (dense grids)
+  std::vector<uint64_t> cell;   // subpartition of each sample
   for (uint32_t n : cand) {
     const double e = L / n;
     auto idx = [&](double x, int a) {
       long i = (long)std::floor((x - O[a]) / e);
       return (uint32_t)std::min<long>(std::max<long>(i, 0), (long)n - 1);
     };
-    // sampled molecules per occupied subpartition
-    std::unordered_map<uint64_t, std::pair<double, double>> occ;  // subpartition -> (molecules, walls)
-    for (const double* p : smp) {
-      const uint64_t s = idx(p[0], 0) + (uint64_t)n * (idx(p[1], 1) + (uint64_t)n * idx(p[2], 2));
-      occ[s].first += 1.0;
-    }
-    for (size_t w = 0; w < nw; w++) {
-      const double* bx = &box[6 * w];
-      const uint32_t x0 = idx(bx[0], 0), y0 = idx(bx[1], 1), z0 = idx(bx[2], 2);
-      const uint32_t x1 = idx(bx[3], 0), y1 = idx(bx[4], 1), z1 = idx(bx[5], 2);
-      if ((uint64_t)(x1 - x0 + 1) * (y1 - y0 + 1) * (z1 - z0 + 1) > 4096) continue;  // huge walls: any n sees them
-      for (uint32_t z = z0; z <= z1; z++)
-        for (uint32_t y = y0; y <= y1; y++)
-          for (uint32_t x = x0; x <= x1; x++) {
-            auto it = occ.find(x + (uint64_t)n * (y + (uint64_t)n * z));
-            if (it != occ.end()) it->second.second += 1.0;
-          }
-    }
+    // molecule-weighted molecules and walls per subpartition: sum over sampled
+    // molecules of the samples in their subpartition, and over walls of the samples
+    // in the subpartitions their grown box covers (integer sums, exact in any order)
     double mates = 0, walls = 0;
-    for (const auto& kv : occ) {
-      mates += kv.second.first * kv.second.first;
-      walls += kv.second.first * kv.second.second;
+    const uint64_t n3c = (uint64_t)n * n * n;
+    if (n3c <= (1ull << 21)) {
+      // dense counts for grids of up to 128 per edge (cleared after use)
+      if (dense.size() < n3c) dense.resize(n3c, 0);
+      cell.resize(smp.size());
+      for (size_t i = 0; i < smp.size(); i++) {
+        const double* p = smp[i];
+        cell[i] = idx(p[0], 0) + (uint64_t)n * (idx(p[1], 1) + (uint64_t)n * idx(p[2], 2));
+        dense[cell[i]]++;
+      }
+      uint64_t m2 = 0, ws = 0;
+      for (uint64_t c : cell) m2 += dense[c];
+      for (size_t w = 0; w < nw; w++) {
+        const double* bx = &box[6 * w];
+        const uint32_t x0 = idx(bx[0], 0), y0 = idx(bx[1], 1), z0 = idx(bx[2], 2);
+        const uint32_t x1 = idx(bx[3], 0), y1 = idx(bx[4], 1), z1 = idx(bx[5], 2);
+        if ((uint64_t)(x1 - x0 + 1) * (y1 - y0 + 1) * (z1 - z0 + 1) > 4096) continue;  // huge walls: any n sees them
+        for (uint32_t z = z0; z <= z1; z++)
+          for (uint32_t y = y0; y <= y1; y++)
+            for (uint32_t x = x0; x <= x1; x++) ws += dense[x + (uint64_t)n * (y + (uint64_t)n * z)];
+      }
+      for (uint64_t c : cell) dense[c] = 0;
+      mates = (double)m2;
+      walls = (double)ws;
+    } else {
+      std::unordered_map<uint64_t, std::pair<double, double>> occ;  // subpartition -> (molecules, walls)
+      for (const double* p : smp) {
+        const uint64_t s = idx(p[0], 0) + (uint64_t)n * (idx(p[1], 1) + (uint64_t)n * idx(p[2], 2));
+        occ[s].first += 1.0;
+      }
+      for (size_t w = 0; w < nw; w++) {
+        const double* bx = &box[6 * w];
+        const uint32_t x0 = idx(bx[0], 0), y0 = idx(bx[1], 1), z0 = idx(bx[2], 2);
+        const uint32_t x1 = idx(bx[3], 0), y1 = idx(bx[4], 1), z1 = idx(bx[5], 2);
+        if ((uint64_t)(x1 - x0 + 1) * (y1 - y0 + 1) * (z1 - z0 + 1) > 4096) continue;
+        for (uint32_t z = z0; z <= z1; z++)
+          for (uint32_t y = y0; y <= y1; y++)
+            for (uint32_t x = x0; x <= x1; x++) {
+              auto it = occ.find(x + (uint64_t)n * (y + (uint64_t)n * z));
+              if (it != occ.end()) it->second.second += 1.0;
+            }
+      }
+      for (const auto& kv : occ) {
+        mates += kv.second.first * kv.second.first;
+        walls += kv.second.first * kv.second.second;
+      }
     }
     mates *= (double)N / (S * S);  // molecule-weighted molecules per subpartition
     walls /= S;                    // molecule-weighted walls per subpartition
