@@ -126,6 +126,28 @@ def test_batch_subpartition_autotuner_choices():
     assert n <= sparse.nsub // 2 and not octants
 
 
+# (model grid, chosen grid, octants) for replica_models(24, seed=7) and
+# replica_models(8, seed=3, n_range=(1e5, 2e6)): the cost model's choices, kept
+# when its sums are computed another way
+AUTOTUNE_PINS = [(18, 21, 1), (28, 17, 0), (10, 24, 1), (12, 20, 0), (8, 13, 1), (14, 20, 1), (10, 10, 1),
+                 (28, 12, 1), (24, 29, 0), (20, 14, 1), (8, 16, 1), (12, 20, 1), (8, 27, 1), (28, 12, 1),
+                 (28, 20, 1), (30, 21, 1), (18, 8, 1), (12, 29, 0), (12, 20, 1), (10, 14, 1), (22, 18, 1),
+                 (24, 17, 1), (10, 10, 1), (8, 10, 1), (8, 19, 1), (14, 20, 1), (30, 25, 1), (8, 23, 1),
+                 (10, 24, 1), (24, 29, 1), (30, 30, 1), (26, 26, 1)]
+
+
+def test_batch_autotuner_choices_are_pinned():
+    from mcell_gb300 import workloads as W
+    ms = W.replica_models(24, seed=7) + W.replica_models(8, seed=3, n_range=(100_000, 2_000_000))
+    got = []
+    for m in ms:
+        h = W.model_handle(m, "fp32")
+        n, octants = h.autotune_subparts()
+        h.close()
+        got.append((m.nsub, n, int(octants)))
+    assert got == AUTOTUNE_PINS
+
+
 def test_server_needs_the_device():
     with pytest.raises(_native.EngineError) as ei:
         _native.Server("fp32", 3, max_slots=0)
