@@ -289,8 +289,8 @@ int mcg_batch_add(mcg_batch* b, uint32_t n, mcg_engine* const* models, const uin
                   uint32_t* ids) {
   if (!b || (n && (!models || !ids))) return MCG_ERR_ARG;
   if (!b->dev) return bfail(b, MCG_ERR_CUDA, "batch has no device engine");
-  // the host halves only read their models: prepared on several threads (256 replicas
-  // of the batching workload take about 30 ms each on one core)
+  // the host halves only read their models: prepared on several threads (a replica of
+  // the batching workload takes about 20 ms on one core, most of it the wall setup)
   std::vector<ReplicaPrep> prep(n);
   std::vector<ReplicaPrep*> pp(n);
   std::vector<int> rcs(n, MCG_OK);

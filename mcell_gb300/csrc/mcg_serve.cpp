@@ -6,7 +6,7 @@
 // their iteration count and frees their slots. A request's state stays resident
 // on the device from admission to its last iteration. The host half of an
 // admission (grid, wall constants and lists) is done at submission, in the
-// submitting thread: in the worker it held the device idle (about 30 ms a request).
+// submitting thread: in the worker it held the device idle (20-30 ms a request).
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
