@@ -274,8 +274,10 @@ def run_gpu(args, rank, world):
                      "peak_kind": peak_kind, "kernel": "k_diffuse",
                      "algorithmic_bytes_per_mol_step": ALG_BYTES_PER_MOL_STEP,
                      "traffic": (tpm * mols_per_launch) if tpm else None},
+        # read back per step: the species counts and the 64-byte head of the engine's
+        # counters (status word and iteration) that mcg_wait_counts checks
         "e2e": {"value": e2e_steps_all / e2e_s_all, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
-                "d2h_bytes_per_step": 8 * model.n_species},
+                "d2h_bytes_per_step": 8 * model.n_species + 64},
         "gpu_launches": int(l1 - l0),
         "clocks": clocks,
         "kernel_ms_per_step": {"diffuse": prof[1] / args.steps, "reactions": prof[2] / args.steps,

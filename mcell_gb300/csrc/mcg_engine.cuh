@@ -13,6 +13,7 @@
 #include <atomic>
 #include <array>
 #include <climits>
+#include <cstddef>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -419,7 +420,10 @@ class DeviceEngineT : public DeviceEngine {
     const uint64_t it = (uint64_t)cnt_.iteration + pending_iters_;
     if (it > g.it0 && it > rebin_it_ && it <= 0xFFFFFFFFull) {
       const uint64_t row = (it - 1) % traj_cap_;
-      MCG_CUDA(cudaMemcpyAsync(&h.c, d_cnt_, sizeof(Counters), cudaMemcpyDeviceToHost, stream_));
+      // the counters' head (through the status word and the iteration: 64 bytes) is
+      // all the wait reads, not the escape records after it
+      static_assert(offsetof(Counters, mol_steps) == 64, "counters head");
+      MCG_CUDA(cudaMemcpyAsync(&h.c, d_cnt_, offsetof(Counters, mol_steps), cudaMemcpyDeviceToHost, stream_));
       MCG_CUDA(cudaMemcpyAsync(h.n, d_traj_ + (row * max_rep_ + rep) * nsp_, sizeof(unsigned long long) * nsp_,
                                cudaMemcpyDeviceToHost, stream_));
       cslot_it_[k] = it;
