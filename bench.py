@@ -179,8 +179,11 @@ def combine_ranks(seconds, units, world, device):
     return t.item(), n.item()
 
 
-GPU_WORKLOAD = ("sphere_in_cube: icosphere r=1um 20480 tris transparent to A in a 2.5um reflective cube, 1M molecules "
-                "A:B 1:1, A+B->C 1e8/M/s, C->0 1e3/s, dt=1us")
+def workload_name(n_mol):
+    """The main line's workload, named by what it is (1M molecules unless --n-mol says otherwise)."""
+    count = "1M" if n_mol == 1_000_000 else f"{n_mol:,}"
+    return ("sphere_in_cube: icosphere r=1um 20480 tris transparent to A in a 2.5um reflective cube, "
+            f"{count} molecules A:B 1:1, A+B->C 1e8/M/s, C->0 1e3/s, dt=1us")
 
 
 def run_gpu(args, rank, world):
@@ -266,7 +269,7 @@ def run_gpu(args, rank, world):
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded uniform release; icosphere + cube mesh generated)",
-        "config": {"workload": GPU_WORKLOAD,
+        "config": {"workload": workload_name(args.n_mol),
                    "molecules": args.n_mol, "walls": int(len(model.walls)), "subparts_per_edge": int(model.nsub),
                    "precision": "fp32 positions", "parallelism": f"replicas x{world}",
                    "l2": "flushed (512 MB write) before every timed step"},
@@ -567,12 +570,12 @@ def main():
         line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": GPU_WORKLOAD, "molecules": args.n_mol,
+                "config": {"workload": workload_name(args.n_mol), "molecules": args.n_mol,
                            "precision": "fp64 positions (the oracle's serial engine restates the reference's fp64 "
                                         "build; the GPU arm computes positions in fp32)",
                            "parallelism": f"{procs} independent seeded processes (MCell4 is single-threaded)"},
                 "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
-                                 "sample": f"{procs} processes x {args.cpu_iters} iterations of the 1M-molecule model "
+                                 "sample": f"{procs} processes x {args.cpu_iters} iterations of the {args.n_mol:,}-molecule model "
                                            f"per step, up to 3 steps"},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -586,7 +589,7 @@ def main():
         rate, res = cpu_measure(procs, args.n_mol, args.cpu_iters)
         cpu = {"value": rate, "unit": UNIT, "cores": procs, "kind": "port",
                "sample": f"{procs} independent seeded processes x {args.cpu_iters} iterations of the "
-                         f"1M-molecule model (oracle serial engine, fp64)"}
+                         f"{args.n_mol:,}-molecule model (oracle serial engine, fp64)"}
         if not args.no_cube:
             cube_pool = mp.get_context("spawn").Pool(8)  # started before the first GPU call
     if world > 1:
