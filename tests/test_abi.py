@@ -20,6 +20,18 @@ def test_header_and_binding_agree():
     assert declared_symbols() == sorted(_native.EXPORTS)
 
 
+def test_headers_compile_as_c_and_cpp():
+    import shutil
+    import subprocess
+    if not shutil.which("gcc") or not shutil.which("g++"):
+        pytest.skip("no host compiler")
+    inc = H.ROOT / "include"
+    subprocess.run(["gcc", "-fsyntax-only", "-std=c99", "-Wall", "-Werror", "-x", "c", str(inc / "mcell_gb300.h")],
+                   check=True)
+    subprocess.run(["g++", "-fsyntax-only", "-std=c++17", "-Wall", "-Werror", "-x", "c++", "-I", str(inc),
+                    str(inc / "mcell_gb300_event.hpp")], check=True)
+
+
 def test_library_exports_every_declared_symbol():
     L = _native.lib()
     for name in declared_symbols():
