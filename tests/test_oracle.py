@@ -124,3 +124,17 @@ def test_space_step_and_probability_conversions():
     lay = conversion.partition_layout([-0.5] * 3, [0.5] * 3, partition_dimension_um=1.2,
                                       subpartition_dimension_um=0.1)
     assert lay.nsub == 12 and abs(lay.edge - 120) < 1e-9 and abs(lay.origin[0] + 60) < 1e-9
+
+
+@pytest.mark.parametrize("name,iters", [("closed_cube", 100), ("sphere_in_cube", 40)])
+def test_ensemble_fixture_reproduces_from_the_oracle(name, iters):
+    """The committed ensemble fixture (tests/golden/make_ensembles.py) is what the
+    oracle's serial engine computes now: seed 1, the first rows."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_ensembles", H.GOLDEN / "make_ensembles.py")
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    z = np.load(H.GOLDEN / f"ensemble_{name}.npz")
+    assert int(z["seeds"][0]) == 1
+    got = mk.run_one((name, 1, iters))
+    assert np.array_equal(got, z["counts"][0, :iters // int(z["every"])])
