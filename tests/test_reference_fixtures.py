@@ -1,5 +1,5 @@
-"""The golden fixtures of the inside tests and the region releases reproduce from the
-reference's own routines (oracle/_ref, compiled from the reference sources by
+"""The golden fixtures of the diffusion cases, the inside tests and the region releases
+reproduce from the reference's own routines (oracle/_ref, compiled from the reference sources by
 oracle/ref/build_ref.py where those sources exist; skipped elsewhere): the recorded
 decisions, volumes, boxes, counts, positions and removals are what the reference
 computes now, on the recorded inputs."""
@@ -48,3 +48,16 @@ def test_inside_fixture_reproduces():
     reg = np.array([[h.inside_region(o, p) for o in (0, 1)] for p in pts], np.int32)
     assert np.array_equal(cv, z["counted"][::7])
     assert np.array_equal(reg, z["inside_region"][::7])
+
+
+@pytest.mark.parametrize("name", H.GOLDEN_SCENES)
+def test_diffusion_fixture_reproduces(name):
+    """Every recorded diffusion case, its wall constants and wall lists, from the
+    reference routines now, bit for bit."""
+    sc, g = H.load_golden(name)
+    r = REF.scene(sc)
+    assert np.array_equal(r.wall_consts(len(sc.tris)), g["wall_consts"])
+    counts, lst = r.walls_in_subparts(sc.nsub ** 3)
+    assert np.array_equal(counts, g["wsp_counts"]) and np.array_equal(lst, g["wsp_list"])
+    got = np.array([r.diffuse_case(int(m), d, dr) for m, d, dr in zip(g["mols"], g["disps"], g["draws"])])
+    assert not H.compare_results(got, g["results"], rel=0.0, scene=sc)
