@@ -1,5 +1,5 @@
-"""The golden fixtures of the diffusion cases, the inside tests and the region releases
-reproduce from the reference's own routines (oracle/_ref, compiled from the reference sources by
+"""The golden fixtures of the diffusion cases, the reaction decisions, the inside tests
+and the region releases reproduce from the reference's own routines (oracle/_ref, compiled from the reference sources by
 oracle/ref/build_ref.py where those sources exist; skipped elsewhere): the recorded
 decisions, volumes, boxes, counts, positions and removals are what the reference
 computes now, on the recorded inputs."""
@@ -61,3 +61,18 @@ def test_diffusion_fixture_reproduces(name):
     assert np.array_equal(counts, g["wsp_counts"]) and np.array_equal(lst, g["wsp_list"])
     got = np.array([r.diffuse_case(int(m), d, dr) for m, d, dr in zip(g["mols"], g["disps"], g["draws"])])
     assert not H.compare_results(got, g["results"], rel=0.0, scene=sc)
+
+
+def test_reaction_fixtures_reproduce():
+    """test_bimolecular, time_of_unimol and which_unimolecular on the recorded draws."""
+    z = np.load(H.GOLDEN / "rxn_tests.npz")
+    tb = np.array([REF.test_bimolecular(p, s, u) for p, s, u in zip(z["P"], z["S"], z["U"])])
+    assert np.array_equal(tb, z["bimol"])
+    tu = np.array([REF.time_of_unimol(k, u) for k, u in zip(z["K"], z["Uu"])])
+    assert np.array_equal(tu, z["unimol"])
+    w = np.load(H.GOLDEN / "rxn_pathways.npz")
+    tb = np.array([REF.test_bimolecular_pw(w["cum"][i, :w["npw"][i]], w["scaling"][i], w["U"][i])
+                   for i in range(len(w["U"]))])
+    assert np.array_equal(tb, w["bimol"])
+    tu = np.array([REF.which_unimolecular(w["ucum"][i, :w["unpw"][i]], w["Uu"][i]) for i in range(len(w["Uu"]))])
+    assert np.array_equal(tu, w["unimol"])
