@@ -48,6 +48,11 @@ def test_inside_fixture_reproduces():
     reg = np.array([[h.inside_region(o, p) for o in (0, 1)] for p in pts], np.int32)
     assert np.array_equal(cv, z["counted"][::7])
     assert np.array_equal(reg, z["inside_region"][::7])
+    for k in range(len(z["rel_shape"])):
+        n = int(z["rel_n"][k])
+        pos, used = REF.release_ellipsoid_or_rectcuboid(int(z["rel_shape"][k]), n, z["rel_loc"][k], z["rel_dia"][k],
+                                                        z["rel_draws"][k])
+        assert used == int(z["rel_used"][k]) and np.array_equal(pos, z["rel_pos"][k, :n]), k
 
 
 @pytest.mark.parametrize("name", H.GOLDEN_SCENES)
