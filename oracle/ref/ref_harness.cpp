@@ -205,6 +205,18 @@ unsigned ref_scene_walls_in_subparts(void* sp, unsigned* counts, unsigned* list,
   return total;
 }
 
+// ExactDiskUtils::exact_disk (exact_disk_utils.inl:840-1145) at one collision point:
+// the molecule `moving` moving by mv from loc, the molecule `target` as the partner
+double ref_exact_disk(void* sp, const double* loc, const double* mv, unsigned moving, unsigned target) {
+  Partition& p = ((Scene*)sp)->p;
+  Molecule& diffused = p.get_m(moving);
+  Molecule& colliding = p.get_m(target);
+  const Vec3 at((pos_t)loc[0], (pos_t)loc[1], (pos_t)loc[2]);
+  Vec3 move((pos_t)mv[0], (pos_t)mv[1], (pos_t)mv[2]);
+  return ExactDiskUtils::exact_disk(p, at, move, p.config.rxn_radius_3d, diffused, colliding,
+                                    p.config.use_expanded_list);
+}
+
 unsigned ref_subpart_index(void* sp, const double* pos) {
   Partition& p = ((Scene*)sp)->p;
   return p.get_subpart_index(Vec3((pos_t)pos[0], (pos_t)pos[1], (pos_t)pos[2]));

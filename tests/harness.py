@@ -152,6 +152,15 @@ class _Handle:
         p = np.ascontiguousarray(pos, np.float64)
         return self.c.fn("subpart_index")(self.h, ptr(p))
 
+    def exact_disk(self, loc, mv, moving, target):
+        """exact_disk at loc for molecule `moving` (move mv) against molecule `target`:
+        the unoccluded fraction of the reaction disk, or < 0 when a wall blocks it."""
+        f = self.c.fn("exact_disk")
+        f.restype = _d
+        l = np.ascontiguousarray(loc, np.float64)
+        m = np.ascontiguousarray(mv, np.float64)
+        return f(self.h, ptr(l), ptr(m), _u(moving), _u(target))
+
     def set_objects(self, object_of_wall, counted):
         """Geometry objects: the object index of each wall; counted[k] marks counted volumes."""
         ow = np.ascontiguousarray(object_of_wall, np.uint32)
